@@ -1,0 +1,258 @@
+/*
+ * lbdem.h - C ABI of the GB300 coupled free-surface lattice-Boltzmann / DEM
+ * impact solver (liblbdem.so).
+ *
+ * This boundary replaces the reference's in-process C++ classes:
+ *   LB  (src/LB.h:32-230)   latticeDefinition, latticeBoltzmannGet,
+ *        latticeBolzmannInit, latticeBolzmannStep,
+ *        latticeBoltzmannCouplingStep, latticeBoltzmannFreeSurfaceStep
+ *   DEM (src/DEM.h:21-190)  discreteElementGet, discreteElementInit,
+ *        discreteElementStep
+ * and the per-step driver goCycle (src/main.cpp:38-67).
+ * All quantities are in the reference's units: configuration values and
+ * particle/object/wall state in physical units, lattice fields in lattice
+ * units. The vertical axis is y, as in the reference.
+ *
+ * Conventions
+ *  - Every call returns an int status (LBDEM_OK == 0). lbdem_last_error()
+ *    gives a message for the most recent failure on a context.
+ *  - Plain pointers and sizes only; caller-owned host buffers; the context
+ *    owns all device memory. One context is one impact run on one GPU.
+ *  - Calls on one context are not thread-safe; distinct contexts are.
+ *  - Download calls synchronise the context's stream; step calls only
+ *    enqueue work (no host synchronisation inside a step).
+ */
+#ifndef LBDEM_H
+#define LBDEM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBDEM_ABI_VERSION 1
+
+/* status codes */
+#define LBDEM_OK 0
+#define LBDEM_ERR_INVALID 1      /* bad argument or unsupported option   */
+#define LBDEM_ERR_CUDA 2         /* CUDA runtime error                   */
+#define LBDEM_ERR_OOM 3          /* device allocation failed             */
+#define LBDEM_ERR_IO 4           /* configuration / input file error     */
+#define LBDEM_ERR_NONFINITE 5    /* NaN or Inf detected in the state     */
+#define LBDEM_ERR_OVERFLOW 6     /* neighbour list or cell list overflow */
+#define LBDEM_ERR_DEVICE_STATE 7 /* kernel reported an internal error    */
+#define LBDEM_ERR_NO_DEVICE 8    /* no CUDA device present               */
+
+/* node types, src/node.h:130-143 */
+#define LBDEM_FLUID 0
+#define LBDEM_GAS 2
+#define LBDEM_INTERFACE 3
+#define LBDEM_PERIODIC 4
+#define LBDEM_SLIP_STAT_WALL 5
+#define LBDEM_SLIP_DYN_WALL 6
+#define LBDEM_STAT_WALL 7
+#define LBDEM_DYN_WALL 8
+#define LBDEM_CYLINDER 9
+#define LBDEM_TOPOGRAPHY 11
+#define LBDEM_OBJECT 12
+
+/* precision forms */
+#define LBDEM_PLAIN_FP64 0 /* FP64 throughout, reproduces the reference    */
+#define LBDEM_MIXED 1      /* FP32 deviation storage, FP64 islands         */
+
+/* One suspended sphere as read from particles.dat (src/DEM.cpp:88-134):
+ * radius, position (after the reader's -0.05 shift and scale), velocity,
+ * angular velocity. */
+typedef struct lbdem_particle_in {
+  double r;
+  double x[3];
+  double v[3];
+  double w[3];
+  int32_t size;  /* constituent count, multiplies mass and inertia        */
+  int32_t index; /* index column of particles.dat (informational)         */
+} lbdem_particle_in;
+
+/* One impactor as read from objects.dat (src/DEM.cpp:142-166). */
+typedef struct lbdem_object_in {
+  int32_t index;
+  double r;
+  double x[3];
+  double v[3];
+} lbdem_object_in;
+
+/* Every configuration key of parameters.cfg the step depends on, with the
+ * reference's names (src/main.cpp:128-185, src/LB.cpp:128-338,
+ * src/DEM.cpp:17-78). Unsupported keys (restart, topography, rotation,
+ * non-Newtonian rheology, bodies) are accepted only at their inert values. */
+typedef struct lbdem_config {
+  /* switches and time integration */
+  int32_t demSolve, lbSolve, freeSurfaceSolve, forceFieldSolve;
+  double demInitialRepeat;
+  int32_t lbmInitialRepeat;
+  double maxTime;
+  int32_t maximumTimeSteps;
+  /* output cadences (host-side IO only) */
+  double screenExpTime, fluidExpTime, fluidLagrangianExpTime, partExpTime,
+      partRecycleExpTime, fluidRecycleExpTime;
+  /* LB */
+  double unitLength, unitTime, unitDensity;
+  double lbSizeX, lbSizeY, lbSizeZ;
+  int32_t lbRestart, lbTopography;
+  double initVelocity[3];
+  double lbF[3];
+  double lbRot[3];
+  double lbRotCenter[3];
+  int32_t boundary[6];
+  double slipCoefficient;
+  double fluidHeight;
+  int32_t rheologyNewtonian; /* 1 when rheologyModel = NEWTONIAN          */
+  double initVisc;
+  int32_t turbulenceSolve;
+  double turbConst;
+  /* DEM */
+  double density, objectDensity, bodyDensity;
+  double linearStiff, frictionCoefPart;
+  double lubNormal, lubTangential, lubRotation, lubCutoff, kinVisc;
+  double debyeLength, electroForce;
+  int32_t objWaitTime, intervalTime;
+  double springDamp, epsilon;
+  int32_t nonLinType;
+  double k13, scale;
+  /* inputs (./input/*.dat) */
+  int32_t n_particles;
+  const lbdem_particle_in* particles;
+  int32_t n_objects;
+  const lbdem_object_in* objects;
+  int32_t n_bodies;
+} lbdem_config;
+
+/* Run options that are not part of the reference's configuration. */
+typedef struct lbdem_options {
+  int32_t precision;   /* LBDEM_PLAIN_FP64 or LBDEM_MIXED                 */
+  int32_t device;      /* CUDA device ordinal                             */
+  int32_t check_every; /* NaN/Inf guard cadence in steps (0 = off)        */
+  int32_t reserved[5];
+} lbdem_options;
+
+typedef struct lbdem_ctx lbdem_ctx;
+
+/* ---- configuration (host only; no GPU needed) ----------------------- */
+
+/* Fill *cfg with the reference's defaults for every key
+ * (the third argument of each PARSE_CLASS_MEMBER). */
+int lbdem_config_defaults(lbdem_config* cfg);
+
+/* Parse a GetPot parameters file plus input_dir/{particles,objects,body}.dat
+ * into *cfg, with "-key value" overrides from argv (src/macros.h:14-19).
+ * Replaces LB::latticeBoltzmannGet (src/LB.cpp:128) and
+ * DEM::discreteElementGet (src/DEM.cpp:17). Arrays are owned by the library
+ * until lbdem_config_release(). */
+int lbdem_config_load(const char* cfg_path, const char* input_dir, int argc,
+                      const char* const* argv, lbdem_config* cfg, char* err,
+                      size_t err_len);
+void lbdem_config_release(lbdem_config* cfg);
+
+/* ---- lifecycle ------------------------------------------------------- */
+
+/* Build the lattice, walls, impactor and particle state on the device.
+ * Replaces LB::latticeDefinition (src/LB.cpp:85), DEM::discreteElementInit
+ * (src/DEM.cpp:199) and LB::latticeBolzmannInit (src/LB.cpp:340), in the
+ * order of src/main.cpp:264-283. */
+int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
+                 lbdem_ctx** out);
+void lbdem_destroy(lbdem_ctx* ctx);
+const char* lbdem_last_error(const lbdem_ctx* ctx);
+/* Use a caller-provided cudaStream_t (NULL restores the context's own). */
+int lbdem_set_stream(lbdem_ctx* ctx, void* cuda_stream);
+
+/* ---- step entry points (enqueue only) -------------------------------- */
+
+/* DEM::discreteElementStep, src/DEM.cpp:359-401 */
+int lbdem_dem_step(lbdem_ctx* ctx);
+/* LB::latticeBoltzmannCouplingStep, src/LB.cpp:432-467 */
+int lbdem_coupling_step(lbdem_ctx* ctx);
+/* LB::latticeBolzmannStep, src/LB.cpp:400-418 */
+int lbdem_lb_step(lbdem_ctx* ctx);
+/* LB::latticeBoltzmannFreeSurfaceStep, src/LB.cpp:422-430 */
+int lbdem_free_surface_step(lbdem_ctx* ctx);
+/* n repetitions of goCycle (src/main.cpp:38-67) without IO */
+int lbdem_cycle(lbdem_ctx* ctx, int32_t n);
+/* wait for all enqueued work; returns the first device-side error */
+int lbdem_sync(lbdem_ctx* ctx);
+
+/* ---- state access (synchronising) ------------------------------------ */
+
+typedef struct lbdem_info {
+  int32_t lb_size[3];
+  int64_t nodes;
+  int32_t n_particles, n_objects, n_walls;
+  int32_t precision;
+  int64_t time_step;   /* goCycle count (LB::time)          */
+  int64_t dem_step;    /* DEM::demTimeStep                  */
+  double dem_time;     /* DEM::demTime                      */
+  double unit_length, unit_time, unit_density;
+  int64_t device_bytes;
+  int32_t neighbour_rebuilds;
+  int32_t reserved[7];
+} lbdem_info;
+int lbdem_get_info(lbdem_ctx* ctx, lbdem_info* info);
+
+/* Lattice fields, dense over all nodes (index = x + y*X + z*X*Y):
+ * type[N], pflag[N] (inside-particle flag), solid[N] (solid index),
+ * n[N], u[3N] (x-block, y-block, z-block), mass[N], f[19N] (direction
+ * blocks). Values of non-active nodes are 0. Any pointer may be NULL. */
+int lbdem_download_lattice(lbdem_ctx* ctx, uint8_t* type, uint8_t* pflag,
+                           int32_t* solid, double* n, double* u, double* mass,
+                           double* f);
+
+/* Particle state, row-major [P][3]; any pointer may be NULL. */
+typedef struct lbdem_particle_view {
+  double* x0;
+  double* x1;
+  double* w1;
+  double* FHydro;
+  double* MHydro;
+  double* FContact;
+  double* MContact;
+  double* FLub;
+  double* MLub;
+  double* FRep;
+  double* FTotal;
+  double* MTotal;
+  double* fluidVolume; /* [P]     */
+  double* SHydro;      /* [P][9]  */
+  int32_t* list;       /* [P][50] neighbour list, slot 0 = count */
+  double* xi;          /* [P][3][50] tangential springs           */
+  double* xiw;         /* [P][3] wall spring                      */
+  double* xio;         /* [P][3] object spring                    */
+} lbdem_particle_view;
+int lbdem_download_particles(lbdem_ctx* ctx, const lbdem_particle_view* v);
+
+/* Object (impactor) state [O][3] and wall forces [W][3]. */
+typedef struct lbdem_object_view {
+  double* x0;
+  double* x1;
+  double* w1;
+  double* FHydro;
+  double* MHydro;
+  double* FContact;
+  double* MContact;
+  double* FLub;
+  double* MLub;
+  double* FTotal;
+} lbdem_object_view;
+int lbdem_download_objects(lbdem_ctx* ctx, const lbdem_object_view* v);
+int lbdem_download_walls(lbdem_ctx* ctx, double* FHydro, double* FContact,
+                         double* FLub, double* FTotal);
+
+/* Diagnostics: total mass of active nodes, interface-node count, active
+ * count (device reductions). */
+int lbdem_mass_summary(lbdem_ctx* ctx, double* total_mass,
+                       int64_t* interface_nodes, int64_t* active_nodes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBDEM_H */

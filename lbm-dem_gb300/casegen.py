@@ -1,0 +1,262 @@
+"""Seeded synthetic impact cases written in the reference's input format.
+
+The reference reads a GetPot ``parameters.cfg`` (keys as parsed in
+src/LB.cpp:128-338, src/DEM.cpp:17-78, src/main.cpp:128-185) and, relative to
+the working directory, ``input/particles.dat`` (20 columns, src/DEM.cpp:85-134,
+positions shifted by -0.05 on read at src/DEM.cpp:101), ``input/objects.dat``
+(8 columns, src/DEM.cpp:142-166) and ``input/body.dat`` (src/DEM.cpp:173-196).
+This module produces those files for seeded random-sequential-addition (RSA)
+packings. The vertical axis is the reference's ``y``.
+
+Everything here is host-side input preparation; nothing is timed.
+"""
+from __future__ import annotations
+
+import math
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# Keys in the order the reference parses them; values are strings written
+# verbatim into parameters.cfg.
+DEFAULT_PARAMS: dict[str, str] = {
+    "demSolve": "1",
+    "lbSolve": "1",
+    "freeSurfaceSolve": "1",
+    "forceFieldSolve": "1",
+    "demInitialRepeat": "0.0",
+    "lbmInitialRepeat": "0",
+    "maximumTimeSteps": "0",
+    "maxTime": "1.0e9",
+    "screenExpTime": "0",
+    "fluidExpTime": "0",
+    "fluidLagrangianExpTime": "0",
+    "partExpTime": "0",
+    "partRecycleExpTime": "0",
+    "fluidRecycleExpTime": "0",
+    "unitLength": "1.0",
+    "unitTime": "1.0",
+    "unitDensity": "1.0",
+    "lbSizeX": "64",
+    "lbSizeY": "80",
+    "lbSizeZ": "64",
+    "lbRestart": "false",
+    "lbRestartFile": '" "',
+    "lbTopography": "false",
+    "lbTopographyFile": "./",
+    "initVelocityX": "0.0",
+    "initVelocityY": "0.0",
+    "initVelocityZ": "0.0",
+    "lbFX": "0.0",
+    "lbFY": "-1.0e-5",
+    "lbFZ": "0.0",
+    "lbRotX": "0.0",
+    "lbRotY": "0.0",
+    "lbRotZ": "0.0",
+    "lbRotCenterX": "0.0",
+    "lbRotCenterY": "0.0",
+    "lbRotCenterZ": "0.0",
+    "boundary0": "7",
+    "boundary1": "7",
+    "boundary2": "7",
+    "boundary3": "7",
+    "boundary4": "7",
+    "boundary5": "7",
+    "slipCoefficient": "0.0",
+    "fluidHeight": "60",
+    "rheologyModel": "NEWTONIAN",
+    "initVisc": "0.1",
+    "turbulenceSolve": "0",
+    "turbConst": "0.0",
+    "density": "1.0",
+    "objectDensity": "5.0",
+    "bodyDensity": "1.0",
+    "linearStiff": "1.0e-2",
+    "frictionCoefPart": "1.0",
+    "lubNormal": "1.5",
+    "lubTangential": "1.5",
+    "lubRotation": "1.5",
+    "lubCutoff": "1.0e-3",
+    "kinVisc": "0.1",
+    "debyeLength": "0.15",
+    "electroForce": "1.0e-5",
+    "objWaitTime": "1",
+    "intervalTime": "0",
+    "springDamp": "0.1",
+    "epsilon": "1.0",
+    "nonLinType": "0",
+    "k13": "1.0",
+    "scale": "1.0",
+}
+
+
+@dataclass
+class Case:
+    """One impact run: parameters plus particle and impactor tables.
+
+    ``particles`` rows: r, x, y, z, vx, vy, vz, wx, wy, wz (physical units,
+    positions as they should be *after* the reader's -0.05 shift).
+    ``objects`` rows: r, x, y, z, vx, vy, vz.
+    """
+
+    params: dict[str, str] = field(default_factory=lambda: dict(DEFAULT_PARAMS))
+    particles: np.ndarray = field(default_factory=lambda: np.zeros((0, 10)))
+    objects: np.ndarray = field(default_factory=lambda: np.zeros((0, 7)))
+    name: str = "case"
+
+    @property
+    def lattice(self) -> tuple[int, int, int]:
+        L = float(self.params["unitLength"])
+        return tuple(int(math.floor(float(self.params[k]) / L + 0.5))
+                     for k in ("lbSizeX", "lbSizeY", "lbSizeZ"))
+
+    def write(self, directory: str) -> str:
+        """Write parameters.cfg and input/*.dat; returns the cfg path."""
+        os.makedirs(os.path.join(directory, "input"), exist_ok=True)
+        cfg = os.path.join(directory, "parameters.cfg")
+        with open(cfg, "w") as fh:
+            for k, v in self.params.items():
+                fh.write(f"{k} = {v}\n")
+        with open(os.path.join(directory, "input", "particles.dat"), "w") as fh:
+            fh.write(f"{len(self.particles)}\n")
+            for i, row in enumerate(self.particles):
+                r, x, y, z, vx, vy, vz, wx, wy, wz = (float(a) for a in row)
+                # the reader subtracts 0.05 from each coordinate
+                vals = [r, x + 0.05, y + 0.05, z + 0.05, vx, vy, vz, wx, wy, wz]
+                fh.write(f"{i} 1 " + " ".join(f"{a:.17g}" for a in vals)
+                         + " 1 0 0 0 0 0 0 0\n")
+        with open(os.path.join(directory, "input", "objects.dat"), "w") as fh:
+            fh.write(f"{len(self.objects)}\n")
+            for i, row in enumerate(self.objects):
+                fh.write(f"{i} " + " ".join(f"{float(a):.17g}" for a in row) + "\n")
+        with open(os.path.join(directory, "input", "body.dat"), "w") as fh:
+            fh.write("0\n")
+        return cfg
+
+
+def rsa_pack(rng: np.random.Generator, lo, hi, radii: np.ndarray,
+             gap: float = 0.05, max_tries: int = 2000) -> np.ndarray:
+    """Random sequential addition of spheres (largest first) into [lo, hi].
+
+    Returns an array (n_placed, 4) of r, x, y, z in insertion order of the
+    input ``radii``. A sphere is placed at the first uniformly drawn centre
+    whose surface stays ``gap`` away from every placed sphere and inside the
+    box; spheres that find no place in ``max_tries`` draws are dropped.
+    """
+    lo = np.asarray(lo, float)
+    hi = np.asarray(hi, float)
+    rmax = float(np.max(radii)) if len(radii) else 1.0
+    cell = 2.0 * rmax + gap
+    dims = np.maximum(1, np.floor((hi - lo) / cell).astype(int))
+    grid: dict[tuple[int, int, int], list[int]] = {}
+    placed = np.zeros((len(radii), 4))
+    n = 0
+    for r in radii:
+        a = lo + r
+        b = hi - r
+        if np.any(b <= a):
+            continue
+        for _ in range(max_tries):
+            c = a + (b - a) * rng.random(3)
+            key = tuple(np.minimum(dims - 1, ((c - lo) / cell).astype(int)))
+            ok = True
+            for dx in (-1, 0, 1):
+                for dy in (-1, 0, 1):
+                    for dz in (-1, 0, 1):
+                        for j in grid.get((key[0] + dx, key[1] + dy, key[2] + dz), ()):
+                            d = placed[j, 1:] - c
+                            if d @ d < (placed[j, 0] + r + gap) ** 2:
+                                ok = False
+                                break
+                        if not ok:
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if ok:
+                placed[n] = (r, *c)
+                grid.setdefault(key, []).append(n)
+                n += 1
+                break
+    return placed[:n]
+
+
+def impact_case(lattice=(64, 80, 64), fill=60.0, n_particles=400,
+                radii=(3.0, 4.2), impactor_r=8.0, impactor_y=70.0,
+                impactor_vy=-0.01, impactor_density=5.0, tau=0.8,
+                gravity=1.0e-5, seed=1, gap=0.05, overrides=None,
+                name="case") -> Case:
+    """Bidisperse suspension under a falling impactor (reference axes).
+
+    Lattice sides are in lattice units (unitLength = unitTime = 1), the walls
+    are the outermost node layers (wall planes at 0.5 and side-1.5, as set by
+    src/LB.cpp:186-193). Particles are RSA-placed below ``fill``; half the
+    spheres (by number) take each radius.
+    """
+    rng = np.random.default_rng(seed)
+    p = dict(DEFAULT_PARAMS)
+    nx, ny, nz = lattice
+    p.update({
+        "lbSizeX": str(nx), "lbSizeY": str(ny), "lbSizeZ": str(nz),
+        "fluidHeight": repr(float(fill)),
+        "initVisc": repr((tau - 0.5) / 3.0),
+        "kinVisc": repr((tau - 0.5) / 3.0),
+        "lbFY": repr(-float(gravity)),
+        "objectDensity": repr(float(impactor_density)),
+    })
+    amean = 0.5 * (radii[0] + radii[1])
+    p["lubNormal"] = p["lubTangential"] = p["lubRotation"] = repr(0.5 * amean)
+    p["debyeLength"] = repr(0.05 * amean)
+    # The reference integrates lubrication explicitly with coefficient
+    # Xa ~ 6 pi nu a (a/h) dt (src/DEM.cpp:2354-2373); with dt = 1 lattice step
+    # the minimum gap must keep Xa dt / m below 1, hence h_min = 0.1 a.
+    p["lubCutoff"] = repr(0.1 * amean)
+    if overrides:
+        p.update({k: str(v) for k, v in overrides.items()})
+    half = n_particles // 2
+    rs = np.array([radii[1]] * (n_particles - half) + [radii[0]] * half)
+    lo = (0.5, 0.5, 0.5)
+    hi = (nx - 1.5, float(fill), nz - 1.5)
+    pk = rsa_pack(rng, lo, hi, rs, gap=gap)
+    order = rng.permutation(len(pk))
+    pk = pk[order]
+    parts = np.zeros((len(pk), 10))
+    parts[:, :4] = pk
+    objs = np.zeros((1, 7))
+    objs[0] = (impactor_r, 0.5 * (nx - 1), impactor_y, 0.5 * (nz - 1),
+               0.0, impactor_vy, 0.0)
+    return Case(params=p, particles=parts, objects=objs, name=name)
+
+
+def volume_fraction(case: Case) -> float:
+    nx, ny, nz = case.lattice
+    fill = float(case.params["fluidHeight"])
+    vol = (nx - 2) * (fill - 0.5) * (nz - 2)
+    return float(np.sum(4.0 / 3.0 * math.pi * case.particles[:, 0] ** 3) / vol)
+
+
+# Named workloads. Sizes follow the benchmark configurations of this project
+# (see the bench and the tests); "c1" is the CPU-runnable plain-FP64 case.
+def named_case(name: str, seed: int = 1) -> Case:
+    if name == "c1":
+        return impact_case((64, 80, 64), 60.0, 400, (3.0, 4.2), 8.0, 70.0,
+                           -0.01, 5.0, 0.8, 1.0e-5, seed, name=name)
+    if name == "c2":
+        return impact_case((256, 320, 256), 240.0, 25000, (3.0, 4.2), 20.0,
+                           262.0, -0.02, 5.0, 0.6, 1.0e-5, seed, name=name)
+    if name == "small_cells":
+        return impact_case((28, 40, 28), 27.0, 16, (3.0, 3.4), 5.0, 32.0,
+                           -0.08, 5.0, 0.8, 1.0e-4, seed,
+                           overrides={"objWaitTime": "3"}, name=name)
+    if name == "small_dup":
+        return impact_case((28, 40, 18), 27.0, 10, (3.0, 3.4), 4.0, 31.5,
+                           -0.08, 5.0, 0.8, 1.0e-4, seed,
+                           overrides={"objWaitTime": "3", "demInitialRepeat": "2.5"},
+                           name=name)
+    if name == "tiny_direct":
+        return impact_case((18, 28, 18), 16.0, 5, (3.0, 3.4), 4.0, 20.5,
+                           -0.05, 5.0, 0.8, 1.0e-4, seed,
+                           overrides={"objWaitTime": "2"}, name=name)
+    raise KeyError(name)

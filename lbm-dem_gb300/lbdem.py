@@ -1,0 +1,323 @@
+"""Python binding of the liblbdem.so C ABI (include/lbdem.h), via ctypes.
+
+This is the reference-facing host interface in Python: a ``Solver`` object
+whose methods mirror the reference's step entry points
+(``DEM::discreteElementStep``, ``LB::latticeBoltzmannCouplingStep``,
+``LB::latticeBolzmannStep``, ``LB::latticeBoltzmannFreeSurfaceStep``,
+goCycle). All compute happens in the CUDA library; if the library or a GPU
+is missing, construction raises instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblbdem.so")
+
+PLAIN_FP64 = 0
+MIXED = 1
+
+ERRORS = {
+    0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
+    4: "input error", 5: "non-finite state", 6: "list overflow",
+    7: "device-side error", 8: "no CUDA device",
+}
+
+
+class ParticleIn(C.Structure):
+    _fields_ = [("r", C.c_double), ("x", C.c_double * 3), ("v", C.c_double * 3),
+                ("w", C.c_double * 3), ("size", C.c_int32), ("index", C.c_int32)]
+
+
+class ObjectIn(C.Structure):
+    _fields_ = [("index", C.c_int32), ("r", C.c_double), ("x", C.c_double * 3),
+                ("v", C.c_double * 3)]
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("demSolve", C.c_int32), ("lbSolve", C.c_int32),
+        ("freeSurfaceSolve", C.c_int32), ("forceFieldSolve", C.c_int32),
+        ("demInitialRepeat", C.c_double), ("lbmInitialRepeat", C.c_int32),
+        ("maxTime", C.c_double), ("maximumTimeSteps", C.c_int32),
+        ("screenExpTime", C.c_double), ("fluidExpTime", C.c_double),
+        ("fluidLagrangianExpTime", C.c_double), ("partExpTime", C.c_double),
+        ("partRecycleExpTime", C.c_double), ("fluidRecycleExpTime", C.c_double),
+        ("unitLength", C.c_double), ("unitTime", C.c_double),
+        ("unitDensity", C.c_double),
+        ("lbSizeX", C.c_double), ("lbSizeY", C.c_double), ("lbSizeZ", C.c_double),
+        ("lbRestart", C.c_int32), ("lbTopography", C.c_int32),
+        ("initVelocity", C.c_double * 3), ("lbF", C.c_double * 3),
+        ("lbRot", C.c_double * 3), ("lbRotCenter", C.c_double * 3),
+        ("boundary", C.c_int32 * 6), ("slipCoefficient", C.c_double),
+        ("fluidHeight", C.c_double), ("rheologyNewtonian", C.c_int32),
+        ("initVisc", C.c_double), ("turbulenceSolve", C.c_int32),
+        ("turbConst", C.c_double),
+        ("density", C.c_double), ("objectDensity", C.c_double),
+        ("bodyDensity", C.c_double), ("linearStiff", C.c_double),
+        ("frictionCoefPart", C.c_double), ("lubNormal", C.c_double),
+        ("lubTangential", C.c_double), ("lubRotation", C.c_double),
+        ("lubCutoff", C.c_double), ("kinVisc", C.c_double),
+        ("debyeLength", C.c_double), ("electroForce", C.c_double),
+        ("objWaitTime", C.c_int32), ("intervalTime", C.c_int32),
+        ("springDamp", C.c_double), ("epsilon", C.c_double),
+        ("nonLinType", C.c_int32), ("k13", C.c_double), ("scale", C.c_double),
+        ("n_particles", C.c_int32), ("particles", C.POINTER(ParticleIn)),
+        ("n_objects", C.c_int32), ("objects", C.POINTER(ObjectIn)),
+        ("n_bodies", C.c_int32),
+    ]
+
+
+class Options(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("device", C.c_int32),
+                ("check_every", C.c_int32), ("reserved", C.c_int32 * 5)]
+
+
+class Info(C.Structure):
+    _fields_ = [("lb_size", C.c_int32 * 3), ("nodes", C.c_int64),
+                ("n_particles", C.c_int32), ("n_objects", C.c_int32),
+                ("n_walls", C.c_int32), ("precision", C.c_int32),
+                ("time_step", C.c_int64), ("dem_step", C.c_int64),
+                ("dem_time", C.c_double), ("unit_length", C.c_double),
+                ("unit_time", C.c_double), ("unit_density", C.c_double),
+                ("device_bytes", C.c_int64), ("neighbour_rebuilds", C.c_int32),
+                ("reserved", C.c_int32 * 7)]
+
+
+_P = C.POINTER(C.c_double)
+_PI = C.POINTER(C.c_int32)
+
+
+class ParticleView(C.Structure):
+    _fields_ = [(k, _P) for k in (
+        "x0", "x1", "w1", "FHydro", "MHydro", "FContact", "MContact", "FLub",
+        "MLub", "FRep", "FTotal", "MTotal", "fluidVolume", "SHydro")] + [
+        ("list", _PI), ("xi", _P), ("xiw", _P), ("xio", _P)]
+
+
+class ObjectView(C.Structure):
+    _fields_ = [(k, _P) for k in (
+        "x0", "x1", "w1", "FHydro", "MHydro", "FContact", "MContact", "FLub",
+        "MLub", "FTotal")]
+
+
+_lib = None
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Load liblbdem.so (built in-tree by __graft_entry__.build())."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"liblbdem.so not built: {p} (run __graft_entry__.build())")
+    lib = C.CDLL(p)
+    c_ctx = C.c_void_p
+    sig = {
+        "lbdem_config_defaults": ([C.POINTER(Config)], C.c_int),
+        "lbdem_config_load": ([C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_char_p),
+                               C.POINTER(Config), C.c_char_p, C.c_size_t], C.c_int),
+        "lbdem_config_release": ([C.POINTER(Config)], None),
+        "lbdem_create": ([C.POINTER(Config), C.POINTER(Options), C.POINTER(c_ctx)], C.c_int),
+        "lbdem_destroy": ([c_ctx], None),
+        "lbdem_last_error": ([c_ctx], C.c_char_p),
+        "lbdem_set_stream": ([c_ctx, C.c_void_p], C.c_int),
+        "lbdem_dem_step": ([c_ctx], C.c_int),
+        "lbdem_coupling_step": ([c_ctx], C.c_int),
+        "lbdem_lb_step": ([c_ctx], C.c_int),
+        "lbdem_free_surface_step": ([c_ctx], C.c_int),
+        "lbdem_cycle": ([c_ctx, C.c_int32], C.c_int),
+        "lbdem_sync": ([c_ctx], C.c_int),
+        "lbdem_get_info": ([c_ctx, C.POINTER(Info)], C.c_int),
+        "lbdem_download_lattice": ([c_ctx, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+        "lbdem_download_particles": ([c_ctx, C.POINTER(ParticleView)], C.c_int),
+        "lbdem_download_objects": ([c_ctx, C.POINTER(ObjectView)], C.c_int),
+        "lbdem_download_walls": ([c_ctx, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
+                                 C.c_int),
+        "lbdem_mass_summary": ([c_ctx, C.POINTER(C.c_double), C.POINTER(C.c_int64),
+                                C.POINTER(C.c_int64)], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.argtypes = args
+        fn.restype = res
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class LoadedConfig:
+    """A parsed case: owns the Config and its arrays (released on close)."""
+
+    def __init__(self, cfg_path: str, input_dir: str | None = None,
+                 overrides: dict | None = None):
+        self.lib = load_library()
+        self.cfg = Config()
+        argv = []
+        for k, v in (overrides or {}).items():
+            argv += [f"-{k}".encode(), str(v).encode()]
+        arr = (C.c_char_p * max(1, len(argv)))(*argv)
+        err = C.create_string_buffer(512)
+        if input_dir is None:
+            input_dir = os.path.join(os.path.dirname(os.path.abspath(cfg_path)), "input")
+        rc = self.lib.lbdem_config_load(cfg_path.encode(), input_dir.encode(), len(argv),
+                                        arr, C.byref(self.cfg), err, 512)
+        if rc != 0:
+            raise RuntimeError(f"lbdem_config_load: {ERRORS.get(rc, rc)}: {err.value.decode()}")
+
+    def close(self):
+        if self.cfg is not None:
+            self.lib.lbdem_config_release(C.byref(self.cfg))
+            self.cfg = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Solver:
+    """One impact run on the GPU (wraps an lbdem_ctx)."""
+
+    def __init__(self, config: LoadedConfig, precision: int = PLAIN_FP64,
+                 device: int = 0, check_every: int = 0):
+        self.lib = load_library()
+        self.ctx = C.c_void_p()
+        opt = Options(precision=precision, device=device, check_every=check_every)
+        rc = self.lib.lbdem_create(C.byref(config.cfg), C.byref(opt), C.byref(self.ctx))
+        if rc != 0:
+            msg = self.lib.lbdem_last_error(self.ctx).decode() if self.ctx else ""
+            if self.ctx:
+                self.lib.lbdem_destroy(self.ctx)
+                self.ctx = None
+            raise RuntimeError(f"lbdem_create: {ERRORS.get(rc, rc)}: {msg}")
+        self.info = self.get_info()
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            raise RuntimeError(f"{what}: {ERRORS.get(rc, rc)}: "
+                               f"{self.lib.lbdem_last_error(self.ctx).decode()}")
+
+    def close(self):
+        if self.ctx:
+            self.lib.lbdem_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- step entry points -------------------------------------------------
+    def dem_step(self):
+        self._check(self.lib.lbdem_dem_step(self.ctx), "dem_step")
+
+    def coupling_step(self):
+        self._check(self.lib.lbdem_coupling_step(self.ctx), "coupling_step")
+
+    def lb_step(self):
+        self._check(self.lib.lbdem_lb_step(self.ctx), "lb_step")
+
+    def free_surface_step(self):
+        self._check(self.lib.lbdem_free_surface_step(self.ctx), "free_surface_step")
+
+    def cycle(self, n: int = 1):
+        self._check(self.lib.lbdem_cycle(self.ctx, n), "cycle")
+
+    def sync(self):
+        self._check(self.lib.lbdem_sync(self.ctx), "sync")
+
+    def set_stream(self, handle: int | None):
+        self._check(self.lib.lbdem_set_stream(self.ctx, C.c_void_p(handle or 0)), "set_stream")
+
+    # --- state ---------------------------------------------------------------
+    def get_info(self) -> Info:
+        info = Info()
+        self._check(self.lib.lbdem_get_info(self.ctx, C.byref(info)), "get_info")
+        return info
+
+    def lattice(self) -> dict:
+        N = int(self.info.nodes)
+        out = {
+            "type": np.zeros(N, np.uint8), "pflag": np.zeros(N, np.uint8),
+            "solid": np.zeros(N, np.int32), "n": np.zeros(N), "u": np.zeros(3 * N),
+            "mass": np.zeros(N), "f": np.zeros(19 * N),
+        }
+        self._check(self.lib.lbdem_download_lattice(
+            self.ctx, _ptr(out["type"]), _ptr(out["pflag"]), _ptr(out["solid"]),
+            _ptr(out["n"]), _ptr(out["u"]), _ptr(out["mass"]), _ptr(out["f"])),
+            "download_lattice")
+        u = out.pop("u").reshape(3, N)
+        out["ux"], out["uy"], out["uz"] = u[0], u[1], u[2]
+        out["f"] = out["f"].reshape(19, N)
+        return out
+
+    def particles(self) -> dict:
+        P = int(self.info.n_particles)
+        names3 = ["x0", "x1", "w1", "FHydro", "MHydro", "FContact", "MContact", "FLub",
+                  "MLub", "FRep", "FTotal", "MTotal", "xiw", "xio"]
+        arr = {k: np.zeros((P, 3)) for k in names3}
+        arr["fluidVolume"] = np.zeros(P)
+        arr["SHydro"] = np.zeros((P, 9))
+        arr["list"] = np.zeros((P, 50), np.int32)
+        arr["xi"] = np.zeros((P, 3, 50))
+        v = ParticleView()
+        for k, a in arr.items():
+            if k == "list":
+                v.list = a.ctypes.data_as(_PI)
+            else:
+                setattr(v, k, a.ctypes.data_as(_P))
+        self._check(self.lib.lbdem_download_particles(self.ctx, C.byref(v)),
+                    "download_particles")
+        return {"p_" + k: a for k, a in arr.items()}
+
+    def objects(self) -> dict:
+        O = int(self.info.n_objects)
+        names = ["x0", "x1", "w1", "FHydro", "MHydro", "FContact", "MContact", "FLub",
+                 "MLub", "FTotal"]
+        arr = {k: np.zeros((O, 3)) for k in names}
+        v = ObjectView(**{k: a.ctypes.data_as(_P) for k, a in arr.items()})
+        self._check(self.lib.lbdem_download_objects(self.ctx, C.byref(v)), "download_objects")
+        return {"o_" + k: a for k, a in arr.items()}
+
+    def walls(self) -> dict:
+        W = int(self.info.n_walls)
+        arr = {k: np.zeros((W, 3)) for k in ("FHydro", "FContact", "FLub", "FTotal")}
+        self._check(self.lib.lbdem_download_walls(
+            self.ctx, *[_ptr(arr[k]) for k in ("FHydro", "FContact", "FLub", "FTotal")]),
+            "download_walls")
+        return {"w_" + k: a for k, a in arr.items()}
+
+    def state(self) -> dict:
+        """Everything, keyed like the oracle's state dumps."""
+        d = {}
+        d.update(self.lattice())
+        d.update(self.particles())
+        d.update(self.objects())
+        d.update(self.walls())
+        info = self.get_info()
+        d["step"] = np.array([info.time_step])
+        d["demTime"] = np.array([info.dem_time])
+        d["demTimeStep"] = np.array([info.dem_step])
+        return d
+
+    def mass_summary(self):
+        m = C.c_double()
+        ni = C.c_int64()
+        na = C.c_int64()
+        self._check(self.lib.lbdem_mass_summary(self.ctx, C.byref(m), C.byref(ni), C.byref(na)),
+                    "mass_summary")
+        return m.value, ni.value, na.value

@@ -1,0 +1,87 @@
+"""Generate the golden fixtures from the pinned reference build.
+
+Run here (where the reference tree exists):
+    make -C oracle ref && python tests/golden/make_golden.py
+
+For every case it writes tests/golden/<case>/ (parameters.cfg + input/*.dat,
+the exact inputs the reference read) and tests/golden/<case>.npz holding, for
+each dumped step, the SHA-256 of every array of the reference's state dump
+(oracle/statedump.h layout) and the full particle / impactor / wall arrays.
+Bit-exact agreement with the reference is then checked by hashing the
+oracle's dump of the same step (tests/test_oracle_golden.py). The lattice
+arrays themselves are too large to commit; their hashes pin them.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "lbm-dem_gb300"))
+sys.path.insert(0, os.path.join(REPO, "tests"))
+
+import casegen  # noqa: E402
+from dumpio import read_dump  # noqa: E402
+
+REF = os.path.join(REPO, "oracle", "_ref", "lbdem_ref")
+
+# case name -> (steps, dump every)
+CASES = {
+    "tiny_direct": (60, 1),
+    "small_cells": (60, 1),
+    "small_dup": (60, 1),
+    "c1": (100, 10),
+}
+
+SMALL_KEYS = ("p_", "o_", "w_", "step", "demTime", "demTimeStep")
+
+
+def array_hash(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def make(name: str, steps: int, every: int) -> None:
+    case = casegen.named_case(name)
+    cdir = os.path.join(HERE, name)
+    if os.path.isdir(cdir):
+        shutil.rmtree(cdir)
+    case.write(cdir)
+    with tempfile.TemporaryDirectory() as tmp:
+        dump = os.path.join(tmp, "dump")
+        subprocess.run([REF, "-c", "parameters.cfg", "-steps", str(steps), "-dump", dump,
+                        "-every", str(every)], cwd=cdir, check=True,
+                       stdout=subprocess.DEVNULL)
+        hashes = {}
+        arrays = {}
+        for s in [0] + list(range(every, steps + 1, every)):
+            d = read_dump(os.path.join(dump, f"dump_{s:06d}.bin"))
+            hashes[str(s)] = {k: array_hash(v) for k, v in d.items()}
+            for k, v in d.items():
+                if k.startswith(SMALL_KEYS):
+                    arrays[f"s{s}/{k}"] = v
+            # a few lattice summaries, useful when a hash differs
+            arrays[f"s{s}/type_counts"] = np.bincount(d["type"], minlength=13)
+            arrays[f"s{s}/mass_sum"] = np.array([d["mass"].sum()])
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"),
+                        hashes=np.frombuffer(json.dumps(hashes).encode(), np.uint8),
+                        **arrays)
+    print(name, "steps", steps, "every", every)
+
+
+def main(names=None):
+    if not os.path.exists(REF):
+        sys.exit("oracle/_ref/lbdem_ref missing: run `make -C oracle ref` first")
+    for name in names or CASES:
+        make(name, *CASES[name])
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:] or None)
