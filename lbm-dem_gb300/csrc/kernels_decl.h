@@ -1,0 +1,124 @@
+// Kernel argument blocks and kernel prototypes shared by the host sequencing
+// (lbdem_capi.cu) and the kernel translation units.
+#pragma once
+#include "lbdem_internal.h"
+
+namespace lbdem {
+
+struct LbArgs {
+  const double* fin;
+  double* fout;
+  uint8_t* mask;
+  const uint32_t* solid;
+  const uint8_t* objIdx;
+  double* mass;
+  double* rhoS;
+  double* uS;
+  double* hS;
+  const double* px0;
+  const double* px1;
+  const double* pw1;
+  double* pFHydro;    // [3][P] lattice-unit sums
+  double* pMHydro;    // [3][P]
+  double* pSHydro;    // [9][P]
+  double* pFluidVol;  // [P]
+  double* obj;        // object records
+  double* wallF;      // [W][12]
+  double* scal;
+  int* iscal;
+};
+
+struct FsArgs {
+  double* fcur;        // post-stream populations (current lattice)
+  const double* fold;  // pre-collision populations of this step
+  uint8_t* mask;
+  const uint32_t* solid;
+  const uint8_t* objIdx;
+  uint8_t* fsflag;
+  double* mass;
+  double* massNew;
+  double* rhoS;
+  const double* uS;
+  const double* hS;
+  const double* px0;
+  const double* px1;
+  const double* pw1;
+  const double* obj;
+  double* scal;
+  int* iscal;
+};
+
+struct DemArgs {
+  double *x0, *x1, *w1, *r, *invm, *invI;
+  double *FHydro, *MHydro, *FContact, *MContact, *FLub, *MLub, *FRep, *FTotal, *MTotal,
+      *FGrav;
+  double *xiw, *xio;
+  int* list[2];
+  double* xi[2];
+  int* partner;
+  int* gorder;
+  double* pairbuf;
+  uint8_t* pairflag;
+  int* pcell;
+  int* ppos;
+  int *cellCount, *cellStart, *cellFill, *cellParts;
+  double* obj;
+  double* wallF;
+  const DeviceWall* walls;
+  double* scal;
+  int* iscal;
+};
+
+// lb_fp64.cu
+__global__ void lbStepFp64(Consts k, LbArgs a);
+__global__ void lbResetKernel(Consts k, double* pAcc, long long pAccLen, double* obj,
+                              double* wallF, double* scal, int* iscal);
+__global__ void lbFinalizeKernel(Consts k, double* pF, double* pM, double* pV, double* obj,
+                                 double* wallF, double* scal, const int* iscal);
+__global__ void fsResetKernel(double* scal, int* iscal);
+__global__ void lbRedistribute(Consts k, FsArgs a);
+__global__ void fsUpdateMass(Consts k, FsArgs a);
+__global__ void fsMutants(Consts k, FsArgs a);
+__global__ void fsSmoothen(Consts k, FsArgs a);
+__global__ void fsMutantsAndFill(Consts k, FsArgs a);
+__global__ void fsEmptyIsolated(Consts k, FsArgs a);
+__global__ void fsRedistribute(Consts k, FsArgs a);
+__global__ void uncoverCollect(Consts k, const uint8_t* mask, const double* obj,
+                               uint32_t* list, int* iscal);
+__global__ void uncoverResolve(Consts k, uint8_t* mask, double* f, double* mass,
+                               uint32_t* list, int* iscal);
+__global__ void voxelizeObjects(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* objIdx,
+                                double* mass, double* obj);
+__global__ void flagClaim(Consts k, const uint8_t* mask, uint32_t* claim, const double* px0,
+                          const double* pr, const int* iscal, unsigned long long* uscal);
+__global__ void flagApply(Consts k, uint8_t* mask, uint32_t* solid, uint32_t* claim,
+                          const int* iscal, unsigned long long* uscal);
+__global__ void findNewActiveKernel(Consts k, uint8_t* mask, uint32_t* solid,
+                                    const double* px0, const double* pr, int* iscal,
+                                    unsigned long long* uscal);
+__global__ void initTypes(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* objIdx,
+                          const int* boundary, const DeviceWall* walls, const int* wallType,
+                          const double* obj, double fluidHeightLattice, int freeSurface);
+__global__ void initFields(Consts k, uint8_t* mask, double* f, double* mass);
+__global__ void massSummaryKernel(Consts k, const uint8_t* mask, const double* mass,
+                                  double* out, unsigned long long* cnt);
+__global__ void momentsKernel(Consts k, const uint8_t* mask, const double* f, double* n,
+                              double* u);
+__global__ void nonfiniteCheck(Consts k, const uint8_t* mask, const double* f, int* iscal);
+
+// dem_fp64.cu
+__global__ void demBegin(Consts k, DemArgs a, int forceRebuild);
+__global__ void nbrCellAssign(Consts k, DemArgs a);
+__global__ void nbrCellScan(Consts k, DemArgs a);
+__global__ void nbrCellScatter(Consts k, DemArgs a);
+__global__ void nbrCellSort(Consts k, DemArgs a);
+__global__ void nbrBuildCells(Consts k, DemArgs a);
+__global__ void nbrBuildDirect(Consts k, DemArgs a);
+__global__ void nbrDirectHistory(Consts k, DemArgs a);
+__global__ void nbrPartners(Consts k, DemArgs a);
+__global__ void nbrFinish(DemArgs a);
+__global__ void demPairs(Consts k, DemArgs a, int lubOn);
+__global__ void demGather(Consts k, DemArgs a, int stepNo);
+__global__ void demObjects(Consts k, DemArgs a, int stepNo);
+
+}  // namespace lbdem

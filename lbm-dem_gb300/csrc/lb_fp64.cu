@@ -1,0 +1,1096 @@
+// Plain FP64 lattice kernels: fused reconstruct / particle forcing /
+// BGK+Guo collision / push streaming with bounce-back and the free-surface
+// gas rule, the free-surface mass update and interface conversion, the
+// impactor uncover/voxelisation and the particle flagging of the coupling
+// step, and device-side initialisation.
+//
+// Arithmetic follows the reference operation by operation (no FMA
+// contraction: this file is compiled with --fmad=false), so that each node
+// update is bit-identical to the reference given identical inputs; only the
+// order of the reductions (forces on particles, walls and the impactor, mass
+// surpluses) differs. Terms with a zero lattice-velocity component are
+// skipped; in the reference they add an exact +-0 (src/node.cpp:65,86,108,200).
+//
+// Reference functions restated here (paths relative to the reference root):
+//   node::reconstruct/shiftVelocity/computeEquilibrium/solveCollision/addForce
+//     src/node.cpp:75-207; LB::reconstruction/collision src/LB.cpp:1261-1332
+//   LB::computeHydroForces src/LB.cpp:1901-1978
+//   LB::streaming src/LB.cpp:1334-1544; LB::redistributeMass :1844-1852
+//   LB::updateMass :1548-1639; LB::updateInterface :1641-1842
+//   LB::updateObjectBoundaries/findNewActiveObject :797-943
+//   LB::updateIndices/initializeParticleBoundaries :1875-1899, 683-711
+//   LB::findNewActive :1980-2029 (its loop-exiting break included)
+//   LB::latticeBolzmannInit and helpers :340-398, 538-564, 713-795, 974-1096
+#include <cfloat>
+#include <climits>
+
+#include "kernels_decl.h"
+
+namespace lbdem {
+
+// D3Q19 velocity set in the reference's order, src/lattice.h:33-57
+__host__ __device__ constexpr int CX(int j) {
+  return j == 1 ? 1 : j == 2 ? -1 : j == 7 ? 1 : j == 8 ? -1 : j == 9 ? -1 : j == 10 ? 1
+       : j == 15 ? 1 : j == 16 ? -1 : j == 17 ? 1 : j == 18 ? -1 : 0;
+}
+__host__ __device__ constexpr int CY(int j) {
+  return j == 3 ? 1 : j == 4 ? -1 : j == 7 ? 1 : j == 8 ? -1 : j == 9 ? 1 : j == 10 ? -1
+       : j == 11 ? 1 : j == 12 ? -1 : j == 13 ? -1 : j == 14 ? 1 : 0;
+}
+__host__ __device__ constexpr int CZ(int j) {
+  return j == 5 ? 1 : j == 6 ? -1 : j == 11 ? 1 : j == 12 ? -1 : j == 13 ? 1 : j == 14 ? -1
+       : j == 15 ? 1 : j == 16 ? -1 : j == 17 ? -1 : j == 18 ? 1 : 0;
+}
+__host__ __device__ constexpr int OPPJ(int j) { return j == 0 ? 0 : (j & 1) ? j + 1 : j - 1; }
+// weights, src/lattice.h:147-150 (same double values as 12/36, 2/36, 1/36)
+__host__ __device__ constexpr double WJ(int j) {
+  return j == 0 ? 12.0 / 36.0 : j <= 6 ? 2.0 / 36.0 : 1.0 / 36.0;
+}
+
+__device__ __forceinline__ bool isActiveT(int t) { return t == 0 || t == 3; }
+
+// u.dot(v[j]) of src/myvector.cpp:121 with the zero components dropped
+__device__ __forceinline__ double dotc(int j, double x, double y, double z) {
+  const int cx = CX(j), cy = CY(j), cz = CZ(j);
+  double s = 0.0;
+  bool any = false;
+  if (cx) { s = cx > 0 ? x : -x; any = true; }
+  if (cy) { const double t = cy > 0 ? y : -y; s = any ? s + t : t; any = true; }
+  if (cz) { const double t = cz > 0 ? z : -z; s = any ? s + t : t; }
+  return s;
+}
+
+__device__ __forceinline__ long long nbrOffset(const Consts& k, int j) {
+  return (long long)CX(j) + (long long)CY(j) * k.sy + (long long)CZ(j) * k.sz;
+}
+
+__device__ __forceinline__ void coords(const Consts& k, long long x, int& ix, int& iy, int& iz) {
+  const unsigned ux = (unsigned)x;
+  iz = (int)(ux / (unsigned)k.sz);
+  const unsigned rem = ux - (unsigned)iz * (unsigned)k.sz;
+  iy = (int)(rem / (unsigned)k.X);
+  ix = (int)(rem - (unsigned)iy * (unsigned)k.X);
+}
+
+// tinyVector::insideSphere, src/myvector.cpp:171-176, on node coordinates
+__device__ __forceinline__ bool insideSphere(double px, double py, double pz, double cx,
+                                             double cy, double cz, double r) {
+  const double dx = px - cx, dy = py - cy, dz = pz - cz;
+  return dx * dx + dy * dy + dz * dz < r * r;
+}
+
+// node::setEquilibrium / computeEquilibrium for one direction,
+// src/node.cpp:52-73, 100-111
+__device__ __forceinline__ double feqj(int j, double n, double ux, double uy, double uz,
+                                       double usq) {
+  const double vu = dotc(j, ux, uy, uz);
+  return WJ(j) * n * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
+}
+
+// One node's collision, exactly as LB::reconstruction + computeHydroForces
+// (node part) + LB::collision: in f = pre-collision populations, out f =
+// post-collision populations (fs). Returns n, the shifted u, the node force.
+struct NodeState {
+  double n, ux, uy, uz, hx, hy, hz;
+  // particle coupling terms for the per-particle reduction
+  double dx, dy, dz, rx, ry, rz;
+};
+
+__device__ __forceinline__ void collideNode(const Consts& k, double* f, bool pflag,
+                                            uint32_t pid, const double* px0,
+                                            const double* px1, const double* pw1,
+                                            int P, double massOld, int ix, int iy, int iz,
+                                            NodeState& s) {
+  // node::reconstruct
+  double n = 0.0;
+#pragma unroll
+  for (int j = 0; j < Q; ++j) n += f[j];
+  double ux = 0.0, uy = 0.0, uz = 0.0;
+  {
+    bool ax = false, ay = false, az = false;
+#pragma unroll
+    for (int j = 1; j < Q; ++j) {
+      if (CX(j)) { const double t = CX(j) > 0 ? f[j] : -f[j]; ux = ax ? ux + t : t; ax = true; }
+      if (CY(j)) { const double t = CY(j) > 0 ? f[j] : -f[j]; uy = ay ? uy + t : t; ay = true; }
+      if (CZ(j)) { const double t = CZ(j) > 0 ? f[j] : -f[j]; uz = az ? uz + t : t; az = true; }
+    }
+  }
+  ux /= n;
+  uy /= n;
+  uz /= n;
+  // LB::computeHydroForces, node part (src/LB.cpp:1920-1940)
+  double hx = 0.0, hy = 0.0, hz = 0.0;
+  s.dx = s.dy = s.dz = 0.0;
+  s.rx = s.ry = s.rz = 0.0;
+  if (pflag && pid < (uint32_t)P) {
+    const double rx = (double)ix - px0[pid] / k.uLength;
+    const double ry = (double)iy - px0[P + pid] / k.uLength;
+    const double rz = (double)iz - px0[2 * P + pid] / k.uLength;
+    const double wx = pw1[pid], wy = pw1[P + pid], wz = pw1[2 * P + pid];
+    const double lvx = px1[pid] / k.uSpeed + (wy * rz - wz * ry) / k.uAngVel;
+    const double lvy = px1[P + pid] / k.uSpeed + (wz * rx - wx * rz) / k.uAngVel;
+    const double lvz = px1[2 * P + pid] / k.uSpeed + (wx * ry - wy * rx) / k.uAngVel;
+    const double lf = massOld / n;
+    s.dx = (ux - lvx) * lf;
+    s.dy = (uy - lvy) * lf;
+    s.dz = (uz - lvz) * lf;
+    s.rx = rx;
+    s.ry = ry;
+    s.rz = rz;
+    hx = 0.0 + s.dx * -1.0;
+    hy = 0.0 + s.dy * -1.0;
+    hz = 0.0 + s.dz * -1.0;
+  }
+  // node::shiftVelocity
+  const double Tx = k.lbF[0] + hx, Ty = k.lbF[1] + hy, Tz = k.lbF[2] + hz;
+  ux = ux + Tx * 0.5 / n;
+  uy = uy + Ty * 0.5 / n;
+  uz = uz + Tz * 0.5 / n;
+  const double usq = ux * ux + uy * uy + uz * uz;
+  // node::solveCollision + node::addForce
+#pragma unroll
+  for (int j = 0; j < Q; ++j) {
+    const double vu = dotc(j, ux, uy, uz);
+    const double feq = WJ(j) * n * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
+    double fj = f[j] + k.omega * (feq - f[j]);
+    const double v9 = 9.0 * vu;
+    const double fpx = CX(j) == 0 ? (-ux) * 3.0 : CX(j) > 0 ? v9 + (1.0 - ux) * 3.0
+                                                             : -v9 + (-1.0 - ux) * 3.0;
+    const double fpy = CY(j) == 0 ? (-uy) * 3.0 : CY(j) > 0 ? v9 + (1.0 - uy) * 3.0
+                                                             : -v9 + (-1.0 - uy) * 3.0;
+    const double fpz = CZ(j) == 0 ? (-uz) * 3.0 : CZ(j) > 0 ? v9 + (1.0 - uz) * 3.0
+                                                             : -v9 + (-1.0 - uz) * 3.0;
+    fj += k.omegaf * WJ(j) * (fpx * Tx + fpy * Ty + fpz * Tz);
+    f[j] = fj;
+  }
+  s.n = n;
+  s.ux = ux;
+  s.uy = uy;
+  s.uz = uz;
+  s.hx = hx;
+  s.hy = hy;
+  s.hz = hz;
+}
+
+
+// per-block accumulator layout in shared memory
+enum { ACC_WALL = 0, ACC_OBJ = ACC_WALL + 3 * MAX_WALL, ACC_EXTRA = ACC_OBJ + 6 * MAX_OBJ,
+       ACC_N = ACC_EXTRA + 1 };
+
+// Reduce 16 per-lane particle terms over the lanes of a warp that share a
+// particle index and add them to the particle's accumulators.
+__device__ __forceinline__ void warpParticleReduce(int key, const double* v, double* pF,
+                                                   double* pM, double* pS, double* pV,
+                                                   int P) {
+  const unsigned FULL = 0xffffffffu;
+  unsigned todo = __ballot_sync(FULL, key >= 0);
+  const int lane = threadIdx.x & 31;
+  while (todo) {
+    const int leader = __ffs(todo) - 1;
+    const int kk = __shfl_sync(FULL, key, leader);
+    const bool mine = key == kk;
+    const unsigned grp = __ballot_sync(FULL, mine);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      double x = mine ? v[i] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+      if (lane == leader) {
+        double* dst = i < 3 ? pF + i * P : i < 6 ? pM + (i - 3) * P : i < 15 ? pS + (i - 6) * P
+                                                                               : pV;
+        atomicAdd(dst + kk, x);
+      }
+    }
+    todo &= ~grp;
+  }
+}
+
+// Fused LB step over all nodes: reconstruct, particle forcing, collision,
+// push streaming with the boundary rules of LB::streaming, and the per-node
+// bookkeeping of cleanLists / updateMass (fluid part).
+__global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
+  __shared__ double acc[ACC_N];
+  __shared__ int sbox[6];
+  __shared__ int snif;
+  for (int i = threadIdx.x; i < ACC_N; i += blockDim.x) acc[i] = 0.0;
+  if (threadIdx.x < 3) sbox[threadIdx.x] = INT_MAX;
+  else if (threadIdx.x < 6) sbox[threadIdx.x] = -1;
+  if (threadIdx.x == 0) snif = 0;
+  __syncthreads();
+  const long long N = k.N;
+  const int lane = threadIdx.x & 31;
+  const long long warpsPerBlock = blockDim.x >> 5;
+  const long long gw = blockIdx.x * warpsPerBlock + (threadIdx.x >> 5);
+  const long long stride = (long long)gridDim.x * warpsPerBlock * 32;
+  const double sp[Q] = {k.initDensity * WJ(0),  k.initDensity * WJ(1),  k.initDensity * WJ(2),
+                        k.initDensity * WJ(3),  k.initDensity * WJ(4),  k.initDensity * WJ(5),
+                        k.initDensity * WJ(6),  k.initDensity * WJ(7),  k.initDensity * WJ(8),
+                        k.initDensity * WJ(9),  k.initDensity * WJ(10), k.initDensity * WJ(11),
+                        k.initDensity * WJ(12), k.initDensity * WJ(13), k.initDensity * WJ(14),
+                        k.initDensity * WJ(15), k.initDensity * WJ(16), k.initDensity * WJ(17),
+                        k.initDensity * WJ(18)};
+  for (long long base = gw * 32; base < N; base += stride) {
+    const long long x = base + lane;
+    const bool valid = x < N;
+    uint8_t m = valid ? a.mask[x] : (uint8_t)2;
+    const int t = m & TYPE_MASK;
+    const bool act = valid && isActiveT(t);
+    if (valid) {  // cleanLists: the active list now equals the active types
+      const bool aBit = (m & ABIT) != 0;
+      if (aBit != act) a.mask[x] = (uint8_t)(act ? (m | ABIT) : (m & ~ABIT));
+    }
+    int key = -1;
+    double pv[16];
+    if (act) {
+      int ix, iy, iz;
+      coords(k, x, ix, iy, iz);
+      double f[Q];
+#pragma unroll
+      for (int j = 0; j < Q; ++j) f[j] = a.fin[(long long)j * N + x];
+      const bool pf = (m & PFLAG) != 0;
+      const uint32_t pid = pf ? a.solid[x] : 0u;
+      const double massOld = a.mass[x];
+      NodeState s;
+      collideNode(k, f, pf, pid, a.px0, a.px1, a.pw1, k.nPart, massOld, ix, iy, iz, s);
+      if (pf && pid < (uint32_t)k.nPart) {
+        key = (int)pid;
+        pv[0] = s.dx * 1.0;
+        pv[1] = s.dy * 1.0;
+        pv[2] = s.dz * 1.0;
+        pv[3] = (s.ry * s.dz - s.rz * s.dy) * 1.0;
+        pv[4] = (s.rz * s.dx - s.rx * s.dz) * 1.0;
+        pv[5] = (s.rx * s.dy - s.ry * s.dx) * 1.0;
+        const double r3[3] = {s.rx, s.ry, s.rz}, d3[3] = {s.dx, s.dy, s.dz};
+#pragma unroll
+        for (int aa = 0; aa < 3; ++aa)
+#pragma unroll
+          for (int bb = 0; bb < 3; ++bb)
+            pv[6 + 3 * aa + bb] = 1.0 * r3[aa] * k.uLength * d3[bb] * k.uForce;
+        pv[15] = massOld;
+      } else if (pf) {
+        atomicOr(a.iscal + IS_ERROR, ERR_PARTICLE_INDEX);
+      }
+      // LB::streaming, push form: population j of this node goes to the
+      // neighbour x+c_j when it is active; otherwise this node receives the
+      // reference's boundary value in direction opp(j).
+      a.fout[x] = f[0];
+      const double usq = s.ux * s.ux + s.uy * s.uy + s.uz * s.uz;
+#pragma unroll
+      for (int j = 1; j < Q; ++j) {
+        const long long lk = x + nbrOffset(k, j);
+        const int tl = a.mask[lk] & TYPE_MASK;
+        const double fs = f[j];
+        const long long dst = (long long)OPPJ(j) * N + x;
+        if (isActiveT(tl)) {
+          a.fout[(long long)j * N + lk] = fs;
+        } else if (tl == 2) {
+          const double vuj = dotc(j, s.ux, s.uy, s.uz);
+          a.fout[dst] = -fs + WJ(j) * k.initDensity * (2.0 + 9.0 * (vuj * vuj) - 3.0 * usq);
+        } else if (tl == 11) {
+          a.fout[dst] = fs;
+        } else if (tl == 7 || tl == 8) {
+          // wall velocity is zero: BBi == 0 for dynamic walls as well
+          const double bb = 2.0 * (fs - sp[j]) - 0.0;
+          const uint32_t w = a.solid[lk];
+          if (w < (uint32_t)k.nWall) {
+            if (CX(j)) atomicAdd(&acc[ACC_WALL + 3 * w + 0], CX(j) > 0 ? bb : -bb);
+            if (CY(j)) atomicAdd(&acc[ACC_WALL + 3 * w + 1], CY(j) > 0 ? bb : -bb);
+            if (CZ(j)) atomicAdd(&acc[ACC_WALL + 3 * w + 2], CZ(j) > 0 ? bb : -bb);
+          }
+          a.fout[dst] = fs;
+        } else if (tl == 12) {
+          const int ov = a.objIdx[lk];
+          const double* ob = a.obj + ov * OB_STRIDE;
+          const double vx = ob[OB_X1] / k.uSpeed, vy = ob[OB_X1 + 1] / k.uSpeed,
+                       vz = ob[OB_X1 + 2] / k.uSpeed;
+          const double BBi = 2.0 * 3.0 * s.n * WJ(j) * dotc(j, vx, vy, vz);
+          const double bb = 2.0 * (fs - sp[j]) - BBi;
+          const uint32_t so = a.solid[lk];
+          if (so < (uint32_t)k.nObj) {
+            const double* os = a.obj + so * OB_STRIDE;
+            int lx, ly, lz;
+            coords(k, lk, lx, ly, lz);
+            const double Fx = CX(j) ? (CX(j) > 0 ? bb : -bb) : 0.0;
+            const double Fy = CY(j) ? (CY(j) > 0 ? bb : -bb) : 0.0;
+            const double Fz = CZ(j) ? (CZ(j) > 0 ? bb : -bb) : 0.0;
+            const double rx = (double)lx - os[OB_X0] / k.uLength;
+            const double ry = (double)ly - os[OB_X0 + 1] / k.uLength;
+            const double rz = (double)lz - os[OB_X0 + 2] / k.uLength;
+            double* ac = &acc[ACC_OBJ + 6 * so];
+            if (CX(j)) atomicAdd(ac + 0, Fx);
+            if (CY(j)) atomicAdd(ac + 1, Fy);
+            if (CZ(j)) atomicAdd(ac + 2, Fz);
+            atomicAdd(ac + 3, ry * Fz - rz * Fy);
+            atomicAdd(ac + 4, rz * Fx - rx * Fz);
+            atomicAdd(ac + 5, rx * Fy - ry * Fx);
+          }
+          a.fout[dst] = fs - BBi;
+          atomicAdd(&acc[ACC_EXTRA], BBi * massOld);
+        } else {
+          atomicOr(a.iscal + IS_ERROR, ERR_TYPE);
+        }
+      }
+      if (t == 3) {
+        a.rhoS[x] = s.n;
+        a.uS[x] = s.ux;
+        a.uS[N + x] = s.uy;
+        a.uS[2 * N + x] = s.uz;
+        a.hS[x] = s.hx;
+        a.hS[N + x] = s.hy;
+        a.hS[2 * N + x] = s.hz;
+        atomicMin(&sbox[0], ix);
+        atomicMin(&sbox[1], iy);
+        atomicMin(&sbox[2], iz);
+        atomicMax(&sbox[3], ix);
+        atomicMax(&sbox[4], iy);
+        atomicMax(&sbox[5], iz);
+      } else if (k.freeSurface) {
+        a.mass[x] = s.n;  // LB::updateMass, fluid nodes (src/LB.cpp:1631-1634)
+      }
+    }
+    const unsigned ifb = __ballot_sync(0xffffffffu, act && t == 3);
+    if (lane == 0 && ifb) atomicAdd(&snif, __popc(ifb));
+    warpParticleReduce(key, pv, a.pFHydro, a.pMHydro, a.pSHydro, a.pFluidVol, k.nPart);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < ACC_N; i += blockDim.x) {
+    const double v = acc[i];
+    if (v == 0.0) continue;
+    if (i < ACC_OBJ) atomicAdd(a.wallF + (i / 3) * 12 + (i % 3), v);
+    else if (i < ACC_EXTRA) {
+      const int o = (i - ACC_OBJ) / 6, c = (i - ACC_OBJ) % 6;
+      atomicAdd(a.obj + o * OB_STRIDE + (c < 3 ? OB_FHYDRO + c : OB_MHYDRO + c - 3), v);
+    } else {
+      atomicAdd(a.scal + SC_EXTRA_MASS, v);
+    }
+  }
+  if (threadIdx.x == 0) {
+    if (snif) atomicAdd(a.iscal + IS_NIF, snif);
+    if (sbox[3] >= 0) {
+      atomicMin(a.iscal + IS_BBOX + 0, sbox[0]);
+      atomicMin(a.iscal + IS_BBOX + 1, sbox[1]);
+      atomicMin(a.iscal + IS_BBOX + 2, sbox[2]);
+      atomicMax(a.iscal + IS_BBOX + 3, sbox[3]);
+      atomicMax(a.iscal + IS_BBOX + 4, sbox[4]);
+      atomicMax(a.iscal + IS_BBOX + 5, sbox[5]);
+    }
+  }
+}
+
+// Reset of the per-step LB reductions (before lbStepFp64).
+__global__ void lbResetKernel(Consts k, double* pAcc, long long pAccLen, double* obj,
+                              double* wallF, double* scal, int* iscal) {
+  const long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  for (long long i = i0; i < pAccLen; i += (long long)gridDim.x * blockDim.x) pAcc[i] = 0.0;
+  if (i0 < k.nObj) {
+    for (int c = 0; c < 3; ++c) {
+      obj[i0 * OB_STRIDE + OB_FHYDRO + c] = 0.0;
+      obj[i0 * OB_STRIDE + OB_MHYDRO + c] = 0.0;
+    }
+  }
+  if (i0 < k.nWall)
+    for (int c = 0; c < 3; ++c) wallF[i0 * 12 + c] = 0.0;
+  if (i0 == 0) {
+    scal[SC_EXTRA_MASS] = 0.0;
+    iscal[IS_NIF] = 0;
+    iscal[IS_BBOX + 0] = iscal[IS_BBOX + 1] = iscal[IS_BBOX + 2] = INT_MAX;
+    iscal[IS_BBOX + 3] = iscal[IS_BBOX + 4] = iscal[IS_BBOX + 5] = -1;
+  }
+}
+
+// Unit conversions at the end of LB::streaming / computeHydroForces and the
+// mass-redistribution amount (src/LB.cpp:1533-1543, 1966-1977, 1844-1847).
+__global__ void lbFinalizeKernel(Consts k, double* pF, double* pM, double* pV, double* obj,
+                                 double* wallF, double* scal, const int* iscal) {
+  const int P = k.nPart;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+    for (int c = 0; c < 3; ++c) {
+      pF[c * P + i] *= k.uForce;
+      pM[c * P + i] *= k.uTorque;
+    }
+    pV[i] *= k.uVolume;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    for (int w = 0; w < k.nWall; ++w)
+      for (int c = 0; c < 3; ++c) wallF[w * 12 + c] *= k.uForce;
+    for (int o = 0; o < k.nObj; ++o)
+      for (int c = 0; c < 3; ++c) {
+        obj[o * OB_STRIDE + OB_FHYDRO + c] *= k.uForce;
+        obj[o * OB_STRIDE + OB_MHYDRO + c] *= k.uTorque;
+      }
+    scal[SC_ADD_MASS] = scal[SC_EXTRA_MASS] / (double)(unsigned)iscal[IS_NIF];
+  }
+}
+
+// ---- free surface ----------------------------------------------------------
+
+
+enum : uint8_t { FS_FILLED = 1, FS_EMPTIED = 2, FS_NEW = 4 };
+
+// Region = interface bounding box of the LB step grown by one node.
+__device__ __forceinline__ bool fsRegion(const Consts& k, const int* iscal, int& x0, int& y0,
+                                         int& z0, int& rx, int& ry, int& rz) {
+  if (iscal[IS_BBOX + 3] < 0) return false;
+  x0 = max(iscal[IS_BBOX + 0] - 1, 0);
+  y0 = max(iscal[IS_BBOX + 1] - 1, 0);
+  z0 = max(iscal[IS_BBOX + 2] - 1, 0);
+  rx = min(iscal[IS_BBOX + 3] + 1, k.X - 1) - x0 + 1;
+  ry = min(iscal[IS_BBOX + 4] + 1, k.Y - 1) - y0 + 1;
+  rz = min(iscal[IS_BBOX + 5] + 1, k.Z - 1) - z0 + 1;
+  return true;
+}
+
+#define FS_LOOP(k, a, ...)                                                               \
+  int _x0, _y0, _z0, _rx, _ry, _rz;                                                      \
+  if (fsRegion(k, a.iscal, _x0, _y0, _z0, _rx, _ry, _rz)) {                              \
+    const long long _vol = (long long)_rx * _ry * _rz;                                   \
+    for (long long _i = blockIdx.x * (long long)blockDim.x + threadIdx.x; _i < _vol;     \
+         _i += (long long)gridDim.x * blockDim.x) {                                      \
+      const int ix = _x0 + (int)(_i % _rx);                                              \
+      const int iy = _y0 + (int)((_i / _rx) % _ry);                                      \
+      const int iz = _z0 + (int)(_i / ((long long)_rx * _ry));                           \
+      const long long x = ix + iy * k.sy + iz * k.sz;                                    \
+      __VA_ARGS__                                                                        \
+    }                                                                                    \
+  }
+
+__device__ __forceinline__ void blockAddDouble(double v, double* dst) {
+  __shared__ double red[32];
+  const unsigned FULL = 0xffffffffu;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    double s = l < (int)(blockDim.x >> 5) ? red[l] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+    if (l == 0 && s != 0.0) atomicAdd(dst, s);
+  }
+  __syncthreads();
+}
+
+// LB::redistributeMass(extraMass) at the end of LB::streaming
+// (src/LB.cpp:1533, 1844-1852): every interface node receives an equal share.
+__global__ void lbRedistribute(Consts k, FsArgs a) {
+  const double addMass = a.scal[SC_ADD_MASS];
+  FS_LOOP(k, a, {
+    if ((a.mask[x] & TYPE_MASK) == 3) {
+      // the mass the collision used, for fsUpdateMass's recomputation
+      a.massNew[x] = a.mass[x];
+      a.mass[x] += addMass;
+    }
+  })
+}
+
+// LB::updateMass (interface part).
+__global__ void fsUpdateMass(Consts k, FsArgs a) {
+  FS_LOOP(k, a, {
+    const uint8_t m = a.mask[x];
+    if ((m & TYPE_MASK) != 3) continue;
+    const double mx = a.mass[x];
+    double fsl[Q];
+    bool haveFs = false;
+    double delta = 0.0;
+    bool first = true;
+#pragma unroll 1
+    for (int j = 1; j < Q; ++j) {
+      const long long lk = x + nbrOffset(k, j);
+      const int tl = a.mask[lk] & TYPE_MASK;
+      double term;
+      if (tl == 3 || tl == 0) {
+        const double ms = a.fcur[(long long)OPPJ(j) * k.N + x] - a.fcur[(long long)j * k.N + lk];
+        term = tl == 3 ? 0.5 * (a.mass[lk] + mx) * ms : 1.0 * ms;
+      } else if (tl == 8 || tl == 12 || tl == 9) {
+        if (!haveFs) {  // post-collision populations of this node, recomputed
+#pragma unroll
+          for (int q = 0; q < Q; ++q) fsl[q] = a.fold[(long long)q * k.N + x];
+          NodeState s;
+          const bool pf = (m & PFLAG) != 0;
+          collideNode(k, fsl, pf, pf ? a.solid[x] : 0u, a.px0, a.px1, a.pw1, k.nPart,
+                      a.massNew[x], ix, iy, iz, s);
+          haveFs = true;
+        }
+        const double ms = a.fcur[(long long)OPPJ(j) * k.N + x] - fsl[j];
+        term = (1.0 * mx) * ms;
+      } else {
+        continue;
+      }
+      delta = first ? term : delta + term;
+      first = false;
+    }
+    a.massNew[x] = mx + delta;
+  })
+}
+
+// findInterfaceMutants (src/LB.cpp:1669-1698) after the interface mass copy.
+__global__ void fsMutants(Consts k, FsArgs a) {
+  FS_LOOP(k, a, {
+    const uint8_t m = a.mask[x];
+    a.fsflag[x] = 0;
+    if ((m & TYPE_MASK) != 3) continue;
+    const double mm = a.massNew[x];
+    a.mass[x] = mm;
+    if (mm > a.rhoS[x]) {
+      a.mask[x] = (uint8_t)((m & ~TYPE_MASK) | 0);
+      a.fsflag[x] = FS_FILLED;
+    } else if (mm < 0.0) {
+      a.mask[x] = (uint8_t)((m & ~TYPE_MASK) | 2);
+      a.fsflag[x] = FS_EMPTIED;
+    }
+  })
+}
+
+// smoothenInterface (src/LB.cpp:1700-1749): gas neighbours of filled nodes
+// become interface nodes initialised from the first filled neighbour in the
+// reference's order (the highest node index); fluid neighbours of emptied
+// nodes become interface nodes holding 99% of their density.
+__global__ void fsSmoothen(Consts k, FsArgs a) {
+  double surplus = 0.0;
+  FS_LOOP(k, a, {
+    const uint8_t m = a.mask[x];
+    const int t = m & TYPE_MASK;
+    if (t == 2) {
+      long long win = -1;
+#pragma unroll 1
+      for (int j = 1; j < Q; ++j) {
+        const long long lk = x + nbrOffset(k, j);
+        if ((a.fsflag[lk] & FS_FILLED) && lk > win) win = lk;
+      }
+      if (win >= 0) {
+        const double rho0 = k.initDensity;
+        const double Fx = a.hS[win] + k.lbF[0], Fy = a.hS[k.N + win] + k.lbF[1],
+                     Fz = a.hS[2 * k.N + win] + k.lbF[2];
+        const double ux = Fx / 2.0 / rho0 + a.uS[win];
+        const double uy = Fy / 2.0 / rho0 + a.uS[k.N + win];
+        const double uz = Fz / 2.0 / rho0 + a.uS[2 * k.N + win];
+        const double usq = ux * ux + uy * uy + uz * uz;
+#pragma unroll
+        for (int j = 0; j < Q; ++j) a.fcur[(long long)j * k.N + x] = feqj(j, rho0, ux, uy, uz, usq);
+        a.mask[x] = (uint8_t)((m & ~TYPE_MASK) | 3);
+        a.fsflag[x] |= FS_NEW;
+        a.rhoS[x] = rho0;
+        a.mass[x] = 0.01 * rho0;
+        surplus -= 0.01 * rho0;
+      }
+    } else if (t == 0) {
+      bool hit = false;
+#pragma unroll 1
+      for (int j = 1; j < Q; ++j)
+        if (a.fsflag[x + nbrOffset(k, j)] & FS_EMPTIED) {
+          hit = true;
+          break;
+        }
+      if (hit) {
+        const double n = (a.fsflag[x] & FS_FILLED) ? a.rhoS[x] : a.mass[x];
+        a.mask[x] = (uint8_t)((m & ~TYPE_MASK) | 3);
+        a.fsflag[x] |= FS_NEW;
+        a.rhoS[x] = n;
+        a.mass[x] = 0.99 * n;
+        surplus += 0.01 * n;
+      }
+    }
+  })
+  blockAddDouble(surplus, a.scal + SC_SURPLUS);
+}
+
+// updateMutants + removeIsolated, first pass (src/LB.cpp:1751-1817).
+__global__ void fsMutantsAndFill(Consts k, FsArgs a) {
+  double surplus = 0.0;
+  FS_LOOP(k, a, {
+    const uint8_t fl = a.fsflag[x];
+    const uint8_t m = a.mask[x];
+    if ((fl & FS_EMPTIED) && !(fl & FS_NEW)) {
+      surplus += a.mass[x];
+      a.mass[x] = 0.0;
+    } else if ((fl & FS_FILLED) && !(fl & FS_NEW)) {
+      surplus += a.mass[x] - a.rhoS[x];
+      a.mass[x] = a.rhoS[x];
+    } else if ((m & TYPE_MASK) == 3) {
+      bool gasNb = false;
+#pragma unroll 1
+      for (int j = 1; j < Q; ++j)
+        if ((a.mask[x + nbrOffset(k, j)] & TYPE_MASK) == 2) {
+          gasNb = true;
+          break;
+        }
+      if (!gasNb) {
+        surplus += a.mass[x] - a.rhoS[x];
+        a.mass[x] = a.rhoS[x];
+        a.mask[x] = (uint8_t)((m & ~TYPE_MASK) | 0);
+      }
+    }
+  })
+  blockAddDouble(surplus, a.scal + SC_SURPLUS);
+}
+
+// removeIsolated, second pass (src/LB.cpp:1819-1841), and the interface count.
+__global__ void fsEmptyIsolated(Consts k, FsArgs a) {
+  double surplus = 0.0;
+  int cnt = 0;
+  FS_LOOP(k, a, {
+    const uint8_t m = a.mask[x];
+    if ((m & TYPE_MASK) != 3) continue;
+    bool fluidNb = false;
+#pragma unroll 1
+    for (int j = 1; j < Q; ++j)
+      if ((a.mask[x + nbrOffset(k, j)] & TYPE_MASK) == 0) {
+        fluidNb = true;
+        break;
+      }
+    if (!fluidNb) {
+      surplus += a.mass[x];
+      a.mass[x] = 0.0;
+      a.mask[x] = (uint8_t)((m & ~TYPE_MASK) | 2);
+    } else {
+      ++cnt;
+    }
+  })
+  blockAddDouble(surplus, a.scal + SC_SURPLUS);
+  if (cnt) atomicAdd(a.iscal + IS_NIF2, cnt);
+}
+
+// redistributeMass(massSurplus) + cleanLists of the free-surface step.
+__global__ void fsRedistribute(Consts k, FsArgs a) {
+  const double addMass = a.scal[SC_SURPLUS] / (double)(unsigned)a.iscal[IS_NIF2];
+  FS_LOOP(k, a, {
+    const uint8_t m = a.mask[x];
+    const int t = m & TYPE_MASK;
+    if (t == 3) a.mass[x] += addMass;
+    const bool act = isActiveT(t);
+    const uint8_t nm = (uint8_t)(act ? (m | ABIT) : (m & ~ABIT));
+    if (nm != m) a.mask[x] = nm;
+    a.fsflag[x] = 0;
+  })
+}
+
+__global__ void fsResetKernel(double* scal, int* iscal) {
+  scal[SC_SURPLUS] = 0.0;
+  iscal[IS_NIF2] = 0;
+}
+
+// ---- coupling step -----------------------------------------------------------
+
+// Bounding box of the nodes inside a sphere (lattice units), clamped.
+__device__ __forceinline__ void sphereBox(const Consts& k, double cx, double cy, double cz,
+                                          double r, int* lo, int* hi) {
+  const double c[3] = {cx, cy, cz};
+  const int lim[3] = {k.X, k.Y, k.Z};
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = max(0, (int)floor(c[a] - r) - 1);
+    hi[a] = min(lim[a] - 1, (int)ceil(c[a] + r) + 1);
+  }
+}
+
+// findNewActiveObject, step 1: collect object nodes that object 0 no longer
+// covers (candidates come from the previous voxelisation boxes).
+__global__ void uncoverCollect(Consts k, const uint8_t* mask, const double* obj,
+                               uint32_t* list, int* iscal) {
+  const double* o0 = obj;
+  const double c0x = o0[OB_X0] / k.uLength, c0y = o0[OB_X0 + 1] / k.uLength,
+               c0z = o0[OB_X0 + 2] / k.uLength, r0 = o0[OB_R] / k.uLength;
+  for (int o = 0; o < k.nObj; ++o) {
+    const double* ob = obj + o * OB_STRIDE;
+    int lo[3], hi[3];
+    sphereBox(k, ob[OB_X0PREV] / k.uLength, ob[OB_X0PREV + 1] / k.uLength,
+              ob[OB_X0PREV + 2] / k.uLength, ob[OB_R] / k.uLength, lo, hi);
+    const long long nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+    const long long vol = nx * ny * nz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol;
+         i += (long long)gridDim.x * blockDim.x) {
+      const int ix = lo[0] + (int)(i % nx), iy = lo[1] + (int)((i / nx) % ny),
+                iz = lo[2] + (int)(i / (nx * ny));
+      const long long x = ix + iy * k.sy + iz * k.sz;
+      if ((mask[x] & TYPE_MASK) != 12) continue;
+      if (insideSphere((double)ix, (double)iy, (double)iz, c0x, c0y, c0z, r0)) continue;
+      const int slot = atomicAdd(iscal + IS_NUNCOVER, 1);
+      if (slot < UNCOVER_CAP) list[slot] = (uint32_t)x;
+      else atomicOr(iscal + IS_ERROR, ERR_UNCOVER_CAP);
+    }
+  }
+}
+
+// findNewActiveObject, step 2 (one CTA): resolve the uncovered nodes in the
+// reference's serial order (ascending node index, each node seeing the new
+// types of the lower-index ones) by fixed-point iteration, then initialise
+// them (src/LB.cpp:874-940).
+__global__ void __launch_bounds__(1024) uncoverResolve(Consts k, uint8_t* mask, double* f,
+                                                       double* mass, uint32_t* list,
+                                                       int* iscal) {
+  __shared__ uint32_t s_idx[UNCOVER_CAP];
+  __shared__ uint8_t s_st[UNCOVER_CAP];
+  int n = min(iscal[IS_NUNCOVER], UNCOVER_CAP);
+  if (n == 0) return;
+  int p2 = 1;
+  while (p2 < n) p2 <<= 1;
+  for (int i = threadIdx.x; i < p2; i += blockDim.x) s_idx[i] = i < n ? list[i] : 0xffffffffu;
+  __syncthreads();
+  // bitonic sort ascending
+  for (int size = 2; size <= p2; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < p2; i += blockDim.x) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const bool up = (i & size) == 0;
+          const uint32_t a = s_idx[i], b = s_idx[j];
+          if ((a > b) == up) {
+            s_idx[i] = b;
+            s_idx[j] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  // the same node can appear once per object box: drop duplicates
+  __shared__ int s_n;
+  if (threadIdx.x == 0) {
+    int w = 0;
+    for (int i = 0; i < n; ++i)
+      if (i == 0 || s_idx[i] != s_idx[i - 1]) s_idx[w++] = s_idx[i];
+    s_n = w;
+  }
+  __syncthreads();
+  n = s_n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s_st[i] = 12;
+  __syncthreads();
+  auto typeOf = [&](long long lk, int self) -> int {
+    // binary search among the candidates
+    int lo = 0, hi = n - 1;
+    while (lo <= hi) {
+      const int mid = (lo + hi) >> 1;
+      const uint32_t v = s_idx[mid];
+      if (v == (uint32_t)lk) return mid < self ? (int)s_st[mid] : 12;
+      if (v < (uint32_t)lk) lo = mid + 1;
+      else hi = mid - 1;
+    }
+    return mask[lk] & TYPE_MASK;
+  };
+  for (int iter = 0; iter <= n; ++iter) {
+    int changed = 0;
+    uint8_t nst[UNCOVER_CAP / 1024];
+    for (int i = threadIdx.x, q = 0; i < n; i += blockDim.x, ++q) {
+      const long long x = s_idx[i];
+      bool fluidNb = false, gasNb = false;
+      for (int j = 1; j < Q; ++j) {
+        const int tl = typeOf(x + nbrOffset(k, j), i);
+        fluidNb |= tl == 0;
+        gasNb |= tl == 2;
+      }
+      nst[q] = !fluidNb ? 2 : gasNb ? 3 : 0;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x, q = 0; i < n; i += blockDim.x, ++q)
+      if (s_st[i] != nst[q]) {
+        s_st[i] = nst[q];
+        changed = 1;
+      }
+    if (!__syncthreads_or(changed)) break;
+  }
+  const double rho0 = k.initDensity;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const long long x = s_idx[i];
+    const int st = s_st[i];
+    const uint8_t m = mask[x];
+    mask[x] = (uint8_t)((m & ~TYPE_MASK) | st);
+    if (st == 2) {
+      mass[x] = 0.0;
+      continue;
+    }
+    // node::initialize(initDensity, initVelocity or 0, mass, visc, lbF)
+    const double vx = st == 0 ? k.initVel[0] : 0.0, vy = st == 0 ? k.initVel[1] : 0.0,
+                 vz = st == 0 ? k.initVel[2] : 0.0;
+    const double ux = k.lbF[0] / 2.0 / rho0 + vx, uy = k.lbF[1] / 2.0 / rho0 + vy,
+                 uz = k.lbF[2] / 2.0 / rho0 + vz;
+    const double usq = ux * ux + uy * uy + uz * uz;
+    for (int j = 0; j < Q; ++j) f[(long long)j * k.N + x] = feqj(j, rho0, ux, uy, uz, usq);
+    mass[x] = st == 0 ? rho0 : 0.5 * rho0;
+  }
+}
+
+// Voxelisation of the impactors (updateObjectBoundaries, src/LB.cpp:806-840).
+__global__ void voxelizeObjects(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* objIdx,
+                                double* mass, double* obj) {
+  int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {-1, -1, -1};
+  for (int o = 0; o < k.nObj; ++o) {
+    const double* ob = obj + o * OB_STRIDE;
+    int l[3], h[3];
+    sphereBox(k, ob[OB_X0] / k.uLength, ob[OB_X0 + 1] / k.uLength, ob[OB_X0 + 2] / k.uLength,
+              ob[OB_R] / k.uLength, l, h);
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = min(lo[a], l[a]);
+      hi[a] = max(hi[a], h[a]);
+    }
+  }
+  if (hi[0] < 0) return;
+  const long long nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+  const long long vol = nx * ny * nz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int ix = lo[0] + (int)(i % nx), iy = lo[1] + (int)((i / nx) % ny),
+              iz = lo[2] + (int)(i / (nx * ny));
+    const long long x = ix + iy * k.sy + iz * k.sz;
+    int last = -1;
+    for (int o = 0; o < k.nObj; ++o) {
+      const double* ob = obj + o * OB_STRIDE;
+      if (insideSphere((double)ix, (double)iy, (double)iz, ob[OB_X0] / k.uLength,
+                       ob[OB_X0 + 1] / k.uLength, ob[OB_X0 + 2] / k.uLength,
+                       ob[OB_R] / k.uLength))
+        last = o;
+    }
+    if (last < 0) continue;
+    mask[x] = (uint8_t)((mask[x] & ~TYPE_MASK) | 12);
+    solid[x] = (uint32_t)obj[last * OB_STRIDE + OB_INDEX];
+    objIdx[x] = (uint8_t)last;
+    mass[x] = 0.0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (unsigned)k.nObj)
+    for (int c = 0; c < 3; ++c)
+      obj[threadIdx.x * OB_STRIDE + OB_X0PREV + c] = obj[threadIdx.x * OB_STRIDE + OB_X0 + c];
+}
+
+// updateIndices, step 1: every particle claims the nodes of the last active
+// list inside it; the highest particle index wins (src/LB.cpp:695-710).
+__global__ void flagClaim(Consts k, const uint8_t* mask, uint32_t* claim, const double* px0,
+                          const double* pr, const int* iscal, unsigned long long* uscal) {
+  if (!iscal[IS_NEWNBR]) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) uscal[US_FIRSTFLAG] = ~0ull;
+  const int P = k.nPart;
+  const int warpsPerBlock = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31;
+  for (int p = blockIdx.x * warpsPerBlock + (threadIdx.x >> 5); p < P;
+       p += gridDim.x * warpsPerBlock) {
+    const double cx = px0[p] / k.uLength, cy = px0[P + p] / k.uLength,
+                 cz = px0[2 * P + p] / k.uLength, r = pr[p] / k.uLength;
+    int lo[3], hi[3];
+    sphereBox(k, cx, cy, cz, r, lo, hi);
+    const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+    if (nx <= 0 || ny <= 0 || nz <= 0) continue;
+    const int vol = nx * ny * nz;
+    for (int i = lane; i < vol; i += 32) {
+      const int ix = lo[0] + i % nx, iy = lo[1] + (i / nx) % ny, iz = lo[2] + i / (nx * ny);
+      const long long x = ix + iy * k.sy + iz * k.sz;
+      if (!(mask[x] & ABIT)) continue;
+      if (insideSphere((double)ix, (double)iy, (double)iz, cx, cy, cz, r))
+        atomicMax(claim + x, (uint32_t)p + 1u);
+    }
+  }
+}
+
+// updateIndices, step 2: the flag reset of every node (solid index 0, walls
+// included) and the new flags (src/LB.cpp:689-693).
+__global__ void flagApply(Consts k, uint8_t* mask, uint32_t* solid, uint32_t* claim,
+                          const int* iscal, unsigned long long* uscal) {
+  if (!iscal[IS_NEWNBR]) return;
+  unsigned long long first = ~0ull;
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
+       x += (long long)gridDim.x * blockDim.x) {
+    const uint32_t c = claim[x];
+    const uint8_t m = mask[x];
+    const uint8_t nm = (uint8_t)(c ? (m | PFLAG) : (m & ~PFLAG));
+    if (nm != m) mask[x] = nm;
+    solid[x] = c ? c - 1u : 0u;
+    if (c) {
+      claim[x] = 0;
+      if ((unsigned long long)x < first) first = (unsigned long long)x;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long v = __shfl_xor_sync(0xffffffffu, first, o);
+    first = v < first ? v : first;
+  }
+  if ((threadIdx.x & 31) == 0 && first != ~0ull) atomicMin(uscal + US_FIRSTFLAG, first);
+}
+
+// LB::findNewActive (one CTA): walk the flagged nodes in ascending order,
+// un-flag those no longer inside their particle and stop at the first one
+// that still is (the reference's loop-exiting break, src/LB.cpp:2001-2007).
+__global__ void __launch_bounds__(1024) findNewActiveKernel(Consts k, uint8_t* mask,
+                                                            uint32_t* solid, const double* px0,
+                                                            const double* pr, int* iscal,
+                                                            unsigned long long* uscal) {
+  __shared__ unsigned long long s_min;
+  if (threadIdx.x == 0) iscal[IS_NEWNBR] = 0;
+  unsigned long long start = uscal[US_FIRSTFLAG];
+  const int P = k.nPart;
+  while (start < (unsigned long long)k.N) {
+    if (threadIdx.x == 0) s_min = ~0ull;
+    __syncthreads();
+    const long long x = (long long)start + threadIdx.x;
+    bool flagged = false, inside = false;
+    if (x < k.N) {
+      flagged = (mask[x] & PFLAG) != 0;
+      if (flagged) {
+        const uint32_t pid = solid[x];
+        if (pid >= (uint32_t)P) {
+          atomicOr(iscal + IS_ERROR, ERR_PARTICLE_INDEX);
+        } else {
+          int ix, iy, iz;
+          coords(k, x, ix, iy, iz);
+          inside = insideSphere((double)ix, (double)iy, (double)iz, px0[pid] / k.uLength,
+                                px0[P + pid] / k.uLength, px0[2 * P + pid] / k.uLength,
+                                pr[pid] / k.uLength);
+        }
+        if (inside) atomicMin(&s_min, (unsigned long long)x);
+      }
+    }
+    __syncthreads();
+    const unsigned long long stop = s_min;
+    if (flagged && (unsigned long long)x < stop) {
+      mask[x] = (uint8_t)(mask[x] & ~PFLAG);
+      solid[x] = 0;
+    }
+    __syncthreads();
+    if (stop != ~0ull) {
+      if (threadIdx.x == 0) uscal[US_FIRSTFLAG] = stop;
+      return;
+    }
+    start += blockDim.x;
+  }
+  if (threadIdx.x == 0) uscal[US_FIRSTFLAG] = ~0ull;
+}
+
+// ---- initialisation (LB::latticeBolzmannInit) ------------------------------
+
+// initializeLatticeBoundaries, initializeWallBoundaries,
+// initializeObjectBoundaries and initializeInterface (src/LB.cpp:538-795, 974-992)
+__global__ void initTypes(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* objIdx,
+                          const int* boundary, const DeviceWall* walls, const int* wallType,
+                          const double* obj, double fluidHeightLattice, int freeSurface) {
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
+       x += (long long)gridDim.x * blockDim.x) {
+    int ix, iy, iz;
+    coords(k, x, ix, iy, iz);
+    int t = 0;
+    uint32_t so = 0;
+    if (ix == 0) t = boundary[0];
+    else if (ix == k.X - 1) t = boundary[1];
+    else if (iy == 0) t = boundary[2];
+    else if (iy == k.Y - 1) t = boundary[3];
+    else if (iz == 0) t = boundary[4];
+    else if (iz == k.Z - 1) t = boundary[5];
+    const double p[3] = {(double)ix, (double)iy, (double)iz};
+    for (int w = 0; w < k.nWall; ++w) {
+      const DeviceWall& W = walls[w];
+      const double d = W.n[0] * (p[0] - W.p[0] / k.uLength) +
+                       W.n[1] * (p[1] - W.p[1] / k.uLength) +
+                       W.n[2] * (p[2] - W.p[2] / k.uLength);
+      if (d < 0.0) {
+        so = (uint32_t)w;
+        t = wallType[w];
+      }
+    }
+    uint8_t oi = 0;
+    for (int o = 0; o < k.nObj; ++o) {
+      const double* ob = obj + o * OB_STRIDE;
+      if (insideSphere(p[0], p[1], p[2], ob[OB_X0] / k.uLength, ob[OB_X0 + 1] / k.uLength,
+                       ob[OB_X0 + 2] / k.uLength, ob[OB_R] / k.uLength)) {
+        so = (uint32_t)ob[OB_INDEX];
+        t = 12;
+        oi = (uint8_t)o;
+      }
+    }
+    if (freeSurface && (double)(unsigned)iy > fluidHeightLattice && t == 0) t = 2;
+    mask[x] = (uint8_t)t;
+    solid[x] = so;
+    objIdx[x] = oi;
+  }
+}
+
+// initializeVariables (src/LB.cpp:1042-1096): fluid nodes next to gas become
+// interface nodes; active nodes start at equilibrium. Typing in place is safe:
+// a fluid->interface change never alters any node's gas neighbourhood. Also
+// the first cleanLists (active-list bit).
+__global__ void initFields(Consts k, uint8_t* mask, double* f, double* mass) {
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
+       x += (long long)gridDim.x * blockDim.x) {
+    int t = mask[x] & TYPE_MASK;
+    if (t == 0) {
+      for (int j = 1; j < Q; ++j)
+        if ((mask[x + nbrOffset(k, j)] & TYPE_MASK) == 2) {
+          t = 3;
+          break;
+        }
+    }
+    double ms = 0.0;
+    if (t == 0 || t == 3) {
+      const double rho0 = k.initDensity;
+      const double ux = k.lbF[0] / 2.0 / rho0 + k.initVel[0];
+      const double uy = k.lbF[1] / 2.0 / rho0 + k.initVel[1];
+      const double uz = k.lbF[2] / 2.0 / rho0 + k.initVel[2];
+      const double usq = ux * ux + uy * uy + uz * uz;
+      for (int j = 0; j < Q; ++j) f[(long long)j * k.N + x] = feqj(j, rho0, ux, uy, uz, usq);
+      ms = t == 0 ? rho0 : 0.5 * rho0;
+      mask[x] = (uint8_t)((mask[x] & ~TYPE_MASK) | t | ABIT);
+    }
+    mass[x] = ms;
+  }
+}
+
+// ---- diagnostics --------------------------------------------------------------
+
+__global__ void massSummaryKernel(Consts k, const uint8_t* mask, const double* mass,
+                                  double* out, unsigned long long* cnt) {
+  double s = 0.0;
+  unsigned long long ni = 0, na = 0;
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
+       x += (long long)gridDim.x * blockDim.x) {
+    const uint8_t m = mask[x];
+    const int t = m & TYPE_MASK;
+    if (isActiveT(t)) {
+      ++na;
+      if (t == 3) ++ni;
+      if (!(m & PFLAG)) s += mass[x];
+    }
+  }
+  blockAddDouble(s, out);
+  for (int o = 16; o > 0; o >>= 1) {
+    ni += __shfl_xor_sync(0xffffffffu, ni, o);
+    na += __shfl_xor_sync(0xffffffffu, na, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(cnt, ni);
+    atomicAdd(cnt + 1, na);
+  }
+}
+
+// Moments of the current populations, for state download.
+__global__ void momentsKernel(Consts k, const uint8_t* mask, const double* f, double* n,
+                              double* u) {
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
+       x += (long long)gridDim.x * blockDim.x) {
+    if (!isActiveT(mask[x] & TYPE_MASK)) {
+      n[x] = 0.0;
+      u[x] = u[k.N + x] = u[2 * k.N + x] = 0.0;
+      continue;
+    }
+    double fl[Q];
+    double s = 0.0;
+    for (int j = 0; j < Q; ++j) {
+      fl[j] = f[(long long)j * k.N + x];
+      s += fl[j];
+    }
+    double ux = 0, uy = 0, uz = 0;
+    for (int j = 0; j < Q; ++j) {
+      ux += CX(j) * fl[j];
+      uy += CY(j) * fl[j];
+      uz += CZ(j) * fl[j];
+    }
+    n[x] = s;
+    u[x] = ux / s;
+    u[k.N + x] = uy / s;
+    u[2 * k.N + x] = uz / s;
+  }
+}
+
+__global__ void nonfiniteCheck(Consts k, const uint8_t* mask, const double* f, int* iscal) {
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
+       x += (long long)gridDim.x * blockDim.x) {
+    if (!isActiveT(mask[x] & TYPE_MASK)) continue;
+    double s = 0.0;
+    for (int j = 0; j < Q; ++j) s += f[(long long)j * k.N + x];
+    if (!isfinite(s)) atomicOr(iscal + IS_ERROR, ERR_NONFINITE);
+  }
+}
+
+}  // namespace lbdem

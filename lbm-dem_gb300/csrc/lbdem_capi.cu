@@ -1,0 +1,780 @@
+// C ABI of liblbdem: context lifecycle, the step entry points and state
+// download. The host side only sequences kernels on the context's stream;
+// every step entry point enqueues work and returns without synchronising.
+//
+// Host arithmetic that feeds the kernels (units, masses, damping) follows
+// the reference operation by operation (src/node.cpp:512-525,
+// src/LB.cpp:153-330, src/DEM.cpp:199-357, src/elmt.cpp:27-63) and is
+// compiled without FMA contraction, so device and reference start from the
+// same bits.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lbdem_internal.h"
+
+#include "kernels_decl.h"
+
+using namespace lbdem;
+
+namespace {
+
+const double PI_D = 3.14159265358979323846;
+
+int setErr(lbdem_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                  \
+  do {                                                                            \
+    cudaError_t _e = (call);                                                      \
+    if (_e != cudaSuccess)                                                        \
+      return setErr(ctx, _e == cudaErrorMemoryAllocation ? LBDEM_ERR_OOM : LBDEM_ERR_CUDA, \
+                    std::string(#call) + ": " + cudaGetErrorString(_e));         \
+  } while (0)
+
+template <class T>
+int dalloc(lbdem_ctx* ctx, T** p, size_t count) {
+  const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  cudaError_t e = cudaMalloc((void**)p, bytes);
+  if (e != cudaSuccess)
+    return setErr(ctx, LBDEM_ERR_OOM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+  ctx->deviceBytes += (long long)bytes;
+  cudaMemsetAsync(*p, 0, bytes, ctx->stream);
+  return LBDEM_OK;
+}
+
+int launchErr(lbdem_ctx* ctx, const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return setErr(ctx, LBDEM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  return LBDEM_OK;
+}
+
+int latticeGrid(lbdem_ctx* ctx) { return std::max(1, ctx->smCount) * 8; }
+
+LbArgs lbArgs(lbdem_ctx* c) {
+  Device& d = c->d;
+  const int P = std::max(c->nPart, 1);
+  LbArgs a;
+  a.fin = (const double*)d.f[c->cur];
+  a.fout = (double*)d.f[1 - c->cur];
+  a.mask = d.mask;
+  a.solid = d.solid;
+  a.objIdx = d.objIdx;
+  a.mass = d.mass;
+  a.rhoS = d.rhoS;
+  a.uS = d.uS;
+  a.hS = d.hS;
+  a.px0 = d.px0;
+  a.px1 = d.px1;
+  a.pw1 = d.pw1;
+  a.pFHydro = d.pFHydro;
+  a.pMHydro = d.pMHydro;
+  a.pSHydro = d.pSHydro;
+  a.pFluidVol = d.pFluidVol;
+  a.obj = d.obj;
+  a.wallF = d.wallF;
+  a.scal = d.scal;
+  a.iscal = d.iscal;
+  (void)P;
+  return a;
+}
+
+FsArgs fsArgs(lbdem_ctx* c) {
+  Device& d = c->d;
+  FsArgs a;
+  a.fcur = (double*)d.f[c->cur];
+  a.fold = (const double*)d.f[1 - c->cur];
+  a.mask = d.mask;
+  a.solid = d.solid;
+  a.objIdx = d.objIdx;
+  a.fsflag = d.fsflag;
+  a.mass = d.mass;
+  a.massNew = d.massNew;
+  a.rhoS = d.rhoS;
+  a.uS = d.uS;
+  a.hS = d.hS;
+  a.px0 = d.px0;
+  a.px1 = d.px1;
+  a.pw1 = d.pw1;
+  a.obj = d.obj;
+  a.scal = d.scal;
+  a.iscal = d.iscal;
+  return a;
+}
+
+DemArgs demArgs(lbdem_ctx* c) {
+  Device& d = c->d;
+  DemArgs a;
+  a.x0 = d.px0;
+  a.x1 = d.px1;
+  a.w1 = d.pw1;
+  a.r = d.pr;
+  a.invm = d.pinvm;
+  a.invI = d.pinvI;
+  a.FHydro = d.pFHydro;
+  a.MHydro = d.pMHydro;
+  a.FContact = d.pFContact;
+  a.MContact = d.pMContact;
+  a.FLub = d.pFLub;
+  a.MLub = d.pMLub;
+  a.FRep = d.pFRep;
+  a.FTotal = d.pFTotal;
+  a.MTotal = d.pMTotal;
+  a.FGrav = d.pFGrav;
+  a.xiw = d.pxiw;
+  a.xio = d.pxio;
+  a.list[0] = d.plist[0];
+  a.list[1] = d.plist[1];
+  a.xi[0] = d.pxi[0];
+  a.xi[1] = d.pxi[1];
+  a.partner = d.partner;
+  a.gorder = d.gorder;
+  a.pairbuf = d.pairbuf;
+  a.pairflag = d.pairflag;
+  a.pcell = d.pcell;
+  a.ppos = d.ppos;
+  a.cellCount = d.cellCount;
+  a.cellStart = d.cellStart;
+  a.cellFill = d.cellFill;
+  a.cellParts = d.cellParts;
+  a.obj = d.obj;
+  a.wallF = d.wallF;
+  a.walls = d.walls;
+  a.scal = d.scal;
+  a.iscal = d.iscal;
+  return a;
+}
+
+int partGrid(lbdem_ctx* c, int block) {
+  return std::max(1, std::min((c->nPart + block - 1) / block, c->smCount * 16));
+}
+
+// Neighbour-list rebuild kernels (gated on the device-side rebuild flag).
+int enqueueNeighbourList(lbdem_ctx* ctx) {
+  const Consts& k = ctx->k;
+  DemArgs a = demArgs(ctx);
+  cudaStream_t s = ctx->stream;
+  const int pg = partGrid(ctx, 128);
+  nbrCellAssign<<<pg, 128, 0, s>>>(k, a);
+  nbrCellScan<<<1, 1024, 0, s>>>(k, a);
+  nbrCellScatter<<<pg, 128, 0, s>>>(k, a);
+  nbrCellSort<<<std::max(1, std::min(MAX_L / 128 + 1, ctx->smCount * 8)), 128, 0, s>>>(k, a);
+  nbrBuildCells<<<pg, 128, 0, s>>>(k, a);
+  nbrBuildDirect<<<pg, 128, 0, s>>>(k, a);
+  nbrDirectHistory<<<pg, 128, 0, s>>>(k, a);
+  nbrPartners<<<pg, 128, 0, s>>>(k, a);
+  nbrFinish<<<1, 1, 0, s>>>(a);
+  return launchErr(ctx, "neighbour list");
+}
+
+}  // namespace
+
+// ============================================================================
+
+extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
+                            lbdem_ctx** out) {
+  if (!cfg || !out) return LBDEM_ERR_INVALID;
+  lbdem_ctx* ctx = new lbdem_ctx();
+  *out = ctx;
+  const int precision = opt ? opt->precision : LBDEM_PLAIN_FP64;
+  ctx->precision = precision;
+  ctx->device = opt ? opt->device : 0;
+  ctx->check_every = opt ? opt->check_every : 0;
+  if (precision != LBDEM_PLAIN_FP64 && precision != LBDEM_MIXED)
+    return setErr(ctx, LBDEM_ERR_INVALID, "unknown precision form");
+  // ---- validation (the supported subset of the reference's inputs) ----
+  if (!cfg->rheologyNewtonian || cfg->turbulenceSolve || cfg->lbRestart || cfg->lbTopography)
+    return setErr(ctx, LBDEM_ERR_INVALID,
+                  "only NEWTONIAN rheology without turbulence, restart or topography");
+  if (cfg->n_bodies != 0) return setErr(ctx, LBDEM_ERR_INVALID, "bodies are not supported");
+  for (int i = 0; i < 6; ++i)
+    if (cfg->boundary[i] != 7 && cfg->boundary[i] != 8)
+      return setErr(ctx, LBDEM_ERR_INVALID, "only no-slip walls (boundary types 7/8)");
+  if (cfg->unitTime <= 0.0 || cfg->unitLength <= 0.0)
+    return setErr(ctx, LBDEM_ERR_INVALID, "unitLength and unitTime must be positive");
+  if (cfg->n_objects > MAX_OBJ) return setErr(ctx, LBDEM_ERR_INVALID, "too many objects");
+  for (int o = 0; o < cfg->n_objects; ++o)
+    if (cfg->objects[o].index != o)
+      return setErr(ctx, LBDEM_ERR_INVALID, "object index column must equal its position");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return setErr(ctx, LBDEM_ERR_NO_DEVICE, "no CUDA device");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+  ctx->stream = ctx->own_stream;
+  CK(cudaDeviceGetAttribute(&ctx->smCount, cudaDevAttrMultiProcessorCount, ctx->device));
+
+  Consts& k = ctx->k;
+  std::memset(&k, 0, sizeof(k));
+  ctx->demSolve = cfg->demSolve != 0;
+  ctx->lbSolve = cfg->lbSolve != 0;
+  ctx->freeSurface = cfg->freeSurfaceSolve != 0;
+  ctx->demInitialRepeat = cfg->demInitialRepeat;
+  k.freeSurface = ctx->freeSurface ? 1 : 0;
+  k.forceField = cfg->forceFieldSolve != 0;
+  // measureUnits::setComposite
+  const double L = cfg->unitLength, T = cfg->unitTime, D = cfg->unitDensity;
+  k.uLength = L;
+  k.uTime = T;
+  k.uVolume = L * L * L;
+  k.uSpeed = L / T;
+  k.uAccel = L / T / T;
+  k.uAngVel = 1.0 / T;
+  const double uDynVisc = D * L * L / T;
+  k.uForce = D * L * L * L * L / T / T;
+  k.uTorque = D * L * L * L * L * L / T / T;
+  // lattice
+  k.X = int(std::floor(cfg->lbSizeX / L + 0.5));
+  k.Y = int(std::floor(cfg->lbSizeY / L + 0.5));
+  k.Z = int(std::floor(cfg->lbSizeZ / L + 0.5));
+  if (k.X < 3 || k.Y < 3 || k.Z < 3) return setErr(ctx, LBDEM_ERR_INVALID, "lattice too small");
+  k.N = (long long)k.X * k.Y * k.Z;
+  if (k.N >= (1ll << 32) / Q) return setErr(ctx, LBDEM_ERR_INVALID, "lattice too large");
+  k.sy = k.X;
+  k.sz = (long long)k.X * k.Y;
+  k.initDensity = 1.0;
+  k.initVisc = cfg->initVisc / uDynVisc;
+  k.omega = 1.0 / (0.5 + 3.0 * k.initVisc);
+  k.omegaf = 1.0 - 1.0 / (1.0 + 6.0 * k.initVisc);
+  for (int a = 0; a < 3; ++a) {
+    k.lbF[a] = cfg->lbF[a] / k.uAccel;
+    ctx->lbFConfig[a] = k.lbF[a];
+    k.initVel[a] = cfg->initVelocity[a] / k.uSpeed;
+  }
+  const unsigned s[3] = {(unsigned)k.X, (unsigned)k.Y, (unsigned)k.Z};
+  double phys[3];
+  for (int a = 0; a < 3; ++a) phys[a] = double(s[a]) * L;
+  double bloc[6][3] = {{0.5 * L, 0, 0}, {double(s[0] - 1.5) * L, 0, 0},
+                       {0, 0.5 * L, 0}, {0, double(s[1] - 1.5) * L, 0},
+                       {0, 0, 0.5 * L}, {0, 0, double(s[2] - 1.5) * L}};
+  const double dirs[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+  // DEM::discreteElementInit
+  k.demSize[0] = phys[0];
+  k.demSize[1] = ctx->freeSurface ? cfg->fluidHeight : phys[1];
+  k.demSize[2] = phys[2];
+  const double demF[3] = {k.lbF[0] * k.uAccel, k.lbF[1] * k.uAccel, k.lbF[2] * k.uAccel};
+  const int P = cfg->n_particles, O = cfg->n_objects;
+  ctx->nPart = P;
+  ctx->nObj = O;
+  k.nPart = P;
+  k.nObj = O;
+  std::vector<double> hx0(3 * P), hx1(3 * P, 0.0), hw1(3 * P, 0.0), hr(P), hinvm(P), hinvI(P),
+      hFG(3 * P);
+  double meanR = 0.0, rmax = 0.0;
+  for (int i = 0; i < P; ++i) {
+    const lbdem_particle_in& q = cfg->particles[i];
+    const double r = q.r;
+    const double singleMass = 4.0 / 3.0 * cfg->density * PI_D * r * r * r;
+    const double m = (unsigned)q.size * singleMass;
+    const double I = (unsigned)q.size * 2.0 / 5.0 * singleMass * r * r;
+    hr[i] = r;
+    hinvm[i] = 1.0 / m;
+    hinvI[i] = 1.0 / I;
+    for (int a = 0; a < 3; ++a) {
+      hx0[a * P + i] = q.x[a];
+      hFG[a * P + i] = demF[a] * m;
+    }
+    meanR += r;
+    rmax = rmax > r ? rmax : r;
+  }
+  if (P > 0) meanR /= double(P);
+  k.dt = T / double(1);
+  k.k = cfg->linearStiff;
+  const double avgMass = 4.0 / 3.0 * cfg->density * PI_D * meanR * meanR * meanR;
+  k.c = std::sqrt(avgMass * cfg->linearStiff);
+  k.mu = cfg->frictionCoefPart;
+  k.kinVisc = cfg->kinVisc;
+  k.lubN = cfg->lubNormal;
+  k.lubT = cfg->lubTangential;
+  k.lubR = cfg->lubRotation;
+  k.lubCut = cfg->lubCutoff;
+  k.electro = cfg->electroForce;
+  k.debye = cfg->debyeLength;
+  k.objWaitTime = cfg->objWaitTime;
+  std::vector<double> hobj((size_t)std::max(O, 1) * OB_STRIDE, 0.0);
+  for (int o = 0; o < O; ++o) {
+    const lbdem_object_in& in = cfg->objects[o];
+    double* ob = &hobj[(size_t)o * OB_STRIDE];
+    const double r = in.r;
+    const double m = 4.0 / 3.0 * cfg->objectDensity * PI_D * r * r * r;
+    const double I = 2.0 / 5.0 * m * r * r;
+    for (int a = 0; a < 3; ++a) {
+      ob[OB_X0 + a] = in.x[a];
+      ob[OB_X0PREV + a] = in.x[a];
+      ob[OB_X1 + a] = in.v[a];
+      ob[OB_FGRAV + a] = demF[a] * m;
+    }
+    ob[OB_R] = r;
+    ob[OB_INVM] = 1.0 / m;
+    ob[OB_INVI] = 1.0 / I;
+    ob[OB_INDEX] = (double)in.index;
+    ctx->objIndexField[o] = in.index;
+  }
+  // walls (DEM::initializeWalls: slip/moving flags of boundary[0] for all)
+  std::vector<DeviceWall> hw;
+  std::vector<int> hwt;
+  for (int i = 0; i < 6; ++i)
+    if (cfg->boundary[i] >= 5 && cfg->boundary[i] <= 8) {
+      DeviceWall w;
+      for (int a = 0; a < 3; ++a) {
+        w.p[a] = bloc[i][a];
+        w.n[a] = dirs[i][a];
+      }
+      hw.push_back(w);
+      const int b0 = cfg->boundary[0];
+      const bool slip = b0 == 5 || b0 == 6, moving = b0 == 6 || b0 == 8;
+      hwt.push_back(slip ? (moving ? 6 : 5) : (moving ? 8 : 7));
+    }
+  ctx->nWall = (int)hw.size();
+  k.nWall = ctx->nWall;
+  // neighbour-list geometry (fixed: radii and the DEM box do not change)
+  const double cut = 2.0 * rmax + 2.0;
+  const int nl[3] = {(int)(k.demSize[0] / cut), (int)(k.demSize[1] / cut),
+                     (int)(k.demSize[2] / cut)};
+  const int direct = std::min(nl[0], nl[1]) < 3 ? 1 : 0;
+  if (!direct && (long long)nl[0] * nl[1] * nl[2] > MAX_L)
+    return setErr(ctx, LBDEM_ERR_OVERFLOW, "more than 100000 neighbour cells");
+
+  // ---- allocation ----
+  Device& d = ctx->d;
+  const size_t N = (size_t)k.N;
+  int rc;
+#define AL(ptr, n)                                      \
+  if ((rc = dalloc(ctx, &(ptr), (n))) != LBDEM_OK) return rc;
+  AL(d.mask, N);
+  AL(d.solid, N);
+  AL(d.objIdx, N);
+  AL(d.claim, N);
+  AL(d.fsflag, N);
+  double* f0 = nullptr;
+  double* f1 = nullptr;
+  AL(f0, (size_t)Q * N);
+  AL(f1, (size_t)Q * N);
+  d.f[0] = f0;
+  d.f[1] = f1;
+  AL(d.mass, N);
+  AL(d.massNew, N);
+  AL(d.rhoS, N);
+  AL(d.uS, 3 * N);
+  AL(d.hS, 3 * N);
+  AL(d.scal, SC_COUNT);
+  AL(d.iscal, IS_COUNT);
+  AL(d.uscal, US_COUNT);
+  const size_t P1 = (size_t)std::max(P, 1);
+  AL(d.px0, 3 * P1);
+  AL(d.px1, 3 * P1);
+  AL(d.pw1, 3 * P1);
+  AL(d.pr, P1);
+  AL(d.pinvm, P1);
+  AL(d.pinvI, P1);
+  // hydro accumulators contiguous (reset together each LB step)
+  double* hyd = nullptr;
+  AL(hyd, 16 * P1);
+  d.pFHydro = hyd;
+  d.pMHydro = hyd + 3 * P1;
+  d.pSHydro = hyd + 6 * P1;
+  d.pFluidVol = hyd + 15 * P1;
+  AL(d.pFContact, 3 * P1);
+  AL(d.pMContact, 3 * P1);
+  AL(d.pFLub, 3 * P1);
+  AL(d.pMLub, 3 * P1);
+  AL(d.pFRep, 3 * P1);
+  AL(d.pFTotal, 3 * P1);
+  AL(d.pMTotal, 3 * P1);
+  AL(d.pFGrav, 3 * P1);
+  AL(d.pxiw, 3 * P1);
+  AL(d.pxio, 3 * P1);
+  AL(d.plist[0], P1 * MAX_N);
+  AL(d.plist[1], P1 * MAX_N);
+  AL(d.pxi[0], P1 * 3 * MAX_N);
+  AL(d.pxi[1], P1 * 3 * MAX_N);
+  AL(d.partner, P1 * MAX_N);
+  AL(d.gorder, P1 * MAX_N);
+  AL(d.pairbuf, P1 * MAX_N * PAIR_VALS);
+  AL(d.pairflag, P1 * MAX_N);
+  AL(d.pcell, P1);
+  AL(d.ppos, P1);
+  AL(d.cellCount, (size_t)MAX_L);
+  AL(d.cellStart, (size_t)MAX_L);
+  AL(d.cellFill, (size_t)MAX_L);
+  AL(d.cellParts, P1);
+  AL(d.obj, (size_t)std::max(O, 1) * OB_STRIDE);
+  AL(d.wallF, (size_t)MAX_WALL * 12);
+  AL(d.walls, (size_t)MAX_WALL);
+  AL(d.uncover, (size_t)UNCOVER_CAP);
+  int* dBoundary = nullptr;
+  int* dWallType = nullptr;
+  AL(dBoundary, 6);
+  AL(dWallType, MAX_WALL);
+#undef AL
+  cudaStream_t st = ctx->stream;
+  // ---- uploads ----
+  CK(cudaMemcpyAsync(d.px0, hx0.data(), 3 * P * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.pr, hr.data(), P * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.pinvm, hinvm.data(), P * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.pinvI, hinvI.data(), P * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.pFGrav, hFG.data(), 3 * P * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.obj, hobj.data(), hobj.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (!hw.empty()) {
+    CK(cudaMemcpyAsync(d.walls, hw.data(), hw.size() * sizeof(DeviceWall), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dWallType, hwt.data(), hwt.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  }
+  CK(cudaMemcpyAsync(dBoundary, cfg->boundary, 6 * sizeof(int), cudaMemcpyHostToDevice, st));
+  std::vector<int> iscal0(IS_COUNT, 0);
+  iscal0[IS_NL] = nl[0];
+  iscal0[IS_NL + 1] = nl[1];
+  iscal0[IS_NL + 2] = nl[2];
+  iscal0[IS_DIRECT] = direct;
+  CK(cudaMemcpyAsync(d.iscal, iscal0.data(), IS_COUNT * sizeof(int), cudaMemcpyHostToDevice, st));
+  const unsigned long long none = ~0ull;
+  CK(cudaMemcpyAsync(d.uscal + US_FIRSTFLAG, &none, sizeof(none), cudaMemcpyHostToDevice, st));
+  // ---- LB::latticeBolzmannInit on the device ----
+  const int lg = latticeGrid(ctx);
+  if (ctx->lbSolve) {
+    initTypes<<<lg, 256, 0, st>>>(k, d.mask, d.solid, d.objIdx, dBoundary, d.walls, dWallType,
+                                  d.obj, cfg->fluidHeight / L, k.freeSurface);
+    initFields<<<lg, 256, 0, st>>>(k, d.mask, (double*)d.f[0], d.mass);
+    if ((rc = launchErr(ctx, "lattice init")) != LBDEM_OK) return rc;
+  }
+  // ---- initial neighbour list (DEM::discreteElementInit, :294-296) ----
+  {
+    DemArgs a = demArgs(ctx);
+    demBegin<<<1, 1024, 0, st>>>(k, a, 1);
+    if ((rc = enqueueNeighbourList(ctx)) != LBDEM_OK) return rc;
+  }
+  CK(cudaStreamSynchronize(st));
+  cudaFree(dBoundary);
+  cudaFree(dWallType);
+  int e = 0;
+  CK(cudaMemcpy(&e, d.iscal + IS_ERROR, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) return setErr(ctx, LBDEM_ERR_DEVICE_STATE, "device error during init: " + std::to_string(e));
+  return LBDEM_OK;
+}
+
+extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
+  if (!ctx) return;
+  Device& d = ctx->d;
+  void* ptrs[] = {d.mask, d.solid, d.objIdx, d.claim, d.fsflag, d.f[0], d.f[1], d.mass,
+                  d.massNew, d.rhoS, d.uS, d.hS, d.scal, d.iscal, d.uscal, d.px0, d.px1,
+                  d.pw1, d.pr, d.pinvm, d.pinvI, d.pFHydro, d.pFContact, d.pMContact,
+                  d.pFLub, d.pMLub, d.pFRep, d.pFTotal, d.pMTotal, d.pFGrav, d.pxiw,
+                  d.pxio, d.plist[0], d.plist[1], d.pxi[0], d.pxi[1], d.partner, d.gorder,
+                  d.pairbuf, d.pairflag, d.pcell, d.ppos, d.cellCount, d.cellStart,
+                  d.cellFill, d.cellParts, d.obj, d.wallF, d.walls, d.uncover};
+  if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+}
+
+extern "C" const char* lbdem_last_error(const lbdem_ctx* ctx) {
+  return ctx ? ctx->err.c_str() : "null context";
+}
+
+extern "C" int lbdem_set_stream(lbdem_ctx* ctx, void* stream) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  return LBDEM_OK;
+}
+
+// DEM::discreteElementStep (multiStep = 1)
+extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  ++ctx->demTimeStep;
+  ctx->demTime += ctx->k.dt;
+  const Consts& k = ctx->k;
+  DemArgs a = demArgs(ctx);
+  cudaStream_t s = ctx->stream;
+  demBegin<<<1, 1024, 0, s>>>(k, a, 0);
+  int rc = enqueueNeighbourList(ctx);
+  if (rc) return rc;
+  const int step = (int)ctx->demTimeStep;
+  const int lubOn = step >= k.objWaitTime ? 1 : 0;
+  demPairs<<<partGrid(ctx, 128), 128, 0, s>>>(k, a, lubOn);
+  demGather<<<partGrid(ctx, 128), 128, 0, s>>>(k, a, step);
+  demObjects<<<1, 32, 0, s>>>(k, a, step);
+  return launchErr(ctx, "dem step");
+}
+
+// LB::latticeBoltzmannCouplingStep
+extern "C" int lbdem_coupling_step(lbdem_ctx* ctx) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  const Consts& k = ctx->k;
+  Device& d = ctx->d;
+  cudaStream_t s = ctx->stream;
+  const int lg = latticeGrid(ctx);
+  if (ctx->nObj > 0) {
+    cudaMemsetAsync(d.iscal + IS_NUNCOVER, 0, sizeof(int), s);
+    uncoverCollect<<<lg, 256, 0, s>>>(k, d.mask, d.obj, d.uncover, d.iscal);
+    uncoverResolve<<<1, 1024, 0, s>>>(k, d.mask, (double*)d.f[ctx->cur], d.mass, d.uncover,
+                                      d.iscal);
+    voxelizeObjects<<<lg, 256, 0, s>>>(k, d.mask, d.solid, d.objIdx, d.mass, d.obj);
+  }
+  flagClaim<<<partGrid(ctx, 4) , 128, 0, s>>>(k, d.mask, d.claim, d.px0, d.pr, d.iscal, d.uscal);
+  flagApply<<<lg, 256, 0, s>>>(k, d.mask, d.solid, d.claim, d.iscal, d.uscal);
+  findNewActiveKernel<<<1, 1024, 0, s>>>(k, d.mask, d.solid, d.px0, d.pr, d.iscal, d.uscal);
+  return launchErr(ctx, "coupling step");
+}
+
+// LB::latticeBolzmannStep
+extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  if (!ctx->k.forceField && !ctx->lbFReset) {  // LB::collision, src/LB.cpp:1303-1305
+    ctx->lbFReset = true;
+    ctx->k.lbF[0] = ctx->k.lbF[1] = ctx->k.lbF[2] = 0.0;
+  }
+  const Consts& k = ctx->k;
+  Device& d = ctx->d;
+  cudaStream_t s = ctx->stream;
+  const int P1 = std::max(ctx->nPart, 1);
+  lbResetKernel<<<std::max(1, std::min(16 * P1 / 256 + 1, 1024)), 256, 0, s>>>(
+      k, d.pFHydro, 16LL * P1, d.obj, d.wallF, d.scal, d.iscal);
+  LbArgs a = lbArgs(ctx);
+  lbStepFp64<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
+  lbFinalizeKernel<<<std::max(1, std::min(P1 / 256 + 1, 256)), 256, 0, s>>>(
+      k, d.pFHydro, d.pMHydro, d.pFluidVol, d.obj, d.wallF, d.scal, d.iscal);
+  ctx->cur = 1 - ctx->cur;
+  if (ctx->freeSurface) lbRedistribute<<<ctx->smCount * 4, 256, 0, s>>>(k, fsArgs(ctx));
+  return launchErr(ctx, "lb step");
+}
+
+// LB::latticeBoltzmannFreeSurfaceStep
+extern "C" int lbdem_free_surface_step(lbdem_ctx* ctx) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  const Consts& k = ctx->k;
+  Device& d = ctx->d;
+  cudaStream_t s = ctx->stream;
+  const int g = ctx->smCount * 4;
+  FsArgs a = fsArgs(ctx);
+  fsResetKernel<<<1, 1, 0, s>>>(d.scal, d.iscal);
+  fsUpdateMass<<<g, 256, 0, s>>>(k, a);
+  fsMutants<<<g, 256, 0, s>>>(k, a);
+  fsSmoothen<<<g, 256, 0, s>>>(k, a);
+  fsMutantsAndFill<<<g, 256, 0, s>>>(k, a);
+  fsEmptyIsolated<<<g, 256, 0, s>>>(k, a);
+  fsRedistribute<<<g, 256, 0, s>>>(k, a);
+  return launchErr(ctx, "free-surface step");
+}
+
+// goCycle, src/main.cpp:38-67 (without IO)
+extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  for (int32_t i = 0; i < n; ++i) {
+    ++ctx->lbTime;
+    int rc = LBDEM_OK;
+    if (ctx->demSolve && (rc = lbdem_dem_step(ctx))) return rc;
+    if (ctx->lbSolve && ctx->demTime >= ctx->demInitialRepeat) {
+      if (ctx->demSolve && (rc = lbdem_coupling_step(ctx))) return rc;
+      if ((rc = lbdem_lb_step(ctx))) return rc;
+      if (ctx->freeSurface && (rc = lbdem_free_surface_step(ctx))) return rc;
+    } else if (ctx->lbSolve && ctx->demTime <= ctx->demInitialRepeat) {
+      if (ctx->demSolve && (rc = lbdem_coupling_step(ctx))) return rc;
+    }
+    if (ctx->check_every > 0 && ctx->lbTime % ctx->check_every == 0 && ctx->lbSolve)
+      nonfiniteCheck<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(
+          ctx->k, ctx->d.mask, (const double*)ctx->d.f[ctx->cur], ctx->d.iscal);
+  }
+  return LBDEM_OK;
+}
+
+extern "C" int lbdem_sync(lbdem_ctx* ctx) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  CK(cudaStreamSynchronize(ctx->stream));
+  int e = 0;
+  CK(cudaMemcpy(&e, ctx->d.iscal + IS_ERROR, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    std::string m = "device error bits " + std::to_string(e) + ":";
+    if (e & ERR_TYPE) m += " streaming-type";
+    if (e & ERR_NBR_OVERFLOW) m += " neighbour-list-overflow";
+    if (e & ERR_CELL_OVERFLOW) m += " cell-overflow";
+    if (e & ERR_UNCOVER_CAP) m += " uncover-capacity";
+    if (e & ERR_PARTICLE_INDEX) m += " particle-index";
+    if (e & ERR_NONFINITE) m += " non-finite";
+    if (e & ERR_GRID) m += " particle-outside-grid";
+    const int code = (e & ERR_NONFINITE) ? LBDEM_ERR_NONFINITE
+                   : (e & (ERR_NBR_OVERFLOW | ERR_CELL_OVERFLOW | ERR_UNCOVER_CAP))
+                       ? LBDEM_ERR_OVERFLOW
+                       : LBDEM_ERR_DEVICE_STATE;
+    return setErr(ctx, code, m);
+  }
+  return LBDEM_OK;
+}
+
+extern "C" int lbdem_get_info(lbdem_ctx* ctx, lbdem_info* info) {
+  if (!ctx || !info) return LBDEM_ERR_INVALID;
+  std::memset(info, 0, sizeof(*info));
+  info->lb_size[0] = ctx->k.X;
+  info->lb_size[1] = ctx->k.Y;
+  info->lb_size[2] = ctx->k.Z;
+  info->nodes = ctx->k.N;
+  info->n_particles = ctx->nPart;
+  info->n_objects = ctx->nObj;
+  info->n_walls = ctx->nWall;
+  info->precision = ctx->precision;
+  info->time_step = ctx->lbTime;
+  info->dem_step = ctx->demTimeStep;
+  info->dem_time = ctx->demTime;
+  info->unit_length = ctx->k.uLength;
+  info->unit_time = ctx->k.uTime;
+  info->device_bytes = ctx->deviceBytes;
+  int rb = 0;
+  cudaStreamSynchronize(ctx->stream);
+  cudaMemcpy(&rb, ctx->d.iscal + IS_REBUILDS, sizeof(int), cudaMemcpyDeviceToHost);
+  info->neighbour_rebuilds = rb;
+  return LBDEM_OK;
+}
+
+namespace {
+int d2h(lbdem_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  if (!dst) return LBDEM_OK;
+  CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+  return LBDEM_OK;
+}
+// [3][P] device -> [P][3] host
+int d2h3(lbdem_ctx* ctx, double* dst, const double* src, int P) {
+  if (!dst) return LBDEM_OK;
+  std::vector<double> tmp(3 * (size_t)P);
+  CK(cudaMemcpy(tmp.data(), src, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < P; ++i)
+    for (int c = 0; c < 3; ++c) dst[3 * i + c] = tmp[(size_t)c * P + i];
+  return LBDEM_OK;
+}
+}  // namespace
+
+extern "C" int lbdem_download_lattice(lbdem_ctx* ctx, uint8_t* type, uint8_t* pflag,
+                                      int32_t* solid, double* n, double* u, double* mass,
+                                      double* f) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  int rc = lbdem_sync(ctx);
+  if (rc) return rc;
+  const size_t N = (size_t)ctx->k.N;
+  Device& d = ctx->d;
+  if (type || pflag) {
+    std::vector<uint8_t> m(N);
+    CK(cudaMemcpy(m.data(), d.mask, N, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < N; ++i) {
+      if (type) type[i] = m[i] & TYPE_MASK;
+      if (pflag) pflag[i] = (m[i] & PFLAG) ? 1 : 0;
+    }
+  }
+  if ((rc = d2h(ctx, solid, d.solid, N * 4))) return rc;
+  if ((rc = d2h(ctx, mass, d.mass, N * 8))) return rc;
+  if (f) {
+    std::vector<double> fv((size_t)Q * N);
+    CK(cudaMemcpy(fv.data(), d.f[ctx->cur], fv.size() * 8, cudaMemcpyDeviceToHost));
+    std::vector<uint8_t> m(N);
+    CK(cudaMemcpy(m.data(), d.mask, N, cudaMemcpyDeviceToHost));
+    for (size_t j = 0; j < (size_t)Q; ++j)
+      for (size_t i = 0; i < N; ++i) {
+        const int t = m[i] & TYPE_MASK;
+        f[j * N + i] = (t == 0 || t == 3) ? fv[j * N + i] : 0.0;
+      }
+  }
+  if (n || u) {
+    double* tmp = nullptr;
+    CK(cudaMalloc(&tmp, 4 * N * sizeof(double)));
+    momentsKernel<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(ctx->k, d.mask,
+                                                             (const double*)d.f[ctx->cur], tmp,
+                                                             tmp + N);
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (n) CK(cudaMemcpy(n, tmp, N * 8, cudaMemcpyDeviceToHost));
+    if (u) CK(cudaMemcpy(u, tmp + N, 3 * N * 8, cudaMemcpyDeviceToHost));
+    cudaFree(tmp);
+  }
+  return LBDEM_OK;
+}
+
+extern "C" int lbdem_download_particles(lbdem_ctx* ctx, const lbdem_particle_view* v) {
+  if (!ctx || !v) return LBDEM_ERR_INVALID;
+  int rc = lbdem_sync(ctx);
+  if (rc) return rc;
+  Device& d = ctx->d;
+  const int P = ctx->nPart;
+  if (P == 0) return LBDEM_OK;
+  const struct { double* dst; const double* src; } m3[] = {
+      {v->x0, d.px0},         {v->x1, d.px1},         {v->w1, d.pw1},
+      {v->FHydro, d.pFHydro}, {v->MHydro, d.pMHydro}, {v->FContact, d.pFContact},
+      {v->MContact, d.pMContact}, {v->FLub, d.pFLub}, {v->MLub, d.pMLub},
+      {v->FRep, d.pFRep},     {v->FTotal, d.pFTotal}, {v->MTotal, d.pMTotal},
+      {v->xiw, d.pxiw},       {v->xio, d.pxio}};
+  for (const auto& e : m3)
+    if ((rc = d2h3(ctx, e.dst, e.src, P))) return rc;
+  if ((rc = d2h(ctx, v->fluidVolume, d.pFluidVol, (size_t)P * 8))) return rc;
+  if (v->SHydro) {
+    std::vector<double> tmp(9 * (size_t)P);
+    CK(cudaMemcpy(tmp.data(), d.pSHydro, tmp.size() * 8, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < P; ++i)
+      for (int c = 0; c < 9; ++c) v->SHydro[9 * i + c] = tmp[(size_t)c * P + i];
+  }
+  int cur = 0;
+  CK(cudaMemcpy(&cur, d.iscal + IS_LISTCUR, sizeof(int), cudaMemcpyDeviceToHost));
+  if ((rc = d2h(ctx, v->list, d.plist[cur], (size_t)P * MAX_N * 4))) return rc;
+  if ((rc = d2h(ctx, v->xi, d.pxi[cur], (size_t)P * 3 * MAX_N * 8))) return rc;
+  return LBDEM_OK;
+}
+
+extern "C" int lbdem_download_objects(lbdem_ctx* ctx, const lbdem_object_view* v) {
+  if (!ctx || !v) return LBDEM_ERR_INVALID;
+  int rc = lbdem_sync(ctx);
+  if (rc) return rc;
+  const int O = ctx->nObj;
+  std::vector<double> h((size_t)std::max(O, 1) * OB_STRIDE);
+  CK(cudaMemcpy(h.data(), ctx->d.obj, h.size() * 8, cudaMemcpyDeviceToHost));
+  const struct { double* dst; int off; } m[] = {
+      {v->x0, OB_X0},       {v->x1, OB_X1},       {v->w1, OB_W1},
+      {v->FHydro, OB_FHYDRO}, {v->MHydro, OB_MHYDRO}, {v->FContact, OB_FCONTACT},
+      {v->MContact, OB_MCONTACT}, {v->FLub, OB_FLUB}, {v->MLub, OB_MLUB},
+      {v->FTotal, OB_FTOTAL}};
+  for (const auto& e : m)
+    if (e.dst)
+      for (int o = 0; o < O; ++o)
+        for (int c = 0; c < 3; ++c) e.dst[3 * o + c] = h[(size_t)o * OB_STRIDE + e.off + c];
+  return LBDEM_OK;
+}
+
+extern "C" int lbdem_download_walls(lbdem_ctx* ctx, double* FHydro, double* FContact,
+                                    double* FLub, double* FTotal) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  int rc = lbdem_sync(ctx);
+  if (rc) return rc;
+  const int W = ctx->nWall;
+  std::vector<double> h((size_t)MAX_WALL * 12);
+  CK(cudaMemcpy(h.data(), ctx->d.wallF, h.size() * 8, cudaMemcpyDeviceToHost));
+  double* outs[4] = {FHydro, FContact, FLub, FTotal};
+  for (int q = 0; q < 4; ++q)
+    if (outs[q])
+      for (int w = 0; w < W; ++w)
+        for (int c = 0; c < 3; ++c) outs[q][3 * w + c] = h[(size_t)w * 12 + 3 * q + c];
+  return LBDEM_OK;
+}
+
+extern "C" int lbdem_mass_summary(lbdem_ctx* ctx, double* total_mass,
+                                  int64_t* interface_nodes, int64_t* active_nodes) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  int rc = lbdem_sync(ctx);
+  if (rc) return rc;
+  double* tmp = nullptr;
+  CK(cudaMalloc(&tmp, 3 * sizeof(double)));
+  CK(cudaMemset(tmp, 0, 3 * sizeof(double)));
+  massSummaryKernel<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(
+      ctx->k, ctx->d.mask, ctx->d.mass, tmp, (unsigned long long*)(tmp + 1));
+  CK(cudaStreamSynchronize(ctx->stream));
+  double m = 0;
+  unsigned long long c[2] = {0, 0};
+  CK(cudaMemcpy(&m, tmp, 8, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(c, tmp + 1, 16, cudaMemcpyDeviceToHost));
+  cudaFree(tmp);
+  if (total_mass) *total_mass = m;
+  if (interface_nodes) *interface_nodes = (int64_t)c[0];
+  if (active_nodes) *active_nodes = (int64_t)c[1];
+  return LBDEM_OK;
+}

@@ -1,0 +1,162 @@
+// Internal definitions shared by the CUDA translation units of liblbdem.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "lbdem.h"
+
+namespace lbdem {
+
+constexpr int Q = 19;
+constexpr int MAX_N = 50;        // neighbour-list slots, src/DEM.cpp:476
+constexpr int MAX_L = 100000;    // cell-list cells,     src/DEM.cpp:479
+constexpr int MAX_OBJ = 8;       // impactors handled on the device
+constexpr int MAX_WALL = 6;
+constexpr int PAIR_VALS = 18;    // per neighbour slot: contact(6) lub(9) rep(3)
+constexpr int UNCOVER_CAP = 8192;// uncovered object nodes resolved per step
+
+// mask byte layout
+constexpr uint8_t TYPE_MASK = 0x0F;
+constexpr uint8_t PFLAG = 0x10;   // inside a particle (nodeType::p)
+constexpr uint8_t ABIT = 0x20;    // member of the last active list (cleanLists)
+
+// device error bits
+enum : int {
+  ERR_TYPE = 1,          // streaming met a type the reference cannot stream to
+  ERR_NBR_OVERFLOW = 2,  // > 49 neighbours
+  ERR_CELL_OVERFLOW = 4, // > 50 particles in a cell or too many cells
+  ERR_UNCOVER_CAP = 8,   // too many uncovered object nodes in one step
+  ERR_PARTICLE_INDEX = 16,
+  ERR_NONFINITE = 32,
+  ERR_GRID = 64,         // particle outside the cell grid
+};
+
+// Physical / lattice constants of one run (passed by value to kernels).
+struct Consts {
+  int X, Y, Z;
+  long long N;
+  long long sy, sz;  // strides of y and z
+  int freeSurface, forceField;
+  double uLength, uTime, uSpeed, uAccel, uAngVel, uForce, uTorque, uVolume;
+  double initDensity, initVisc;
+  double omega, omegaf;  // 1/(0.5+3 visc), 1-1/(1+6 visc) (src/node.cpp:183,196)
+  double lbF[3];        // after the forceField reset rule of LB::collision
+  double initVel[3];
+  int nObj, nWall, nPart;
+  // DEM
+  double demSize[3];
+  double dt;
+  double k, c, mu, kinVisc, lubN, lubT, lubR, lubCut, electro, debye;
+  int objWaitTime;
+};
+
+struct DeviceWall {
+  double p[3], n[3];
+};
+
+// All device allocations of one run.
+struct Device {
+  // lattice
+  uint8_t* mask = nullptr;
+  uint32_t* solid = nullptr;
+  uint8_t* objIdx = nullptr;   // object whose velocity an object node carries
+  uint32_t* claim = nullptr;   // particle claims during updateIndices
+  uint8_t* fsflag = nullptr;   // transient free-surface flags
+  void* f[2] = {nullptr, nullptr};  // distributions, ping-pong
+  double* mass = nullptr;
+  double* massNew = nullptr;
+  double* rhoS = nullptr;      // density of interface nodes
+  double* uS = nullptr;        // shifted velocity of interface nodes [3][N]
+  double* hS = nullptr;        // hydrodynamic force of interface nodes [3][N]
+  // scalars / reductions (double unless noted)
+  double* scal = nullptr;      // see SC_* offsets
+  int* iscal = nullptr;        // see IS_* offsets
+  unsigned long long* uscal = nullptr;
+  // particles (SoA, [3][P] for vectors)
+  double *px0 = nullptr, *px1 = nullptr, *pw1 = nullptr;
+  double *pr = nullptr, *pinvm = nullptr, *pinvI = nullptr;
+  double *pFHydro = nullptr, *pMHydro = nullptr, *pFluidVol = nullptr, *pSHydro = nullptr;
+  double *pFContact = nullptr, *pMContact = nullptr, *pFLub = nullptr, *pMLub = nullptr;
+  double *pFRep = nullptr, *pFTotal = nullptr, *pMTotal = nullptr, *pFGrav = nullptr;
+  double *pxiw = nullptr, *pxio = nullptr;
+  int* plist[2] = {nullptr, nullptr};    // [P][50]
+  double* pxi[2] = {nullptr, nullptr};   // [P][3][50]
+  int* partner = nullptr;                // [P][50] slot of i in list[j]
+  int* gorder = nullptr;                 // [P][50] gather order of slots
+  double* pairbuf = nullptr;             // [P][50][PAIR_VALS]
+  uint8_t* pairflag = nullptr;           // [P][50] bit0 = lubrication valid
+  int* pcell = nullptr;                  // [P] cell of particle
+  int* ppos = nullptr;                   // [P] position in its cell (1-based)
+  int* cellCount = nullptr;              // [MAX_L]
+  int* cellStart = nullptr;              // [MAX_L]
+  int* cellFill = nullptr;               // [MAX_L]
+  int* cellParts = nullptr;              // [P]
+  // objects / walls (small)
+  double* obj = nullptr;                 // see OB_* layout, [nObj][OB_STRIDE]
+  double* wallF = nullptr;               // [W][12]: FHydro FContact FLub FTotal
+  DeviceWall* walls = nullptr;
+  uint32_t* uncover = nullptr;           // [UNCOVER_CAP] candidate list
+};
+
+// offsets into Device::scal (doubles)
+enum {
+  SC_EXTRA_MASS = 0,  // bounce-back extra mass of this LB step
+  SC_ADD_MASS,        // extraMass / #interface
+  SC_SURPLUS,         // free-surface mass surplus
+  SC_MAXDISP,         // DEM::maxDisp
+  SC_TOTAL_MASS,      // diagnostics
+  SC_COUNT
+};
+// offsets into Device::iscal (ints)
+enum {
+  IS_ERROR = 0,
+  IS_NEWNBR,        // DEM::newNeighborList
+  IS_REBUILD,       // neighbour list rebuild requested in this DEM step
+  IS_NIF,           // interface count after the LB step (redistribution)
+  IS_NIF2,          // interface count after removeIsolated
+  IS_BBOX,          // 6 ints: xmin,ymin,zmin,xmax,ymax,zmax of interface nodes
+  IS_NUNCOVER = IS_BBOX + 6,
+  IS_NL = IS_NUNCOVER + 1,  // 3 ints: nlx, nly, nlz
+  IS_DIRECT = IS_NL + 3,    // direct-sum branch in use
+  IS_LISTCUR,               // which list buffer is current
+  IS_REBUILDS,              // rebuild counter
+  IS_COUNT
+};
+// offsets into Device::uscal
+enum { US_FIRSTFLAG = 0, US_COUNT };
+
+// object record layout (doubles)
+enum {
+  OB_X0 = 0, OB_X1 = 3, OB_W1 = 6, OB_R = 9, OB_INVM = 10, OB_INVI = 11,
+  OB_FHYDRO = 12, OB_MHYDRO = 15, OB_FCONTACT = 18, OB_MCONTACT = 21,
+  OB_FLUB = 24, OB_MLUB = 27, OB_FGRAV = 30, OB_FTOTAL = 33, OB_MTOTAL = 36,
+  OB_X0PREV = 39, OB_INDEX = 42, OB_STRIDE = 44
+};
+
+}  // namespace lbdem
+
+struct lbdem_ctx {
+  std::string err;
+  lbdem::Consts k{};
+  lbdem::Device d;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  int device = 0;
+  int precision = LBDEM_PLAIN_FP64;
+  int check_every = 0;
+  int cur = 0;  // current lattice buffer
+  // host-side mirrors of the reference's step counters
+  bool demSolve = false, lbSolve = false, freeSurface = false;
+  double demInitialRepeat = 0.0;
+  double demTime = 0.0;
+  long long demTimeStep = 0, lbTime = 0;
+  bool lbFReset = false;  // lbF reset by the first collision when !forceField
+  double lbFConfig[3] = {0, 0, 0};
+  int nPart = 0, nObj = 0, nWall = 0;
+  int objIndexField[lbdem::MAX_OBJ] = {0};
+  long long deviceBytes = 0;
+  int smCount = 0;
+};

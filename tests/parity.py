@@ -1,0 +1,79 @@
+"""Comparison of a GPU state against the oracle's state dump (same keys).
+
+Discrete state (node types, particle flags, solid indices, neighbour lists)
+must be identical. Floating-point state must agree to ``rtol`` relative to
+the field's own scale (the reductions over nodes and particles are summed
+in a different order than in the reference, everything else rounds
+identically).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+LATTICE_FLOAT = ("f", "mass")
+PARTICLE_FLOAT = ("p_x0", "p_x1", "p_w1", "p_FHydro", "p_MHydro", "p_FContact", "p_MContact",
+                  "p_FLub", "p_MLub", "p_FRep", "p_FTotal", "p_MTotal", "p_xiw", "p_xio",
+                  "p_fluidVolume", "p_SHydro")
+OBJECT_FLOAT = ("o_x0", "o_x1", "o_w1", "o_FHydro", "o_MHydro", "o_FContact", "o_FLub",
+                "o_FTotal")
+TORQUE_FORCE = {"o_MHydro": "o_FHydro", "o_w1": "o_x1", "p_MHydro": "p_FHydro",
+                "p_MContact": "p_FContact", "p_MLub": "p_FLub", "p_MTotal": "p_FTotal",
+                "p_w1": "p_x1"}
+LEVER = 10.0  # lattice units, of the order of the sphere radii
+
+
+def rel_err(a, b, scale=None):
+    a = np.asarray(a, float)
+    b = np.asarray(b, float)
+    if a.size == 0:
+        return 0.0
+    s = scale if scale is not None else max(float(np.max(np.abs(b))), 1e-300)
+    return float(np.max(np.abs(a - b))) / s
+
+
+def compare(gpu: dict, orc: dict, rtol: float = 1e-10, lattice: bool = True,
+            fluid_mass: bool = True) -> list[str]:
+    """fluid_mass=False skips the mass of fluid nodes: between the LB step
+    and the free-surface step the GPU already holds updateMass's fluid rule
+    (mass = density), which the reference applies in the free-surface step."""
+    bad: list[str] = []
+    if lattice:
+        for k in ("type", "pflag"):
+            if not np.array_equal(gpu[k], orc[k]):
+                n = int(np.sum(gpu[k] != orc[k]))
+                bad.append(f"{k}: {n} nodes differ")
+        if not np.array_equal(gpu["solid"], orc["solid"]):
+            bad.append(f"solid: {int(np.sum(gpu['solid'] != orc['solid']))} nodes differ")
+        act = (orc["type"] == 0) | (orc["type"] == 3)
+        for k in LATTICE_FLOAT:
+            sel = act if (fluid_mass or k != "mass") else (orc["type"] == 3)
+            g = gpu[k][..., sel]
+            o = orc[k][..., sel]
+            e = rel_err(g, o)
+            if not e <= rtol:
+                bad.append(f"{k}: rel err {e:.3e}")
+    for k in PARTICLE_FLOAT + OBJECT_FLOAT:
+        if k in orc and k in gpu:
+            scale = max(float(np.max(np.abs(orc[k]))) if orc[k].size else 0.0, 1e-300)
+            # a torque that cancels to ~0 is judged against force x lever arm
+            fk = TORQUE_FORCE.get(k)
+            if fk and fk in orc and orc[fk].size:
+                scale = max(scale, float(np.max(np.abs(orc[fk]))) * LEVER)
+            e = rel_err(gpu[k], orc[k], scale)
+            if not e <= rtol:
+                bad.append(f"{k}: rel err {e:.3e}")
+    # neighbour lists: the valid slots only (slots past the count are stale)
+    gl, ol = gpu["p_list"], orc["p_list"]
+    if not np.array_equal(gl[:, 0], ol[:, 0]):
+        bad.append("neighbour counts differ")
+    else:
+        for i in range(len(ol)):
+            c = ol[i, 0]
+            if not np.array_equal(gl[i, 1:c + 1], ol[i, 1:c + 1]):
+                bad.append(f"neighbour list of particle {i} differs")
+                break
+    e = rel_err(gpu["p_xi"][:, :, 1:], orc["p_xi"][:, :, 1:],
+                scale=max(float(np.max(np.abs(orc["p_xi"][:, :, 1:]))), 1e-12))
+    if not e <= rtol:
+        bad.append(f"p_xi: rel err {e:.3e}")
+    return bad
