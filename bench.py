@@ -1,0 +1,306 @@
+#!/usr/bin/env python
+"""Benchmark of the coupled free-surface LB / DEM impact step on GB300.
+
+One "step" is one goCycle of the reference (DEM step, coupling step, LB
+step, free-surface step) on the configured workload. ``value`` is the
+coupled MLUPS (active-node updates per second over the whole cycle) with the
+run resident in HBM; ``e2e`` is the same metric through the C ABI from host
+inputs (case upload, per-step impactor read-back). ``roofline`` covers the
+dominant kernel (the fused collide+stream lattice kernel), timed live with
+CUDA events on the stream it runs on. ``cpu_baseline`` times the CPU
+restatement of the reference algorithm on a bounded sample of the same
+workload.
+
+usage: python bench.py [--gpus N] [--steps K] [--warmup W]
+                       [--impl ours|reference] [--precision mixed|fp64]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "lbm-dem_gb300"))
+sys.path.insert(0, os.path.join(REPO, "tests"))
+
+CACHE = os.path.join(REPO, "bench_cache")
+WORKLOADS = {
+    "c2": "256x320x256 lattice (y vertical) filled to y=240, 25000 bidisperse spheres "
+          "(r 3.0/4.2, seeded RSA), impactor r=20 density 5 vy=-0.02, tau=0.6",
+    "c1": "64x80x64 lattice filled to y=60, 400 bidisperse spheres (r 3.0/4.2, seeded RSA), "
+          "impactor r=8 density 5 vy=-0.01, tau=0.8",
+}
+# Algorithmic bytes per active-node update of the lattice kernel: 19
+# populations read + 19 written, 8 B (plain FP64) or 4 B (FP32 storage).
+BYTES_PER_NODE = {"fp64": 304, "mixed": 152}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def case_path(workload: str) -> str:
+    import casegen
+    d = os.path.join(CACHE, workload)
+    cfg = os.path.join(d, "parameters.cfg")
+    if not os.path.exists(cfg):
+        log(f"generating workload {workload} ...")
+        casegen.named_case(workload).write(d)
+    return cfg
+
+
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            j = json.load(fh)
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(CACHE, f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)], stdout=self.fh,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.remove(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, v: float) -> float:
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(world, v: float) -> float:
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def upload_bytes(cfg) -> int:
+    c = cfg.cfg
+    P, O = c.n_particles, c.n_objects
+    return int(P * 8 * (3 + 1 + 1 + 1 + 3) + max(O, 1) * 44 * 8 + 6 * 48 + 6 * 4 + 6 * 4 + 8
+               + 32 * 4)
+
+
+def cpu_baseline(cfg, workload, warm=1, steps=2, budget_s=60.0) -> dict:
+    """Oracle (CPU restatement of the reference algorithm) on a bounded sample."""
+    import oracle_ffi
+    oracle_ffi.build_oracle()
+    orc = oracle_ffi.Oracle(cfg)
+    orc.cycle(warm)
+    done, upd, t0 = 0, 0, time.perf_counter()
+    while done < steps and time.perf_counter() - t0 < budget_s:
+        orc.cycle(1)
+        upd += orc.counters()[3]
+        done += 1
+    dt = time.perf_counter() - t0
+    orc.close()
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": round(upd / dt / 1e6, 4), "unit": "MLUPS", "cores": cores, "kind": "port",
+            "sample": f"{done} coupled steps of workload {workload} after {warm} warm-up step(s), "
+                      f"CPU restatement (oracle) with OpenMP on reconstruction/collision"}
+
+
+def run_reference(args, world, rank):
+    """Reference arm: the CPU restatement of the reference's algorithm (the
+    reference itself cannot be built on the GPU host), timed on the host."""
+    if rank != 0:
+        return
+    import lbdem
+    cfg = lbdem.LoadedConfig(case_path(args.workload))
+    cb = cpu_baseline(cfg, args.workload, warm=min(args.warmup, 1), steps=args.steps,
+                      budget_s=150.0)
+    line = {"impl": "reference", "metric": "coupled MLUPS", "value": cb["value"],
+            "unit": "MLUPS", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": args.workload,
+                                            "description": WORKLOADS[args.workload]},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import lbdem
+    torch.cuda.set_device(local)
+    prec = lbdem.MIXED if args.precision == "mixed" else lbdem.PLAIN_FP64
+    cfg = lbdem.LoadedConfig(case_path(args.workload))
+    K, W = args.steps, args.warmup
+
+    # ---- device-resident timed region ----
+    solver = lbdem.Solver(cfg, precision=prec, device=local)
+    stream = torch.cuda.Stream(device=local)
+    solver.set_stream(stream.cuda_stream)
+    solver.cycle(W)
+    solver.sync()
+    solver.profile_read(reset=True)
+    solver.profile_enable(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    solver.cycle(K)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    solver.sync()
+    ms = ev0.elapsed_time(ev1)
+    prof = solver.profile_read(reset=True)
+    ms_max = allmax(world, ms)
+    upd_all = allsum(world, float(prof.active_node_updates))
+    value = upd_all / (ms_max * 1e-3) / 1e6
+    info = solver.get_info()
+    solver.close()
+
+    # ---- end to end through the C ABI: upload, K cycles, per-step read-back ----
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s2 = lbdem.Solver(cfg, precision=prec, device=local)
+    s2.profile_read(reset=True)
+    for _ in range(K):
+        s2.cycle(1)
+        s2.objects()  # impactor state back to the host every step
+    p2 = s2.profile_read(reset=True)
+    t_e2e = time.perf_counter() - t0
+    s2.close()
+    e2e_val = allsum(world, float(p2.active_node_updates)) / allmax(world, t_e2e) / 1e6
+
+    peak, peak_kind = peaks()
+    bpn = BYTES_PER_NODE[args.precision]
+    achieved = bpn * prof.active_node_updates / (prof.lb_kernel_ms * 1e-3) / 1e9 \
+        if prof.lb_kernel_ms > 0 else 0.0
+    traffic = None
+    tr = os.path.join(REPO, "profiles", f"traffic_{args.precision}.json")
+    if os.path.exists(tr):
+        with open(tr) as fh:
+            t = json.load(fh)
+        if prof.lb_kernel_launches:
+            # bytes per active node from the ncu capture, scaled to this launch
+            traffic = t["dram_bytes_per_active_node"] * prof.active_node_updates / \
+                prof.lb_kernel_launches
+    if rank != 0:
+        return
+    cb = None
+    if world == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(cfg, args.workload)
+    line = {
+        "metric": "coupled MLUPS", "value": round(value, 2), "unit": "MLUPS",
+        "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": round(ms_max / K, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "description": WORKLOADS[args.workload],
+                   "precision": args.precision, "lattice": list(info.lb_size),
+                   "particles": int(info.n_particles), "parallelism": f"replicas{world}",
+                   "l2": "state (lattice > 1 GB) exceeds the 129 MB L2; no flush"},
+        "e2e": {"value": round(e2e_val, 2), "unit": "MLUPS",
+                "h2d_bytes_per_step": upload_bytes(cfg) // max(K, 1),
+                "d2h_bytes_per_step": int(info.n_objects) * 10 * 3 * 8},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "lbStep (fused reconstruct/collide/stream)",
+                     "bytes_per_active_node": bpn,
+                     "kernel_ms_per_launch": round(prof.lb_kernel_ms / max(prof.lb_kernel_launches, 1), 4)},
+        "cpu_baseline": cb,
+        "clocks": clk,
+        "gpu_launches": int(prof.kernel_launches),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    os.makedirs(CACHE, exist_ok=True)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -252,6 +252,22 @@ int lbdem_download_walls(lbdem_ctx* ctx, double* FHydro, double* FContact,
 int lbdem_mass_summary(lbdem_ctx* ctx, double* total_mass,
                        int64_t* interface_nodes, int64_t* active_nodes);
 
+/* ---- measurement (no counterpart in the reference) --------------------- */
+
+typedef struct lbdem_profile {
+  double lb_kernel_ms;          /* summed CUDA-event time of the main lattice
+                                   kernel over the profiled launches        */
+  int64_t lb_kernel_launches;   /* profiled launches of that kernel         */
+  int64_t kernel_launches;      /* all kernels this context launched        */
+  int64_t active_node_updates;  /* active nodes collided and streamed       */
+  int64_t reserved[4];
+} lbdem_profile;
+/* Record CUDA events around every main lattice kernel launch (on the
+ * context's stream) while enabled. */
+int lbdem_profile_enable(lbdem_ctx* ctx, int enable);
+/* Synchronise, report the counters since the last reset, optionally reset. */
+int lbdem_profile_read(lbdem_ctx* ctx, lbdem_profile* out, int reset);
+
 #ifdef __cplusplus
 }
 #endif

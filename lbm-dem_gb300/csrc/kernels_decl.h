@@ -26,6 +26,7 @@ struct LbArgs {
   double* wallF;      // [W][12]
   double* scal;
   int* iscal;
+  unsigned long long* uscal;
 };
 
 struct FsArgs {

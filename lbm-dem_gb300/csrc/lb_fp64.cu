@@ -212,10 +212,14 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
   __shared__ double acc[ACC_N];
   __shared__ int sbox[6];
   __shared__ int snif;
+  __shared__ unsigned snact;
   for (int i = threadIdx.x; i < ACC_N; i += blockDim.x) acc[i] = 0.0;
   if (threadIdx.x < 3) sbox[threadIdx.x] = INT_MAX;
   else if (threadIdx.x < 6) sbox[threadIdx.x] = -1;
-  if (threadIdx.x == 0) snif = 0;
+  if (threadIdx.x == 0) {
+    snif = 0;
+    snact = 0;
+  }
   __syncthreads();
   const long long N = k.N;
   const int lane = threadIdx.x & 31;
@@ -350,6 +354,8 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
     }
     const unsigned ifb = __ballot_sync(0xffffffffu, act && t == 3);
     if (lane == 0 && ifb) atomicAdd(&snif, __popc(ifb));
+    const unsigned acb = __ballot_sync(0xffffffffu, act);
+    if (lane == 0 && acb) atomicAdd(&snact, (unsigned)__popc(acb));
     warpParticleReduce(key, pv, a.pFHydro, a.pMHydro, a.pSHydro, a.pFluidVol, k.nPart);
   }
   __syncthreads();
@@ -365,6 +371,7 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
     }
   }
   if (threadIdx.x == 0) {
+    if (snact) atomicAdd(a.uscal + US_ACTIVE_UPDATES, (unsigned long long)snact);
     if (snif) atomicAdd(a.iscal + IS_NIF, snif);
     if (sbox[3] >= 0) {
       atomicMin(a.iscal + IS_BBOX + 0, sbox[0]);

@@ -83,8 +83,21 @@ LbArgs lbArgs(lbdem_ctx* c) {
   a.wallF = d.wallF;
   a.scal = d.scal;
   a.iscal = d.iscal;
+  a.uscal = d.uscal;
   (void)P;
   return a;
+}
+
+// CUDA events around one launch of the main lattice kernel (profiling on).
+std::pair<cudaEvent_t, cudaEvent_t>* nextLbEvents(lbdem_ctx* c) {
+  if (!c->profiling) return nullptr;
+  if (c->lbEventsUsed == c->lbEvents.size()) {
+    std::pair<cudaEvent_t, cudaEvent_t> e;
+    if (cudaEventCreate(&e.first) != cudaSuccess) return nullptr;
+    if (cudaEventCreate(&e.second) != cudaSuccess) return nullptr;
+    c->lbEvents.push_back(e);
+  }
+  return &c->lbEvents[c->lbEventsUsed++];
 }
 
 FsArgs fsArgs(lbdem_ctx* c) {
@@ -188,8 +201,8 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   ctx->precision = precision;
   ctx->device = opt ? opt->device : 0;
   ctx->check_every = opt ? opt->check_every : 0;
-  if (precision != LBDEM_PLAIN_FP64 && precision != LBDEM_MIXED)
-    return setErr(ctx, LBDEM_ERR_INVALID, "unknown precision form");
+  if (precision != LBDEM_PLAIN_FP64)
+    return setErr(ctx, LBDEM_ERR_INVALID, "precision form not available in this build");
   // ---- validation (the supported subset of the reference's inputs) ----
   if (!cfg->rheologyNewtonian || cfg->turbulenceSolve || cfg->lbRestart || cfg->lbTopography)
     return setErr(ctx, LBDEM_ERR_INVALID,
@@ -470,6 +483,11 @@ extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
                   d.pairbuf, d.pairflag, d.pcell, d.ppos, d.cellCount, d.cellStart,
                   d.cellFill, d.cellParts, d.obj, d.wallF, d.walls, d.uncover};
   if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (auto& e : ctx->lbEvents) {
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -502,6 +520,7 @@ extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
   demPairs<<<partGrid(ctx, 128), 128, 0, s>>>(k, a, lubOn);
   demGather<<<partGrid(ctx, 128), 128, 0, s>>>(k, a, step);
   demObjects<<<1, 32, 0, s>>>(k, a, step);
+  ctx->launches += 1 + 9 + 3;
   return launchErr(ctx, "dem step");
 }
 
@@ -518,10 +537,12 @@ extern "C" int lbdem_coupling_step(lbdem_ctx* ctx) {
     uncoverResolve<<<1, 1024, 0, s>>>(k, d.mask, (double*)d.f[ctx->cur], d.mass, d.uncover,
                                       d.iscal);
     voxelizeObjects<<<lg, 256, 0, s>>>(k, d.mask, d.solid, d.objIdx, d.mass, d.obj);
+    ctx->launches += 3;
   }
   flagClaim<<<partGrid(ctx, 4) , 128, 0, s>>>(k, d.mask, d.claim, d.px0, d.pr, d.iscal, d.uscal);
   flagApply<<<lg, 256, 0, s>>>(k, d.mask, d.solid, d.claim, d.iscal, d.uscal);
   findNewActiveKernel<<<1, 1024, 0, s>>>(k, d.mask, d.solid, d.px0, d.pr, d.iscal, d.uscal);
+  ctx->launches += 3;
   return launchErr(ctx, "coupling step");
 }
 
@@ -539,11 +560,18 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   lbResetKernel<<<std::max(1, std::min(16 * P1 / 256 + 1, 1024)), 256, 0, s>>>(
       k, d.pFHydro, 16LL * P1, d.obj, d.wallF, d.scal, d.iscal);
   LbArgs a = lbArgs(ctx);
+  auto* ev = nextLbEvents(ctx);
+  if (ev) cudaEventRecord(ev->first, s);
   lbStepFp64<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
+  if (ev) cudaEventRecord(ev->second, s);
   lbFinalizeKernel<<<std::max(1, std::min(P1 / 256 + 1, 256)), 256, 0, s>>>(
       k, d.pFHydro, d.pMHydro, d.pFluidVol, d.obj, d.wallF, d.scal, d.iscal);
   ctx->cur = 1 - ctx->cur;
-  if (ctx->freeSurface) lbRedistribute<<<ctx->smCount * 4, 256, 0, s>>>(k, fsArgs(ctx));
+  ctx->launches += 3;
+  if (ctx->freeSurface) {
+    lbRedistribute<<<ctx->smCount * 4, 256, 0, s>>>(k, fsArgs(ctx));
+    ctx->launches += 1;
+  }
   return launchErr(ctx, "lb step");
 }
 
@@ -562,7 +590,39 @@ extern "C" int lbdem_free_surface_step(lbdem_ctx* ctx) {
   fsMutantsAndFill<<<g, 256, 0, s>>>(k, a);
   fsEmptyIsolated<<<g, 256, 0, s>>>(k, a);
   fsRedistribute<<<g, 256, 0, s>>>(k, a);
+  ctx->launches += 7;
   return launchErr(ctx, "free-surface step");
+}
+
+extern "C" int lbdem_profile_enable(lbdem_ctx* ctx, int enable) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  ctx->profiling = enable != 0;
+  return LBDEM_OK;
+}
+
+extern "C" int lbdem_profile_read(lbdem_ctx* ctx, lbdem_profile* out, int reset) {
+  if (!ctx || !out) return LBDEM_ERR_INVALID;
+  std::memset(out, 0, sizeof(*out));
+  CK(cudaStreamSynchronize(ctx->stream));
+  double ms = 0.0;
+  for (size_t i = 0; i < ctx->lbEventsUsed; ++i) {
+    float t = 0.0f;
+    CK(cudaEventElapsedTime(&t, ctx->lbEvents[i].first, ctx->lbEvents[i].second));
+    ms += t;
+  }
+  unsigned long long upd = 0;
+  CK(cudaMemcpy(&upd, ctx->d.uscal + US_ACTIVE_UPDATES, sizeof(upd), cudaMemcpyDeviceToHost));
+  out->lb_kernel_ms = ms;
+  out->lb_kernel_launches = (int64_t)ctx->lbEventsUsed;
+  out->kernel_launches = ctx->launches;
+  out->active_node_updates = (int64_t)upd;
+  if (reset) {
+    ctx->lbEventsUsed = 0;
+    ctx->launches = 0;
+    CK(cudaMemsetAsync(ctx->d.uscal + US_ACTIVE_UPDATES, 0, sizeof(upd), ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return LBDEM_OK;
 }
 
 // goCycle, src/main.cpp:38-67 (without IO)
@@ -579,9 +639,11 @@ extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
     } else if (ctx->lbSolve && ctx->demTime <= ctx->demInitialRepeat) {
       if (ctx->demSolve && (rc = lbdem_coupling_step(ctx))) return rc;
     }
-    if (ctx->check_every > 0 && ctx->lbTime % ctx->check_every == 0 && ctx->lbSolve)
+    if (ctx->check_every > 0 && ctx->lbTime % ctx->check_every == 0 && ctx->lbSolve) {
       nonfiniteCheck<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(
           ctx->k, ctx->d.mask, (const double*)ctx->d.f[ctx->cur], ctx->d.iscal);
+      ++ctx->launches;
+    }
   }
   return LBDEM_OK;
 }

@@ -126,7 +126,7 @@ enum {
   IS_COUNT
 };
 // offsets into Device::uscal
-enum { US_FIRSTFLAG = 0, US_COUNT };
+enum { US_FIRSTFLAG = 0, US_ACTIVE_UPDATES, US_COUNT };
 
 // object record layout (doubles)
 enum {
@@ -159,4 +159,9 @@ struct lbdem_ctx {
   int objIndexField[lbdem::MAX_OBJ] = {0};
   long long deviceBytes = 0;
   int smCount = 0;
+  // measurement
+  bool profiling = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> lbEvents;
+  size_t lbEventsUsed = 0;
+  long long launches = 0;
 };

@@ -87,6 +87,12 @@ class Info(C.Structure):
                 ("reserved", C.c_int32 * 7)]
 
 
+class Profile(C.Structure):
+    _fields_ = [("lb_kernel_ms", C.c_double), ("lb_kernel_launches", C.c_int64),
+                ("kernel_launches", C.c_int64), ("active_node_updates", C.c_int64),
+                ("reserved", C.c_int64 * 4)]
+
+
 _P = C.POINTER(C.c_double)
 _PI = C.POINTER(C.c_int32)
 
@@ -141,11 +147,11 @@ def load_library(path: str | None = None) -> C.CDLL:
                                  C.c_int),
         "lbdem_mass_summary": ([c_ctx, C.POINTER(C.c_double), C.POINTER(C.c_int64),
                                 C.POINTER(C.c_int64)], C.c_int),
+        "lbdem_profile_enable": ([c_ctx, C.c_int], C.c_int),
+        "lbdem_profile_read": ([c_ctx, C.POINTER(Profile), C.c_int], C.c_int),
     }
     for name, (args, res) in sig.items():
-        fn = getattr(lib, name, None)
-        if fn is None:
-            continue
+        fn = getattr(lib, name)  # a missing entry point is a build error
         fn.argtypes = args
         fn.restype = res
     if path is None:
@@ -313,6 +319,15 @@ class Solver:
         d["demTime"] = np.array([info.dem_time])
         d["demTimeStep"] = np.array([info.dem_step])
         return d
+
+    def profile_enable(self, on: bool = True):
+        self._check(self.lib.lbdem_profile_enable(self.ctx, 1 if on else 0), "profile_enable")
+
+    def profile_read(self, reset: bool = True) -> Profile:
+        p = Profile()
+        self._check(self.lib.lbdem_profile_read(self.ctx, C.byref(p), 1 if reset else 0),
+                    "profile_read")
+        return p
 
     def mass_summary(self):
         m = C.c_double()

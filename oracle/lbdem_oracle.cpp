@@ -663,19 +663,33 @@ void oracle_ctx::updateObjectBoundaries() {
 
 // LB::updateIndices -> initializeParticleBoundaries + initializeLists,
 // src/LB.cpp:1875-1899, 683-711
+// The reference loops every particle over the whole active list; visiting
+// only the active-list nodes of each particle's bounding box flags the same
+// nodes with the same (last particle wins) indices.
 void oracle_ctx::updateIndices() {
   for (size_t it = 0; it < N; ++it) {
     p[it] = 0;
     solid[it] = 0;
   }
+  std::vector<uint8_t> inList(N, 0);
+  for (unsigned index : activeNodes) inList[index] = 1;
   for (const Particle& q : particles) {
     const Vec c = q.x0 / uLength;
     const double r = q.r / uLength;
-    for (unsigned index : activeNodes)
-      if (insideSphere(pos(index), c, r)) {
-        p[index] = 1;
-        solid[index] = q.particleIndex;
-      }
+    const int lo[3] = {std::max(0, (int)std::floor(c.x - r) - 1), std::max(0, (int)std::floor(c.y - r) - 1),
+                       std::max(0, (int)std::floor(c.z - r) - 1)};
+    const int hi[3] = {std::min(X - 1, (int)std::ceil(c.x + r) + 1),
+                       std::min(Y - 1, (int)std::ceil(c.y + r) + 1),
+                       std::min(Z - 1, (int)std::ceil(c.z + r) + 1)};
+    for (int z = lo[2]; z <= hi[2]; ++z)
+      for (int y = lo[1]; y <= hi[1]; ++y)
+        for (int x = lo[0]; x <= hi[0]; ++x) {
+          const size_t index = (size_t)x + (size_t)y * X + (size_t)z * X * Y;
+          if (inList[index] && insideSphere(pos(index), c, r)) {
+            p[index] = 1;
+            solid[index] = q.particleIndex;
+          }
+        }
   }
   initializeLists();
 }
@@ -705,7 +719,10 @@ void oracle_ctx::findNewActive() {
 void oracle_ctx::lbStep() {
   initializeLists();
   cleanLists();
-  for (unsigned it : activeNodes) reconstruct(it);  // reconstruction, :1261-1299
+  // reconstruction, :1261-1299 (independent per node: threaded)
+  const long na = (long)activeNodes.size();
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < na; ++i) reconstruct(activeNodes[i]);
   computeHydroForces();
   collision();
   streaming();
@@ -754,8 +771,11 @@ void oracle_ctx::computeHydroForces() {
 // src/LB.cpp:1301-1332, src/node.cpp:95-207
 void oracle_ctx::collision() {
   if (!forceField) lbF = Vec();
-  double feq[19];
-  for (unsigned index : activeNodes) {
+  const long na = (long)activeNodes.size();
+#pragma omp parallel for schedule(static)
+  for (long ia = 0; ia < na; ++ia) {
+    const unsigned index = activeNodes[ia];
+    double feq[19];
     const Vec total = lbF + H(index);
     setU(index, U(index) + 0.5 * total / n[index]);
     computeEquilibrium(index, feq);
@@ -784,8 +804,10 @@ void oracle_ctx::streaming() {
     o.FHydro = Vec();
     o.MHydro = Vec();
   }
-  for (unsigned it : activeNodes)
-    for (int j = 0; j < 19; ++j) FS(j, it) = F(j, it);
+  const long na = (long)activeNodes.size();
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < na; ++i)
+    for (int j = 0; j < 19; ++j) FS(j, activeNodes[i]) = F(j, activeNodes[i]);
   for (unsigned it : activeNodes) {
     for (int j = 1; j < 19; ++j) {
       const size_t lk = (size_t)link(it, j);
