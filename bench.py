@@ -34,6 +34,8 @@ WORKLOADS = {
           "(r 3.0/4.2, seeded RSA), impactor r=20 density 5 vy=-0.02, tau=0.6",
     "c1": "64x80x64 lattice filled to y=60, 400 bidisperse spheres (r 3.0/4.2, seeded RSA), "
           "impactor r=8 density 5 vy=-0.01, tau=0.8",
+    "c2s": "160x200x160 lattice filled to y=150, 6100 bidisperse spheres (r 3.0/4.2, seeded "
+           "RSA), impactor r=14 density 5 vy=-0.02, tau=0.6 (profiling size of c2)",
 }
 # Algorithmic bytes per active-node update of the lattice kernel: 19
 # populations read + 19 written, 8 B (plain FP64) or 4 B (FP32 storage).

@@ -246,6 +246,9 @@ def named_case(name: str, seed: int = 1) -> Case:
     if name == "c2":
         return impact_case((256, 320, 256), 240.0, 25000, (3.0, 4.2), 20.0,
                            262.0, -0.02, 5.0, 0.6, 1.0e-5, seed, name=name)
+    if name == "c2s":  # config-2 physics on a 160x200x160 lattice (profiling size)
+        return impact_case((160, 200, 160), 150.0, 6100, (3.0, 4.2), 14.0, 166.0,
+                           -0.02, 5.0, 0.6, 1.0e-5, seed, name=name)
     if name == "small_cells":
         return impact_case((28, 40, 28), 27.0, 16, (3.0, 3.4), 5.0, 32.0,
                            -0.08, 5.0, 0.8, 1.0e-4, seed,

@@ -6,8 +6,9 @@
 namespace lbdem {
 
 struct LbArgs {
-  const double* fin;
-  double* fout;
+  const void* fin;    // double (plain) or float deviations f - w (mixed)
+  void* fout;
+  float* nF;          // density of fluid nodes (mixed form)
   uint8_t* mask;
   const uint32_t* solid;
   const uint8_t* objIdx;
@@ -18,10 +19,13 @@ struct LbArgs {
   const double* px0;
   const double* px1;
   const double* pw1;
+  const double* pkd;  // [6][P] x0/L, x1/S (double)
+  const float* pkf;   // [9][P] x0/L, x1/S, w1/W (float, mixed form)
   double* pFHydro;    // [3][P] lattice-unit sums
   double* pMHydro;    // [3][P]
   double* pSHydro;    // [9][P]
   double* pFluidVol;  // [P]
+  float* pAccF;       // [ACCF_N][P] float particle sums (mixed form)
   double* obj;        // object records
   double* wallF;      // [W][12]
   double* scal;
@@ -30,8 +34,9 @@ struct LbArgs {
 };
 
 struct FsArgs {
-  double* fcur;        // post-stream populations (current lattice)
-  const double* fold;  // pre-collision populations of this step
+  void* fcur;          // post-stream populations (current lattice)
+  const void* fold;    // pre-collision populations of this step
+  float* nF;           // density of fluid nodes (mixed form)
   uint8_t* mask;
   const uint32_t* solid;
   const uint8_t* objIdx;
@@ -44,6 +49,8 @@ struct FsArgs {
   const double* px0;
   const double* px1;
   const double* pw1;
+  const double* pkd;
+  const float* pkf;
   const double* obj;
   double* scal;
   int* iscal;
@@ -70,12 +77,16 @@ struct DemArgs {
   int* iscal;
 };
 
-// lb_fp64.cu
+// lb_fp64.cu / lb_mixed.cu
 __global__ void lbStepFp64(Consts k, LbArgs a);
+__global__ void lbStepMixed(Consts k, LbArgs a);
+__global__ void particleKinematics(Consts k, const double* px0, const double* px1,
+                                   const double* pw1, double* pkd, float* pkf);
 __global__ void lbResetKernel(Consts k, double* pAcc, long long pAccLen, double* obj,
                               double* wallF, double* scal, int* iscal);
 __global__ void lbFinalizeKernel(Consts k, double* pF, double* pM, double* pV, double* obj,
-                                 double* wallF, double* scal, const int* iscal);
+                                 double* wallF, double* scal, const int* iscal,
+                                 const float* pAccF, double* pS);
 __global__ void fsResetKernel(double* scal, int* iscal);
 __global__ void lbRedistribute(Consts k, FsArgs a);
 __global__ void fsUpdateMass(Consts k, FsArgs a);
@@ -84,9 +95,10 @@ __global__ void fsSmoothen(Consts k, FsArgs a);
 __global__ void fsMutantsAndFill(Consts k, FsArgs a);
 __global__ void fsEmptyIsolated(Consts k, FsArgs a);
 __global__ void fsRedistribute(Consts k, FsArgs a);
+__global__ void fsClearBulk(Consts k, uint8_t* mask, const int* iscal);
 __global__ void uncoverCollect(Consts k, const uint8_t* mask, const double* obj,
                                uint32_t* list, int* iscal);
-__global__ void uncoverResolve(Consts k, uint8_t* mask, double* f, double* mass,
+__global__ void uncoverResolve(Consts k, uint8_t* mask, void* f, double* mass, float* nF,
                                uint32_t* list, int* iscal);
 __global__ void voxelizeObjects(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* objIdx,
                                 double* mass, double* obj);
@@ -100,12 +112,14 @@ __global__ void findNewActiveKernel(Consts k, uint8_t* mask, uint32_t* solid,
 __global__ void initTypes(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* objIdx,
                           const int* boundary, const DeviceWall* walls, const int* wallType,
                           const double* obj, double fluidHeightLattice, int freeSurface);
-__global__ void initFields(Consts k, uint8_t* mask, double* f, double* mass);
+__global__ void initFields(Consts k, uint8_t* mask, void* f, double* mass, float* nF);
 __global__ void massSummaryKernel(Consts k, const uint8_t* mask, const double* mass,
-                                  double* out, unsigned long long* cnt);
-__global__ void momentsKernel(Consts k, const uint8_t* mask, const double* f, double* n,
+                                  const float* nF, double* out, unsigned long long* cnt);
+__global__ void momentsKernel(Consts k, const uint8_t* mask, const void* f, double* n,
                               double* u);
-__global__ void nonfiniteCheck(Consts k, const uint8_t* mask, const double* f, int* iscal);
+__global__ void nonfiniteCheck(Consts k, const uint8_t* mask, const void* f, int* iscal);
+__global__ void exportLattice(Consts k, const uint8_t* mask, const void* f, const double* mass,
+                              const float* nF, double* fOut, double* massOut);
 
 // dem_fp64.cu
 __global__ void demBegin(Consts k, DemArgs a, int forceRebuild);

@@ -1,0 +1,360 @@
+// Lattice helpers shared by the FP64 and the mixed-precision kernels:
+// the D3Q19 set in the reference's order, index arithmetic, the exact FP64
+// node collision, the FP32-deviation node collision, population storage
+// accessors and the warp-level particle reduction.
+#pragma once
+#include <cfloat>
+#include <climits>
+
+#include "kernels_decl.h"
+
+namespace lbdem {
+
+// D3Q19 velocity set in the reference's order, src/lattice.h:33-57
+__host__ __device__ constexpr int CX(int j) {
+  return j == 1 ? 1 : j == 2 ? -1 : j == 7 ? 1 : j == 8 ? -1 : j == 9 ? -1 : j == 10 ? 1
+       : j == 15 ? 1 : j == 16 ? -1 : j == 17 ? 1 : j == 18 ? -1 : 0;
+}
+__host__ __device__ constexpr int CY(int j) {
+  return j == 3 ? 1 : j == 4 ? -1 : j == 7 ? 1 : j == 8 ? -1 : j == 9 ? 1 : j == 10 ? -1
+       : j == 11 ? 1 : j == 12 ? -1 : j == 13 ? -1 : j == 14 ? 1 : 0;
+}
+__host__ __device__ constexpr int CZ(int j) {
+  return j == 5 ? 1 : j == 6 ? -1 : j == 11 ? 1 : j == 12 ? -1 : j == 13 ? 1 : j == 14 ? -1
+       : j == 15 ? 1 : j == 16 ? -1 : j == 17 ? -1 : j == 18 ? 1 : 0;
+}
+__host__ __device__ constexpr int OPPJ(int j) { return j == 0 ? 0 : (j & 1) ? j + 1 : j - 1; }
+// weights, src/lattice.h:147-150 (same double values as 12/36, 2/36, 1/36)
+__host__ __device__ constexpr double WJ(int j) {
+  return j == 0 ? 12.0 / 36.0 : j <= 6 ? 2.0 / 36.0 : 1.0 / 36.0;
+}
+
+__device__ __forceinline__ bool isActiveT(int t) { return t == 0 || t == 3; }
+
+// u.dot(v[j]) of src/myvector.cpp:121 with the zero components dropped
+__device__ __forceinline__ double dotc(int j, double x, double y, double z) {
+  const int cx = CX(j), cy = CY(j), cz = CZ(j);
+  double s = 0.0;
+  bool any = false;
+  if (cx) { s = cx > 0 ? x : -x; any = true; }
+  if (cy) { const double t = cy > 0 ? y : -y; s = any ? s + t : t; any = true; }
+  if (cz) { const double t = cz > 0 ? z : -z; s = any ? s + t : t; }
+  return s;
+}
+
+__device__ __forceinline__ long long nbrOffset(const Consts& k, int j) {
+  return (long long)CX(j) + (long long)CY(j) * k.sy + (long long)CZ(j) * k.sz;
+}
+
+__device__ __forceinline__ void coords(const Consts& k, long long x, int& ix, int& iy, int& iz) {
+  const unsigned ux = (unsigned)x;
+  iz = (int)(ux / (unsigned)k.sz);
+  const unsigned rem = ux - (unsigned)iz * (unsigned)k.sz;
+  iy = (int)(rem / (unsigned)k.X);
+  ix = (int)(rem - (unsigned)iy * (unsigned)k.X);
+}
+
+// tinyVector::insideSphere, src/myvector.cpp:171-176, on node coordinates
+__device__ __forceinline__ bool insideSphere(double px, double py, double pz, double cx,
+                                             double cy, double cz, double r) {
+  const double dx = px - cx, dy = py - cy, dz = pz - cz;
+  return dx * dx + dy * dy + dz * dz < r * r;
+}
+
+// node::setEquilibrium / computeEquilibrium for one direction,
+// src/node.cpp:52-73, 100-111
+__device__ __forceinline__ double feqj(int j, double n, double ux, double uy, double uz,
+                                       double usq) {
+  const double vu = dotc(j, ux, uy, uz);
+  return WJ(j) * n * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
+}
+
+// One node's collision, exactly as LB::reconstruction + computeHydroForces
+// (node part) + LB::collision: in f = pre-collision populations, out f =
+// post-collision populations (fs). Returns n, the shifted u, the node force.
+struct NodeState {
+  double n, ux, uy, uz, hx, hy, hz;
+  // particle coupling terms for the per-particle reduction
+  double dx, dy, dz, rx, ry, rz;
+};
+
+__device__ __forceinline__ void collideNode(const Consts& k, double* f, bool pflag,
+                                            uint32_t pid, const double* px0,
+                                            const double* px1, const double* pw1,
+                                            int P, double massOld, int ix, int iy, int iz,
+                                            NodeState& s) {
+  // node::reconstruct
+  double n = 0.0;
+#pragma unroll
+  for (int j = 0; j < Q; ++j) n += f[j];
+  double ux = 0.0, uy = 0.0, uz = 0.0;
+  {
+    bool ax = false, ay = false, az = false;
+#pragma unroll
+    for (int j = 1; j < Q; ++j) {
+      if (CX(j)) { const double t = CX(j) > 0 ? f[j] : -f[j]; ux = ax ? ux + t : t; ax = true; }
+      if (CY(j)) { const double t = CY(j) > 0 ? f[j] : -f[j]; uy = ay ? uy + t : t; ay = true; }
+      if (CZ(j)) { const double t = CZ(j) > 0 ? f[j] : -f[j]; uz = az ? uz + t : t; az = true; }
+    }
+  }
+  ux /= n;
+  uy /= n;
+  uz /= n;
+  // LB::computeHydroForces, node part (src/LB.cpp:1920-1940)
+  double hx = 0.0, hy = 0.0, hz = 0.0;
+  s.dx = s.dy = s.dz = 0.0;
+  s.rx = s.ry = s.rz = 0.0;
+  if (pflag && pid < (uint32_t)P) {
+    // px0 = x0/unit.Length and px1 = x1/unit.Speed, divided once per particle
+    // (particleKinematics); the quotients are the same bits the reference
+    // computes at every node.
+    const double rx = (double)ix - px0[pid];
+    const double ry = (double)iy - px0[P + pid];
+    const double rz = (double)iz - px0[2 * P + pid];
+    const double wx = pw1[pid], wy = pw1[P + pid], wz = pw1[2 * P + pid];
+    const double lvx = px1[pid] + (wy * rz - wz * ry) / k.uAngVel;
+    const double lvy = px1[P + pid] + (wz * rx - wx * rz) / k.uAngVel;
+    const double lvz = px1[2 * P + pid] + (wx * ry - wy * rx) / k.uAngVel;
+    const double lf = massOld / n;
+    s.dx = (ux - lvx) * lf;
+    s.dy = (uy - lvy) * lf;
+    s.dz = (uz - lvz) * lf;
+    s.rx = rx;
+    s.ry = ry;
+    s.rz = rz;
+    hx = 0.0 + s.dx * -1.0;
+    hy = 0.0 + s.dy * -1.0;
+    hz = 0.0 + s.dz * -1.0;
+  }
+  // node::shiftVelocity
+  const double Tx = k.lbF[0] + hx, Ty = k.lbF[1] + hy, Tz = k.lbF[2] + hz;
+  ux = ux + Tx * 0.5 / n;
+  uy = uy + Ty * 0.5 / n;
+  uz = uz + Tz * 0.5 / n;
+  const double usq = ux * ux + uy * uy + uz * uz;
+  // node::solveCollision + node::addForce
+#pragma unroll
+  for (int j = 0; j < Q; ++j) {
+    const double vu = dotc(j, ux, uy, uz);
+    const double feq = WJ(j) * n * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
+    double fj = f[j] + k.omega * (feq - f[j]);
+    const double v9 = 9.0 * vu;
+    const double fpx = CX(j) == 0 ? (-ux) * 3.0 : CX(j) > 0 ? v9 + (1.0 - ux) * 3.0
+                                                             : -v9 + (-1.0 - ux) * 3.0;
+    const double fpy = CY(j) == 0 ? (-uy) * 3.0 : CY(j) > 0 ? v9 + (1.0 - uy) * 3.0
+                                                             : -v9 + (-1.0 - uy) * 3.0;
+    const double fpz = CZ(j) == 0 ? (-uz) * 3.0 : CZ(j) > 0 ? v9 + (1.0 - uz) * 3.0
+                                                             : -v9 + (-1.0 - uz) * 3.0;
+    fj += k.omegaf * WJ(j) * (fpx * Tx + fpy * Ty + fpz * Tz);
+    f[j] = fj;
+  }
+  s.n = n;
+  s.ux = ux;
+  s.uy = uy;
+  s.uz = uz;
+  s.hx = hx;
+  s.hy = hy;
+  s.hz = hz;
+}
+
+
+// per-block accumulator layout in shared memory
+enum { ACC_WALL = 0, ACC_OBJ = ACC_WALL + 3 * MAX_WALL, ACC_EXTRA = ACC_OBJ + 6 * MAX_OBJ,
+       ACC_N = ACC_EXTRA + 1 };
+
+// Reduce 16 per-lane particle terms over the lanes of a warp that share a
+// particle index and add them to the particle's accumulators.
+__device__ __forceinline__ void warpParticleReduce(int key, const double* v, double* pF,
+                                                   double* pM, double* pS, double* pV,
+                                                   int P) {
+  const unsigned FULL = 0xffffffffu;
+  unsigned todo = __ballot_sync(FULL, key >= 0);
+  const int lane = threadIdx.x & 31;
+  while (todo) {
+    const int leader = __ffs(todo) - 1;
+    const int kk = __shfl_sync(FULL, key, leader);
+    const bool mine = key == kk;
+    const unsigned grp = __ballot_sync(FULL, mine);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      double x = mine ? v[i] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+      if (lane == leader) {
+        double* dst = i < 3 ? pF + i * P : i < 6 ? pM + (i - 3) * P : i < 15 ? pS + (i - 6) * P
+                                                                               : pV;
+        atomicAdd(dst + kk, x);
+      }
+    }
+    todo &= ~grp;
+  }
+}
+
+// Per-thread accumulation of the bounce-back force sums. The wall and the
+// impactor a thread last touched are kept in registers and flushed to the
+// block's shared accumulators only when the index changes and at the end,
+// instead of one shared-memory atomic per boundary link.
+template <typename WT>
+struct BBAccT {
+  int wId = -1, oId = -1;
+  WT w[3] = {0, 0, 0};
+  double o[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  double extra = 0.0;
+  __device__ __forceinline__ void flushWall(double* acc) {
+    if (wId >= 0)
+      for (int c = 0; c < 3; ++c)
+        if (w[c] != 0) {
+          atomicAdd(&acc[ACC_WALL + 3 * wId + c], (double)w[c]);
+          w[c] = 0;
+        }
+  }
+  __device__ __forceinline__ void flushObj(double* acc) {
+    if (oId >= 0)
+      for (int c = 0; c < 6; ++c)
+        if (o[c] != 0.0) {
+          atomicAdd(&acc[ACC_OBJ + 6 * oId + c], o[c]);
+          o[c] = 0.0;
+        }
+  }
+  __device__ __forceinline__ void wall(double* acc, int id, int c, WT v) {
+    if (id != wId) {
+      flushWall(acc);
+      wId = id;
+    }
+    w[c] += v;
+  }
+  __device__ __forceinline__ void obj(double* acc, int id, int c, double v) {
+    if (id != oId) {
+      flushObj(acc);
+      oId = id;
+    }
+    o[c] += v;
+  }
+  __device__ __forceinline__ void flush(double* acc) {
+    flushWall(acc);
+    flushObj(acc);
+    if (extra != 0.0) atomicAdd(&acc[ACC_EXTRA], extra);
+    extra = 0.0;
+  }
+};
+using BBAcc = BBAccT<double>;   // plain form
+using BBAccF = BBAccT<float>;   // mixed form: wall sums (diagnostic) in float
+
+// ---- population storage ------------------------------------------------------
+// Plain form: f itself in double. Mixed form: the deviation f - w_j in float
+// (w_j = initDensity * weight, initDensity is 1 in the reference,
+// src/LB.cpp:330), which keeps the float's precision for the part that
+// varies.
+__device__ __forceinline__ double fget(const Consts& k, const void* f, int j, long long x) {
+  return k.mixed ? (double)((const float*)f)[(long long)j * k.N + x] + WJ(j)
+                 : ((const double*)f)[(long long)j * k.N + x];
+}
+__device__ __forceinline__ void fset(const Consts& k, void* f, int j, long long x, double v) {
+  if (k.mixed) ((float*)f)[(long long)j * k.N + x] = (float)(v - WJ(j));
+  else ((double*)f)[(long long)j * k.N + x] = v;
+}
+// f_j1(x1) - f_j2(x2) for two directions of equal weight
+__device__ __forceinline__ double fdiff(const Consts& k, const void* f, int j1, long long x1,
+                                        int j2, long long x2) {
+  if (k.mixed)
+    return (double)((const float*)f)[(long long)j1 * k.N + x1] -
+           (double)((const float*)f)[(long long)j2 * k.N + x2];
+  return ((const double*)f)[(long long)j1 * k.N + x1] -
+         ((const double*)f)[(long long)j2 * k.N + x2];
+}
+
+// u.dot(v[j]) in float
+__device__ __forceinline__ float dotcf(int j, float x, float y, float z) {
+  float s = 0.0f;
+  if (CX(j)) s = CX(j) > 0 ? x : -x;
+  if (CY(j)) s = CY(j) > 0 ? s + y : s - y;
+  if (CZ(j)) s = CZ(j) > 0 ? s + z : s - z;
+  return s;
+}
+
+struct NodeStateF {
+  float n, ux, uy, uz, hx, hy, hz;
+  float dx, dy, dz, rx, ry, rz;
+};
+
+// Mixed form of collideNode: BGK + Guo forcing with the particle coupling of
+// LB::computeHydroForces, on float deviations g = f - w (in/out). Explicit
+// fused multiply-adds, so the result is the same in every translation unit
+// whatever its contraction flags.
+__device__ __forceinline__ void collideNodeMixed(const Consts& k, float* g, bool pflag,
+                                                 uint32_t pid, const float* pkf, int P,
+                                                 float massOld, int ix, int iy, int iz,
+                                                 NodeStateF& s) {
+  // moments from the sums and differences of opposite pairs (j odd, j + 1)
+  float dr = g[0];
+  float jx = 0.0f, jy = 0.0f, jz = 0.0f;
+#pragma unroll
+  for (int j = 1; j < Q; j += 2) {
+    dr += g[j] + g[j + 1];
+    const float dj = g[j] - g[j + 1];
+    if (CX(j)) jx = CX(j) > 0 ? jx + dj : jx - dj;
+    if (CY(j)) jy = CY(j) > 0 ? jy + dj : jy - dj;
+    if (CZ(j)) jz = CZ(j) > 0 ? jz + dj : jz - dj;
+  }
+  const float n = 1.0f + dr;
+  const float inv = 1.0f / n;
+  float ux = jx * inv, uy = jy * inv, uz = jz * inv;
+  float hx = 0.0f, hy = 0.0f, hz = 0.0f;
+  s.dx = s.dy = s.dz = s.rx = s.ry = s.rz = 0.0f;
+  if (pflag && pid < (uint32_t)P) {
+    // pkf: [9][P] float x0/L, x1/S, w1/W of every particle (particleKinematics)
+    const float rx = (float)ix - pkf[pid];
+    const float ry = (float)iy - pkf[P + pid];
+    const float rz = (float)iz - pkf[2 * P + pid];
+    const float wx = pkf[6 * P + pid], wy = pkf[7 * P + pid], wz = pkf[8 * P + pid];
+    const float lvx = pkf[3 * P + pid] + __fmaf_rn(wy, rz, -wz * ry);
+    const float lvy = pkf[4 * P + pid] + __fmaf_rn(wz, rx, -wx * rz);
+    const float lvz = pkf[5 * P + pid] + __fmaf_rn(wx, ry, -wy * rx);
+    const float lf = massOld * inv;
+    s.dx = (ux - lvx) * lf;
+    s.dy = (uy - lvy) * lf;
+    s.dz = (uz - lvz) * lf;
+    s.rx = rx;
+    s.ry = ry;
+    s.rz = rz;
+    hx = -s.dx;
+    hy = -s.dy;
+    hz = -s.dz;
+  }
+  const float Tx = k.lbFf[0] + hx, Ty = k.lbFf[1] + hy, Tz = k.lbFf[2] + hz;
+  const float hinv = 0.5f * inv;
+  ux = __fmaf_rn(Tx, hinv, ux);
+  uy = __fmaf_rn(Ty, hinv, uy);
+  uz = __fmaf_rn(Tz, hinv, uz);
+  const float usq = __fmaf_rn(ux, ux, __fmaf_rn(uy, uy, uz * uz));
+  const float uT = __fmaf_rn(ux, Tx, __fmaf_rn(uy, Ty, uz * Tz));
+  const float om = k.omegaF, omf = k.omegafF;
+  const float omc = 1.0f - om;
+  const float base = __fmaf_rn(-1.5f * n, usq, dr);  // dr - 1.5 n u^2
+  // g' = (1 - om) g + om geq + omf guo with
+  //   geq = w (dr + n (3 vu + 4.5 vu^2 - 1.5 u^2)),  guo = w (9 vu c.T + 3 (c.T - u.T)),
+  // split into the part even in c (S) and the part odd in c (A), so that
+  // g'_j = (1 - om) g_j + S + A and g'_opp = (1 - om) g_opp + S - A.
+  const float a0s = om * base - omf * 3.0f * uT;
+  const float a1s = om * 4.5f * n, a2s = omf * 9.0f, b1s = om * 3.0f * n, b2s = omf * 3.0f;
+  g[0] = __fmaf_rn(omc, g[0], (float)WJ(0) * a0s);
+#pragma unroll
+  for (int j = 1; j < Q; j += 2) {
+    const float w = (float)WJ(j);
+    const float vu = dotcf(j, ux, uy, uz);
+    const float cT = dotcf(j, Tx, Ty, Tz);
+    const float S = w * __fmaf_rn(vu, __fmaf_rn(a1s, vu, a2s * cT), a0s);
+    const float A = w * __fmaf_rn(b1s, vu, b2s * cT);
+    g[j] = __fmaf_rn(omc, g[j], S + A);
+    g[j + 1] = __fmaf_rn(omc, g[j + 1], S - A);
+  }
+  s.n = n;
+  s.ux = ux;
+  s.uy = uy;
+  s.uz = uz;
+  s.hx = hx;
+  s.hy = hy;
+  s.hz = hz;
+}
+
+}  // namespace lbdem

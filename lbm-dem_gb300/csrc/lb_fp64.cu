@@ -24,186 +24,9 @@
 #include <cfloat>
 #include <climits>
 
-#include "kernels_decl.h"
+#include "lattice_common.cuh"
 
 namespace lbdem {
-
-// D3Q19 velocity set in the reference's order, src/lattice.h:33-57
-__host__ __device__ constexpr int CX(int j) {
-  return j == 1 ? 1 : j == 2 ? -1 : j == 7 ? 1 : j == 8 ? -1 : j == 9 ? -1 : j == 10 ? 1
-       : j == 15 ? 1 : j == 16 ? -1 : j == 17 ? 1 : j == 18 ? -1 : 0;
-}
-__host__ __device__ constexpr int CY(int j) {
-  return j == 3 ? 1 : j == 4 ? -1 : j == 7 ? 1 : j == 8 ? -1 : j == 9 ? 1 : j == 10 ? -1
-       : j == 11 ? 1 : j == 12 ? -1 : j == 13 ? -1 : j == 14 ? 1 : 0;
-}
-__host__ __device__ constexpr int CZ(int j) {
-  return j == 5 ? 1 : j == 6 ? -1 : j == 11 ? 1 : j == 12 ? -1 : j == 13 ? 1 : j == 14 ? -1
-       : j == 15 ? 1 : j == 16 ? -1 : j == 17 ? -1 : j == 18 ? 1 : 0;
-}
-__host__ __device__ constexpr int OPPJ(int j) { return j == 0 ? 0 : (j & 1) ? j + 1 : j - 1; }
-// weights, src/lattice.h:147-150 (same double values as 12/36, 2/36, 1/36)
-__host__ __device__ constexpr double WJ(int j) {
-  return j == 0 ? 12.0 / 36.0 : j <= 6 ? 2.0 / 36.0 : 1.0 / 36.0;
-}
-
-__device__ __forceinline__ bool isActiveT(int t) { return t == 0 || t == 3; }
-
-// u.dot(v[j]) of src/myvector.cpp:121 with the zero components dropped
-__device__ __forceinline__ double dotc(int j, double x, double y, double z) {
-  const int cx = CX(j), cy = CY(j), cz = CZ(j);
-  double s = 0.0;
-  bool any = false;
-  if (cx) { s = cx > 0 ? x : -x; any = true; }
-  if (cy) { const double t = cy > 0 ? y : -y; s = any ? s + t : t; any = true; }
-  if (cz) { const double t = cz > 0 ? z : -z; s = any ? s + t : t; }
-  return s;
-}
-
-__device__ __forceinline__ long long nbrOffset(const Consts& k, int j) {
-  return (long long)CX(j) + (long long)CY(j) * k.sy + (long long)CZ(j) * k.sz;
-}
-
-__device__ __forceinline__ void coords(const Consts& k, long long x, int& ix, int& iy, int& iz) {
-  const unsigned ux = (unsigned)x;
-  iz = (int)(ux / (unsigned)k.sz);
-  const unsigned rem = ux - (unsigned)iz * (unsigned)k.sz;
-  iy = (int)(rem / (unsigned)k.X);
-  ix = (int)(rem - (unsigned)iy * (unsigned)k.X);
-}
-
-// tinyVector::insideSphere, src/myvector.cpp:171-176, on node coordinates
-__device__ __forceinline__ bool insideSphere(double px, double py, double pz, double cx,
-                                             double cy, double cz, double r) {
-  const double dx = px - cx, dy = py - cy, dz = pz - cz;
-  return dx * dx + dy * dy + dz * dz < r * r;
-}
-
-// node::setEquilibrium / computeEquilibrium for one direction,
-// src/node.cpp:52-73, 100-111
-__device__ __forceinline__ double feqj(int j, double n, double ux, double uy, double uz,
-                                       double usq) {
-  const double vu = dotc(j, ux, uy, uz);
-  return WJ(j) * n * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
-}
-
-// One node's collision, exactly as LB::reconstruction + computeHydroForces
-// (node part) + LB::collision: in f = pre-collision populations, out f =
-// post-collision populations (fs). Returns n, the shifted u, the node force.
-struct NodeState {
-  double n, ux, uy, uz, hx, hy, hz;
-  // particle coupling terms for the per-particle reduction
-  double dx, dy, dz, rx, ry, rz;
-};
-
-__device__ __forceinline__ void collideNode(const Consts& k, double* f, bool pflag,
-                                            uint32_t pid, const double* px0,
-                                            const double* px1, const double* pw1,
-                                            int P, double massOld, int ix, int iy, int iz,
-                                            NodeState& s) {
-  // node::reconstruct
-  double n = 0.0;
-#pragma unroll
-  for (int j = 0; j < Q; ++j) n += f[j];
-  double ux = 0.0, uy = 0.0, uz = 0.0;
-  {
-    bool ax = false, ay = false, az = false;
-#pragma unroll
-    for (int j = 1; j < Q; ++j) {
-      if (CX(j)) { const double t = CX(j) > 0 ? f[j] : -f[j]; ux = ax ? ux + t : t; ax = true; }
-      if (CY(j)) { const double t = CY(j) > 0 ? f[j] : -f[j]; uy = ay ? uy + t : t; ay = true; }
-      if (CZ(j)) { const double t = CZ(j) > 0 ? f[j] : -f[j]; uz = az ? uz + t : t; az = true; }
-    }
-  }
-  ux /= n;
-  uy /= n;
-  uz /= n;
-  // LB::computeHydroForces, node part (src/LB.cpp:1920-1940)
-  double hx = 0.0, hy = 0.0, hz = 0.0;
-  s.dx = s.dy = s.dz = 0.0;
-  s.rx = s.ry = s.rz = 0.0;
-  if (pflag && pid < (uint32_t)P) {
-    const double rx = (double)ix - px0[pid] / k.uLength;
-    const double ry = (double)iy - px0[P + pid] / k.uLength;
-    const double rz = (double)iz - px0[2 * P + pid] / k.uLength;
-    const double wx = pw1[pid], wy = pw1[P + pid], wz = pw1[2 * P + pid];
-    const double lvx = px1[pid] / k.uSpeed + (wy * rz - wz * ry) / k.uAngVel;
-    const double lvy = px1[P + pid] / k.uSpeed + (wz * rx - wx * rz) / k.uAngVel;
-    const double lvz = px1[2 * P + pid] / k.uSpeed + (wx * ry - wy * rx) / k.uAngVel;
-    const double lf = massOld / n;
-    s.dx = (ux - lvx) * lf;
-    s.dy = (uy - lvy) * lf;
-    s.dz = (uz - lvz) * lf;
-    s.rx = rx;
-    s.ry = ry;
-    s.rz = rz;
-    hx = 0.0 + s.dx * -1.0;
-    hy = 0.0 + s.dy * -1.0;
-    hz = 0.0 + s.dz * -1.0;
-  }
-  // node::shiftVelocity
-  const double Tx = k.lbF[0] + hx, Ty = k.lbF[1] + hy, Tz = k.lbF[2] + hz;
-  ux = ux + Tx * 0.5 / n;
-  uy = uy + Ty * 0.5 / n;
-  uz = uz + Tz * 0.5 / n;
-  const double usq = ux * ux + uy * uy + uz * uz;
-  // node::solveCollision + node::addForce
-#pragma unroll
-  for (int j = 0; j < Q; ++j) {
-    const double vu = dotc(j, ux, uy, uz);
-    const double feq = WJ(j) * n * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
-    double fj = f[j] + k.omega * (feq - f[j]);
-    const double v9 = 9.0 * vu;
-    const double fpx = CX(j) == 0 ? (-ux) * 3.0 : CX(j) > 0 ? v9 + (1.0 - ux) * 3.0
-                                                             : -v9 + (-1.0 - ux) * 3.0;
-    const double fpy = CY(j) == 0 ? (-uy) * 3.0 : CY(j) > 0 ? v9 + (1.0 - uy) * 3.0
-                                                             : -v9 + (-1.0 - uy) * 3.0;
-    const double fpz = CZ(j) == 0 ? (-uz) * 3.0 : CZ(j) > 0 ? v9 + (1.0 - uz) * 3.0
-                                                             : -v9 + (-1.0 - uz) * 3.0;
-    fj += k.omegaf * WJ(j) * (fpx * Tx + fpy * Ty + fpz * Tz);
-    f[j] = fj;
-  }
-  s.n = n;
-  s.ux = ux;
-  s.uy = uy;
-  s.uz = uz;
-  s.hx = hx;
-  s.hy = hy;
-  s.hz = hz;
-}
-
-
-// per-block accumulator layout in shared memory
-enum { ACC_WALL = 0, ACC_OBJ = ACC_WALL + 3 * MAX_WALL, ACC_EXTRA = ACC_OBJ + 6 * MAX_OBJ,
-       ACC_N = ACC_EXTRA + 1 };
-
-// Reduce 16 per-lane particle terms over the lanes of a warp that share a
-// particle index and add them to the particle's accumulators.
-__device__ __forceinline__ void warpParticleReduce(int key, const double* v, double* pF,
-                                                   double* pM, double* pS, double* pV,
-                                                   int P) {
-  const unsigned FULL = 0xffffffffu;
-  unsigned todo = __ballot_sync(FULL, key >= 0);
-  const int lane = threadIdx.x & 31;
-  while (todo) {
-    const int leader = __ffs(todo) - 1;
-    const int kk = __shfl_sync(FULL, key, leader);
-    const bool mine = key == kk;
-    const unsigned grp = __ballot_sync(FULL, mine);
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      double x = mine ? v[i] : 0.0;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
-      if (lane == leader) {
-        double* dst = i < 3 ? pF + i * P : i < 6 ? pM + (i - 3) * P : i < 15 ? pS + (i - 6) * P
-                                                                               : pV;
-        atomicAdd(dst + kk, x);
-      }
-    }
-    todo &= ~grp;
-  }
-}
 
 // Fused LB step over all nodes: reconstruct, particle forcing, collision,
 // push streaming with the boundary rules of LB::streaming, and the per-node
@@ -222,6 +45,8 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
   }
   __syncthreads();
   const long long N = k.N;
+  const double* fin = (const double*)a.fin;
+  double* fout = (double*)a.fout;
   const int lane = threadIdx.x & 31;
   const long long warpsPerBlock = blockDim.x >> 5;
   const long long gw = blockIdx.x * warpsPerBlock + (threadIdx.x >> 5);
@@ -233,16 +58,18 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
                         k.initDensity * WJ(12), k.initDensity * WJ(13), k.initDensity * WJ(14),
                         k.initDensity * WJ(15), k.initDensity * WJ(16), k.initDensity * WJ(17),
                         k.initDensity * WJ(18)};
+  BBAcc bba;
   for (long long base = gw * 32; base < N; base += stride) {
     const long long x = base + lane;
     const bool valid = x < N;
     uint8_t m = valid ? a.mask[x] : (uint8_t)2;
     const int t = m & TYPE_MASK;
     const bool act = valid && isActiveT(t);
-    if (valid) {  // cleanLists: the active list now equals the active types
-      const bool aBit = (m & ABIT) != 0;
-      if (aBit != act) a.mask[x] = (uint8_t)(act ? (m | ABIT) : (m & ~ABIT));
-    }
+    // cleanLists (the active list now equals the active types) and the
+    // neighbour cache, written back once the links are classified
+    uint8_t nm = (uint8_t)(act ? ((m | ABIT) & ~BULK) : (m & ~(ABIT | BULK)));
+    const bool bulk = (m & BULK) != 0;
+    bool allAct = true;
     int key = -1;
     double pv[16];
     if (act) {
@@ -250,12 +77,13 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
       coords(k, x, ix, iy, iz);
       double f[Q];
 #pragma unroll
-      for (int j = 0; j < Q; ++j) f[j] = a.fin[(long long)j * N + x];
+      for (int j = 0; j < Q; ++j) f[j] = fin[(long long)j * N + x];
       const bool pf = (m & PFLAG) != 0;
       const uint32_t pid = pf ? a.solid[x] : 0u;
       const double massOld = a.mass[x];
       NodeState s;
-      collideNode(k, f, pf, pid, a.px0, a.px1, a.pw1, k.nPart, massOld, ix, iy, iz, s);
+      collideNode(k, f, pf, pid, a.pkd, a.pkd + 3 * k.nPart, a.pw1, k.nPart, massOld, ix, iy, iz,
+                  s);
       if (pf && pid < (uint32_t)k.nPart) {
         key = (int)pid;
         pv[0] = s.dx * 1.0;
@@ -277,31 +105,32 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
       // LB::streaming, push form: population j of this node goes to the
       // neighbour x+c_j when it is active; otherwise this node receives the
       // reference's boundary value in direction opp(j).
-      a.fout[x] = f[0];
+      fout[x] = f[0];
       const double usq = s.ux * s.ux + s.uy * s.uy + s.uz * s.uz;
 #pragma unroll
       for (int j = 1; j < Q; ++j) {
         const long long lk = x + nbrOffset(k, j);
-        const int tl = a.mask[lk] & TYPE_MASK;
+        const int tl = bulk ? 0 : (a.mask[lk] & TYPE_MASK);
         const double fs = f[j];
         const long long dst = (long long)OPPJ(j) * N + x;
+        allAct = allAct && isActiveT(tl);
         if (isActiveT(tl)) {
-          a.fout[(long long)j * N + lk] = fs;
+          fout[(long long)j * N + lk] = fs;
         } else if (tl == 2) {
           const double vuj = dotc(j, s.ux, s.uy, s.uz);
-          a.fout[dst] = -fs + WJ(j) * k.initDensity * (2.0 + 9.0 * (vuj * vuj) - 3.0 * usq);
+          fout[dst] = -fs + WJ(j) * k.initDensity * (2.0 + 9.0 * (vuj * vuj) - 3.0 * usq);
         } else if (tl == 11) {
-          a.fout[dst] = fs;
+          fout[dst] = fs;
         } else if (tl == 7 || tl == 8) {
           // wall velocity is zero: BBi == 0 for dynamic walls as well
           const double bb = 2.0 * (fs - sp[j]) - 0.0;
           const uint32_t w = a.solid[lk];
           if (w < (uint32_t)k.nWall) {
-            if (CX(j)) atomicAdd(&acc[ACC_WALL + 3 * w + 0], CX(j) > 0 ? bb : -bb);
-            if (CY(j)) atomicAdd(&acc[ACC_WALL + 3 * w + 1], CY(j) > 0 ? bb : -bb);
-            if (CZ(j)) atomicAdd(&acc[ACC_WALL + 3 * w + 2], CZ(j) > 0 ? bb : -bb);
+            if (CX(j)) bba.wall(acc, (int)w, 0, CX(j) > 0 ? bb : -bb);
+            if (CY(j)) bba.wall(acc, (int)w, 1, CY(j) > 0 ? bb : -bb);
+            if (CZ(j)) bba.wall(acc, (int)w, 2, CZ(j) > 0 ? bb : -bb);
           }
-          a.fout[dst] = fs;
+          fout[dst] = fs;
         } else if (tl == 12) {
           const int ov = a.objIdx[lk];
           const double* ob = a.obj + ov * OB_STRIDE;
@@ -320,16 +149,15 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
             const double rx = (double)lx - os[OB_X0] / k.uLength;
             const double ry = (double)ly - os[OB_X0 + 1] / k.uLength;
             const double rz = (double)lz - os[OB_X0 + 2] / k.uLength;
-            double* ac = &acc[ACC_OBJ + 6 * so];
-            if (CX(j)) atomicAdd(ac + 0, Fx);
-            if (CY(j)) atomicAdd(ac + 1, Fy);
-            if (CZ(j)) atomicAdd(ac + 2, Fz);
-            atomicAdd(ac + 3, ry * Fz - rz * Fy);
-            atomicAdd(ac + 4, rz * Fx - rx * Fz);
-            atomicAdd(ac + 5, rx * Fy - ry * Fx);
+            if (CX(j)) bba.obj(acc, (int)so, 0, Fx);
+            if (CY(j)) bba.obj(acc, (int)so, 1, Fy);
+            if (CZ(j)) bba.obj(acc, (int)so, 2, Fz);
+            bba.obj(acc, (int)so, 3, ry * Fz - rz * Fy);
+            bba.obj(acc, (int)so, 4, rz * Fx - rx * Fz);
+            bba.obj(acc, (int)so, 5, rx * Fy - ry * Fx);
           }
-          a.fout[dst] = fs - BBi;
-          atomicAdd(&acc[ACC_EXTRA], BBi * massOld);
+          fout[dst] = fs - BBi;
+          bba.extra += BBi * massOld;
         } else {
           atomicOr(a.iscal + IS_ERROR, ERR_TYPE);
         }
@@ -351,13 +179,16 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
       } else if (k.freeSurface) {
         a.mass[x] = s.n;  // LB::updateMass, fluid nodes (src/LB.cpp:1631-1634)
       }
+      if (allAct) nm |= BULK;
     }
+    if (valid && nm != m) a.mask[x] = nm;
     const unsigned ifb = __ballot_sync(0xffffffffu, act && t == 3);
     if (lane == 0 && ifb) atomicAdd(&snif, __popc(ifb));
     const unsigned acb = __ballot_sync(0xffffffffu, act);
     if (lane == 0 && acb) atomicAdd(&snact, (unsigned)__popc(acb));
     warpParticleReduce(key, pv, a.pFHydro, a.pMHydro, a.pSHydro, a.pFluidVol, k.nPart);
   }
+  bba.flush(acc);
   __syncthreads();
   for (int i = threadIdx.x; i < ACC_N; i += blockDim.x) {
     const double v = acc[i];
@@ -380,6 +211,25 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
       atomicMax(a.iscal + IS_BBOX + 3, sbox[3]);
       atomicMax(a.iscal + IS_BBOX + 4, sbox[4]);
       atomicMax(a.iscal + IS_BBOX + 5, sbox[5]);
+    }
+  }
+}
+
+// Particle kinematics in lattice units, once per LB step: x0/unit.Length and
+// x1/unit.Speed in double (the exact path divides them at every node of the
+// particle in the reference; the quotients are identical), and x0/L, x1/S,
+// w1/unit.AngVel in float for the mixed form.
+__global__ void particleKinematics(Consts k, const double* px0, const double* px1,
+                                   const double* pw1, double* pkd, float* pkf) {
+  const int P = k.nPart;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * P; i += gridDim.x * blockDim.x) {
+    const double xl = px0[i] / k.uLength, vl = px1[i] / k.uSpeed;
+    pkd[i] = xl;
+    pkd[3 * P + i] = vl;
+    if (pkf) {
+      pkf[i] = (float)xl;
+      pkf[3 * P + i] = (float)vl;
+      pkf[6 * P + i] = (float)(pw1[i] / k.uAngVel);
     }
   }
 }
@@ -408,9 +258,24 @@ __global__ void lbResetKernel(Consts k, double* pAcc, long long pAccLen, double*
 // Unit conversions at the end of LB::streaming / computeHydroForces and the
 // mass-redistribution amount (src/LB.cpp:1533-1543, 1966-1977, 1844-1847).
 __global__ void lbFinalizeKernel(Consts k, double* pF, double* pM, double* pV, double* obj,
-                                 double* wallF, double* scal, const int* iscal) {
+                                 double* wallF, double* scal, const int* iscal,
+                                 const float* pAccF, double* pS) {
   const int P = k.nPart;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+    if (pAccF) {
+      // mixed form: float sums [ACCF_N][P] of d (3), R_ab = sum r_a d_b (9)
+      // and massOld (1); torque = antisymmetric part of R, stresslet = R
+      // in physical units (src/LB.cpp:1941-1958)
+      const long long PP = P;
+      double R[9];
+      for (int c = 0; c < 9; ++c) R[c] = (double)pAccF[(3 + c) * PP + i];
+      for (int c = 0; c < 3; ++c) pF[c * P + i] = (double)pAccF[c * PP + i];
+      pM[i] = R[5] - R[7];
+      pM[P + i] = R[6] - R[2];
+      pM[2 * P + i] = R[1] - R[3];
+      for (int c = 0; c < 9; ++c) pS[c * P + i] = R[c] * k.uLength * k.uForce;
+      pV[i] = (double)pAccF[12 * PP + i];
+    }
     for (int c = 0; c < 3; ++c) {
       pF[c * P + i] *= k.uForce;
       pM[c * P + i] *= k.uTorque;
@@ -507,19 +372,33 @@ __global__ void fsUpdateMass(Consts k, FsArgs a) {
       const int tl = a.mask[lk] & TYPE_MASK;
       double term;
       if (tl == 3 || tl == 0) {
-        const double ms = a.fcur[(long long)OPPJ(j) * k.N + x] - a.fcur[(long long)j * k.N + lk];
+        const double ms = fdiff(k, a.fcur, OPPJ(j), x, j, lk);
         term = tl == 3 ? 0.5 * (a.mass[lk] + mx) * ms : 1.0 * ms;
       } else if (tl == 8 || tl == 12 || tl == 9) {
         if (!haveFs) {  // post-collision populations of this node, recomputed
-#pragma unroll
-          for (int q = 0; q < Q; ++q) fsl[q] = a.fold[(long long)q * k.N + x];
-          NodeState s;
           const bool pf = (m & PFLAG) != 0;
-          collideNode(k, fsl, pf, pf ? a.solid[x] : 0u, a.px0, a.px1, a.pw1, k.nPart,
-                      a.massNew[x], ix, iy, iz, s);
+          if (k.mixed) {
+            float g[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) g[q] = ((const float*)a.fold)[(long long)q * k.N + x];
+            NodeStateF s;
+            collideNodeMixed(k, g, pf, pf ? a.solid[x] : 0u, a.pkf, k.nPart,
+                             (float)a.massNew[x], ix, iy, iz, s);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) fsl[q] = (double)g[q];  // deviations
+          } else {
+#pragma unroll
+            for (int q = 0; q < Q; ++q) fsl[q] = ((const double*)a.fold)[(long long)q * k.N + x];
+            NodeState s;
+            collideNode(k, fsl, pf, pf ? a.solid[x] : 0u, a.pkd, a.pkd + 3 * k.nPart, a.pw1, k.nPart,
+                        a.massNew[x], ix, iy, iz, s);
+          }
           haveFs = true;
         }
-        const double ms = a.fcur[(long long)OPPJ(j) * k.N + x] - fsl[j];
+        // f_opp(x) after streaming minus the population x sent into the wall
+        const double ms = k.mixed
+            ? (double)((const float*)a.fcur)[(long long)OPPJ(j) * k.N + x] - fsl[j]
+            : ((const double*)a.fcur)[(long long)OPPJ(j) * k.N + x] - fsl[j];
         term = (1.0 * mx) * ms;
       } else {
         continue;
@@ -574,7 +453,7 @@ __global__ void fsSmoothen(Consts k, FsArgs a) {
         const double uz = Fz / 2.0 / rho0 + a.uS[2 * k.N + win];
         const double usq = ux * ux + uy * uy + uz * uz;
 #pragma unroll
-        for (int j = 0; j < Q; ++j) a.fcur[(long long)j * k.N + x] = feqj(j, rho0, ux, uy, uz, usq);
+        for (int j = 0; j < Q; ++j) fset(k, a.fcur, j, x, feqj(j, rho0, ux, uy, uz, usq));
         a.mask[x] = (uint8_t)((m & ~TYPE_MASK) | 3);
         a.fsflag[x] |= FS_NEW;
         a.rhoS[x] = rho0;
@@ -590,7 +469,8 @@ __global__ void fsSmoothen(Consts k, FsArgs a) {
           break;
         }
       if (hit) {
-        const double n = (a.fsflag[x] & FS_FILLED) ? a.rhoS[x] : a.mass[x];
+        const double n = (a.fsflag[x] & FS_FILLED) ? a.rhoS[x]
+                       : (k.mixed ? (double)a.nF[x] : a.mass[x]);
         a.mask[x] = (uint8_t)((m & ~TYPE_MASK) | 3);
         a.fsflag[x] |= FS_NEW;
         a.rhoS[x] = n;
@@ -614,6 +494,7 @@ __global__ void fsMutantsAndFill(Consts k, FsArgs a) {
     } else if ((fl & FS_FILLED) && !(fl & FS_NEW)) {
       surplus += a.mass[x] - a.rhoS[x];
       a.mass[x] = a.rhoS[x];
+      if (k.mixed) a.nF[x] = (float)a.rhoS[x];
     } else if ((m & TYPE_MASK) == 3) {
       bool gasNb = false;
 #pragma unroll 1
@@ -625,6 +506,7 @@ __global__ void fsMutantsAndFill(Consts k, FsArgs a) {
       if (!gasNb) {
         surplus += a.mass[x] - a.rhoS[x];
         a.mass[x] = a.rhoS[x];
+        if (k.mixed) a.nF[x] = (float)a.rhoS[x];
         a.mask[x] = (uint8_t)((m & ~TYPE_MASK) | 0);
       }
     }
@@ -722,8 +604,8 @@ __global__ void uncoverCollect(Consts k, const uint8_t* mask, const double* obj,
 // reference's serial order (ascending node index, each node seeing the new
 // types of the lower-index ones) by fixed-point iteration, then initialise
 // them (src/LB.cpp:874-940).
-__global__ void __launch_bounds__(1024) uncoverResolve(Consts k, uint8_t* mask, double* f,
-                                                       double* mass, uint32_t* list,
+__global__ void __launch_bounds__(1024) uncoverResolve(Consts k, uint8_t* mask, void* f,
+                                                       double* mass, float* nF, uint32_t* list,
                                                        int* iscal) {
   __shared__ uint32_t s_idx[UNCOVER_CAP];
   __shared__ uint8_t s_st[UNCOVER_CAP];
@@ -810,8 +692,28 @@ __global__ void __launch_bounds__(1024) uncoverResolve(Consts k, uint8_t* mask, 
     const double ux = k.lbF[0] / 2.0 / rho0 + vx, uy = k.lbF[1] / 2.0 / rho0 + vy,
                  uz = k.lbF[2] / 2.0 / rho0 + vz;
     const double usq = ux * ux + uy * uy + uz * uz;
-    for (int j = 0; j < Q; ++j) f[(long long)j * k.N + x] = feqj(j, rho0, ux, uy, uz, usq);
+    for (int j = 0; j < Q; ++j) fset(k, f, j, x, feqj(j, rho0, ux, uy, uz, usq));
     mass[x] = st == 0 ? rho0 : 0.5 * rho0;
+    if (k.mixed && st == 0) nF[x] = (float)rho0;
+  }
+}
+
+// Neighbour-cache upkeep after the free-surface step: the nodes that left
+// the active types (interface -> gas) lie in the interface box grown by 1,
+// so their neighbours lie in the box grown by 2.
+__global__ void fsClearBulk(Consts k, uint8_t* mask, const int* iscal) {
+  if (iscal[IS_BBOX + 3] < 0) return;
+  const int x0 = max(iscal[IS_BBOX + 0] - 2, 0), y0 = max(iscal[IS_BBOX + 1] - 2, 0),
+            z0 = max(iscal[IS_BBOX + 2] - 2, 0);
+  const long long rx = min(iscal[IS_BBOX + 3] + 2, k.X - 1) - x0 + 1,
+                  ry = min(iscal[IS_BBOX + 4] + 2, k.Y - 1) - y0 + 1,
+                  rz = min(iscal[IS_BBOX + 5] + 2, k.Z - 1) - z0 + 1;
+  const long long vol = rx * ry * rz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long x = (x0 + i % rx) + (y0 + (i / rx) % ry) * k.sy + (z0 + i / (rx * ry)) * k.sz;
+    const uint8_t m = mask[x];
+    if (m & BULK) mask[x] = (uint8_t)(m & ~BULK);
   }
 }
 
@@ -845,8 +747,14 @@ __global__ void voxelizeObjects(Consts k, uint8_t* mask, uint32_t* solid, uint8_
                        ob[OB_R] / k.uLength))
         last = o;
     }
-    if (last < 0) continue;
-    mask[x] = (uint8_t)((mask[x] & ~TYPE_MASK) | 12);
+    // the box reaches one node past the sphere, so it holds every neighbour
+    // of a node turned into an impactor node: drop their neighbour cache
+    const uint8_t m0 = mask[x];
+    if (last < 0) {
+      if (m0 & BULK) mask[x] = (uint8_t)(m0 & ~BULK);
+      continue;
+    }
+    mask[x] = (uint8_t)((m0 & ~(TYPE_MASK | BULK)) | 12);
     solid[x] = (uint32_t)obj[last * OB_STRIDE + OB_INDEX];
     objIdx[x] = (uint8_t)last;
     mass[x] = 0.0;
@@ -1008,7 +916,7 @@ __global__ void initTypes(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* obj
 // interface nodes; active nodes start at equilibrium. Typing in place is safe:
 // a fluid->interface change never alters any node's gas neighbourhood. Also
 // the first cleanLists (active-list bit).
-__global__ void initFields(Consts k, uint8_t* mask, double* f, double* mass) {
+__global__ void initFields(Consts k, uint8_t* mask, void* f, double* mass, float* nF) {
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
        x += (long long)gridDim.x * blockDim.x) {
     int t = mask[x] & TYPE_MASK;
@@ -1026,9 +934,10 @@ __global__ void initFields(Consts k, uint8_t* mask, double* f, double* mass) {
       const double uy = k.lbF[1] / 2.0 / rho0 + k.initVel[1];
       const double uz = k.lbF[2] / 2.0 / rho0 + k.initVel[2];
       const double usq = ux * ux + uy * uy + uz * uz;
-      for (int j = 0; j < Q; ++j) f[(long long)j * k.N + x] = feqj(j, rho0, ux, uy, uz, usq);
+      for (int j = 0; j < Q; ++j) fset(k, f, j, x, feqj(j, rho0, ux, uy, uz, usq));
       ms = t == 0 ? rho0 : 0.5 * rho0;
       mask[x] = (uint8_t)((mask[x] & ~TYPE_MASK) | t | ABIT);
+      if (k.mixed && t == 0) nF[x] = (float)rho0;
     }
     mass[x] = ms;
   }
@@ -1037,7 +946,7 @@ __global__ void initFields(Consts k, uint8_t* mask, double* f, double* mass) {
 // ---- diagnostics --------------------------------------------------------------
 
 __global__ void massSummaryKernel(Consts k, const uint8_t* mask, const double* mass,
-                                  double* out, unsigned long long* cnt) {
+                                  const float* nF, double* out, unsigned long long* cnt) {
   double s = 0.0;
   unsigned long long ni = 0, na = 0;
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
@@ -1047,7 +956,7 @@ __global__ void massSummaryKernel(Consts k, const uint8_t* mask, const double* m
     if (isActiveT(t)) {
       ++na;
       if (t == 3) ++ni;
-      if (!(m & PFLAG)) s += mass[x];
+      if (!(m & PFLAG)) s += (k.mixed && t == 0) ? (double)nF[x] : mass[x];
     }
   }
   blockAddDouble(s, out);
@@ -1062,7 +971,7 @@ __global__ void massSummaryKernel(Consts k, const uint8_t* mask, const double* m
 }
 
 // Moments of the current populations, for state download.
-__global__ void momentsKernel(Consts k, const uint8_t* mask, const double* f, double* n,
+__global__ void momentsKernel(Consts k, const uint8_t* mask, const void* f, double* n,
                               double* u) {
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
        x += (long long)gridDim.x * blockDim.x) {
@@ -1071,17 +980,13 @@ __global__ void momentsKernel(Consts k, const uint8_t* mask, const double* f, do
       u[x] = u[k.N + x] = u[2 * k.N + x] = 0.0;
       continue;
     }
-    double fl[Q];
-    double s = 0.0;
+    double s = 0.0, ux = 0.0, uy = 0.0, uz = 0.0;
     for (int j = 0; j < Q; ++j) {
-      fl[j] = f[(long long)j * k.N + x];
-      s += fl[j];
-    }
-    double ux = 0, uy = 0, uz = 0;
-    for (int j = 0; j < Q; ++j) {
-      ux += CX(j) * fl[j];
-      uy += CY(j) * fl[j];
-      uz += CZ(j) * fl[j];
+      const double fj = fget(k, f, j, x);
+      s += fj;
+      ux += CX(j) * fj;
+      uy += CY(j) * fj;
+      uz += CZ(j) * fj;
     }
     n[x] = s;
     u[x] = ux / s;
@@ -1090,12 +995,24 @@ __global__ void momentsKernel(Consts k, const uint8_t* mask, const double* f, do
   }
 }
 
-__global__ void nonfiniteCheck(Consts k, const uint8_t* mask, const double* f, int* iscal) {
+// Populations and masses of the active nodes as doubles, for state download.
+__global__ void exportLattice(Consts k, const uint8_t* mask, const void* f, const double* mass,
+                              const float* nF, double* fOut, double* massOut) {
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
+       x += (long long)gridDim.x * blockDim.x) {
+    const int t = mask[x] & TYPE_MASK;
+    const bool act = isActiveT(t);
+    for (int j = 0; j < Q; ++j) fOut[(long long)j * k.N + x] = act ? fget(k, f, j, x) : 0.0;
+    massOut[x] = (k.mixed && t == 0 && k.freeSurface) ? (double)nF[x] : mass[x];
+  }
+}
+
+__global__ void nonfiniteCheck(Consts k, const uint8_t* mask, const void* f, int* iscal) {
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
        x += (long long)gridDim.x * blockDim.x) {
     if (!isActiveT(mask[x] & TYPE_MASK)) continue;
     double s = 0.0;
-    for (int j = 0; j < Q; ++j) s += f[(long long)j * k.N + x];
+    for (int j = 0; j < Q; ++j) s += fget(k, f, j, x);
     if (!isfinite(s)) atomicOr(iscal + IS_ERROR, ERR_NONFINITE);
   }
 }

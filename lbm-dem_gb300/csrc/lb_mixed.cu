@@ -1,0 +1,329 @@
+// Mixed-precision lattice step: FP32 deviation storage (f - w, 76 B per
+// node per lattice), FP32 collision with the reference's BGK + Guo forcing
+// and particle coupling, push streaming with the reference's boundary rules
+// rewritten for deviations. Interface masses, the free-surface mass budget
+// and all DEM state stay FP64; the per-particle coupling sums are float
+// partial sums converted once per particle (lbFinalizeKernel).
+//
+// Reference: LB::latticeBolzmannStep (src/LB.cpp:400-418) with
+// node::reconstruct/shiftVelocity/computeEquilibrium/solveCollision/addForce
+// (src/node.cpp:75-207), LB::computeHydroForces (src/LB.cpp:1901-1978) and
+// LB::streaming (src/LB.cpp:1334-1544). In deviation form (initDensity = 1):
+//   gas neighbour:     g_opp = -g_j + w_j (9 (c_j.u)^2 - 3 u^2)
+//   static wall:       g_opp = g_j,           force 2 g_j c_j
+//   moving object:     g_opp = g_j - BBi,     force (2 g_j - BBi) c_j
+// This file is compiled without implicit FMA contraction; the collision uses
+// explicit fused multiply-adds (lattice_common.cuh).
+//
+// Layout of the work: one warp handles 32 consecutive nodes of the x-major
+// lattice per iteration of a grid-stride loop. The 18 streaming links are
+// resolved in an unrolled loop that only knows "active neighbour" and "gas
+// neighbour"; links to walls, slip walls and impactors are marked and
+// handled afterwards in one non-unrolled loop, which keeps the hot loop
+// small enough for the instruction caches.
+#include "lattice_common.cuh"
+
+namespace lbdem {
+
+namespace {
+
+// direction j packed for the dynamic-index boundary path:
+// bits 0-1 cx+1, 2-3 cy+1, 4-5 cz+1, 8-12 opposite direction
+__host__ __device__ constexpr int packDir(int j) {
+  return (CX(j) + 1) | ((CY(j) + 1) << 2) | ((CZ(j) + 1) << 4) | (OPPJ(j) << 8);
+}
+__constant__ int c_dir[Q] = {packDir(0),  packDir(1),  packDir(2),  packDir(3),  packDir(4),
+                             packDir(5),  packDir(6),  packDir(7),  packDir(8),  packDir(9),
+                             packDir(10), packDir(11), packDir(12), packDir(13), packDir(14),
+                             packDir(15), packDir(16), packDir(17), packDir(18)};
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr unsigned ALL_LINKS = 0x7FFFEu;  // bits 1..18
+
+// Segmented reduction of the particle coupling terms over runs of
+// consecutive lanes that share a particle index and a lattice row, then one
+// set of float atomics per run (issued by the run heads together).
+//
+// Per run only 7 sums are needed: D = sum d, L = sum o d with o the lane's
+// offset from the run head, and V = sum massOld. With r the node position
+// relative to the particle centre, r_y and r_z are the same for every node
+// of a run and r_x = r_x(head) + o, so
+//   R_ab = sum r_a d_b:  R_xb = L_b + r_x(head) D_b,  R_yb = r_y D_b,
+//   R_zb = r_z D_b.
+// The accumulators hold D (3), R (9, row-major a*3+b) and V; the torque
+// (antisymmetric part of R) and the stresslet (R scaled) are formed per
+// particle in lbFinalizeKernel.
+__device__ __forceinline__ void particleRunReduce(int key, int ix, float dx, float dy, float dz,
+                                                  float rx, float ry, float rz, float massOld,
+                                                  float* acc, int P) {
+  const int lane = threadIdx.x & 31;
+  const unsigned pm = __ballot_sync(FULL, key >= 0);
+  const int prevKey = __shfl_up_sync(FULL, key, 1);
+  const bool head = key >= 0 && (lane == 0 || prevKey != key || ix == 0);
+  const unsigned hm = __ballot_sync(FULL, head);
+  const unsigned stop = hm | ~pm;
+  const unsigned upto = lane == 31 ? FULL : (2u << lane) - 1u;  // lanes 0..lane
+  const unsigned above = stop & ~upto;
+  const int end = above ? __ffs(above) - 1 : 32;
+  const int headLane = 31 - __clz(hm & upto);  // meaningful for key >= 0
+  const int maxLen = (int)__reduce_max_sync(FULL, head ? (unsigned)(end - lane) : 0u);
+  const float o = key >= 0 ? (float)(lane - headLane) : 0.0f;
+  float v[7] = {dx, dy, dz, o * dx, o * dy, o * dz, massOld};
+  for (int st = 1; st < maxLen; st <<= 1) {
+    const bool take = lane + st < end;
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+      const float t = __shfl_down_sync(FULL, v[i], st);
+      if (take) v[i] += t;
+    }
+  }
+  if (head) {
+    float* q = acc + key;
+    const long long PP = P;
+    atomicAdd(q, v[0]);
+    atomicAdd(q + PP, v[1]);
+    atomicAdd(q + 2 * PP, v[2]);
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      atomicAdd(q + (3 + b) * PP, __fmaf_rn(rx, v[b], v[3 + b]));
+      atomicAdd(q + (6 + b) * PP, ry * v[b]);
+      atomicAdd(q + (9 + b) * PP, rz * v[b]);
+    }
+    atomicAdd(q + 12 * PP, v[6]);
+  }
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
+  __shared__ float accW[3 * MAX_WALL];
+  __shared__ float accO[6 * MAX_OBJ];
+  __shared__ double accX;
+  __shared__ int sbox[6];
+  __shared__ unsigned scnt[2];
+  for (int i = threadIdx.x; i < 3 * MAX_WALL; i += blockDim.x) accW[i] = 0.0f;
+  for (int i = threadIdx.x; i < 6 * MAX_OBJ; i += blockDim.x) accO[i] = 0.0f;
+  if (threadIdx.x < 3) sbox[threadIdx.x] = INT_MAX;
+  else if (threadIdx.x < 6) sbox[threadIdx.x] = -1;
+  if (threadIdx.x == 0) {
+    accX = 0.0;
+    scnt[0] = scnt[1] = 0u;
+  }
+  __syncthreads();
+  const float* __restrict__ gin = (const float*)a.fin;
+  float* __restrict__ gout = (float*)a.fout;
+  const uint8_t* mk = a.mask;
+  // node indices fit 32 bits (checked when the run is created)
+  const unsigned N = (unsigned)k.N;
+  const size_t NN = (size_t)k.N;
+  const int lane = threadIdx.x & 31;
+  const unsigned warpsPerBlock = blockDim.x >> 5;
+  const unsigned gw = blockIdx.x * warpsPerBlock + (threadIdx.x >> 5);
+  const unsigned stride = gridDim.x * warpsPerBlock * 32u;
+  const int X = k.X, Y = k.Y, sy = (int)k.sy, sz = (int)k.sz;
+  // coordinates of this lane's node, advanced by the stride each iteration
+  int ix, iy, iz;
+  coords(k, (long long)gw * 32 + lane, ix, iy, iz);
+  int dsx, dsy, dsz;
+  coords(k, (long long)stride, dsx, dsy, dsz);
+  double extra = 0.0;
+  unsigned nact = 0, nif = 0;
+  for (unsigned base = gw * 32u; base < N; base += stride) {
+    const unsigned x = base + lane;
+    const bool valid = x < N;
+    const uint8_t m = valid ? mk[x] : (uint8_t)2;
+    const int t = m & TYPE_MASK;
+    const bool act = valid && isActiveT(t);
+    // cleanLists (ABIT) and the neighbour cache (BULK) of this node
+    uint8_t nm = (uint8_t)(m & ~(ABIT | BULK));
+    if (__any_sync(FULL, act)) {
+      float g[Q];
+      unsigned actN = ALL_LINKS, gasN = 0;
+      NodeStateF s;
+      s.dx = s.dy = s.dz = s.rx = s.ry = s.rz = 0.0f;
+      float massOld = 0.0f;
+      int key = -1;
+      if (act) {
+#pragma unroll
+        for (int j = 0; j < Q; ++j) g[j] = __ldcs(gin + j * NN + x);
+        if (!(m & BULK)) {
+          actN = 0;
+#pragma unroll
+          for (int j = 1; j < Q; ++j) {
+            const int tl = mk[x + (unsigned)(CX(j) + CY(j) * sy + CZ(j) * sz)] & TYPE_MASK;
+            actN |= (unsigned)isActiveT(tl) << j;
+            gasN |= (unsigned)(tl == 2) << j;
+          }
+        }
+        nm |= (uint8_t)(ABIT | (actN == ALL_LINKS ? BULK : 0));
+        const bool pf = (m & PFLAG) != 0;
+        const uint32_t pid = pf ? a.solid[x] : 0u;
+        if (pf) massOld = t == 3 ? (float)a.mass[x] : a.nF[x];
+        collideNodeMixed(k, g, pf, pid, a.pkf, k.nPart, massOld, ix, iy, iz, s);
+        if (pf) {
+          if (pid < (uint32_t)k.nPart) key = (int)pid;
+          else atomicOr(a.iscal + IS_ERROR, ERR_PARTICLE_INDEX);
+        }
+        if (key < 0) massOld = 0.0f;
+      }
+      if (__any_sync(FULL, key >= 0))
+        particleRunReduce(key, ix, s.dx, s.dy, s.dz, s.rx, s.ry, s.rz, massOld, a.pAccF,
+                          k.nPart);
+      if (act) {
+        ++nact;
+        __stcs(gout + x, g[0]);
+        const float usq3 = 3.0f * __fmaf_rn(s.ux, s.ux, __fmaf_rn(s.uy, s.uy, s.uz * s.uz));
+#pragma unroll
+        for (int j = 1; j < Q; ++j) {
+          if ((actN >> j) & 1u) {
+            __stcs(gout + j * NN + (x + (unsigned)(CX(j) + CY(j) * sy + CZ(j) * sz)), g[j]);
+          } else {
+            float out = g[j];
+            if ((gasN >> j) & 1u) {
+              const float vu = dotcf(j, s.ux, s.uy, s.uz);
+              out = __fmaf_rn((float)WJ(j), __fmaf_rn(9.0f * vu, vu, -usq3), -g[j]);
+            }
+            gout[OPPJ(j) * NN + x] = out;
+          }
+        }
+        // walls, slip walls, impactors and unexpected types: the value
+        // stored above is g_j; fix it up and add the link forces
+        unsigned special = ~(actN | gasN) & ALL_LINKS;
+        if (special) {
+          float fw[3] = {0.0f, 0.0f, 0.0f}, fo[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+          int wcur = -1, ocur = -1;
+#pragma unroll 1
+          for (; special; special &= special - 1u) {
+            const int j = __ffs(special) - 1;
+            const int dj = c_dir[j];
+            const int cx = (dj & 3) - 1, cy = ((dj >> 2) & 3) - 1, cz = ((dj >> 4) & 3) - 1;
+            const unsigned lk = x + (unsigned)(cx + cy * sy + cz * sz);
+            const int tl = mk[lk] & TYPE_MASK;
+            float* dst = gout + (size_t)(dj >> 8) * NN + x;
+            const float gj = *dst;
+            if (tl == 11) continue;
+            if (tl == 7 || tl == 8) {
+              const uint32_t w = a.solid[lk];
+              if (w < (uint32_t)k.nWall) {
+                if ((int)w != wcur) {
+                  if (wcur >= 0)
+                    for (int c = 0; c < 3; ++c) atomicAdd(&accW[3 * wcur + c], fw[c]);
+                  fw[0] = fw[1] = fw[2] = 0.0f;
+                  wcur = (int)w;
+                }
+                const float bb = 2.0f * gj;
+                fw[0] += (float)cx * bb;
+                fw[1] += (float)cy * bb;
+                fw[2] += (float)cz * bb;
+              }
+            } else if (tl == 12) {
+              const double* ob = a.obj + a.objIdx[lk] * OB_STRIDE;
+              const float vx = (float)(ob[OB_X1] / k.uSpeed),
+                          vy = (float)(ob[OB_X1 + 1] / k.uSpeed),
+                          vz = (float)(ob[OB_X1 + 2] / k.uSpeed);
+              const float wj = j == 0 ? (float)WJ(0) : j <= 6 ? (float)WJ(1) : (float)WJ(7);
+              const float cv = __fmaf_rn((float)cx, vx, __fmaf_rn((float)cy, vy, (float)cz * vz));
+              const float BBi = 6.0f * s.n * wj * cv;
+              const uint32_t so = a.solid[lk];
+              if (so < (uint32_t)k.nObj) {
+                if ((int)so != ocur) {
+                  if (ocur >= 0)
+                    for (int c = 0; c < 6; ++c) atomicAdd(&accO[6 * ocur + c], fo[c]);
+                  for (int c = 0; c < 6; ++c) fo[c] = 0.0f;
+                  ocur = (int)so;
+                }
+                const double* os = a.obj + so * OB_STRIDE;
+                const float bb = 2.0f * gj - BBi;
+                const float Fx = (float)cx * bb, Fy = (float)cy * bb, Fz = (float)cz * bb;
+                const int lx = ix + cx, ly = iy + cy, lz = iz + cz;
+                const float rx = (float)((double)lx - os[OB_X0] / k.uLength);
+                const float ry = (float)((double)ly - os[OB_X0 + 1] / k.uLength);
+                const float rz = (float)((double)lz - os[OB_X0 + 2] / k.uLength);
+                fo[0] += Fx;
+                fo[1] += Fy;
+                fo[2] += Fz;
+                fo[3] += ry * Fz - rz * Fy;
+                fo[4] += rz * Fx - rx * Fz;
+                fo[5] += rx * Fy - ry * Fx;
+              }
+              *dst = gj - BBi;
+              const double mo = t == 3 ? a.mass[x] : (double)a.nF[x];
+              extra += (double)BBi * mo;
+            } else {
+              atomicOr(a.iscal + IS_ERROR, ERR_TYPE);
+            }
+          }
+          if (wcur >= 0)
+            for (int c = 0; c < 3; ++c) atomicAdd(&accW[3 * wcur + c], fw[c]);
+          if (ocur >= 0)
+            for (int c = 0; c < 6; ++c) atomicAdd(&accO[6 * ocur + c], fo[c]);
+        }
+        if (t == 3) {
+          ++nif;
+          a.rhoS[x] = s.n;
+          a.uS[x] = s.ux;
+          a.uS[NN + x] = s.uy;
+          a.uS[2 * NN + x] = s.uz;
+          a.hS[x] = s.hx;
+          a.hS[NN + x] = s.hy;
+          a.hS[2 * NN + x] = s.hz;
+          atomicMin(&sbox[0], ix);
+          atomicMin(&sbox[1], iy);
+          atomicMin(&sbox[2], iz);
+          atomicMax(&sbox[3], ix);
+          atomicMax(&sbox[4], iy);
+          atomicMax(&sbox[5], iz);
+        } else if (k.freeSurface) {
+          a.nF[x] = s.n;  // LB::updateMass fluid rule: mass = density
+        }
+      }
+    }
+    if (valid && nm != m) a.mask[x] = nm;
+    // advance this lane's coordinates by the stride
+    ix += dsx;
+    iy += dsy;
+    iz += dsz;
+    if (ix >= X) {
+      ix -= X;
+      ++iy;
+    }
+    if (iy >= Y) {
+      iy -= Y;
+      ++iz;
+    }
+  }
+  // block totals
+  nact = __reduce_add_sync(FULL, nact);
+  nif = __reduce_add_sync(FULL, nif);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) extra += __shfl_xor_sync(FULL, extra, o);
+  if (lane == 0) {
+    if (nact) atomicAdd(&scnt[0], nact);
+    if (nif) atomicAdd(&scnt[1], nif);
+    if (extra != 0.0) atomicAdd(&accX, extra);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 3 * MAX_WALL; i += blockDim.x)
+    if (accW[i] != 0.0f) atomicAdd(a.wallF + (i / 3) * 12 + (i % 3), (double)accW[i]);
+  for (int i = threadIdx.x; i < 6 * MAX_OBJ; i += blockDim.x) {
+    if (accO[i] == 0.0f) continue;
+    const int o = i / 6, c = i % 6;
+    atomicAdd(a.obj + o * OB_STRIDE + (c < 3 ? OB_FHYDRO + c : OB_MHYDRO + c - 3),
+              (double)accO[i]);
+  }
+  if (threadIdx.x == 0) {
+    if (accX != 0.0) atomicAdd(a.scal + SC_EXTRA_MASS, accX);
+    if (scnt[0]) atomicAdd(a.uscal + US_ACTIVE_UPDATES, (unsigned long long)scnt[0]);
+    if (scnt[1]) atomicAdd(a.iscal + IS_NIF, (int)scnt[1]);
+    if (sbox[3] >= 0) {
+      atomicMin(a.iscal + IS_BBOX + 0, sbox[0]);
+      atomicMin(a.iscal + IS_BBOX + 1, sbox[1]);
+      atomicMin(a.iscal + IS_BBOX + 2, sbox[2]);
+      atomicMax(a.iscal + IS_BBOX + 3, sbox[3]);
+      atomicMax(a.iscal + IS_BBOX + 4, sbox[4]);
+      atomicMax(a.iscal + IS_BBOX + 5, sbox[5]);
+    }
+  }
+}
+
+}  // namespace lbdem

@@ -63,8 +63,9 @@ LbArgs lbArgs(lbdem_ctx* c) {
   Device& d = c->d;
   const int P = std::max(c->nPart, 1);
   LbArgs a;
-  a.fin = (const double*)d.f[c->cur];
-  a.fout = (double*)d.f[1 - c->cur];
+  a.fin = d.f[c->cur];
+  a.fout = d.f[1 - c->cur];
+  a.nF = d.nF;
   a.mask = d.mask;
   a.solid = d.solid;
   a.objIdx = d.objIdx;
@@ -75,10 +76,13 @@ LbArgs lbArgs(lbdem_ctx* c) {
   a.px0 = d.px0;
   a.px1 = d.px1;
   a.pw1 = d.pw1;
+  a.pkd = d.pkd;
+  a.pkf = d.pkf;
   a.pFHydro = d.pFHydro;
   a.pMHydro = d.pMHydro;
   a.pSHydro = d.pSHydro;
   a.pFluidVol = d.pFluidVol;
+  a.pAccF = d.pAccF;
   a.obj = d.obj;
   a.wallF = d.wallF;
   a.scal = d.scal;
@@ -103,8 +107,9 @@ std::pair<cudaEvent_t, cudaEvent_t>* nextLbEvents(lbdem_ctx* c) {
 FsArgs fsArgs(lbdem_ctx* c) {
   Device& d = c->d;
   FsArgs a;
-  a.fcur = (double*)d.f[c->cur];
-  a.fold = (const double*)d.f[1 - c->cur];
+  a.fcur = d.f[c->cur];
+  a.fold = d.f[1 - c->cur];
+  a.nF = d.nF;
   a.mask = d.mask;
   a.solid = d.solid;
   a.objIdx = d.objIdx;
@@ -117,6 +122,8 @@ FsArgs fsArgs(lbdem_ctx* c) {
   a.px0 = d.px0;
   a.px1 = d.px1;
   a.pw1 = d.pw1;
+  a.pkd = d.pkd;
+  a.pkf = d.pkf;
   a.obj = d.obj;
   a.scal = d.scal;
   a.iscal = d.iscal;
@@ -201,8 +208,8 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   ctx->precision = precision;
   ctx->device = opt ? opt->device : 0;
   ctx->check_every = opt ? opt->check_every : 0;
-  if (precision != LBDEM_PLAIN_FP64)
-    return setErr(ctx, LBDEM_ERR_INVALID, "precision form not available in this build");
+  if (precision != LBDEM_PLAIN_FP64 && precision != LBDEM_MIXED)
+    return setErr(ctx, LBDEM_ERR_INVALID, "unknown precision form");
   // ---- validation (the supported subset of the reference's inputs) ----
   if (!cfg->rheologyNewtonian || cfg->turbulenceSolve || cfg->lbRestart || cfg->lbTopography)
     return setErr(ctx, LBDEM_ERR_INVALID,
@@ -224,6 +231,11 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
   ctx->stream = ctx->own_stream;
   CK(cudaDeviceGetAttribute(&ctx->smCount, cudaDevAttrMultiProcessorCount, ctx->device));
+  {
+    int perSm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, lbStepMixed, 256, 0));
+    ctx->lbMixedBlocks = std::max(1, perSm) * std::max(1, ctx->smCount);
+  }
 
   Consts& k = ctx->k;
   std::memset(&k, 0, sizeof(k));
@@ -257,9 +269,16 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   k.initVisc = cfg->initVisc / uDynVisc;
   k.omega = 1.0 / (0.5 + 3.0 * k.initVisc);
   k.omegaf = 1.0 - 1.0 / (1.0 + 6.0 * k.initVisc);
+  k.mixed = precision == LBDEM_MIXED ? 1 : 0;
+  if (k.mixed && k.N >= (1LL << 31))
+    return setErr(ctx, LBDEM_ERR_INVALID, "mixed form: lattice larger than 2^31 nodes");
+  k.omegaF = (float)k.omega;
+  k.omegafF = (float)k.omegaf;
+  k.sLF = (float)(k.uLength * k.uForce);
   for (int a = 0; a < 3; ++a) {
     k.lbF[a] = cfg->lbF[a] / k.uAccel;
     ctx->lbFConfig[a] = k.lbF[a];
+    k.lbFf[a] = (float)k.lbF[a];
     k.initVel[a] = cfg->initVelocity[a] / k.uSpeed;
   }
   const unsigned s[3] = {(unsigned)k.X, (unsigned)k.Y, (unsigned)k.Z};
@@ -367,12 +386,22 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   AL(d.objIdx, N);
   AL(d.claim, N);
   AL(d.fsflag, N);
-  double* f0 = nullptr;
-  double* f1 = nullptr;
-  AL(f0, (size_t)Q * N);
-  AL(f1, (size_t)Q * N);
-  d.f[0] = f0;
-  d.f[1] = f1;
+  if (k.mixed) {
+    float* f0 = nullptr;
+    float* f1 = nullptr;
+    AL(f0, (size_t)Q * N);
+    AL(f1, (size_t)Q * N);
+    d.f[0] = f0;
+    d.f[1] = f1;
+    AL(d.nF, N);
+  } else {
+    double* f0 = nullptr;
+    double* f1 = nullptr;
+    AL(f0, (size_t)Q * N);
+    AL(f1, (size_t)Q * N);
+    d.f[0] = f0;
+    d.f[1] = f1;
+  }
   AL(d.mass, N);
   AL(d.massNew, N);
   AL(d.rhoS, N);
@@ -388,6 +417,9 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   AL(d.pr, P1);
   AL(d.pinvm, P1);
   AL(d.pinvI, P1);
+  AL(d.pkd, 6 * P1);
+  if (k.mixed) AL(d.pkf, 9 * P1);
+  if (k.mixed) AL(d.pAccF, ACCF_N * P1);
   // hydro accumulators contiguous (reset together each LB step)
   double* hyd = nullptr;
   AL(hyd, 16 * P1);
@@ -454,7 +486,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   if (ctx->lbSolve) {
     initTypes<<<lg, 256, 0, st>>>(k, d.mask, d.solid, d.objIdx, dBoundary, d.walls, dWallType,
                                   d.obj, cfg->fluidHeight / L, k.freeSurface);
-    initFields<<<lg, 256, 0, st>>>(k, d.mask, (double*)d.f[0], d.mass);
+    initFields<<<lg, 256, 0, st>>>(k, d.mask, d.f[0], d.mass, d.nF);
     if ((rc = launchErr(ctx, "lattice init")) != LBDEM_OK) return rc;
   }
   // ---- initial neighbour list (DEM::discreteElementInit, :294-296) ----
@@ -479,7 +511,7 @@ extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
                   d.massNew, d.rhoS, d.uS, d.hS, d.scal, d.iscal, d.uscal, d.px0, d.px1,
                   d.pw1, d.pr, d.pinvm, d.pinvI, d.pFHydro, d.pFContact, d.pMContact,
                   d.pFLub, d.pMLub, d.pFRep, d.pFTotal, d.pMTotal, d.pFGrav, d.pxiw,
-                  d.pxio, d.plist[0], d.plist[1], d.pxi[0], d.pxi[1], d.partner, d.gorder,
+                  d.pxio, d.nF, d.pkd, d.pkf, d.pAccF, d.plist[0], d.plist[1], d.pxi[0], d.pxi[1], d.partner, d.gorder,
                   d.pairbuf, d.pairflag, d.pcell, d.ppos, d.cellCount, d.cellStart,
                   d.cellFill, d.cellParts, d.obj, d.wallF, d.walls, d.uncover};
   if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
@@ -534,7 +566,7 @@ extern "C" int lbdem_coupling_step(lbdem_ctx* ctx) {
   if (ctx->nObj > 0) {
     cudaMemsetAsync(d.iscal + IS_NUNCOVER, 0, sizeof(int), s);
     uncoverCollect<<<lg, 256, 0, s>>>(k, d.mask, d.obj, d.uncover, d.iscal);
-    uncoverResolve<<<1, 1024, 0, s>>>(k, d.mask, (double*)d.f[ctx->cur], d.mass, d.uncover,
+    uncoverResolve<<<1, 1024, 0, s>>>(k, d.mask, d.f[ctx->cur], d.mass, d.nF, d.uncover,
                                       d.iscal);
     voxelizeObjects<<<lg, 256, 0, s>>>(k, d.mask, d.solid, d.objIdx, d.mass, d.obj);
     ctx->launches += 3;
@@ -552,6 +584,7 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   if (!ctx->k.forceField && !ctx->lbFReset) {  // LB::collision, src/LB.cpp:1303-1305
     ctx->lbFReset = true;
     ctx->k.lbF[0] = ctx->k.lbF[1] = ctx->k.lbF[2] = 0.0;
+    ctx->k.lbFf[0] = ctx->k.lbFf[1] = ctx->k.lbFf[2] = 0.0f;
   }
   const Consts& k = ctx->k;
   Device& d = ctx->d;
@@ -559,13 +592,19 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   const int P1 = std::max(ctx->nPart, 1);
   lbResetKernel<<<std::max(1, std::min(16 * P1 / 256 + 1, 1024)), 256, 0, s>>>(
       k, d.pFHydro, 16LL * P1, d.obj, d.wallF, d.scal, d.iscal);
+  if (d.pAccF) cudaMemsetAsync(d.pAccF, 0, ACCF_N * (size_t)P1 * sizeof(float), s);
+  if (ctx->nPart > 0) {
+    particleKinematics<<<partGrid(ctx, 256), 256, 0, s>>>(k, d.px0, d.px1, d.pw1, d.pkd, d.pkf);
+    ctx->launches += 1;
+  }
   LbArgs a = lbArgs(ctx);
   auto* ev = nextLbEvents(ctx);
   if (ev) cudaEventRecord(ev->first, s);
-  lbStepFp64<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
+  if (k.mixed) lbStepMixed<<<ctx->lbMixedBlocks, 256, 0, s>>>(k, a);
+  else lbStepFp64<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
   if (ev) cudaEventRecord(ev->second, s);
   lbFinalizeKernel<<<std::max(1, std::min(P1 / 256 + 1, 256)), 256, 0, s>>>(
-      k, d.pFHydro, d.pMHydro, d.pFluidVol, d.obj, d.wallF, d.scal, d.iscal);
+      k, d.pFHydro, d.pMHydro, d.pFluidVol, d.obj, d.wallF, d.scal, d.iscal, d.pAccF, d.pSHydro);
   ctx->cur = 1 - ctx->cur;
   ctx->launches += 3;
   if (ctx->freeSurface) {
@@ -590,7 +629,8 @@ extern "C" int lbdem_free_surface_step(lbdem_ctx* ctx) {
   fsMutantsAndFill<<<g, 256, 0, s>>>(k, a);
   fsEmptyIsolated<<<g, 256, 0, s>>>(k, a);
   fsRedistribute<<<g, 256, 0, s>>>(k, a);
-  ctx->launches += 7;
+  fsClearBulk<<<g, 256, 0, s>>>(k, d.mask, d.iscal);
+  ctx->launches += 8;
   return launchErr(ctx, "free-surface step");
 }
 
@@ -641,7 +681,7 @@ extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
     }
     if (ctx->check_every > 0 && ctx->lbTime % ctx->check_every == 0 && ctx->lbSolve) {
       nonfiniteCheck<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(
-          ctx->k, ctx->d.mask, (const double*)ctx->d.f[ctx->cur], ctx->d.iscal);
+          ctx->k, ctx->d.mask, ctx->d.f[ctx->cur], ctx->d.iscal);
       ++ctx->launches;
     }
   }
@@ -729,23 +769,21 @@ extern "C" int lbdem_download_lattice(lbdem_ctx* ctx, uint8_t* type, uint8_t* pf
     }
   }
   if ((rc = d2h(ctx, solid, d.solid, N * 4))) return rc;
-  if ((rc = d2h(ctx, mass, d.mass, N * 8))) return rc;
-  if (f) {
-    std::vector<double> fv((size_t)Q * N);
-    CK(cudaMemcpy(fv.data(), d.f[ctx->cur], fv.size() * 8, cudaMemcpyDeviceToHost));
-    std::vector<uint8_t> m(N);
-    CK(cudaMemcpy(m.data(), d.mask, N, cudaMemcpyDeviceToHost));
-    for (size_t j = 0; j < (size_t)Q; ++j)
-      for (size_t i = 0; i < N; ++i) {
-        const int t = m[i] & TYPE_MASK;
-        f[j * N + i] = (t == 0 || t == 3) ? fv[j * N + i] : 0.0;
-      }
+  if (mass || f) {
+    double* tmp = nullptr;
+    CK(cudaMalloc(&tmp, (size_t)(Q + 1) * N * sizeof(double)));
+    exportLattice<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(ctx->k, d.mask, d.f[ctx->cur], d.mass,
+                                                             d.nF, tmp, tmp + (size_t)Q * N);
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (f) CK(cudaMemcpy(f, tmp, (size_t)Q * N * 8, cudaMemcpyDeviceToHost));
+    if (mass) CK(cudaMemcpy(mass, tmp + (size_t)Q * N, N * 8, cudaMemcpyDeviceToHost));
+    cudaFree(tmp);
   }
   if (n || u) {
     double* tmp = nullptr;
     CK(cudaMalloc(&tmp, 4 * N * sizeof(double)));
     momentsKernel<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(ctx->k, d.mask,
-                                                             (const double*)d.f[ctx->cur], tmp,
+                                                             d.f[ctx->cur], tmp,
                                                              tmp + N);
     CK(cudaStreamSynchronize(ctx->stream));
     if (n) CK(cudaMemcpy(n, tmp, N * 8, cudaMemcpyDeviceToHost));
@@ -828,7 +866,7 @@ extern "C" int lbdem_mass_summary(lbdem_ctx* ctx, double* total_mass,
   CK(cudaMalloc(&tmp, 3 * sizeof(double)));
   CK(cudaMemset(tmp, 0, 3 * sizeof(double)));
   massSummaryKernel<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(
-      ctx->k, ctx->d.mask, ctx->d.mass, tmp, (unsigned long long*)(tmp + 1));
+      ctx->k, ctx->d.mask, ctx->d.mass, ctx->d.nF, tmp, (unsigned long long*)(tmp + 1));
   CK(cudaStreamSynchronize(ctx->stream));
   double m = 0;
   unsigned long long c[2] = {0, 0};

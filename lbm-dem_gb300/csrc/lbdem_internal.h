@@ -17,11 +17,16 @@ constexpr int MAX_OBJ = 8;       // impactors handled on the device
 constexpr int MAX_WALL = 6;
 constexpr int PAIR_VALS = 18;    // per neighbour slot: contact(6) lub(9) rep(3)
 constexpr int UNCOVER_CAP = 8192;// uncovered object nodes resolved per step
+constexpr int ACCF_N = 13;       // mixed-form particle sums: d(3), r (x) d (9), mass(1)
 
 // mask byte layout
 constexpr uint8_t TYPE_MASK = 0x0F;
 constexpr uint8_t PFLAG = 0x10;   // inside a particle (nodeType::p)
 constexpr uint8_t ABIT = 0x20;    // member of the last active list (cleanLists)
+// Cache: every streaming neighbour was active when the lattice step last
+// checked. Set only by the lattice step; cleared around every node that
+// leaves the active types (free-surface emptying, impactor voxelisation).
+constexpr uint8_t BULK = 0x40;
 
 // device error bits
 enum : int {
@@ -43,6 +48,9 @@ struct Consts {
   double uLength, uTime, uSpeed, uAccel, uAngVel, uForce, uTorque, uVolume;
   double initDensity, initVisc;
   double omega, omegaf;  // 1/(0.5+3 visc), 1-1/(1+6 visc) (src/node.cpp:183,196)
+  int mixed;             // FP32 deviation storage / FP32 collision form
+  float omegaF, omegafF, lbFf[3];
+  float sLF;             // unit.Length * unit.Force, stresslet scale (mixed form)
   double lbF[3];        // after the forceField reset rule of LB::collision
   double initVel[3];
   int nObj, nWall, nPart;
@@ -67,6 +75,7 @@ struct Device {
   uint8_t* fsflag = nullptr;   // transient free-surface flags
   void* f[2] = {nullptr, nullptr};  // distributions, ping-pong
   double* mass = nullptr;
+  float* nF = nullptr;         // fluid-node density, mixed form only
   double* massNew = nullptr;
   double* rhoS = nullptr;      // density of interface nodes
   double* uS = nullptr;        // shifted velocity of interface nodes [3][N]
@@ -82,6 +91,9 @@ struct Device {
   double *pFContact = nullptr, *pMContact = nullptr, *pFLub = nullptr, *pMLub = nullptr;
   double *pFRep = nullptr, *pFTotal = nullptr, *pMTotal = nullptr, *pFGrav = nullptr;
   double *pxiw = nullptr, *pxio = nullptr;
+  double* pkd = nullptr;                 // [6][P] lattice-unit kinematics
+  float* pkf = nullptr;                  // [9][P] (mixed form)
+  float* pAccF = nullptr;                // [ACCF_N][P] particle sums (mixed form)
   int* plist[2] = {nullptr, nullptr};    // [P][50]
   double* pxi[2] = {nullptr, nullptr};   // [P][3][50]
   int* partner = nullptr;                // [P][50] slot of i in list[j]
@@ -159,6 +171,7 @@ struct lbdem_ctx {
   int objIndexField[lbdem::MAX_OBJ] = {0};
   long long deviceBytes = 0;
   int smCount = 0;
+  int lbMixedBlocks = 0;  // resident blocks of the mixed lattice kernel (one wave)
   // measurement
   bool profiling = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> lbEvents;

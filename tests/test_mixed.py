@@ -1,0 +1,77 @@
+"""Mixed form (FP32 deviation storage / FP32 collision, FP64 DEM and mass
+budget) against the plain FP64 oracle.
+
+Tolerance (north star of this project): impactor trajectory within 1e-3
+relative error, measured on the displacement y(t) - y(0) over the run, and
+total fluid mass conserved to the same level as the FP64 reference run.
+"""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+TRAJ_RTOL = 1e-3
+
+
+def _run(name, steps, every):
+    import lbdem
+    import oracle_ffi
+    cfg = lbdem.LoadedConfig(os.path.join(GOLDEN, name, "parameters.cfg"))
+    mix = lbdem.Solver(cfg, precision=lbdem.MIXED)
+    orc = oracle_ffi.Oracle(cfg)
+    y0 = orc.object0()[1]
+    traj_m, traj_o, mass_m, mass_o = [], [], [], []
+    with tempfile.TemporaryDirectory() as tmp:
+        for s in range(every, steps + 1, every):
+            mix.cycle(every)
+            orc.cycle(every)
+            traj_m.append(mix.objects()["o_x0"][0].copy())
+            traj_o.append(np.array(orc.object0()[:3]))
+            mass_m.append(mix.mass_summary()[0])
+            o = orc.state(tmp)
+            mass_o.append(float(np.sum(o["mass"][(o["type"] == 0) | (o["type"] == 3)]
+                                        * (o["pflag"][(o["type"] == 0) | (o["type"] == 3)] == 0))))
+    mix.close()
+    orc.close()
+    cfg.close()
+    return y0, np.array(traj_m), np.array(traj_o), np.array(mass_m), np.array(mass_o)
+
+
+@pytest.mark.parametrize("name,steps,every", [("small_cells", 60, 5), ("c1", 100, 10)])
+def test_mixed_impactor_trajectory_within_1e3(name, steps, every, lib, oracle_lib):
+    y0, tm, to, mm, mo = _run(name, steps, every)
+    disp_o = to[:, 1] - y0
+    disp_m = tm[:, 1] - y0
+    err = np.max(np.abs(disp_m - disp_o)) / max(np.max(np.abs(disp_o)), 1e-12)
+    assert err <= TRAJ_RTOL, f"{name}: impactor displacement rel err {err:.3e}"
+    # masses of the non-particle active nodes agree as well
+    merr = np.max(np.abs(mm - mo) / np.abs(mo))
+    assert merr <= TRAJ_RTOL, f"{name}: fluid mass rel err {merr:.3e}"
+
+
+def test_mixed_lattice_close_to_fp64(lib, oracle_lib):
+    """Field-level agreement after 20 steps of the small case: populations
+    within 1e-4 absolute (FP32 deviation storage), node types mostly equal."""
+    import lbdem
+    import oracle_ffi
+    cfg = lbdem.LoadedConfig(os.path.join(GOLDEN, "small_cells", "parameters.cfg"))
+    mix = lbdem.Solver(cfg, precision=lbdem.MIXED)
+    orc = oracle_ffi.Oracle(cfg)
+    mix.cycle(20)
+    orc.cycle(20)
+    with tempfile.TemporaryDirectory() as tmp:
+        o = orc.state(tmp)
+    g = mix.lattice()
+    same = np.mean(g["type"] == o["type"])
+    assert same > 0.999, f"node types agree on only {same:.5f} of the nodes"
+    act = ((o["type"] == 0) | (o["type"] == 3)) & (g["type"] == o["type"])
+    ferr = np.max(np.abs(g["f"][:, act] - o["f"][:, act]))
+    assert ferr < 1e-4, f"population abs err {ferr:.3e}"
+    mix.close()
+    orc.close()
+    cfg.close()
