@@ -7,8 +7,9 @@
  * It restates the reference's algorithm serially, on dense arrays, in the
  * reference's own operation order (see the file:line citations in
  * lbdem_oracle.cpp), including its defined-behaviour pins and its quirks.
- * Its output is pinned against the compiled reference (oracle/ref_driver.cpp)
- * by tests/test_oracle_vs_reference.py and the committed golden dumps.
+ * Its output is pinned against the compiled reference (oracle/ref_driver.cpp):
+ * tests/test_oracle_golden.py compares it bit for bit with the per-step
+ * hashes of the reference's state that tests/golden/make_golden.py recorded.
  */
 #ifndef LBDEM_ORACLE_H
 #define LBDEM_ORACLE_H
