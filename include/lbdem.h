@@ -268,6 +268,33 @@ int lbdem_profile_enable(lbdem_ctx* ctx, int enable);
 /* Synchronise, report the counters since the last reset, optionally reset. */
 int lbdem_profile_read(lbdem_ctx* ctx, lbdem_profile* out, int reset);
 
+/* ---- readback without device allocation (no counterpart in the
+ * reference; a diagnostic of this library) ------------------------------ */
+
+/* Largest node range one lbdem_download_nodes_noalloc call accepts. */
+#define LBDEM_NOALLOC_MAX_NODES 16384
+
+/* Populations and mass of the `count` consecutive nodes starting at node
+ * index `first` (index = x + y*X + z*X*Y): f[19*count] (direction blocks of
+ * `count`), mass[count]; the same values lbdem_download_lattice returns for
+ * those nodes. Either pointer may be NULL.
+ *
+ * Allocates no device memory (no cudaMalloc/cudaFree): it stages through a
+ * fixed buffer of LBDEM_NOALLOC_MAX_NODES nodes (2.5 MiB) compiled into the
+ * library. For callers that cannot allocate device memory at the time of the
+ * call, e.g. a monitor sampling lattice rows every step while the run holds
+ * nearly all of HBM: lbdem_download_lattice takes a temporary of 160 bytes
+ * per lattice node with cudaMalloc, which also synchronises the device.
+ * count > LBDEM_NOALLOC_MAX_NODES or a range outside the lattice returns
+ * LBDEM_ERR_INVALID with a message in lbdem_last_error.
+ *
+ * The buffer is shared by every context on a device: calls that overlap in
+ * time on one device race on it; serialise them. The first call on each
+ * device looks up the buffer's address (cudaGetSymbolAddress); make that
+ * first call before any stream capture. Synchronises the context's stream. */
+int lbdem_download_nodes_noalloc(lbdem_ctx* ctx, int64_t first, int64_t count,
+                                 double* f, double* mass);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(HERE, "liblbdem.so")
 
 PLAIN_FP64 = 0
 MIXED = 1
+NOALLOC_MAX_NODES = 16384  # LBDEM_NOALLOC_MAX_NODES in include/lbdem.h
 
 ERRORS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
@@ -149,6 +150,8 @@ def load_library(path: str | None = None) -> C.CDLL:
                                 C.POINTER(C.c_int64)], C.c_int),
         "lbdem_profile_enable": ([c_ctx, C.c_int], C.c_int),
         "lbdem_profile_read": ([c_ctx, C.POINTER(Profile), C.c_int], C.c_int),
+        "lbdem_download_nodes_noalloc": ([c_ctx, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p],
+                                         C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)  # a missing entry point is a build error
@@ -336,3 +339,14 @@ class Solver:
         self._check(self.lib.lbdem_mass_summary(self.ctx, C.byref(m), C.byref(ni), C.byref(na)),
                     "mass_summary")
         return m.value, ni.value, na.value
+
+    def nodes_noalloc(self, first: int, count: int):
+        """Populations [19, count] and masses [count] of nodes first ..
+        first+count-1 through lbdem_download_nodes_noalloc (no device
+        allocation; at most NOALLOC_MAX_NODES nodes per call)."""
+        f = np.zeros((19, max(count, 0)))
+        mass = np.zeros(max(count, 0))
+        self._check(self.lib.lbdem_download_nodes_noalloc(
+            self.ctx, int(first), int(count), f.ctypes.data_as(C.c_void_p),
+            mass.ctypes.data_as(C.c_void_p)), "download_nodes_noalloc")
+        return f, mass
