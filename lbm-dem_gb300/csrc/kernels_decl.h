@@ -80,6 +80,7 @@ struct DemArgs {
 // lb_fp64.cu / lb_mixed.cu
 __global__ void lbStepFp64(Consts k, LbArgs a);
 __global__ void lbStepMixed(Consts k, LbArgs a);
+__global__ void lbWallForceMixed(Consts k, LbArgs a);
 __global__ void particleKinematics(Consts k, const double* px0, const double* px1,
                                    const double* pw1, double* pkd, float* pkf);
 __global__ void lbResetKernel(Consts k, double* pAcc, long long pAccLen, double* obj,

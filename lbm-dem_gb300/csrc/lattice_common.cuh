@@ -297,7 +297,7 @@ __device__ __forceinline__ void collideNodeMixed(const Consts& k, float* g, bool
     if (CZ(j)) jz = CZ(j) > 0 ? jz + dj : jz - dj;
   }
   const float n = 1.0f + dr;
-  const float inv = 1.0f / n;
+  const float inv = __frcp_rn(n);
   float ux = jx * inv, uy = jy * inv, uz = jz * inv;
   float hx = 0.0f, hy = 0.0f, hz = 0.0f;
   s.dx = s.dy = s.dz = s.rx = s.ry = s.rz = 0.0f;

@@ -39,6 +39,10 @@ __constant__ int c_dir[Q] = {packDir(0),  packDir(1),  packDir(2),  packDir(3), 
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr unsigned ALL_LINKS = 0x7FFFEu;  // bits 1..18
+// neighbour types whose link needs no fix-up after the unrolled streaming
+// loop: fluid 0, gas 2, interface 3, walls 7/8, slip wall 11
+constexpr unsigned PLAIN_TYPES = (1u << 0) | (1u << 2) | (1u << 3) | (1u << 7) | (1u << 8) |
+                                 (1u << 11);
 
 // Segmented reduction of the particle coupling terms over runs of
 // consecutive lanes that share a particle index and a lattice row, then one
@@ -96,13 +100,19 @@ __device__ __forceinline__ void particleRunReduce(int key, int ix, float dx, flo
 }  // namespace
 
 __global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
-  __shared__ float accW[3 * MAX_WALL];
   __shared__ float accO[6 * MAX_OBJ];
+  __shared__ float sObj[6 * MAX_OBJ];  // impactor centre (x0/L) and velocity (x1/S)
   __shared__ double accX;
   __shared__ int sbox[6];
   __shared__ unsigned scnt[2];
-  for (int i = threadIdx.x; i < 3 * MAX_WALL; i += blockDim.x) accW[i] = 0.0f;
   for (int i = threadIdx.x; i < 6 * MAX_OBJ; i += blockDim.x) accO[i] = 0.0f;
+  if (threadIdx.x < (unsigned)k.nObj) {
+    const double* ob = a.obj + threadIdx.x * OB_STRIDE;
+    for (int c = 0; c < 3; ++c) {
+      sObj[6 * threadIdx.x + c] = (float)(ob[OB_X0 + c] / k.uLength);
+      sObj[6 * threadIdx.x + 3 + c] = (float)(ob[OB_X1 + c] / k.uSpeed);
+    }
+  }
   if (threadIdx.x < 3) sbox[threadIdx.x] = INT_MAX;
   else if (threadIdx.x < 6) sbox[threadIdx.x] = -1;
   if (threadIdx.x == 0) {
@@ -138,7 +148,7 @@ __global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
     uint8_t nm = (uint8_t)(m & ~(ABIT | BULK));
     if (__any_sync(FULL, act)) {
       float g[Q];
-      unsigned actN = ALL_LINKS, gasN = 0;
+      unsigned actN = ALL_LINKS, gasN = 0, spcN = 0;
       NodeStateF s;
       s.dx = s.dy = s.dz = s.rx = s.ry = s.rz = 0.0f;
       float massOld = 0.0f;
@@ -153,6 +163,7 @@ __global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
             const int tl = mk[x + (unsigned)(CX(j) + CY(j) * sy + CZ(j) * sz)] & TYPE_MASK;
             actN |= (unsigned)isActiveT(tl) << j;
             gasN |= (unsigned)(tl == 2) << j;
+            spcN |= ((PLAIN_TYPES >> tl) & 1u ^ 1u) << j;
           }
         }
         nm |= (uint8_t)(ABIT | (actN == ALL_LINKS ? BULK : 0));
@@ -186,12 +197,13 @@ __global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
             gout[OPPJ(j) * NN + x] = out;
           }
         }
-        // walls, slip walls, impactors and unexpected types: the value
-        // stored above is g_j; fix it up and add the link forces
-        unsigned special = ~(actN | gasN) & ALL_LINKS;
+        // impactor links and unexpected types: the value stored above is
+        // g_j; fix it up and add the link forces. Walls (plain bounce-back)
+        // get their force from lbWallForceMixed after this kernel.
+        unsigned special = spcN;
         if (special) {
-          float fw[3] = {0.0f, 0.0f, 0.0f}, fo[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-          int wcur = -1, ocur = -1;
+          float fo[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+          int ocur = -1;
 #pragma unroll 1
           for (; special; special &= special - 1u) {
             const int j = __ffs(special) - 1;
@@ -199,62 +211,42 @@ __global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
             const int cx = (dj & 3) - 1, cy = ((dj >> 2) & 3) - 1, cz = ((dj >> 4) & 3) - 1;
             const unsigned lk = x + (unsigned)(cx + cy * sy + cz * sz);
             const int tl = mk[lk] & TYPE_MASK;
+            const int oi = a.objIdx[lk];
+            if (tl != 12 || oi >= k.nObj) {
+              atomicOr(a.iscal + IS_ERROR, ERR_TYPE);
+              continue;
+            }
             float* dst = gout + (size_t)(dj >> 8) * NN + x;
             const float gj = *dst;
-            if (tl == 11) continue;
-            if (tl == 7 || tl == 8) {
-              const uint32_t w = a.solid[lk];
-              if (w < (uint32_t)k.nWall) {
-                if ((int)w != wcur) {
-                  if (wcur >= 0)
-                    for (int c = 0; c < 3; ++c) atomicAdd(&accW[3 * wcur + c], fw[c]);
-                  fw[0] = fw[1] = fw[2] = 0.0f;
-                  wcur = (int)w;
-                }
-                const float bb = 2.0f * gj;
-                fw[0] += (float)cx * bb;
-                fw[1] += (float)cy * bb;
-                fw[2] += (float)cz * bb;
+            const float* ov = sObj + 6 * oi;
+            const float wj = j <= 6 ? (float)WJ(1) : (float)WJ(7);
+            const float cv = __fmaf_rn((float)cx, ov[3], __fmaf_rn((float)cy, ov[4], (float)cz * ov[5]));
+            const float BBi = 6.0f * s.n * wj * cv;
+            const uint32_t so = a.solid[lk];
+            if (so < (uint32_t)k.nObj) {
+              if ((int)so != ocur) {
+                if (ocur >= 0)
+                  for (int c = 0; c < 6; ++c) atomicAdd(&accO[6 * ocur + c], fo[c]);
+                for (int c = 0; c < 6; ++c) fo[c] = 0.0f;
+                ocur = (int)so;
               }
-            } else if (tl == 12) {
-              const double* ob = a.obj + a.objIdx[lk] * OB_STRIDE;
-              const float vx = (float)(ob[OB_X1] / k.uSpeed),
-                          vy = (float)(ob[OB_X1 + 1] / k.uSpeed),
-                          vz = (float)(ob[OB_X1 + 2] / k.uSpeed);
-              const float wj = j == 0 ? (float)WJ(0) : j <= 6 ? (float)WJ(1) : (float)WJ(7);
-              const float cv = __fmaf_rn((float)cx, vx, __fmaf_rn((float)cy, vy, (float)cz * vz));
-              const float BBi = 6.0f * s.n * wj * cv;
-              const uint32_t so = a.solid[lk];
-              if (so < (uint32_t)k.nObj) {
-                if ((int)so != ocur) {
-                  if (ocur >= 0)
-                    for (int c = 0; c < 6; ++c) atomicAdd(&accO[6 * ocur + c], fo[c]);
-                  for (int c = 0; c < 6; ++c) fo[c] = 0.0f;
-                  ocur = (int)so;
-                }
-                const double* os = a.obj + so * OB_STRIDE;
-                const float bb = 2.0f * gj - BBi;
-                const float Fx = (float)cx * bb, Fy = (float)cy * bb, Fz = (float)cz * bb;
-                const int lx = ix + cx, ly = iy + cy, lz = iz + cz;
-                const float rx = (float)((double)lx - os[OB_X0] / k.uLength);
-                const float ry = (float)((double)ly - os[OB_X0 + 1] / k.uLength);
-                const float rz = (float)((double)lz - os[OB_X0 + 2] / k.uLength);
-                fo[0] += Fx;
-                fo[1] += Fy;
-                fo[2] += Fz;
-                fo[3] += ry * Fz - rz * Fy;
-                fo[4] += rz * Fx - rx * Fz;
-                fo[5] += rx * Fy - ry * Fx;
-              }
-              *dst = gj - BBi;
-              const double mo = t == 3 ? a.mass[x] : (double)a.nF[x];
-              extra += (double)BBi * mo;
-            } else {
-              atomicOr(a.iscal + IS_ERROR, ERR_TYPE);
+              const float* os = sObj + 6 * so;
+              const float bb = 2.0f * gj - BBi;
+              const float Fx = (float)cx * bb, Fy = (float)cy * bb, Fz = (float)cz * bb;
+              const float rx = (float)(ix + cx) - os[0];
+              const float ry = (float)(iy + cy) - os[1];
+              const float rz = (float)(iz + cz) - os[2];
+              fo[0] += Fx;
+              fo[1] += Fy;
+              fo[2] += Fz;
+              fo[3] += ry * Fz - rz * Fy;
+              fo[4] += rz * Fx - rx * Fz;
+              fo[5] += rx * Fy - ry * Fx;
             }
+            *dst = gj - BBi;
+            const double mo = t == 3 ? a.mass[x] : (double)a.nF[x];
+            extra += (double)BBi * mo;
           }
-          if (wcur >= 0)
-            for (int c = 0; c < 3; ++c) atomicAdd(&accW[3 * wcur + c], fw[c]);
           if (ocur >= 0)
             for (int c = 0; c < 6; ++c) atomicAdd(&accO[6 * ocur + c], fo[c]);
         }
@@ -303,8 +295,6 @@ __global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
     if (extra != 0.0) atomicAdd(&accX, extra);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < 3 * MAX_WALL; i += blockDim.x)
-    if (accW[i] != 0.0f) atomicAdd(a.wallF + (i / 3) * 12 + (i % 3), (double)accW[i]);
   for (int i = threadIdx.x; i < 6 * MAX_OBJ; i += blockDim.x) {
     if (accO[i] == 0.0f) continue;
     const int o = i / 6, c = i % 6;
@@ -324,6 +314,78 @@ __global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
       atomicMax(a.iscal + IS_BBOX + 5, sbox[5]);
     }
   }
+}
+
+// Hydrodynamic force on the walls, mixed form: the wall branch of
+// LB::streaming (src/LB.cpp:1334-1544) accumulates (2 (f_j - w_j rho0) - BBi) c_j
+// with BBi = 0 for walls at rest, i.e. 2 g_j c_j in deviation form. For an
+// active node x next to a wall node x + c_j, lbStepMixed stored g_j(x) in
+// direction opp(j) of x (bounce-back), so the sums are formed here from the
+// lattice it wrote, before anything else changes it. Walls are the outer
+// node layer of the box (the only wall layout a run accepts), so only the
+// layer inside it is visited: 2 (XY + YZ + XZ) nodes instead of N.
+__global__ void lbWallForceMixed(Consts k, LbArgs a) {
+  __shared__ float accW[3 * MAX_WALL];
+  for (int i = threadIdx.x; i < 3 * MAX_WALL; i += blockDim.x) accW[i] = 0.0f;
+  __syncthreads();
+  const int X = k.X, Y = k.Y, Z = k.Z;
+  const long long nx = X - 2, ny = Y - 2, nz = Z - 2;  // inner box 1..dim-2
+  const float* gout = (const float*)a.fout;
+  const size_t NN = (size_t)k.N;
+  if (nx > 0 && ny > 0 && nz > 0) {
+    // faces x = 1, X-2 (all y, z); y = 1, Y-2 (x inside); z = 1, Z-2 (x, y inside)
+    const long long cA = ny * nz, cB = max(nx - 2, 0LL) * nz,
+                    cC = max(nx - 2, 0LL) * max(ny - 2, 0LL);
+    const int fA = nx > 1 ? 2 : 1, fB = ny > 1 ? 2 : 1, fC = nz > 1 ? 2 : 1;
+    const long long total = fA * cA + fB * cB + fC * cC;
+    float fw[3] = {0.0f, 0.0f, 0.0f};
+    int wcur = -1;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+      int ix, iy, iz;
+      if (i < fA * cA) {
+        const long long r = i % cA;
+        ix = i < cA ? 1 : X - 2;
+        iy = 1 + (int)(r % ny);
+        iz = 1 + (int)(r / ny);
+      } else if (i < fA * cA + fB * cB) {
+        const long long q = i - fA * cA, r = q % cB;
+        iy = q < cB ? 1 : Y - 2;
+        ix = 2 + (int)(r % (nx - 2));
+        iz = 1 + (int)(r / (nx - 2));
+      } else {
+        const long long q = i - fA * cA - fB * cB, r = q % cC;
+        iz = q < cC ? 1 : Z - 2;
+        ix = 2 + (int)(r % (nx - 2));
+        iy = 2 + (int)(r / (nx - 2));
+      }
+      const long long x = ix + iy * k.sy + iz * k.sz;
+      if (!isActiveT(a.mask[x] & TYPE_MASK)) continue;
+#pragma unroll
+      for (int j = 1; j < Q; ++j) {
+        const long long lk = x + nbrOffset(k, j);
+        const int tl = a.mask[lk] & TYPE_MASK;
+        if (tl != 7 && tl != 8) continue;
+        const uint32_t w = a.solid[lk];
+        if (w >= (uint32_t)k.nWall) continue;
+        if ((int)w != wcur) {
+          if (wcur >= 0)
+            for (int c = 0; c < 3; ++c) atomicAdd(&accW[3 * wcur + c], fw[c]);
+          fw[0] = fw[1] = fw[2] = 0.0f;
+          wcur = (int)w;
+        }
+        const float bb = 2.0f * gout[OPPJ(j) * NN + x];
+        if (CX(j)) fw[0] += CX(j) > 0 ? bb : -bb;
+        if (CY(j)) fw[1] += CY(j) > 0 ? bb : -bb;
+        if (CZ(j)) fw[2] += CZ(j) > 0 ? bb : -bb;
+      }
+    }
+    if (wcur >= 0)
+      for (int c = 0; c < 3; ++c) atomicAdd(&accW[3 * wcur + c], fw[c]);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 3 * MAX_WALL; i += blockDim.x)
+    if (accW[i] != 0.0f) atomicAdd(a.wallF + (i / 3) * 12 + (i % 3), (double)accW[i]);
 }
 
 }  // namespace lbdem

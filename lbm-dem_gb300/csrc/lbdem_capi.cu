@@ -603,6 +603,10 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   if (k.mixed) lbStepMixed<<<ctx->lbMixedBlocks, 256, 0, s>>>(k, a);
   else lbStepFp64<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
   if (ev) cudaEventRecord(ev->second, s);
+  if (k.mixed && k.nWall > 0) {
+    lbWallForceMixed<<<ctx->smCount * 2, 256, 0, s>>>(k, a);
+    ctx->launches += 1;
+  }
   lbFinalizeKernel<<<std::max(1, std::min(P1 / 256 + 1, 256)), 256, 0, s>>>(
       k, d.pFHydro, d.pMHydro, d.pFluidVol, d.obj, d.wallF, d.scal, d.iscal, d.pAccF, d.pSHydro);
   ctx->cur = 1 - ctx->cur;

@@ -72,6 +72,15 @@ def test_mixed_lattice_close_to_fp64(lib, oracle_lib):
     act = ((o["type"] == 0) | (o["type"] == 3)) & (g["type"] == o["type"])
     ferr = np.max(np.abs(g["f"][:, act] - o["f"][:, act]))
     assert ferr < 1e-4, f"population abs err {ferr:.3e}"
+    # hydrodynamic forces on the walls and on the impactor, relative to the
+    # largest component of each (tolerance 1e-3)
+    for key, got in (("w_FHydro", mix.walls()["w_FHydro"]),
+                     ("o_FHydro", mix.objects()["o_FHydro"])):
+        ref = np.asarray(o[key]).reshape(got.shape)
+        scale = np.max(np.abs(ref))
+        assert scale > 0, key
+        err = np.max(np.abs(got - ref)) / scale
+        assert err < 1e-3, f"{key}: rel err {err:.3e}"
     mix.close()
     orc.close()
     cfg.close()
