@@ -77,6 +77,15 @@ struct DemArgs {
   int* iscal;
 };
 
+// Mixed lattice step launch shape: chunks of MIXED_CHUNK consecutive nodes
+// (one per thread), staged through MIXED_STAGES shared-memory buffers of 19
+// FP32 planes + the mask bytes that thread 0 fills with bulk copies.
+constexpr int MIXED_CHUNK = 256;
+constexpr int MIXED_STAGES = 3;
+constexpr int MIXED_STAGE_BYTES = Q * MIXED_CHUNK * 4 + MIXED_CHUNK;
+constexpr int MIXED_THREADS = MIXED_CHUNK;
+constexpr int MIXED_SMEM = MIXED_STAGES * MIXED_STAGE_BYTES;
+
 // lb_fp64.cu / lb_mixed.cu
 __global__ void lbStepFp64(Consts k, LbArgs a);
 __global__ void lbStepMixed(Consts k, LbArgs a);

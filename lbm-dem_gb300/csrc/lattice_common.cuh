@@ -31,6 +31,30 @@ __host__ __device__ constexpr double WJ(int j) {
 
 __device__ __forceinline__ bool isActiveT(int t) { return t == 0 || t == 3; }
 
+// bits j = 1..18 of the links whose lattice velocity has the given component sign
+__host__ __device__ constexpr unsigned linksWith(int axis, int sign) {
+  unsigned m = 0;
+  for (int j = 1; j < 19; ++j) {
+    const int c = axis == 0 ? CX(j) : axis == 1 ? CY(j) : CZ(j);
+    if (c == sign) m |= 1u << j;
+  }
+  return m;
+}
+
+// Links of node (ix, iy, iz) that end in the outer node layer of the box.
+// A run accepts walls on all six faces and no other boundary, so the outer
+// layer is all wall nodes and these are exactly the node's wall links.
+__device__ __forceinline__ unsigned boxWallLinks(const Consts& k, int ix, int iy, int iz) {
+  unsigned w = 0;
+  if (ix == 1) w |= linksWith(0, -1);
+  if (ix == k.X - 2) w |= linksWith(0, 1);
+  if (iy == 1) w |= linksWith(1, -1);
+  if (iy == k.Y - 2) w |= linksWith(1, 1);
+  if (iz == 1) w |= linksWith(2, -1);
+  if (iz == k.Z - 2) w |= linksWith(2, 1);
+  return w;
+}
+
 // u.dot(v[j]) of src/myvector.cpp:121 with the zero components dropped
 __device__ __forceinline__ double dotc(int j, double x, double y, double z) {
   const int cx = CX(j), cy = CY(j), cz = CZ(j);
@@ -246,21 +270,21 @@ using BBAccF = BBAccT<float>;   // mixed form: wall sums (diagnostic) in float
 // src/LB.cpp:330), which keeps the float's precision for the part that
 // varies.
 __device__ __forceinline__ double fget(const Consts& k, const void* f, int j, long long x) {
-  return k.mixed ? (double)((const float*)f)[(long long)j * k.N + x] + WJ(j)
-                 : ((const double*)f)[(long long)j * k.N + x];
+  return k.mixed ? (double)((const float*)f)[(long long)j * k.NP + x] + WJ(j)
+                 : ((const double*)f)[(long long)j * k.NP + x];
 }
 __device__ __forceinline__ void fset(const Consts& k, void* f, int j, long long x, double v) {
-  if (k.mixed) ((float*)f)[(long long)j * k.N + x] = (float)(v - WJ(j));
-  else ((double*)f)[(long long)j * k.N + x] = v;
+  if (k.mixed) ((float*)f)[(long long)j * k.NP + x] = (float)(v - WJ(j));
+  else ((double*)f)[(long long)j * k.NP + x] = v;
 }
 // f_j1(x1) - f_j2(x2) for two directions of equal weight
 __device__ __forceinline__ double fdiff(const Consts& k, const void* f, int j1, long long x1,
                                         int j2, long long x2) {
   if (k.mixed)
-    return (double)((const float*)f)[(long long)j1 * k.N + x1] -
-           (double)((const float*)f)[(long long)j2 * k.N + x2];
-  return ((const double*)f)[(long long)j1 * k.N + x1] -
-         ((const double*)f)[(long long)j2 * k.N + x2];
+    return (double)((const float*)f)[(long long)j1 * k.NP + x1] -
+           (double)((const float*)f)[(long long)j2 * k.NP + x2];
+  return ((const double*)f)[(long long)j1 * k.NP + x1] -
+         ((const double*)f)[(long long)j2 * k.NP + x2];
 }
 
 // u.dot(v[j]) in float

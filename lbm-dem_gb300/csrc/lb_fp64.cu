@@ -45,6 +45,7 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
   }
   __syncthreads();
   const long long N = k.N;
+  const long long NP = k.NP;  // population plane stride
   const double* fin = (const double*)a.fin;
   double* fout = (double*)a.fout;
   const int lane = threadIdx.x & 31;
@@ -77,7 +78,7 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
       coords(k, x, ix, iy, iz);
       double f[Q];
 #pragma unroll
-      for (int j = 0; j < Q; ++j) f[j] = fin[(long long)j * N + x];
+      for (int j = 0; j < Q; ++j) f[j] = fin[(long long)j * NP + x];
       const bool pf = (m & PFLAG) != 0;
       const uint32_t pid = pf ? a.solid[x] : 0u;
       const double massOld = a.mass[x];
@@ -107,15 +108,18 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
       // reference's boundary value in direction opp(j).
       fout[x] = f[0];
       const double usq = s.ux * s.ux + s.uy * s.uy + s.uz * s.uz;
+      const unsigned wallN = boxWallLinks(k, ix, iy, iz);
 #pragma unroll
       for (int j = 1; j < Q; ++j) {
         const long long lk = x + nbrOffset(k, j);
-        const int tl = bulk ? 0 : (a.mask[lk] & TYPE_MASK);
+        const bool wl = (wallN >> j) & 1u;
+        // a cached node's links are active or box walls (type 7 and 8 stream alike)
+        const int tl = bulk ? (wl ? 7 : 0) : (a.mask[lk] & TYPE_MASK);
         const double fs = f[j];
-        const long long dst = (long long)OPPJ(j) * N + x;
-        allAct = allAct && isActiveT(tl);
+        const long long dst = (long long)OPPJ(j) * NP + x;
+        allAct = allAct && (isActiveT(tl) || wl);
         if (isActiveT(tl)) {
-          fout[(long long)j * N + lk] = fs;
+          fout[(long long)j * NP + lk] = fs;
         } else if (tl == 2) {
           const double vuj = dotc(j, s.ux, s.uy, s.uz);
           fout[dst] = -fs + WJ(j) * k.initDensity * (2.0 + 9.0 * (vuj * vuj) - 3.0 * usq);
@@ -380,7 +384,7 @@ __global__ void fsUpdateMass(Consts k, FsArgs a) {
           if (k.mixed) {
             float g[Q];
 #pragma unroll
-            for (int q = 0; q < Q; ++q) g[q] = ((const float*)a.fold)[(long long)q * k.N + x];
+            for (int q = 0; q < Q; ++q) g[q] = ((const float*)a.fold)[(long long)q * k.NP + x];
             NodeStateF s;
             collideNodeMixed(k, g, pf, pf ? a.solid[x] : 0u, a.pkf, k.nPart,
                              (float)a.massNew[x], ix, iy, iz, s);
@@ -388,7 +392,7 @@ __global__ void fsUpdateMass(Consts k, FsArgs a) {
             for (int q = 0; q < Q; ++q) fsl[q] = (double)g[q];  // deviations
           } else {
 #pragma unroll
-            for (int q = 0; q < Q; ++q) fsl[q] = ((const double*)a.fold)[(long long)q * k.N + x];
+            for (int q = 0; q < Q; ++q) fsl[q] = ((const double*)a.fold)[(long long)q * k.NP + x];
             NodeState s;
             collideNode(k, fsl, pf, pf ? a.solid[x] : 0u, a.pkd, a.pkd + 3 * k.nPart, a.pw1, k.nPart,
                         a.massNew[x], ix, iy, iz, s);
@@ -397,8 +401,8 @@ __global__ void fsUpdateMass(Consts k, FsArgs a) {
         }
         // f_opp(x) after streaming minus the population x sent into the wall
         const double ms = k.mixed
-            ? (double)((const float*)a.fcur)[(long long)OPPJ(j) * k.N + x] - fsl[j]
-            : ((const double*)a.fcur)[(long long)OPPJ(j) * k.N + x] - fsl[j];
+            ? (double)((const float*)a.fcur)[(long long)OPPJ(j) * k.NP + x] - fsl[j]
+            : ((const double*)a.fcur)[(long long)OPPJ(j) * k.NP + x] - fsl[j];
         term = (1.0 * mx) * ms;
       } else {
         continue;

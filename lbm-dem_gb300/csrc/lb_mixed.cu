@@ -44,6 +44,60 @@ constexpr unsigned ALL_LINKS = 0x7FFFEu;  // bits 1..18
 constexpr unsigned PLAIN_TYPES = (1u << 0) | (1u << 2) | (1u << 3) | (1u << 7) | (1u << 8) |
                                  (1u << 11);
 
+// ---- asynchronous bulk copies into shared memory (cp.async.bulk) tracked
+// by mbarriers; every wait is bounded ----
+constexpr int WAIT_LIMIT = 1 << 22;  // try_wait rounds before a wait gives up
+
+__device__ __forceinline__ uint32_t smemAddr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbarInit(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(count)
+               : "memory");
+}
+// make the initialised barriers visible to the async proxy
+__device__ __forceinline__ void fenceBarrierInit() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbarExpectTx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbarArrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smemAddr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbarTryWait(uint64_t* bar, unsigned parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smemAddr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// one thread waits for the phase of the given parity to complete
+__device__ __forceinline__ bool mbarWait(uint64_t* bar, unsigned parity) {
+  for (int it = 0; it < WAIT_LIMIT; ++it)
+    if (mbarTryWait(bar, parity)) return true;
+  return false;
+}
+// all lanes of a warp wait together; the result is warp-uniform
+__device__ __forceinline__ bool warpWait(uint64_t* bar, unsigned parity) {
+  for (int it = 0; it < WAIT_LIMIT; ++it)
+    if (__all_sync(0xffffffffu, mbarTryWait(bar, parity))) return true;
+  return false;
+}
+// global -> shared bulk copy; both addresses 16-byte aligned, bytes % 16 == 0
+__device__ __forceinline__ void bulkLoad(void* dst, const void* src, unsigned bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(smemAddr(dst)), "l"(src), "r"(bytes), "r"(smemAddr(bar))
+      : "memory");
+}
+
 // Segmented reduction of the particle coupling terms over runs of
 // consecutive lanes that share a particle index and a lattice row, then one
 // set of float atomics per run (issued by the run heads together).
@@ -99,23 +153,35 @@ __device__ __forceinline__ void particleRunReduce(int key, int ix, float dx, flo
 
 }  // namespace
 
-__global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
+__global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs a) {
+  extern __shared__ __align__(128) unsigned char stageMem[];  // MIXED_STAGES x stage
+  __shared__ uint64_t fullBar[MIXED_STAGES], emptyBar[MIXED_STAGES];
+  __shared__ int abortFlag;
   __shared__ float accO[6 * MAX_OBJ];
   __shared__ float sObj[6 * MAX_OBJ];  // impactor centre (x0/L) and velocity (x1/S)
   __shared__ double accX;
   __shared__ int sbox[6];
   __shared__ unsigned scnt[2];
-  for (int i = threadIdx.x; i < 6 * MAX_OBJ; i += blockDim.x) accO[i] = 0.0f;
-  if (threadIdx.x < (unsigned)k.nObj) {
-    const double* ob = a.obj + threadIdx.x * OB_STRIDE;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    for (int st = 0; st < MIXED_STAGES; ++st) {
+      mbarInit(&fullBar[st], 1);                  // thread 0's expect_tx
+      mbarInit(&emptyBar[st], MIXED_THREADS / 32);  // one arrival per warp
+    }
+    abortFlag = 0;
+    fenceBarrierInit();
+  }
+  for (int i = tid; i < 6 * MAX_OBJ; i += blockDim.x) accO[i] = 0.0f;
+  if (tid < k.nObj) {
+    const double* ob = a.obj + tid * OB_STRIDE;
     for (int c = 0; c < 3; ++c) {
-      sObj[6 * threadIdx.x + c] = (float)(ob[OB_X0 + c] / k.uLength);
-      sObj[6 * threadIdx.x + 3 + c] = (float)(ob[OB_X1 + c] / k.uSpeed);
+      sObj[6 * tid + c] = (float)(ob[OB_X0 + c] / k.uLength);
+      sObj[6 * tid + 3 + c] = (float)(ob[OB_X1 + c] / k.uSpeed);
     }
   }
-  if (threadIdx.x < 3) sbox[threadIdx.x] = INT_MAX;
-  else if (threadIdx.x < 6) sbox[threadIdx.x] = -1;
-  if (threadIdx.x == 0) {
+  if (tid < 3) sbox[tid] = INT_MAX;
+  else if (tid < 6) sbox[tid] = -1;
+  if (tid == 0) {
     accX = 0.0;
     scnt[0] = scnt[1] = 0u;
   }
@@ -125,38 +191,88 @@ __global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
   const uint8_t* mk = a.mask;
   // node indices fit 32 bits (checked when the run is created)
   const unsigned N = (unsigned)k.N;
-  const size_t NN = (size_t)k.N;
-  const int lane = threadIdx.x & 31;
-  const unsigned warpsPerBlock = blockDim.x >> 5;
-  const unsigned gw = blockIdx.x * warpsPerBlock + (threadIdx.x >> 5);
-  const unsigned stride = gridDim.x * warpsPerBlock * 32u;
-  const int X = k.X, Y = k.Y, sy = (int)k.sy, sz = (int)k.sz;
-  // coordinates of this lane's node, advanced by the stride each iteration
-  int ix, iy, iz;
-  coords(k, (long long)gw * 32 + lane, ix, iy, iz);
-  int dsx, dsy, dsz;
-  coords(k, (long long)stride, dsx, dsy, dsz);
+  const size_t NN = (size_t)k.N;    // stride of the interface arrays uS, hS
+  const size_t NP = (size_t)k.NP;   // population plane stride (multiple of the chunk)
+  const unsigned nChunks = (unsigned)(k.NP / MIXED_CHUNK);
+  // chunks of this block: blockIdx.x, blockIdx.x + gridDim.x, ...
+  const unsigned nMine =
+      nChunks > blockIdx.x ? (nChunks - 1u - blockIdx.x) / gridDim.x + 1u : 0u;
+  const int lane = tid & 31;
   double extra = 0.0;
   unsigned nact = 0, nif = 0;
-  for (unsigned base = gw * 32u; base < N; base += stride) {
-    const unsigned x = base + lane;
+  // Thread 0 keeps the stage ring filled: bulk copies of the 19 population
+  // planes and the mask bytes of a chunk, completing on the stage's full
+  // barrier. Iterations 0 .. MIXED_STAGES-1 are issued up front; iteration
+  // i + MIXED_STAGES - 1 is issued at iteration i once every warp has
+  // released iteration i - 1.
+  auto issue = [&](unsigned it) {
+    const int st = (int)(it % MIXED_STAGES);
+    unsigned char* sb = stageMem + st * MIXED_STAGE_BYTES;
+    const size_t off = (size_t)(blockIdx.x + it * gridDim.x) * MIXED_CHUNK;
+    mbarExpectTx(&fullBar[st], MIXED_STAGE_BYTES);
+#pragma unroll 1
+    for (int j = 0; j < Q; ++j)
+      bulkLoad(sb + j * MIXED_CHUNK * 4, gin + j * NP + off, MIXED_CHUNK * 4, &fullBar[st]);
+    bulkLoad(sb + Q * MIXED_CHUNK * 4, mk + off, MIXED_CHUNK, &fullBar[st]);
+  };
+  unsigned issued = 0;  // meaningful in thread 0
+  if (tid == 0)
+    for (; issued < nMine && issued < (unsigned)MIXED_STAGES; ++issued) issue(issued);
+  const int X = k.X, Y = k.Y, sy = (int)k.sy, sz = (int)k.sz;
+  const unsigned stride = gridDim.x * (unsigned)MIXED_CHUNK;
+  // coordinates of this thread's node, advanced by the stride each chunk
+  int ix, iy, iz;
+  coords(k, (long long)blockIdx.x * MIXED_CHUNK + tid, ix, iy, iz);
+  int dsx, dsy, dsz;
+  coords(k, (long long)stride, dsx, dsy, dsz);
+  unsigned i = 0;
+  for (; i < nMine; ++i) {
+    const unsigned c = blockIdx.x + i * gridDim.x;
+    const int st = (int)(i % MIXED_STAGES);
+    const unsigned ph = (i / MIXED_STAGES) & 1u;
+    if (__any_sync(FULL, *(volatile int*)&abortFlag != 0) || !warpWait(&fullBar[st], ph)) {
+      if (lane == 0) {
+        atomicOr(a.iscal + IS_ERROR, ERR_PIPELINE);
+        abortFlag = 1;
+      }
+      break;
+    }
+    const unsigned char* sb = stageMem + st * MIXED_STAGE_BYTES;
+    const unsigned x = c * MIXED_CHUNK + tid;
     const bool valid = x < N;
-    const uint8_t m = valid ? mk[x] : (uint8_t)2;
+    float g[Q];
+#pragma unroll
+    for (int j = 0; j < Q; ++j) g[j] = ((const float*)sb)[j * MIXED_CHUNK + tid];
+    const uint8_t m = valid ? sb[Q * MIXED_CHUNK * 4 + tid] : (uint8_t)2;
+    __syncwarp();
+    if (lane == 0) mbarArrive(&emptyBar[st]);  // this warp is done with the stage
+    if (tid == 0 && i >= 1 && issued < nMine) {
+      // refill the stage of iteration i - 1 with iteration i - 1 + MIXED_STAGES
+      const unsigned pi = i - 1u;
+      if (mbarWait(&emptyBar[pi % MIXED_STAGES], (pi / MIXED_STAGES) & 1u)) {
+        issue(issued);
+        ++issued;
+      } else {
+        atomicOr(a.iscal + IS_ERROR, ERR_PIPELINE);
+        abortFlag = 1;
+      }
+    }
     const int t = m & TYPE_MASK;
     const bool act = valid && isActiveT(t);
     // cleanLists (ABIT) and the neighbour cache (BULK) of this node
     uint8_t nm = (uint8_t)(m & ~(ABIT | BULK));
     if (__any_sync(FULL, act)) {
-      float g[Q];
       unsigned actN = ALL_LINKS, gasN = 0, spcN = 0;
       NodeStateF s;
       s.dx = s.dy = s.dz = s.rx = s.ry = s.rz = 0.0f;
       float massOld = 0.0f;
       int key = -1;
       if (act) {
-#pragma unroll
-        for (int j = 0; j < Q; ++j) g[j] = __ldcs(gin + j * NN + x);
-        if (!(m & BULK)) {
+        // links into the box's wall layer, known from the coordinates
+        const unsigned wallN = boxWallLinks(k, ix, iy, iz);
+        if (m & BULK) {
+          actN = ALL_LINKS & ~wallN;
+        } else {
           actN = 0;
 #pragma unroll
           for (int j = 1; j < Q; ++j) {
@@ -166,7 +282,7 @@ __global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
             spcN |= ((PLAIN_TYPES >> tl) & 1u ^ 1u) << j;
           }
         }
-        nm |= (uint8_t)(ABIT | (actN == ALL_LINKS ? BULK : 0));
+        nm |= (uint8_t)(ABIT | ((actN | wallN) == ALL_LINKS ? BULK : 0));
         const bool pf = (m & PFLAG) != 0;
         const uint32_t pid = pf ? a.solid[x] : 0u;
         if (pf) massOld = t == 3 ? (float)a.mass[x] : a.nF[x];
@@ -180,21 +296,30 @@ __global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
       if (__any_sync(FULL, key >= 0))
         particleRunReduce(key, ix, s.dx, s.dy, s.dz, s.rx, s.ry, s.rz, massOld, a.pAccF,
                           k.nPart);
+      // warps whose 32 nodes push every population to an active neighbour
+      // skip the per-link tests
+      const bool pushAll = __all_sync(FULL, act && actN == ALL_LINKS);
       if (act) {
         ++nact;
         __stcs(gout + x, g[0]);
+      }
+      if (pushAll) {
+#pragma unroll
+        for (int j = 1; j < Q; ++j)
+          __stcs(gout + j * NP + (x + (unsigned)(CX(j) + CY(j) * sy + CZ(j) * sz)), g[j]);
+      } else if (act) {
         const float usq3 = 3.0f * __fmaf_rn(s.ux, s.ux, __fmaf_rn(s.uy, s.uy, s.uz * s.uz));
 #pragma unroll
         for (int j = 1; j < Q; ++j) {
           if ((actN >> j) & 1u) {
-            __stcs(gout + j * NN + (x + (unsigned)(CX(j) + CY(j) * sy + CZ(j) * sz)), g[j]);
+            __stcs(gout + j * NP + (x + (unsigned)(CX(j) + CY(j) * sy + CZ(j) * sz)), g[j]);
           } else {
             float out = g[j];
             if ((gasN >> j) & 1u) {
               const float vu = dotcf(j, s.ux, s.uy, s.uz);
               out = __fmaf_rn((float)WJ(j), __fmaf_rn(9.0f * vu, vu, -usq3), -g[j]);
             }
-            gout[OPPJ(j) * NN + x] = out;
+            gout[OPPJ(j) * NP + x] = out;
           }
         }
         // impactor links and unexpected types: the value stored above is
@@ -216,7 +341,7 @@ __global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
               atomicOr(a.iscal + IS_ERROR, ERR_TYPE);
               continue;
             }
-            float* dst = gout + (size_t)(dj >> 8) * NN + x;
+            float* dst = gout + (size_t)(dj >> 8) * NP + x;
             const float gj = *dst;
             const float* ov = sObj + 6 * oi;
             const float wj = j <= 6 ? (float)WJ(1) : (float)WJ(7);
@@ -250,6 +375,8 @@ __global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
           if (ocur >= 0)
             for (int c = 0; c < 6; ++c) atomicAdd(&accO[6 * ocur + c], fo[c]);
         }
+      }
+      if (act) {
         if (t == 3) {
           ++nif;
           a.rhoS[x] = s.n;
@@ -271,7 +398,7 @@ __global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
       }
     }
     if (valid && nm != m) a.mask[x] = nm;
-    // advance this lane's coordinates by the stride
+    // advance this thread's coordinates by the stride
     ix += dsx;
     iy += dsy;
     iz += dsz;
@@ -284,6 +411,12 @@ __global__ void __launch_bounds__(256, 3) lbStepMixed(Consts k, LbArgs a) {
       ++iz;
     }
   }
+  // no bulk copy may still be in flight when the block exits: on an early
+  // exit, wait (bounded) for the copies issued beyond the last iteration used
+  if (tid == 0)
+    for (unsigned q = i; q < issued; ++q)
+      if (!mbarWait(&fullBar[q % MIXED_STAGES], (q / MIXED_STAGES) & 1u))
+        atomicOr(a.iscal + IS_ERROR, ERR_PIPELINE);
   // block totals
   nact = __reduce_add_sync(FULL, nact);
   nif = __reduce_add_sync(FULL, nif);
@@ -374,7 +507,7 @@ __global__ void lbWallForceMixed(Consts k, LbArgs a) {
           fw[0] = fw[1] = fw[2] = 0.0f;
           wcur = (int)w;
         }
-        const float bb = 2.0f * gout[OPPJ(j) * NN + x];
+        const float bb = 2.0f * gout[OPPJ(j) * (size_t)k.NP + x];
         if (CX(j)) fw[0] += CX(j) > 0 ? bb : -bb;
         if (CY(j)) fw[1] += CY(j) > 0 ? bb : -bb;
         if (CZ(j)) fw[2] += CZ(j) > 0 ? bb : -bb;

@@ -233,7 +233,10 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   CK(cudaDeviceGetAttribute(&ctx->smCount, cudaDevAttrMultiProcessorCount, ctx->device));
   {
     int perSm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, lbStepMixed, 256, 0));
+    CK(cudaFuncSetAttribute(lbStepMixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            MIXED_SMEM));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, lbStepMixed, MIXED_THREADS,
+                                                     MIXED_SMEM));
     ctx->lbMixedBlocks = std::max(1, perSm) * std::max(1, ctx->smCount);
   }
 
@@ -262,7 +265,9 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   k.Z = int(std::floor(cfg->lbSizeZ / L + 0.5));
   if (k.X < 3 || k.Y < 3 || k.Z < 3) return setErr(ctx, LBDEM_ERR_INVALID, "lattice too small");
   k.N = (long long)k.X * k.Y * k.Z;
-  if (k.N >= (1ll << 32) / Q) return setErr(ctx, LBDEM_ERR_INVALID, "lattice too large");
+  // population planes start on 1 KB boundaries (bulk copies of 256-node chunks)
+  k.NP = (k.N + 255) / 256 * 256;
+  if (k.NP >= (1ll << 32) / Q) return setErr(ctx, LBDEM_ERR_INVALID, "lattice too large");
   k.sy = k.X;
   k.sz = (long long)k.X * k.Y;
   k.initDensity = 1.0;
@@ -270,7 +275,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   k.omega = 1.0 / (0.5 + 3.0 * k.initVisc);
   k.omegaf = 1.0 - 1.0 / (1.0 + 6.0 * k.initVisc);
   k.mixed = precision == LBDEM_MIXED ? 1 : 0;
-  if (k.mixed && k.N >= (1LL << 31))
+  if (k.mixed && k.NP >= (1LL << 31))
     return setErr(ctx, LBDEM_ERR_INVALID, "mixed form: lattice larger than 2^31 nodes");
   k.omegaF = (float)k.omega;
   k.omegafF = (float)k.omegaf;
@@ -378,10 +383,11 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   // ---- allocation ----
   Device& d = ctx->d;
   const size_t N = (size_t)k.N;
+  const size_t NP = (size_t)k.NP;
   int rc;
 #define AL(ptr, n)                                      \
   if ((rc = dalloc(ctx, &(ptr), (n))) != LBDEM_OK) return rc;
-  AL(d.mask, N);
+  AL(d.mask, NP);  // padded: the lattice step copies whole 256-node chunks
   AL(d.solid, N);
   AL(d.objIdx, N);
   AL(d.claim, N);
@@ -389,16 +395,16 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   if (k.mixed) {
     float* f0 = nullptr;
     float* f1 = nullptr;
-    AL(f0, (size_t)Q * N);
-    AL(f1, (size_t)Q * N);
+    AL(f0, (size_t)Q * NP);
+    AL(f1, (size_t)Q * NP);
     d.f[0] = f0;
     d.f[1] = f1;
     AL(d.nF, N);
   } else {
     double* f0 = nullptr;
     double* f1 = nullptr;
-    AL(f0, (size_t)Q * N);
-    AL(f1, (size_t)Q * N);
+    AL(f0, (size_t)Q * NP);
+    AL(f1, (size_t)Q * NP);
     d.f[0] = f0;
     d.f[1] = f1;
   }
@@ -600,7 +606,9 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   LbArgs a = lbArgs(ctx);
   auto* ev = nextLbEvents(ctx);
   if (ev) cudaEventRecord(ev->first, s);
-  if (k.mixed) lbStepMixed<<<ctx->lbMixedBlocks, 256, 0, s>>>(k, a);
+  if (k.mixed)
+    lbStepMixed<<<(int)std::min<long long>(ctx->lbMixedBlocks, k.NP / MIXED_CHUNK),
+                  MIXED_THREADS, MIXED_SMEM, s>>>(k, a);
   else lbStepFp64<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
   if (ev) cudaEventRecord(ev->second, s);
   if (k.mixed && k.nWall > 0) {
@@ -706,6 +714,7 @@ extern "C" int lbdem_sync(lbdem_ctx* ctx) {
     if (e & ERR_PARTICLE_INDEX) m += " particle-index";
     if (e & ERR_NONFINITE) m += " non-finite";
     if (e & ERR_GRID) m += " particle-outside-grid";
+    if (e & ERR_PIPELINE) m += " lattice-copy-pipeline-timeout";
     const int code = (e & ERR_NONFINITE) ? LBDEM_ERR_NONFINITE
                    : (e & (ERR_NBR_OVERFLOW | ERR_CELL_OVERFLOW | ERR_UNCOVER_CAP))
                        ? LBDEM_ERR_OVERFLOW

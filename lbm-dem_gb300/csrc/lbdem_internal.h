@@ -23,9 +23,10 @@ constexpr int ACCF_N = 13;       // mixed-form particle sums: d(3), r (x) d (9),
 constexpr uint8_t TYPE_MASK = 0x0F;
 constexpr uint8_t PFLAG = 0x10;   // inside a particle (nodeType::p)
 constexpr uint8_t ABIT = 0x20;    // member of the last active list (cleanLists)
-// Cache: every streaming neighbour was active when the lattice step last
-// checked. Set only by the lattice step; cleared around every node that
-// leaves the active types (free-surface emptying, impactor voxelisation).
+// Cache: every streaming neighbour was active, or a wall of the box's outer
+// node layer, when the lattice step last checked. Set only by the lattice
+// step; cleared around every node that leaves the active types
+// (free-surface emptying, impactor voxelisation); box walls never change.
 constexpr uint8_t BULK = 0x40;
 
 // device error bits
@@ -37,12 +38,14 @@ enum : int {
   ERR_PARTICLE_INDEX = 16,
   ERR_NONFINITE = 32,
   ERR_GRID = 64,         // particle outside the cell grid
+  ERR_PIPELINE = 128,    // a bounded wait of the lattice step's copy pipeline gave up
 };
 
 // Physical / lattice constants of one run (passed by value to kernels).
 struct Consts {
   int X, Y, Z;
   long long N;
+  long long NP;      // population plane stride: N rounded up to a multiple of 256
   long long sy, sz;  // strides of y and z
   int freeSurface, forceField;
   double uLength, uTime, uSpeed, uAccel, uAngVel, uForce, uTorque, uVolume;
