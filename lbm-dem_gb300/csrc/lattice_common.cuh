@@ -41,6 +41,13 @@ __host__ __device__ constexpr unsigned linksWith(int axis, int sign) {
   return m;
 }
 
+// A node became active outside the lattice step (free-surface filling, an
+// uncovered impactor node): flag its warp of its 256-node chunk so that the
+// next mixed lattice step does not skip the chunk.
+__device__ __forceinline__ void markActive(const Consts& k, long long x) {
+  if (k.chunkAct) atomicOr(k.chunkAct + (x >> 8), 1u << ((x >> 5) & 7));
+}
+
 // Links of node (ix, iy, iz) that end in the outer node layer of the box.
 // A run accepts walls on all six faces and no other boundary, so the outer
 // layer is all wall nodes and these are exactly the node's wall links.

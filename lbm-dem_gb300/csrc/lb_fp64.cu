@@ -459,6 +459,7 @@ __global__ void fsSmoothen(Consts k, FsArgs a) {
 #pragma unroll
         for (int j = 0; j < Q; ++j) fset(k, a.fcur, j, x, feqj(j, rho0, ux, uy, uz, usq));
         a.mask[x] = (uint8_t)((m & ~TYPE_MASK) | 3);
+        markActive(k, x);
         a.fsflag[x] |= FS_NEW;
         a.rhoS[x] = rho0;
         a.mass[x] = 0.01 * rho0;
@@ -686,6 +687,7 @@ __global__ void __launch_bounds__(1024) uncoverResolve(Consts k, uint8_t* mask, 
     const int st = s_st[i];
     const uint8_t m = mask[x];
     mask[x] = (uint8_t)((m & ~TYPE_MASK) | st);
+    if (st != 2) markActive(k, x);
     if (st == 2) {
       mass[x] = 0.0;
       continue;

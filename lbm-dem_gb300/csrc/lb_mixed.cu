@@ -162,6 +162,10 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
   __shared__ double accX;
   __shared__ int sbox[6];
   __shared__ unsigned scnt[2];
+  __shared__ int4 stageHdr[MIXED_STAGES];        // chunk index and its first node's x, y, z
+  __shared__ uint8_t sAct[MIXED_MAX_MINE];       // warp activity bits of this block's chunks
+  __shared__ uint16_t sList[MIXED_MAX_MINE];     // which of them to process
+  __shared__ unsigned sCount;
   const int tid = threadIdx.x;
   if (tid == 0) {
     for (int st = 0; st < MIXED_STAGES; ++st) {
@@ -198,6 +202,29 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
   const unsigned nMine =
       nChunks > blockIdx.x ? (nChunks - 1u - blockIdx.x) / gridDim.x + 1u : 0u;
   const int lane = tid & 31;
+  const int warp = tid >> 5;
+  // Chunks with no active node are skipped: their activity bits (kept by
+  // this kernel and set by whatever activates a node in between) are read
+  // once, and warp 0 compacts the list of chunks to process.
+  const bool useList = k.chunkAct != nullptr && nMine <= (unsigned)MIXED_MAX_MINE;
+  if (useList) {
+    for (unsigned it = tid; it < nMine; it += blockDim.x)
+      sAct[it] = (uint8_t)k.chunkAct[blockIdx.x + it * gridDim.x];
+    __syncthreads();
+    if (warp == 0) {
+      unsigned run = 0;
+      for (unsigned b = 0; b < nMine; b += 32) {
+        const unsigned it = b + lane;
+        const bool on = it < nMine && sAct[it] != 0;
+        const unsigned bal = __ballot_sync(FULL, on);
+        if (on) sList[run + __popc(bal & ((1u << lane) - 1u))] = (uint16_t)it;
+        run += __popc(bal);
+      }
+      if (lane == 0) sCount = run;
+    }
+    __syncthreads();
+  }
+  const unsigned nIter = useList ? sCount : nMine;
   double extra = 0.0;
   unsigned nact = 0, nif = 0;
   // Thread 0 keeps the stage ring filled: bulk copies of the 19 population
@@ -205,29 +232,27 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
   // barrier. Iterations 0 .. MIXED_STAGES-1 are issued up front; iteration
   // i + MIXED_STAGES - 1 is issued at iteration i once every warp has
   // released iteration i - 1.
-  auto issue = [&](unsigned it) {
-    const int st = (int)(it % MIXED_STAGES);
+  auto issue = [&](unsigned q) {
+    const int st = (int)(q % MIXED_STAGES);
     unsigned char* sb = stageMem + st * MIXED_STAGE_BYTES;
-    const size_t off = (size_t)(blockIdx.x + it * gridDim.x) * MIXED_CHUNK;
+    const unsigned c = blockIdx.x + (useList ? sList[q] : q) * gridDim.x;
+    const size_t off = (size_t)c * MIXED_CHUNK;
+    int cx0, cy0, cz0;
+    coords(k, (long long)off, cx0, cy0, cz0);
+    stageHdr[st] = make_int4((int)c, cx0, cy0, cz0);
     mbarExpectTx(&fullBar[st], MIXED_STAGE_BYTES);
 #pragma unroll 1
     for (int j = 0; j < Q; ++j)
       bulkLoad(sb + j * MIXED_CHUNK * 4, gin + j * NP + off, MIXED_CHUNK * 4, &fullBar[st]);
-    bulkLoad(sb + Q * MIXED_CHUNK * 4, mk + off, MIXED_CHUNK, &fullBar[st]);
+    bulkLoad(sb + MIXED_STAGE_SOLID, a.solid + off, MIXED_CHUNK * 4, &fullBar[st]);
+    bulkLoad(sb + MIXED_STAGE_MASK, mk + off, MIXED_CHUNK, &fullBar[st]);
   };
   unsigned issued = 0;  // meaningful in thread 0
   if (tid == 0)
-    for (; issued < nMine && issued < (unsigned)MIXED_STAGES; ++issued) issue(issued);
+    for (; issued < nIter && issued < (unsigned)MIXED_STAGES; ++issued) issue(issued);
   const int X = k.X, Y = k.Y, sy = (int)k.sy, sz = (int)k.sz;
-  const unsigned stride = gridDim.x * (unsigned)MIXED_CHUNK;
-  // coordinates of this thread's node, advanced by the stride each chunk
-  int ix, iy, iz;
-  coords(k, (long long)blockIdx.x * MIXED_CHUNK + tid, ix, iy, iz);
-  int dsx, dsy, dsz;
-  coords(k, (long long)stride, dsx, dsy, dsz);
   unsigned i = 0;
-  for (; i < nMine; ++i) {
-    const unsigned c = blockIdx.x + i * gridDim.x;
+  for (; i < nIter; ++i) {
     const int st = (int)(i % MIXED_STAGES);
     const unsigned ph = (i / MIXED_STAGES) & 1u;
     if (__any_sync(FULL, *(volatile int*)&abortFlag != 0) || !warpWait(&fullBar[st], ph)) {
@@ -238,15 +263,27 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
       break;
     }
     const unsigned char* sb = stageMem + st * MIXED_STAGE_BYTES;
+    const int4 hdr = stageHdr[st];
+    const unsigned c = (unsigned)hdr.x;
     const unsigned x = c * MIXED_CHUNK + tid;
     const bool valid = x < N;
+    // this thread's node coordinates from the chunk's first node
+    int ix = hdr.y + tid, iy = hdr.z, iz = hdr.w;
+    while (ix >= X) {
+      ix -= X;
+      if (++iy >= Y) {
+        iy = 0;
+        ++iz;
+      }
+    }
     float g[Q];
 #pragma unroll
     for (int j = 0; j < Q; ++j) g[j] = ((const float*)sb)[j * MIXED_CHUNK + tid];
-    const uint8_t m = valid ? sb[Q * MIXED_CHUNK * 4 + tid] : (uint8_t)2;
+    const uint8_t m = valid ? sb[MIXED_STAGE_MASK + tid] : (uint8_t)2;
+    const uint32_t sol = ((const uint32_t*)(sb + MIXED_STAGE_SOLID))[tid];
     __syncwarp();
     if (lane == 0) mbarArrive(&emptyBar[st]);  // this warp is done with the stage
-    if (tid == 0 && i >= 1 && issued < nMine) {
+    if (tid == 0 && i >= 1 && issued < nIter) {
       // refill the stage of iteration i - 1 with iteration i - 1 + MIXED_STAGES
       const unsigned pi = i - 1u;
       if (mbarWait(&emptyBar[pi % MIXED_STAGES], (pi / MIXED_STAGES) & 1u)) {
@@ -284,7 +321,7 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
         }
         nm |= (uint8_t)(ABIT | ((actN | wallN) == ALL_LINKS ? BULK : 0));
         const bool pf = (m & PFLAG) != 0;
-        const uint32_t pid = pf ? a.solid[x] : 0u;
+        const uint32_t pid = pf ? sol : 0u;
         if (pf) massOld = t == 3 ? (float)a.mass[x] : a.nF[x];
         collideNodeMixed(k, g, pf, pid, a.pkf, k.nPart, massOld, ix, iy, iz, s);
         if (pf) {
@@ -398,17 +435,14 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
       }
     }
     if (valid && nm != m) a.mask[x] = nm;
-    // advance this thread's coordinates by the stride
-    ix += dsx;
-    iy += dsy;
-    iz += dsz;
-    if (ix >= X) {
-      ix -= X;
-      ++iy;
-    }
-    if (iy >= Y) {
-      iy -= Y;
-      ++iz;
+    if (useList) {  // keep this warp's activity bit of the chunk current
+      const bool any = __any_sync(FULL, act);
+      const unsigned bit = 1u << warp;
+      const bool was = (sAct[sList[i]] & bit) != 0;
+      if (lane == 0 && any != was) {
+        if (any) atomicOr(k.chunkAct + c, bit);
+        else atomicAnd(k.chunkAct + c, ~bit);
+      }
     }
   }
   // no bulk copy may still be in flight when the block exits: on an early

@@ -388,7 +388,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
 #define AL(ptr, n)                                      \
   if ((rc = dalloc(ctx, &(ptr), (n))) != LBDEM_OK) return rc;
   AL(d.mask, NP);  // padded: the lattice step copies whole 256-node chunks
-  AL(d.solid, N);
+  AL(d.solid, NP);  // padded: the mixed lattice step copies whole chunks
   AL(d.objIdx, N);
   AL(d.claim, N);
   AL(d.fsflag, N);
@@ -426,6 +426,12 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   AL(d.pkd, 6 * P1);
   if (k.mixed) AL(d.pkf, 9 * P1);
   if (k.mixed) AL(d.pAccF, ACCF_N * P1);
+  if (k.mixed) {
+    AL(d.chunkAct, NP / 256);
+    // every chunk may hold active nodes until the first lattice step checks
+    CK(cudaMemsetAsync(d.chunkAct, 0xFF, NP / 256 * sizeof(uint32_t), ctx->stream));
+    k.chunkAct = d.chunkAct;
+  }
   // hydro accumulators contiguous (reset together each LB step)
   double* hyd = nullptr;
   AL(hyd, 16 * P1);
@@ -517,7 +523,8 @@ extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
                   d.massNew, d.rhoS, d.uS, d.hS, d.scal, d.iscal, d.uscal, d.px0, d.px1,
                   d.pw1, d.pr, d.pinvm, d.pinvI, d.pFHydro, d.pFContact, d.pMContact,
                   d.pFLub, d.pMLub, d.pFRep, d.pFTotal, d.pMTotal, d.pFGrav, d.pxiw,
-                  d.pxio, d.nF, d.pkd, d.pkf, d.pAccF, d.plist[0], d.plist[1], d.pxi[0], d.pxi[1], d.partner, d.gorder,
+                  d.pxio, d.nF, d.pkd, d.pkf, d.pAccF, d.chunkAct, d.plist[0], d.plist[1], d.pxi[0],
+                  d.pxi[1], d.partner, d.gorder,
                   d.pairbuf, d.pairflag, d.pcell, d.ppos, d.cellCount, d.cellStart,
                   d.cellFill, d.cellParts, d.obj, d.wallF, d.walls, d.uncover};
   if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);

@@ -62,6 +62,10 @@ struct Consts {
   double dt;
   double k, c, mu, kinVisc, lubN, lubT, lubR, lubCut, electro, debye;
   int objWaitTime;
+  // mixed form: per 256-node chunk, bit w set = warp w of the chunk may hold
+  // active nodes (the lattice step skips chunks with no bit set); null in
+  // the plain form
+  uint32_t* chunkAct;
 };
 
 struct DeviceWall {
@@ -97,6 +101,7 @@ struct Device {
   double* pkd = nullptr;                 // [6][P] lattice-unit kinematics
   float* pkf = nullptr;                  // [9][P] (mixed form)
   float* pAccF = nullptr;                // [ACCF_N][P] particle sums (mixed form)
+  uint32_t* chunkAct = nullptr;          // [NP/256] chunk activity (mixed form)
   int* plist[2] = {nullptr, nullptr};    // [P][50]
   double* pxi[2] = {nullptr, nullptr};   // [P][3][50]
   int* partner = nullptr;                // [P][50] slot of i in list[j]
