@@ -31,11 +31,16 @@ __device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : 
 
 // ---- evalMaxDisp and the rebuild trigger -----------------------------------
 
-__global__ void __launch_bounds__(1024) demBegin(Consts k, DemArgs a, int forceRebuild) {
-  __shared__ double red[32];
+// DEM::evalMaxDisp and the rebuild trigger of DEM::discreteElementStep
+// (src/DEM.cpp:460-470, 368-378): the maximum of |x1|^2 over the particles
+// (exact in any order: atomicMax on the bit patterns of non-negative
+// doubles), then the last block to finish decides on a rebuild.
+__global__ void __launch_bounds__(256) demBegin(Consts k, DemArgs a, int forceRebuild) {
+  __shared__ double red[8];
+  __shared__ bool last;
   double m = 0.0;
   const int P = k.nPart;
-  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
     const double vx = a.x1[i], vy = a.x1[P + i], vz = a.x1[2 * P + i];
     const double n2 = vx * vx + vy * vy + vz * vz;
     if (n2 > m) m = n2;
@@ -47,6 +52,17 @@ __global__ void __launch_bounds__(1024) demBegin(Consts k, DemArgs a, int forceR
     double mv = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
       if (red[w] > mv) mv = red[w];
+    if (mv > 0.0)
+      atomicMax(a.uscal + US_MAXV2, (unsigned long long)__double_as_longlong(mv));
+    __threadfence();
+    last = atomicAdd(a.iscal + IS_BLOCKS_DONE, 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    double mv = __longlong_as_double((long long)atomicExch(a.uscal + US_MAXV2, 0ull));
+    a.iscal[IS_BLOCKS_DONE] = 0;
     bool rebuild = forceRebuild != 0;
     if (!forceRebuild) {
       mv = sqrt(mv);
@@ -60,6 +76,7 @@ __global__ void __launch_bounds__(1024) demBegin(Consts k, DemArgs a, int forceR
     if (rebuild) {
       a.iscal[IS_NEWNBR] = 1;
       a.iscal[IS_REBUILDS] += 1;
+      a.iscal[IS_NPAIRS] = 0;
     }
   }
   // reset of the per-step impactor and wall accumulators
@@ -371,6 +388,26 @@ __global__ void nbrPartners(Consts k, DemArgs a) {
   }
 }
 
+// Owner slots of the new lists (slot s of particle i with list[i][s] < i),
+// so that the pair pass runs one thread per pair. The order of the entries
+// does not matter: every pair writes only its own slot's outputs.
+__global__ void nbrPairList(Consts k, DemArgs a) {
+  if (!a.iscal[IS_REBUILD]) return;
+  const int* L = a.list[1 - a.iscal[IS_LISTCUR]];
+  const long long total = (long long)k.nPart * MAX_N;
+  const int cap = max(k.nPart, 1) * (MAX_N / 2);
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int s = (int)(idx % MAX_N);
+    if (s == 0) continue;
+    const int i = (int)(idx / MAX_N);
+    if (s > L[(long long)i * MAX_N] || L[idx] >= i) continue;
+    const int pos = atomicAdd(a.iscal + IS_NPAIRS, 1);
+    if (pos < cap) a.pairList[pos] = (int)idx;
+    else atomicOr(a.iscal + IS_ERROR, ERR_NBR_OVERFLOW);
+  }
+}
+
 __global__ void nbrFinish(DemArgs a) {
   if (!a.iscal[IS_REBUILD]) return;
   a.iscal[IS_LISTCUR] = 1 - a.iscal[IS_LISTCUR];
@@ -566,40 +603,37 @@ __device__ __forceinline__ void load3(const double* a, int P, int i, double* v) 
   v[2] = a[2 * P + i];
 }
 
-// Owner pass: every pair (n1 > n2) evaluated once from n1's slot.
+// Owner pass: every pair (n1 > n2) evaluated once from n1's slot, one
+// thread per entry of the owner-pair list.
 __global__ void demPairs(Consts k, DemArgs a, int lubOn) {
   const int cur = a.iscal[IS_LISTCUR];
   const int* L = a.list[cur];
   double* XI = a.xi[cur];
   const int P = k.nPart;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
-    const int* li = L + (long long)i * MAX_N;
+  const int npairs = min(a.iscal[IS_NPAIRS], max(P, 1) * (MAX_N / 2));
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < npairs; e += gridDim.x * blockDim.x) {
+    const int idx = a.pairList[e];
+    const int i = idx / MAX_N, s = idx % MAX_N;
+    const int j = L[idx];
     double* xii = XI + (long long)i * 3 * MAX_N;
-    double xa[3], va[3], wa[3];
+    double xa[3], va[3], wa[3], xb[3], vb[3], wb[3];
     load3(a.x0, P, i, xa);
     load3(a.x1, P, i, va);
     load3(a.w1, P, i, wa);
-    const double ra = a.r[i];
-    const int cnt = li[0];
-    for (int s = 1; s <= cnt; ++s) {
-      const int j = li[s];
-      if (j >= i) continue;
-      double xb[3], vb[3], wb[3];
-      load3(a.x0, P, j, xb);
-      load3(a.x1, P, j, vb);
-      load3(a.w1, P, j, wb);
-      const double rb = a.r[j];
-      double* out = a.pairbuf + ((long long)i * MAX_N + s) * PAIR_VALS;
-      uint8_t flag = 0;
-      if (lubOn && pairLub(k, ra, rb, xa, xb, va, vb, wa, wb, out + 6)) flag |= 1;
-      double xi[3] = {xii[s], xii[MAX_N + s], xii[2 * MAX_N + s]};
-      pairContact(k, ra, rb, xa, xb, va, vb, wa, wb, xi, out);
-      xii[s] = xi[0];
-      xii[MAX_N + s] = xi[1];
-      xii[2 * MAX_N + s] = xi[2];
-      pairRep(k, ra, rb, xa, xb, out + 15);
-      a.pairflag[(long long)i * MAX_N + s] = flag;
-    }
+    load3(a.x0, P, j, xb);
+    load3(a.x1, P, j, vb);
+    load3(a.w1, P, j, wb);
+    const double ra = a.r[i], rb = a.r[j];
+    double* out = a.pairbuf + (long long)idx * PAIR_VALS;
+    uint8_t flag = 0;
+    if (lubOn && pairLub(k, ra, rb, xa, xb, va, vb, wa, wb, out + 6)) flag |= 1;
+    double xi[3] = {xii[s], xii[MAX_N + s], xii[2 * MAX_N + s]};
+    pairContact(k, ra, rb, xa, xb, va, vb, wa, wb, xi, out);
+    xii[s] = xi[0];
+    xii[MAX_N + s] = xi[1];
+    xii[2 * MAX_N + s] = xi[2];
+    pairRep(k, ra, rb, xa, xb, out + 15);
+    a.pairflag[idx] = flag;
   }
 }
 
@@ -869,9 +903,8 @@ __global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a, int stepNo
         if (wallLubOne(k, ra, va, wa, x12, y12, z12, F, T)) {
           add3(FL, F);
           add3(ML, T);
-          atomicAdd(&acc[GA_WALL + 6 * w + 3], -F[0]);
-          atomicAdd(&acc[GA_WALL + 6 * w + 4], -F[1]);
-          atomicAdd(&acc[GA_WALL + 6 * w + 5], -F[2]);
+          for (int c = 0; c < 3; ++c)
+            if (F[c] != 0.0) atomicAdd(&acc[GA_WALL + 6 * w + 3 + c], -F[c]);
         }
       }
       for (int o = 0; o < k.nObj; ++o) {
@@ -882,9 +915,10 @@ __global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a, int stepNo
         MC[0] += ra * dt[0];
         MC[1] += ra * dt[1];
         MC[2] += ra * dt[2];
+        // a zero addend leaves a sum unchanged: only contacts touch the sums
         for (int c = 0; c < 3; ++c) {
-          atomicAdd(&acc[GA_OBJ + 12 * o + c], -df[c]);
-          atomicAdd(&acc[GA_OBJ + 12 * o + 3 + c], ob[OB_R] * dt[c]);
+          if (df[c] != 0.0) atomicAdd(&acc[GA_OBJ + 12 * o + c], -df[c]);
+          if (dt[c] != 0.0) atomicAdd(&acc[GA_OBJ + 12 * o + 3 + c], ob[OB_R] * dt[c]);
         }
       }
       for (int o = 0; o < k.nObj; ++o) {
@@ -894,8 +928,8 @@ __global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a, int stepNo
           add3(FL, lo);
           add3(ML, lo + 3);
           for (int c = 0; c < 3; ++c) {
-            atomicAdd(&acc[GA_OBJ + 12 * o + 6 + c], -lo[c]);
-            atomicAdd(&acc[GA_OBJ + 12 * o + 9 + c], lo[6 + c]);
+            if (lo[c] != 0.0) atomicAdd(&acc[GA_OBJ + 12 * o + 6 + c], -lo[c]);
+            if (lo[6 + c] != 0.0) atomicAdd(&acc[GA_OBJ + 12 * o + 9 + c], lo[6 + c]);
           }
         }
       }
@@ -945,9 +979,8 @@ __global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a, int stepNo
         MC[0] += ra * dt[0];
         MC[1] += ra * dt[1];
         MC[2] += ra * dt[2];
-        atomicAdd(&acc[GA_WALL + 6 * w + 0], -df[0]);
-        atomicAdd(&acc[GA_WALL + 6 * w + 1], -df[1]);
-        atomicAdd(&acc[GA_WALL + 6 * w + 2], -df[2]);
+        for (int c = 0; c < 3; ++c)
+          if (df[c] != 0.0) atomicAdd(&acc[GA_WALL + 6 * w + c], -df[c]);
       }
     }
     // totals (src/DEM.cpp:745-762) and integration (:2681-2707)

@@ -65,6 +65,7 @@ struct DemArgs {
   double* xi[2];
   int* partner;
   int* gorder;
+  int* pairList;
   double* pairbuf;
   uint8_t* pairflag;
   int* pcell;
@@ -75,6 +76,7 @@ struct DemArgs {
   const DeviceWall* walls;
   double* scal;
   int* iscal;
+  unsigned long long* uscal;
 };
 
 // Mixed lattice step launch shape: chunks of MIXED_CHUNK consecutive nodes
@@ -146,6 +148,7 @@ __global__ void nbrBuildCells(Consts k, DemArgs a);
 __global__ void nbrBuildDirect(Consts k, DemArgs a);
 __global__ void nbrDirectHistory(Consts k, DemArgs a);
 __global__ void nbrPartners(Consts k, DemArgs a);
+__global__ void nbrPairList(Consts k, DemArgs a);
 __global__ void nbrFinish(DemArgs a);
 __global__ void demPairs(Consts k, DemArgs a, int lubOn);
 __global__ void demGather(Consts k, DemArgs a, int stepNo);

@@ -157,6 +157,7 @@ DemArgs demArgs(lbdem_ctx* c) {
   a.xi[1] = d.pxi[1];
   a.partner = d.partner;
   a.gorder = d.gorder;
+  a.pairList = d.pairList;
   a.pairbuf = d.pairbuf;
   a.pairflag = d.pairflag;
   a.pcell = d.pcell;
@@ -170,6 +171,7 @@ DemArgs demArgs(lbdem_ctx* c) {
   a.walls = d.walls;
   a.scal = d.scal;
   a.iscal = d.iscal;
+  a.uscal = d.uscal;
   return a;
 }
 
@@ -191,6 +193,8 @@ int enqueueNeighbourList(lbdem_ctx* ctx) {
   nbrBuildDirect<<<pg, 128, 0, s>>>(k, a);
   nbrDirectHistory<<<pg, 128, 0, s>>>(k, a);
   nbrPartners<<<pg, 128, 0, s>>>(k, a);
+  nbrPairList<<<std::max(1, std::min(ctx->nPart * MAX_N / 256 + 1, ctx->smCount * 8)), 256, 0,
+                s>>>(k, a);
   nbrFinish<<<1, 1, 0, s>>>(a);
   return launchErr(ctx, "neighbour list");
 }
@@ -455,6 +459,8 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   AL(d.pxi[1], P1 * 3 * MAX_N);
   AL(d.partner, P1 * MAX_N);
   AL(d.gorder, P1 * MAX_N);
+  // each owner pair is one slot of one list: at most (MAX_N - 1) / 2 per particle
+  AL(d.pairList, (size_t)P1 * (MAX_N / 2));
   AL(d.pairbuf, P1 * MAX_N * PAIR_VALS);
   AL(d.pairflag, P1 * MAX_N);
   AL(d.pcell, P1);
@@ -504,7 +510,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   // ---- initial neighbour list (DEM::discreteElementInit, :294-296) ----
   {
     DemArgs a = demArgs(ctx);
-    demBegin<<<1, 1024, 0, st>>>(k, a, 1);
+    demBegin<<<partGrid(ctx, 256), 256, 0, st>>>(k, a, 1);
     if ((rc = enqueueNeighbourList(ctx)) != LBDEM_OK) return rc;
   }
   CK(cudaStreamSynchronize(st));
@@ -523,7 +529,7 @@ extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
                   d.massNew, d.rhoS, d.uS, d.hS, d.scal, d.iscal, d.uscal, d.px0, d.px1,
                   d.pw1, d.pr, d.pinvm, d.pinvI, d.pFHydro, d.pFContact, d.pMContact,
                   d.pFLub, d.pMLub, d.pFRep, d.pFTotal, d.pMTotal, d.pFGrav, d.pxiw,
-                  d.pxio, d.nF, d.pkd, d.pkf, d.pAccF, d.chunkAct, d.plist[0], d.plist[1], d.pxi[0],
+                  d.pxio, d.nF, d.pkd, d.pkf, d.pAccF, d.chunkAct, d.pairList, d.plist[0], d.plist[1], d.pxi[0],
                   d.pxi[1], d.partner, d.gorder,
                   d.pairbuf, d.pairflag, d.pcell, d.ppos, d.cellCount, d.cellStart,
                   d.cellFill, d.cellParts, d.obj, d.wallF, d.walls, d.uncover};
@@ -557,15 +563,16 @@ extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
   const Consts& k = ctx->k;
   DemArgs a = demArgs(ctx);
   cudaStream_t s = ctx->stream;
-  demBegin<<<1, 1024, 0, s>>>(k, a, 0);
+  demBegin<<<partGrid(ctx, 256), 256, 0, s>>>(k, a, 0);
   int rc = enqueueNeighbourList(ctx);
   if (rc) return rc;
   const int step = (int)ctx->demTimeStep;
   const int lubOn = step >= k.objWaitTime ? 1 : 0;
-  demPairs<<<partGrid(ctx, 128), 128, 0, s>>>(k, a, lubOn);
+  demPairs<<<std::max(1, std::min(ctx->nPart * (MAX_N / 2) / 128 + 1, ctx->smCount * 16)), 128, 0,
+             s>>>(k, a, lubOn);
   demGather<<<partGrid(ctx, 128), 128, 0, s>>>(k, a, step);
   demObjects<<<1, 32, 0, s>>>(k, a, step);
-  ctx->launches += 1 + 9 + 3;
+  ctx->launches += 1 + 10 + 3;
   return launchErr(ctx, "dem step");
 }
 

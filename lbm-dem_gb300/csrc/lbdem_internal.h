@@ -106,6 +106,7 @@ struct Device {
   double* pxi[2] = {nullptr, nullptr};   // [P][3][50]
   int* partner = nullptr;                // [P][50] slot of i in list[j]
   int* gorder = nullptr;                 // [P][50] gather order of slots
+  int* pairList = nullptr;               // [25 P] owner slots i*50+s with list[i][s] < i
   double* pairbuf = nullptr;             // [P][50][PAIR_VALS]
   uint8_t* pairflag = nullptr;           // [P][50] bit0 = lubrication valid
   int* pcell = nullptr;                  // [P] cell of particle
@@ -143,10 +144,14 @@ enum {
   IS_DIRECT = IS_NL + 3,    // direct-sum branch in use
   IS_LISTCUR,               // which list buffer is current
   IS_REBUILDS,              // rebuild counter
+  IS_NPAIRS,                // entries of the owner-pair list
+  IS_BLOCKS_DONE,           // demBegin: blocks that have posted their maximum
   IS_COUNT
 };
 // offsets into Device::uscal
-enum { US_FIRSTFLAG = 0, US_ACTIVE_UPDATES, US_COUNT };
+enum { US_FIRSTFLAG = 0, US_ACTIVE_UPDATES,
+       US_MAXV2,  // demBegin: max |x1|^2 as the bit pattern of a non-negative double
+       US_COUNT };
 
 // object record layout (doubles)
 enum {
