@@ -577,18 +577,37 @@ __device__ __forceinline__ void sphereBox(const Consts& k, double cx, double cy,
   }
 }
 
+// One impactor in lattice units (the quotients the reference forms at every
+// node, formed once per block) with its node box.
+struct SphereL {
+  double c[3], r;
+  int lo[3], hi[3];
+};
+// threads 0 .. nObj-1 fill s[] from the records' position at offset xoff
+// (OB_X0 or OB_X0PREV); the caller synchronises the block afterwards
+__device__ __forceinline__ void loadSpheres(const Consts& k, const double* obj, int xoff,
+                                            SphereL* s) {
+  const int o = threadIdx.x;
+  if (o < k.nObj) {
+    const double* ob = obj + o * OB_STRIDE;
+    for (int a = 0; a < 3; ++a) s[o].c[a] = ob[xoff + a] / k.uLength;
+    s[o].r = ob[OB_R] / k.uLength;
+    sphereBox(k, s[o].c[0], s[o].c[1], s[o].c[2], s[o].r, s[o].lo, s[o].hi);
+  }
+}
+
 // findNewActiveObject, step 1: collect object nodes that object 0 no longer
 // covers (candidates come from the previous voxelisation boxes).
 __global__ void uncoverCollect(Consts k, const uint8_t* mask, const double* obj,
                                uint32_t* list, int* iscal) {
-  const double* o0 = obj;
-  const double c0x = o0[OB_X0] / k.uLength, c0y = o0[OB_X0 + 1] / k.uLength,
-               c0z = o0[OB_X0 + 2] / k.uLength, r0 = o0[OB_R] / k.uLength;
+  __shared__ SphereL cur[MAX_OBJ], prev[MAX_OBJ];
+  loadSpheres(k, obj, OB_X0, cur);
+  loadSpheres(k, obj, OB_X0PREV, prev);
+  __syncthreads();
+  const double c0x = cur[0].c[0], c0y = cur[0].c[1], c0z = cur[0].c[2], r0 = cur[0].r;
   for (int o = 0; o < k.nObj; ++o) {
-    const double* ob = obj + o * OB_STRIDE;
-    int lo[3], hi[3];
-    sphereBox(k, ob[OB_X0PREV] / k.uLength, ob[OB_X0PREV + 1] / k.uLength,
-              ob[OB_X0PREV + 2] / k.uLength, ob[OB_R] / k.uLength, lo, hi);
+    const int* lo = prev[o].lo;
+    const int* hi = prev[o].hi;
     const long long nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
     const long long vol = nx * ny * nz;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol;
@@ -726,17 +745,15 @@ __global__ void fsClearBulk(Consts k, uint8_t* mask, const int* iscal) {
 // Voxelisation of the impactors (updateObjectBoundaries, src/LB.cpp:806-840).
 __global__ void voxelizeObjects(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* objIdx,
                                 double* mass, double* obj) {
+  __shared__ SphereL sph[MAX_OBJ];
+  loadSpheres(k, obj, OB_X0, sph);
+  __syncthreads();
   int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {-1, -1, -1};
-  for (int o = 0; o < k.nObj; ++o) {
-    const double* ob = obj + o * OB_STRIDE;
-    int l[3], h[3];
-    sphereBox(k, ob[OB_X0] / k.uLength, ob[OB_X0 + 1] / k.uLength, ob[OB_X0 + 2] / k.uLength,
-              ob[OB_R] / k.uLength, l, h);
+  for (int o = 0; o < k.nObj; ++o)
     for (int a = 0; a < 3; ++a) {
-      lo[a] = min(lo[a], l[a]);
-      hi[a] = max(hi[a], h[a]);
+      lo[a] = min(lo[a], sph[o].lo[a]);
+      hi[a] = max(hi[a], sph[o].hi[a]);
     }
-  }
   if (hi[0] < 0) return;
   const long long nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
   const long long vol = nx * ny * nz;
@@ -746,13 +763,10 @@ __global__ void voxelizeObjects(Consts k, uint8_t* mask, uint32_t* solid, uint8_
               iz = lo[2] + (int)(i / (nx * ny));
     const long long x = ix + iy * k.sy + iz * k.sz;
     int last = -1;
-    for (int o = 0; o < k.nObj; ++o) {
-      const double* ob = obj + o * OB_STRIDE;
-      if (insideSphere((double)ix, (double)iy, (double)iz, ob[OB_X0] / k.uLength,
-                       ob[OB_X0 + 1] / k.uLength, ob[OB_X0 + 2] / k.uLength,
-                       ob[OB_R] / k.uLength))
+    for (int o = 0; o < k.nObj; ++o)
+      if (insideSphere((double)ix, (double)iy, (double)iz, sph[o].c[0], sph[o].c[1],
+                       sph[o].c[2], sph[o].r))
         last = o;
-    }
     // the box reaches one node past the sphere, so it holds every neighbour
     // of a node turned into an impactor node: drop their neighbour cache
     const uint8_t m0 = mask[x];

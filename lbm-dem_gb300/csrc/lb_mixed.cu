@@ -528,11 +528,12 @@ __global__ void lbWallForceMixed(Consts k, LbArgs a) {
       }
       const long long x = ix + iy * k.sy + iz * k.sz;
       if (!isActiveT(a.mask[x] & TYPE_MASK)) continue;
+      // the outer layer is all wall nodes: the wall links follow from x
+      const unsigned wl = boxWallLinks(k, ix, iy, iz);
 #pragma unroll
       for (int j = 1; j < Q; ++j) {
+        if (!((wl >> j) & 1u)) continue;
         const long long lk = x + nbrOffset(k, j);
-        const int tl = a.mask[lk] & TYPE_MASK;
-        if (tl != 7 && tl != 8) continue;
         const uint32_t w = a.solid[lk];
         if (w >= (uint32_t)k.nWall) continue;
         if ((int)w != wcur) {

@@ -626,7 +626,7 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   else lbStepFp64<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
   if (ev) cudaEventRecord(ev->second, s);
   if (k.mixed && k.nWall > 0) {
-    lbWallForceMixed<<<ctx->smCount * 2, 256, 0, s>>>(k, a);
+    lbWallForceMixed<<<ctx->smCount * 8, 256, 0, s>>>(k, a);
     ctx->launches += 1;
   }
   lbFinalizeKernel<<<std::max(1, std::min(P1 / 256 + 1, 256)), 256, 0, s>>>(
