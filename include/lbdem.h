@@ -268,6 +268,56 @@ int lbdem_profile_enable(lbdem_ctx* ctx, int enable);
 /* Synchronise, report the counters since the last reset, optionally reset. */
 int lbdem_profile_read(lbdem_ctx* ctx, lbdem_profile* out, int reset);
 
+/* ---- many runs on one GPU (no counterpart in the reference: a serving
+ * layer of this library) ------------------------------------------------- */
+
+/* Device bytes lbdem_create would allocate for cfg in the given form. */
+int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t precision,
+                                int64_t* bytes);
+
+typedef struct lbdem_server lbdem_server;
+typedef struct lbdem_server_options {
+  int32_t device;
+  int32_t precision;      /* LBDEM_PLAIN_FP64 or LBDEM_MIXED for every run */
+  int32_t max_active;     /* runs resident at once                         */
+  int32_t slice_cycles;   /* goCycles enqueued per run per turn            */
+  int64_t device_budget_bytes; /* 0: 90 % of the free memory at creation   */
+  int32_t reserved[6];
+} lbdem_server_options;
+
+typedef struct lbdem_job_result {
+  int64_t job_id;
+  int32_t status;         /* LBDEM_OK or the failing call's status         */
+  int32_t cycles;         /* goCycles run                                  */
+  double submit_time, start_time, end_time; /* s since lbdem_server_create */
+  double impactor_x0[3], impactor_x1[3];    /* object 0 at the end         */
+  double fluid_mass;      /* as lbdem_mass_summary                         */
+  int64_t active_node_updates;
+  int64_t device_bytes;   /* the run's footprint estimate                  */
+} lbdem_job_result;
+
+/* Jobs queue in submission order. A job is admitted when its footprint fits
+ * the budget next to the runs in progress and fewer than max_active runs
+ * are resident. Each admitted job is a context with its own stream, and
+ * lbdem_server_poll advances every resident run by slice_cycles goCycles
+ * per turn, so their kernels overlap on the device. A finished run frees
+ * its memory for the next job. The server's calls must come from one host
+ * thread. */
+int lbdem_server_create(const lbdem_server_options* opt, lbdem_server** out);
+/* Queue a run of `cycles` goCycles; the configuration and its tables are
+ * copied. A run larger than the whole budget is refused (LBDEM_ERR_OOM). */
+int lbdem_server_submit(lbdem_server* s, const lbdem_config* cfg, int32_t cycles,
+                        int64_t* job_id);
+/* Admit and advance runs for up to wait_seconds, or until a run finishes
+ * or nothing is left; hand back up to max_out finished runs. */
+int lbdem_server_poll(lbdem_server* s, double wait_seconds, lbdem_job_result* out,
+                      int32_t max_out, int32_t* n_out);
+int lbdem_server_status(const lbdem_server* s, int32_t* queued, int32_t* running,
+                        int32_t* unread, int64_t* device_bytes_in_use);
+const char* lbdem_server_last_error(const lbdem_server* s);
+/* Ends the runs still resident (without results) and frees everything. */
+void lbdem_server_destroy(lbdem_server* s);
+
 /* ---- readback without device allocation (no counterpart in the
  * reference; a diagnostic of this library) ------------------------------ */
 

@@ -39,10 +39,13 @@ int setErr(lbdem_ctx* c, int code, const std::string& msg) {
                     std::string(#call) + ": " + cudaGetErrorString(_e));         \
   } while (0)
 
+// Context memory comes from the stream-ordered allocator on the context's
+// own stream: freeing it (lbdem_destroy) then waits for that stream only,
+// not for the whole device, so runs sharing a GPU do not stall each other.
 template <class T>
 int dalloc(lbdem_ctx* ctx, T** p, size_t count) {
   const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
-  cudaError_t e = cudaMalloc((void**)p, bytes);
+  cudaError_t e = cudaMallocAsync((void**)p, bytes, ctx->stream);
   if (e != cudaSuccess)
     return setErr(ctx, LBDEM_ERR_OOM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
   ctx->deviceBytes += (long long)bytes;
@@ -514,8 +517,8 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
     if ((rc = enqueueNeighbourList(ctx)) != LBDEM_OK) return rc;
   }
   CK(cudaStreamSynchronize(st));
-  cudaFree(dBoundary);
-  cudaFree(dWallType);
+  cudaFreeAsync(dBoundary, st);
+  cudaFreeAsync(dWallType, st);
   int e = 0;
   CK(cudaMemcpy(&e, d.iscal + IS_ERROR, sizeof(int), cudaMemcpyDeviceToHost));
   if (e) return setErr(ctx, LBDEM_ERR_DEVICE_STATE, "device error during init: " + std::to_string(e));
@@ -540,8 +543,11 @@ extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
     cudaEventDestroy(e.second);
   }
   for (void* p : ptrs)
-    if (p) cudaFree(p);
-  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    if (p) cudaFreeAsync(p, ctx->own_stream);
+  if (ctx->own_stream) {
+    cudaStreamSynchronize(ctx->own_stream);
+    cudaStreamDestroy(ctx->own_stream);
+  }
   delete ctx;
 }
 
@@ -738,6 +744,71 @@ extern "C" int lbdem_sync(lbdem_ctx* ctx) {
   return LBDEM_OK;
 }
 
+// Device bytes lbdem_create allocates for cfg, array by array as it does
+// (each allocation rounded up to the allocator's 512-byte granularity).
+extern "C" int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t precision,
+                                           int64_t* bytes) {
+  if (!cfg || !bytes || cfg->unitLength <= 0.0) return LBDEM_ERR_INVALID;
+  if (precision != LBDEM_PLAIN_FP64 && precision != LBDEM_MIXED) return LBDEM_ERR_INVALID;
+  const double L = cfg->unitLength;
+  const long long X = (long long)std::floor(cfg->lbSizeX / L + 0.5),
+                  Y = (long long)std::floor(cfg->lbSizeY / L + 0.5),
+                  Z = (long long)std::floor(cfg->lbSizeZ / L + 0.5);
+  if (X < 3 || Y < 3 || Z < 3) return LBDEM_ERR_INVALID;
+  const long long N = X * Y * Z, NP = (N + 255) / 256 * 256;
+  const long long P1 = std::max(cfg->n_particles, 1), O1 = std::max(cfg->n_objects, 1);
+  const bool mixed = precision == LBDEM_MIXED;
+  long long total = 0;
+  auto add = [&](long long n, long long elem) {
+    total += (std::max(n, 1LL) * elem + 511) / 512 * 512;
+  };
+  // lattice
+  add(NP, 1);                       // mask
+  add(NP, 4);                       // solid
+  add(N, 1);                        // objIdx
+  add(N, 4);                        // claim
+  add(N, 1);                        // fsflag
+  add((long long)Q * NP, mixed ? 4 : 8);
+  add((long long)Q * NP, mixed ? 4 : 8);
+  if (mixed) add(N, 4);             // nF
+  for (int i = 0; i < 3; ++i) add(N, 8);  // mass, massNew, rhoS
+  add(3 * N, 8);                    // uS
+  add(3 * N, 8);                    // hS
+  add(SC_COUNT, 8);
+  add(IS_COUNT, 4);
+  add(US_COUNT, 8);
+  // particles
+  for (int i = 0; i < 3; ++i) add(3 * P1, 8);  // x0, x1, w1
+  for (int i = 0; i < 3; ++i) add(P1, 8);      // r, invm, invI
+  add(6 * P1, 8);                              // pkd
+  if (mixed) {
+    add(9 * P1, 4);                            // pkf
+    add(ACCF_N * P1, 4);                       // pAccF
+    add(NP / 256, 4);                          // chunkAct
+  }
+  add(16 * P1, 8);                             // FHydro, MHydro, SHydro, fluidVolume
+  for (int i = 0; i < 10; ++i) add(3 * P1, 8); // contact .. xio
+  add(P1 * MAX_N, 4);
+  add(P1 * MAX_N, 4);                          // lists
+  add(P1 * 3 * MAX_N, 8);
+  add(P1 * 3 * MAX_N, 8);                      // tangential springs
+  add(P1 * MAX_N, 4);                          // partner
+  add(P1 * MAX_N, 4);                          // gorder
+  add(P1 * (MAX_N / 2), 4);                    // pairList
+  add(P1 * MAX_N * PAIR_VALS, 8);              // pairbuf
+  add(P1 * MAX_N, 1);                          // pairflag
+  add(P1, 4);
+  add(P1, 4);                                  // pcell, ppos
+  for (int i = 0; i < 3; ++i) add(MAX_L, 4);   // cell arrays
+  add(P1, 4);                                  // cellParts
+  add(O1 * OB_STRIDE, 8);
+  add(MAX_WALL * 12, 8);
+  add(MAX_WALL, (long long)sizeof(DeviceWall));
+  add(UNCOVER_CAP, 4);
+  *bytes = total;
+  return LBDEM_OK;
+}
+
 extern "C" int lbdem_get_info(lbdem_ctx* ctx, lbdem_info* info) {
   if (!ctx || !info) return LBDEM_ERR_INVALID;
   std::memset(info, 0, sizeof(*info));
@@ -889,17 +960,18 @@ extern "C" int lbdem_mass_summary(lbdem_ctx* ctx, double* total_mass,
   if (!ctx) return LBDEM_ERR_INVALID;
   int rc = lbdem_sync(ctx);
   if (rc) return rc;
+  // stream-ordered temporary: no device-wide synchronisation
   double* tmp = nullptr;
-  CK(cudaMalloc(&tmp, 3 * sizeof(double)));
-  CK(cudaMemset(tmp, 0, 3 * sizeof(double)));
+  CK(cudaMallocAsync(&tmp, 3 * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(tmp, 0, 3 * sizeof(double), ctx->stream));
   massSummaryKernel<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(
       ctx->k, ctx->d.mask, ctx->d.mass, ctx->d.nF, tmp, (unsigned long long*)(tmp + 1));
-  CK(cudaStreamSynchronize(ctx->stream));
   double m = 0;
   unsigned long long c[2] = {0, 0};
-  CK(cudaMemcpy(&m, tmp, 8, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(c, tmp + 1, 16, cudaMemcpyDeviceToHost));
-  cudaFree(tmp);
+  CK(cudaMemcpyAsync(&m, tmp, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(c, tmp + 1, 16, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaFreeAsync(tmp, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   if (total_mass) *total_mass = m;
   if (interface_nodes) *interface_nodes = (int64_t)c[0];
   if (active_nodes) *active_nodes = (int64_t)c[1];

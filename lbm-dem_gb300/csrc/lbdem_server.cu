@@ -1,0 +1,276 @@
+// Impact-run server: many independent runs resident on one GPU at once.
+//
+// Jobs (a configuration and a number of goCycles) queue in submission order
+// and are admitted while their device footprint (lbdem_estimate_device_bytes)
+// fits the memory budget and a run slot is free. Each admitted job is one
+// lbdem context with its own stream; the host advances every job by slices
+// of cycles, so the kernels of different runs overlap on the device, and a
+// job that ends frees its memory (stream-ordered, no device-wide wait) for
+// the next one in the queue. Results carry the submit, start and end times
+// for latency statistics.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "lbdem_internal.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Job {
+  int64_t id = 0;
+  lbdem_config cfg{};
+  std::vector<lbdem_particle_in> parts;
+  std::vector<lbdem_object_in> objs;
+  int32_t cycles = 0;
+  int32_t done = 0;
+  int64_t bytes = 0;
+  double submitTime = 0.0, startTime = 0.0;
+  lbdem_ctx* ctx = nullptr;
+  cudaEvent_t sliceDone = nullptr;
+  bool inFlight = false;
+  bool counted = false;  // its bytes are part of the server's memory in use
+};
+
+}  // namespace
+
+struct lbdem_server {
+  lbdem_server_options opt{};
+  std::string err;
+  Clock::time_point origin;
+  int64_t budget = 0, used = 0, nextId = 1;
+  std::deque<Job*> pending;
+  std::vector<Job*> active;
+  std::deque<lbdem_job_result> finished;
+  double now() const {
+    return std::chrono::duration<double>(Clock::now() - origin).count();
+  }
+};
+
+namespace {
+
+int serverErr(lbdem_server* s, int code, const std::string& msg) {
+  s->err = msg;
+  return code;
+}
+
+void releaseJob(lbdem_server* s, Job* j) {
+  if (j->sliceDone) cudaEventDestroy(j->sliceDone);
+  if (j->ctx) lbdem_destroy(j->ctx);
+  if (j->counted) s->used -= j->bytes;
+  delete j;
+}
+
+// End a job: its state after the last slice (or the failing status).
+void finishJob(lbdem_server* s, Job* j, int status) {
+  lbdem_job_result r;
+  std::memset(&r, 0, sizeof r);
+  r.job_id = j->id;
+  r.status = status;
+  r.cycles = j->done;
+  r.submit_time = j->submitTime;
+  r.start_time = j->startTime;
+  r.device_bytes = j->bytes;
+  if (status == LBDEM_OK && j->ctx) {
+    int rc = lbdem_sync(j->ctx);
+    if (rc == LBDEM_OK && j->cfg.n_objects > 0) {
+      std::vector<double> x0(3 * j->cfg.n_objects), x1(3 * j->cfg.n_objects);
+      lbdem_object_view v;
+      std::memset(&v, 0, sizeof v);
+      v.x0 = x0.data();
+      v.x1 = x1.data();
+      rc = lbdem_download_objects(j->ctx, &v);
+      for (int c = 0; c < 3; ++c) {
+        r.impactor_x0[c] = x0[c];
+        r.impactor_x1[c] = x1[c];
+      }
+    }
+    if (rc == LBDEM_OK) {
+      int64_t ni = 0, na = 0;
+      rc = lbdem_mass_summary(j->ctx, &r.fluid_mass, &ni, &na);
+    }
+    if (rc == LBDEM_OK) {
+      lbdem_profile p;
+      rc = lbdem_profile_read(j->ctx, &p, 0);
+      r.active_node_updates = p.active_node_updates;
+    }
+    r.status = rc;
+  }
+  r.end_time = s->now();
+  s->finished.push_back(r);
+  releaseJob(s, j);
+}
+
+// Admit queued jobs, in order, while memory and run slots allow.
+void admit(lbdem_server* s) {
+  while (!s->pending.empty() && (int)s->active.size() < s->opt.max_active) {
+    Job* j = s->pending.front();
+    if (s->used + j->bytes > s->budget && !s->active.empty()) break;
+    s->pending.pop_front();
+    lbdem_options o;
+    std::memset(&o, 0, sizeof o);
+    o.precision = s->opt.precision;
+    o.device = s->opt.device;
+    j->startTime = s->now();
+    int rc = lbdem_create(&j->cfg, &o, &j->ctx);
+    if (rc == LBDEM_OK && cudaEventCreateWithFlags(&j->sliceDone, cudaEventDisableTiming) !=
+                              cudaSuccess)
+      rc = LBDEM_ERR_CUDA;
+    if (rc != LBDEM_OK) {
+      finishJob(s, j, rc);
+      continue;
+    }
+    s->used += j->bytes;
+    j->counted = true;
+    s->active.push_back(j);
+  }
+}
+
+// One pass over the running jobs: finished slices are noticed, jobs that
+// reached their cycle count end, the others get their next slice. Returns
+// whether anything changed.
+bool progress(lbdem_server* s) {
+  bool changed = false;
+  for (size_t q = 0; q < s->active.size();) {
+    Job* j = s->active[q];
+    if (j->inFlight) {
+      const cudaError_t e = cudaEventQuery(j->sliceDone);
+      if (e == cudaErrorNotReady) {
+        ++q;
+        continue;
+      }
+      j->inFlight = false;
+      changed = true;
+      if (e != cudaSuccess) {
+        s->active.erase(s->active.begin() + q);
+        finishJob(s, j, LBDEM_ERR_CUDA);
+        continue;
+      }
+    }
+    if (j->done >= j->cycles) {
+      s->active.erase(s->active.begin() + q);
+      finishJob(s, j, LBDEM_OK);
+      changed = true;
+      continue;
+    }
+    const int32_t n = std::min(s->opt.slice_cycles, j->cycles - j->done);
+    int rc = lbdem_cycle(j->ctx, n);
+    if (rc == LBDEM_OK && cudaEventRecord(j->sliceDone, j->ctx->stream) != cudaSuccess)
+      rc = LBDEM_ERR_CUDA;
+    if (rc != LBDEM_OK) {
+      s->active.erase(s->active.begin() + q);
+      finishJob(s, j, rc);
+      changed = true;
+      continue;
+    }
+    j->done += n;
+    j->inFlight = true;
+    changed = true;
+    ++q;
+  }
+  return changed;
+}
+
+}  // namespace
+
+extern "C" int lbdem_server_create(const lbdem_server_options* opt, lbdem_server** out) {
+  if (!opt || !out) return LBDEM_ERR_INVALID;
+  *out = nullptr;
+  if (opt->precision != LBDEM_PLAIN_FP64 && opt->precision != LBDEM_MIXED)
+    return LBDEM_ERR_INVALID;
+  if (opt->max_active < 1 || opt->slice_cycles < 1) return LBDEM_ERR_INVALID;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return LBDEM_ERR_NO_DEVICE;
+  if (opt->device < 0 || opt->device >= ndev) return LBDEM_ERR_INVALID;
+  if (cudaSetDevice(opt->device) != cudaSuccess) return LBDEM_ERR_CUDA;
+  lbdem_server* s = new lbdem_server();
+  s->opt = *opt;
+  s->origin = Clock::now();
+  s->budget = opt->device_budget_bytes;
+  if (s->budget <= 0) {
+    size_t freeB = 0, totalB = 0;
+    if (cudaMemGetInfo(&freeB, &totalB) != cudaSuccess) {
+      delete s;
+      return LBDEM_ERR_CUDA;
+    }
+    s->budget = (int64_t)(0.9 * (double)freeB);
+  }
+  *out = s;
+  return LBDEM_OK;
+}
+
+extern "C" int lbdem_server_submit(lbdem_server* s, const lbdem_config* cfg, int32_t cycles,
+                                   int64_t* job_id) {
+  if (!s || !cfg || cycles < 0) return LBDEM_ERR_INVALID;
+  if (cfg->n_particles < 0 || (cfg->n_particles > 0 && !cfg->particles) ||
+      cfg->n_objects < 0 || (cfg->n_objects > 0 && !cfg->objects))
+    return serverErr(s, LBDEM_ERR_INVALID, "configuration tables missing");
+  int64_t bytes = 0;
+  int rc = lbdem_estimate_device_bytes(cfg, s->opt.precision, &bytes);
+  if (rc) return serverErr(s, rc, "cannot size the run's lattice");
+  if (bytes > s->budget)
+    return serverErr(s, LBDEM_ERR_OOM,
+                     "run needs " + std::to_string(bytes) + " device bytes, budget is " +
+                         std::to_string(s->budget));
+  Job* j = new Job();
+  j->id = s->nextId++;
+  j->cfg = *cfg;
+  j->parts.assign(cfg->particles, cfg->particles + cfg->n_particles);
+  j->objs.assign(cfg->objects, cfg->objects + cfg->n_objects);
+  j->cfg.particles = j->parts.empty() ? nullptr : j->parts.data();
+  j->cfg.objects = j->objs.empty() ? nullptr : j->objs.data();
+  j->cycles = cycles;
+  j->bytes = bytes;
+  j->submitTime = s->now();
+  s->pending.push_back(j);
+  if (job_id) *job_id = j->id;
+  return LBDEM_OK;
+}
+
+extern "C" int lbdem_server_poll(lbdem_server* s, double wait_seconds, lbdem_job_result* out,
+                                 int32_t max_out, int32_t* n_out) {
+  if (!s || (max_out > 0 && !out) || !n_out) return LBDEM_ERR_INVALID;
+  *n_out = 0;
+  if (cudaSetDevice(s->opt.device) != cudaSuccess) return LBDEM_ERR_CUDA;
+  const double until = s->now() + (wait_seconds > 0.0 ? wait_seconds : 0.0);
+  for (;;) {
+    admit(s);
+    const bool changed = progress(s);
+    if (!s->finished.empty() || (s->pending.empty() && s->active.empty()) || s->now() >= until)
+      break;
+    if (!changed) std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+  while (*n_out < max_out && !s->finished.empty()) {
+    out[(*n_out)++] = s->finished.front();
+    s->finished.pop_front();
+  }
+  return LBDEM_OK;
+}
+
+extern "C" int lbdem_server_status(const lbdem_server* s, int32_t* queued, int32_t* running,
+                                   int32_t* unread, int64_t* device_bytes_in_use) {
+  if (!s) return LBDEM_ERR_INVALID;
+  if (queued) *queued = (int32_t)s->pending.size();
+  if (running) *running = (int32_t)s->active.size();
+  if (unread) *unread = (int32_t)s->finished.size();
+  if (device_bytes_in_use) *device_bytes_in_use = s->used;
+  return LBDEM_OK;
+}
+
+extern "C" const char* lbdem_server_last_error(const lbdem_server* s) {
+  return s ? s->err.c_str() : "null server";
+}
+
+extern "C" void lbdem_server_destroy(lbdem_server* s) {
+  if (!s) return;
+  cudaSetDevice(s->opt.device);
+  for (Job* j : s->active) releaseJob(s, j);
+  for (Job* j : s->pending) delete j;
+  delete s;
+}

@@ -94,6 +94,20 @@ class Profile(C.Structure):
                 ("reserved", C.c_int64 * 4)]
 
 
+class ServerOptions(C.Structure):
+    _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("max_active", C.c_int32),
+                ("slice_cycles", C.c_int32), ("device_budget_bytes", C.c_int64),
+                ("reserved", C.c_int32 * 6)]
+
+
+class JobResult(C.Structure):
+    _fields_ = [("job_id", C.c_int64), ("status", C.c_int32), ("cycles", C.c_int32),
+                ("submit_time", C.c_double), ("start_time", C.c_double),
+                ("end_time", C.c_double), ("impactor_x0", C.c_double * 3),
+                ("impactor_x1", C.c_double * 3), ("fluid_mass", C.c_double),
+                ("active_node_updates", C.c_int64), ("device_bytes", C.c_int64)]
+
+
 _P = C.POINTER(C.c_double)
 _PI = C.POINTER(C.c_int32)
 
@@ -150,6 +164,17 @@ def load_library(path: str | None = None) -> C.CDLL:
                                 C.POINTER(C.c_int64)], C.c_int),
         "lbdem_profile_enable": ([c_ctx, C.c_int], C.c_int),
         "lbdem_profile_read": ([c_ctx, C.POINTER(Profile), C.c_int], C.c_int),
+        "lbdem_estimate_device_bytes": ([C.POINTER(Config), C.c_int32, C.POINTER(C.c_int64)],
+                                        C.c_int),
+        "lbdem_server_create": ([C.POINTER(ServerOptions), C.POINTER(C.c_void_p)], C.c_int),
+        "lbdem_server_submit": ([C.c_void_p, C.POINTER(Config), C.c_int32,
+                                 C.POINTER(C.c_int64)], C.c_int),
+        "lbdem_server_poll": ([C.c_void_p, C.c_double, C.POINTER(JobResult), C.c_int32,
+                               C.POINTER(C.c_int32)], C.c_int),
+        "lbdem_server_status": ([C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                 C.POINTER(C.c_int32), C.POINTER(C.c_int64)], C.c_int),
+        "lbdem_server_last_error": ([C.c_void_p], C.c_char_p),
+        "lbdem_server_destroy": ([C.c_void_p], None),
         "lbdem_download_nodes_noalloc": ([c_ctx, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p],
                                          C.c_int),
     }
@@ -350,3 +375,83 @@ class Solver:
             self.ctx, int(first), int(count), f.ctypes.data_as(C.c_void_p),
             mass.ctypes.data_as(C.c_void_p)), "download_nodes_noalloc")
         return f, mass
+
+
+def estimate_device_bytes(cfg: "LoadedConfig", precision: int = PLAIN_FP64) -> int:
+    """Device bytes a run of this configuration allocates (lbdem_create)."""
+    lib = load_library()
+    b = C.c_int64()
+    rc = lib.lbdem_estimate_device_bytes(C.byref(cfg.cfg), precision, C.byref(b))
+    if rc:
+        raise RuntimeError(f"lbdem_estimate_device_bytes: {ERRORS.get(rc, rc)}")
+    return b.value
+
+
+class Server:
+    """Many impact runs resident on one GPU (lbdem_server_*): jobs queue in
+    submission order, are admitted while their device footprint fits the
+    budget, and advance by slices of goCycles on their own streams."""
+
+    def __init__(self, precision=PLAIN_FP64, device=0, max_active=16, slice_cycles=25,
+                 device_budget_bytes=0):
+        self.lib = load_library()
+        o = ServerOptions(device=device, precision=precision, max_active=max_active,
+                          slice_cycles=slice_cycles, device_budget_bytes=device_budget_bytes)
+        h = C.c_void_p()
+        rc = self.lib.lbdem_server_create(C.byref(o), C.byref(h))
+        if rc:
+            raise RuntimeError(f"lbdem_server_create: {ERRORS.get(rc, rc)}")
+        self.h = h
+
+    def submit(self, cfg: "LoadedConfig", cycles: int) -> int:
+        jid = C.c_int64()
+        rc = self.lib.lbdem_server_submit(self.h, C.byref(cfg.cfg), int(cycles), C.byref(jid))
+        if rc:
+            raise RuntimeError(f"lbdem_server_submit: {ERRORS.get(rc, rc)}: "
+                               f"{self.lib.lbdem_server_last_error(self.h).decode()}")
+        return jid.value
+
+    def poll(self, wait_seconds: float = 0.0, max_out: int = 64) -> list:
+        buf = (JobResult * max_out)()
+        n = C.c_int32()
+        rc = self.lib.lbdem_server_poll(self.h, float(wait_seconds), buf, max_out, C.byref(n))
+        if rc:
+            raise RuntimeError(f"lbdem_server_poll: {ERRORS.get(rc, rc)}")
+        out = []
+        for r in buf[:n.value]:
+            out.append({"job_id": r.job_id, "status": r.status, "cycles": r.cycles,
+                        "submit_time": r.submit_time, "start_time": r.start_time,
+                        "end_time": r.end_time, "impactor_x0": list(r.impactor_x0),
+                        "impactor_x1": list(r.impactor_x1), "fluid_mass": r.fluid_mass,
+                        "active_node_updates": r.active_node_updates,
+                        "device_bytes": r.device_bytes})
+        return out
+
+    def status(self) -> dict:
+        q, r, u = C.c_int32(), C.c_int32(), C.c_int32()
+        b = C.c_int64()
+        self.lib.lbdem_server_status(self.h, C.byref(q), C.byref(r), C.byref(u), C.byref(b))
+        return {"queued": q.value, "running": r.value, "unread": u.value,
+                "device_bytes": b.value}
+
+    def drain(self, timeout: float = 600.0) -> list:
+        """Poll until every submitted job has finished."""
+        import time
+        res, t0 = [], time.perf_counter()
+        while time.perf_counter() - t0 < timeout:
+            res += self.poll(0.05)
+            st = self.status()
+            if st["queued"] == 0 and st["running"] == 0 and st["unread"] == 0:
+                return res
+        raise RuntimeError("server drain timed out")
+
+    def close(self):
+        if self.h:
+            self.lib.lbdem_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,113 @@
+"""The run server (lbdem_server_*): many impact runs resident on one GPU.
+
+Each run's result must be the same alone and in the mix:
+- plain FP64 form: the impactor state to 1e-10 relative, the tolerance of
+  the FP64 parity tests;
+- mixed form: the impactor displacement to 1e-3 relative, the mixed form's
+  stated tolerance.
+Admission follows the memory budget.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+CASES = ["small_cells", "tiny_direct", "small_dup"]
+CYCLES = 20
+
+
+def _cfg(name):
+    import lbdem
+    return lbdem.LoadedConfig(os.path.join(GOLDEN, name, "parameters.cfg"))
+
+
+def test_estimate_scales_with_lattice_and_form(lib):
+    import lbdem
+    small = _cfg("tiny_direct")
+    big = _cfg("c1")
+    for prec in (lbdem.MIXED, lbdem.PLAIN_FP64):
+        assert lbdem.estimate_device_bytes(big, prec) > lbdem.estimate_device_bytes(small, prec)
+    # the plain form keeps FP64 populations: more bytes per node
+    assert lbdem.estimate_device_bytes(big, lbdem.PLAIN_FP64) > \
+        lbdem.estimate_device_bytes(big, lbdem.MIXED)
+    small.close()
+    big.close()
+
+
+def _solo(name, precision):
+    import lbdem
+    cfg = _cfg(name)
+    s = lbdem.Solver(cfg, precision=precision)
+    x0 = np.array(s.objects()["o_x0"][0])
+    s.cycle(CYCLES)
+    o = s.objects()
+    out = x0, np.array(o["o_x0"][0]), np.array(o["o_x1"][0])
+    s.close()
+    cfg.close()
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec_name", ["fp64", "mixed"])
+def test_runs_in_the_mix_equal_runs_alone(prec_name, lib):
+    import lbdem
+    prec = lbdem.PLAIN_FP64 if prec_name == "fp64" else lbdem.MIXED
+    srv = lbdem.Server(precision=prec, max_active=len(CASES), slice_cycles=7)
+    cfgs = [_cfg(n) for n in CASES]
+    ids = {srv.submit(c, CYCLES): n for c, n in zip(cfgs, CASES)}
+    res = srv.drain()
+    srv.close()
+    for c in cfgs:
+        c.close()
+    assert len(res) == len(CASES)
+    # the runs overlapped: every run started before the first one ended
+    first_end = min(r["end_time"] for r in res)
+    assert all(r["start_time"] < first_end for r in res)
+    for r in res:
+        name = ids[r["job_id"]]
+        assert r["status"] == 0 and r["cycles"] == CYCLES, name
+        y0, x0, x1 = _solo(name, prec)
+        got0, got1 = np.array(r["impactor_x0"]), np.array(r["impactor_x1"])
+        if prec == lbdem.PLAIN_FP64:
+            np.testing.assert_allclose(got0, x0, rtol=1e-10, atol=0)
+            np.testing.assert_allclose(got1, x1, rtol=1e-10, atol=1e-300)
+        else:
+            disp, ref = got0 - y0, x0 - y0
+            err = np.max(np.abs(disp - ref)) / max(np.max(np.abs(ref)), 1e-12)
+            assert err <= 1e-3, f"{name}: impactor displacement rel err {err:.2e}"
+
+
+@pytest.mark.gpu
+def test_budget_admits_one_run_at_a_time(lib):
+    import lbdem
+    # three runs of one size and a budget that holds one of them, not two
+    cfgs = [_cfg("small_cells") for _ in range(3)]
+    need = lbdem.estimate_device_bytes(cfgs[0], lbdem.MIXED)
+    srv = lbdem.Server(precision=lbdem.MIXED, max_active=8, slice_cycles=5,
+                       device_budget_bytes=int(need * 1.5))
+    for c in cfgs:
+        srv.submit(c, 10)
+    res = sorted(srv.drain(), key=lambda r: r["job_id"])
+    srv.close()
+    for c in cfgs:
+        c.close()
+    assert [r["status"] for r in res] == [0, 0, 0]
+    # with room for one run, each starts after the previous one ended
+    for a, b in zip(res, res[1:]):
+        assert b["start_time"] >= a["end_time"]
+
+
+@pytest.mark.gpu
+def test_estimate_bounds_the_allocation(lib):
+    import lbdem
+    for name in ("tiny_direct", "c1"):
+        cfg = _cfg(name)
+        for prec in (lbdem.MIXED, lbdem.PLAIN_FP64):
+            est = lbdem.estimate_device_bytes(cfg, prec)
+            s = lbdem.Solver(cfg, precision=prec)
+            got = int(s.get_info().device_bytes)
+            s.close()
+            assert got <= est <= got + 64 * 1024, (name, prec, got, est)
+        cfg.close()
