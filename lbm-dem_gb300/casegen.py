@@ -230,6 +230,65 @@ def impact_case(lattice=(64, 80, 64), fill=60.0, n_particles=400,
     return Case(params=p, particles=parts, objects=objs, name=name)
 
 
+def grid_pack(rng: np.random.Generator, lo, hi, radii=(3.0, 4.2), phi=0.3,
+              gap: float = 0.05) -> np.ndarray:
+    """Spheres on a jittered cubic grid (vectorised, for many cases at once).
+
+    Cells of side 2 r_max + 2 gap tile [lo, hi]; a cell holds a sphere with
+    the probability that gives volume fraction ``phi`` (at most about 0.3
+    for radii 3.0/4.2), half of them of each radius, each moved at random
+    inside its cell by at most the slack its radius leaves, so no two
+    spheres overlap. Returns (n, 4) rows of r, x, y, z.
+    """
+    lo = np.asarray(lo, float)
+    hi = np.asarray(hi, float)
+    a = 2.0 * max(radii) + 2.0 * gap
+    n = np.maximum(np.floor((hi - lo) / a).astype(int), 0)
+    if np.any(n == 0):
+        return np.zeros((0, 4))
+    centres = np.stack(np.meshgrid(*[lo[d] + a * (np.arange(n[d]) + 0.5) for d in range(3)],
+                                   indexing="ij"), axis=-1).reshape(-1, 3)
+    r = rng.choice(np.asarray(radii, float), size=len(centres))
+    vol_box = float(np.prod(hi - lo))
+    p = min(1.0, phi * vol_box / float(np.sum(4.0 / 3.0 * math.pi * r ** 3)))
+    keep = rng.random(len(centres)) < p
+    centres, r = centres[keep], r[keep]
+    slack = (a - 2.0 * r - 2.0 * gap)[:, None] / 2.0
+    pos = centres + slack * (2.0 * rng.random((len(r), 3)) - 1.0)
+    return np.column_stack([r, pos])
+
+
+def serving_case(rng: np.random.Generator, name: str = "job") -> Case:
+    """One impact run of a varied job stream: lattice sides 48-128 (vertical
+    up to 160), fluid to 60 % of the height, a grid-packed bidisperse
+    suspension (phi 0.25-0.30), an impactor of radius 6-16 (at most what the
+    gas layer holds) falling at 0.005-0.05 just above the surface."""
+    nx, nz = (int(v) for v in rng.integers(48, 129, size=2))
+    ny = int(rng.integers(48, 161))
+    fill = 0.6 * ny
+    r_imp = float(min(rng.uniform(6.0, 16.0), (ny - 2.0 - fill) / 2.0 - 1.0, (nx - 4) / 2.0,
+                      (nz - 4) / 2.0))
+    vy = -float(rng.uniform(0.005, 0.05))
+    p = dict(DEFAULT_PARAMS)
+    tau = 0.6
+    p.update({
+        "lbSizeX": str(nx), "lbSizeY": str(ny), "lbSizeZ": str(nz),
+        "fluidHeight": repr(float(fill)), "initVisc": repr((tau - 0.5) / 3.0),
+        "kinVisc": repr((tau - 0.5) / 3.0), "lbFY": repr(-1.0e-5),
+        "objectDensity": "5.0",
+    })
+    amean = 3.6
+    p["lubNormal"] = p["lubTangential"] = p["lubRotation"] = repr(0.5 * amean)
+    p["debyeLength"] = repr(0.05 * amean)
+    p["lubCutoff"] = repr(0.1 * amean)
+    pk = grid_pack(rng, (0.5, 0.5, 0.5), (nx - 1.5, fill, nz - 1.5),
+                   phi=float(rng.uniform(0.25, 0.30)))
+    parts = np.zeros((len(pk), 10))
+    parts[:, :4] = pk[rng.permutation(len(pk))]
+    objs = np.array([[r_imp, 0.5 * (nx - 1), fill + r_imp + 1.0, 0.5 * (nz - 1), 0.0, vy, 0.0]])
+    return Case(params=p, particles=parts, objects=objs, name=name)
+
+
 def volume_fraction(case: Case) -> float:
     nx, ny, nz = case.lattice
     fill = float(case.params["fluidHeight"])

@@ -63,6 +63,7 @@ __global__ void __launch_bounds__(256) demBegin(Consts k, DemArgs a, int forceRe
     __threadfence();
     double mv = __longlong_as_double((long long)atomicExch(a.uscal + US_MAXV2, 0ull));
     a.iscal[IS_BLOCKS_DONE] = 0;
+    if (!forceRebuild) a.iscal[IS_DEMSTEP] += 1;  // ++demTimeStep (src/DEM.cpp:364)
     bool rebuild = forceRebuild != 0;
     if (!forceRebuild) {
       mv = sqrt(mv);
@@ -605,7 +606,9 @@ __device__ __forceinline__ void load3(const double* a, int P, int i, double* v) 
 
 // Owner pass: every pair (n1 > n2) evaluated once from n1's slot, one
 // thread per entry of the owner-pair list.
-__global__ void demPairs(Consts k, DemArgs a, int lubOn) {
+__global__ void demPairs(Consts k, DemArgs a) {
+  // lubrication only after objWaitTime (src/DEM.cpp:716-725)
+  const bool lubOn = a.iscal[IS_DEMSTEP] >= k.objWaitTime;
   const int cur = a.iscal[IS_LISTCUR];
   const int* L = a.list[cur];
   double* XI = a.xi[cur];
@@ -850,7 +853,8 @@ __device__ __forceinline__ void sub3(double* a, const double* b) {
 // per-block shared accumulators for the impactor and wall sums
 enum { GA_OBJ = 0, GA_WALL = GA_OBJ + 12 * MAX_OBJ, GA_N = GA_WALL + 6 * MAX_WALL };
 
-__global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a, int stepNo) {
+__global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a) {
+  const int stepNo = a.iscal[IS_DEMSTEP];
   __shared__ double acc[GA_N];
   for (int t = threadIdx.x; t < GA_N; t += blockDim.x) acc[t] = 0.0;
   __syncthreads();
@@ -1027,7 +1031,8 @@ __global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a, int stepNo
 }
 
 // Impactor totals and integration, wall totals (src/DEM.cpp:773-790, 2742-2760).
-__global__ void demObjects(Consts k, DemArgs a, int stepNo) {
+__global__ void demObjects(Consts k, DemArgs a) {
+  const int stepNo = a.iscal[IS_DEMSTEP];
   const int o = threadIdx.x;
   if (o < k.nObj) {
     double* ob = a.obj + o * OB_STRIDE;

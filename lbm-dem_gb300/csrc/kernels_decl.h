@@ -150,8 +150,9 @@ __global__ void nbrDirectHistory(Consts k, DemArgs a);
 __global__ void nbrPartners(Consts k, DemArgs a);
 __global__ void nbrPairList(Consts k, DemArgs a);
 __global__ void nbrFinish(DemArgs a);
-__global__ void demPairs(Consts k, DemArgs a, int lubOn);
-__global__ void demGather(Consts k, DemArgs a, int stepNo);
-__global__ void demObjects(Consts k, DemArgs a, int stepNo);
+// the DEM step number comes from iscal[IS_DEMSTEP] (advanced by demBegin)
+__global__ void demPairs(Consts k, DemArgs a);
+__global__ void demGather(Consts k, DemArgs a);
+__global__ void demObjects(Consts k, DemArgs a);
 
 }  // namespace lbdem

@@ -146,6 +146,7 @@ enum {
   IS_REBUILDS,              // rebuild counter
   IS_NPAIRS,                // entries of the owner-pair list
   IS_BLOCKS_DONE,           // demBegin: blocks that have posted their maximum
+  IS_DEMSTEP,               // DEM::demTimeStep, advanced by demBegin
   IS_COUNT
 };
 // offsets into Device::uscal
@@ -190,4 +191,7 @@ struct lbdem_ctx {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> lbEvents;
   size_t lbEventsUsed = 0;
   long long launches = 0;
+  // two goCycles as one CUDA graph, per starting lattice buffer
+  cudaGraphExec_t pairGraph[2] = {nullptr, nullptr};
+  long long pairKernels = 0;
 };
