@@ -287,10 +287,57 @@ def run_ours(args, world, rank, local):
                      "kernel_ms_per_launch": round(prof.lb_kernel_ms / max(prof.lb_kernel_launches, 1), 4)},
         "cpu_baseline": cb,
         "serving": None if (args.no_serving or world > 1) else serving(args),
+        "accuracy": None if (args.no_accuracy or world > 1) else accuracy(args, cfg),
         "clocks": clk,
         "gpu_launches": int(timed.kernel_launches),
     }
     print(json.dumps(line), flush=True)
+
+
+def accuracy(args, cfg) -> dict:
+    """The mixed form against the plain FP64 form on the benchmark workload.
+
+    Both run ``--accuracy-steps`` goCycles side by side. Reported:
+    - the impactor trajectory error (largest difference of the vertical
+      displacement, relative to the largest FP64 displacement);
+    - the maximum penetration fluidHeight + r - y of each form;
+    - each form's fluid-mass drift over the run.
+    """
+    import lbdem
+    import numpy as np
+    S, blk = args.accuracy_steps, 25
+    runs = {p: lbdem.Solver(cfg, precision=p) for p in (lbdem.MIXED, lbdem.PLAIN_FP64)}
+    fill = float(cfg.cfg.fluidHeight)
+    r0 = float(cfg.cfg.objects[0].r) if cfg.cfg.n_objects else 0.0
+    traj = {p: [] for p in runs}
+    mass = {p: [] for p in runs}
+    for p, sv in runs.items():
+        traj[p].append(float(sv.objects()["o_x0"][0][1]))
+        mass[p].append(sv.mass_total())
+    done = 0
+    while done < S:
+        n = min(blk, S - done)
+        for p, sv in runs.items():
+            sv.cycle(n)
+        for p, sv in runs.items():
+            traj[p].append(float(sv.objects()["o_x0"][0][1]))
+            mass[p].append(sv.mass_total())
+        done += n
+    for sv in runs.values():
+        sv.close()
+    ym, yf = np.array(traj[lbdem.MIXED]), np.array(traj[lbdem.PLAIN_FP64])
+    dm, df = ym - ym[0], yf - yf[0]
+    pen = {p: float(np.max(fill + r0 - np.array(traj[p]))) for p in runs}
+    drift = {p: float((mass[p][-1] - mass[p][0]) / mass[p][0]) for p in runs}
+    return {
+        "steps": S, "reference": "plain FP64 form (GPU), same workload and steps",
+        "impactor_traj_rel_err": float(np.max(np.abs(dm - df)) / max(np.max(np.abs(df)), 1e-300)),
+        "impactor_displacement_fp64": float(df[-1]),
+        "max_penetration": {"mixed": pen[lbdem.MIXED], "fp64": pen[lbdem.PLAIN_FP64]},
+        "max_penetration_rel_err": abs(pen[lbdem.MIXED] - pen[lbdem.PLAIN_FP64]) /
+                                   max(abs(pen[lbdem.PLAIN_FP64]), 1e-300),
+        "mass_drift": {"mixed": drift[lbdem.MIXED], "fp64": drift[lbdem.PLAIN_FP64]},
+    }
 
 
 def serving(args) -> dict:
@@ -390,6 +437,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--accuracy-steps", type=int, default=300)
     ap.add_argument("--serve-jobs", type=int, default=24)
     ap.add_argument("--serve-fp64-jobs", type=int, default=8)
     ap.add_argument("--serve-cycles", type=int, default=200)

@@ -251,6 +251,9 @@ int lbdem_download_walls(lbdem_ctx* ctx, double* FHydro, double* FContact,
  * count (device reductions). */
 int lbdem_mass_summary(lbdem_ctx* ctx, double* total_mass,
                        int64_t* interface_nodes, int64_t* active_nodes);
+/* Total mass of every active node, those inside particles included (the
+ * conserved quantity of the free-surface mass budget). */
+int lbdem_mass_total(lbdem_ctx* ctx, double* total_mass);
 
 /* ---- measurement (no counterpart in the reference) --------------------- */
 

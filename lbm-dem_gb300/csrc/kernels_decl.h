@@ -130,8 +130,10 @@ __global__ void initTypes(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* obj
                           const int* boundary, const DeviceWall* walls, const int* wallType,
                           const double* obj, double fluidHeightLattice, int freeSurface);
 __global__ void initFields(Consts k, uint8_t* mask, void* f, double* mass, float* nF);
+// mass of the active nodes (outside particles unless withParticles), counts
 __global__ void massSummaryKernel(Consts k, const uint8_t* mask, const double* mass,
-                                  const float* nF, double* out, unsigned long long* cnt);
+                                  const float* nF, double* out, unsigned long long* cnt,
+                                  int withParticles);
 __global__ void momentsKernel(Consts k, const uint8_t* mask, const void* f, double* n,
                               double* u);
 __global__ void nonfiniteCheck(Consts k, const uint8_t* mask, const void* f, int* iscal);

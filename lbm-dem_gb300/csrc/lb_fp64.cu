@@ -966,7 +966,8 @@ __global__ void initFields(Consts k, uint8_t* mask, void* f, double* mass, float
 // ---- diagnostics --------------------------------------------------------------
 
 __global__ void massSummaryKernel(Consts k, const uint8_t* mask, const double* mass,
-                                  const float* nF, double* out, unsigned long long* cnt) {
+                                  const float* nF, double* out, unsigned long long* cnt,
+                                  int withParticles) {
   double s = 0.0;
   unsigned long long ni = 0, na = 0;
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
@@ -976,7 +977,7 @@ __global__ void massSummaryKernel(Consts k, const uint8_t* mask, const double* m
     if (isActiveT(t)) {
       ++na;
       if (t == 3) ++ni;
-      if (!(m & PFLAG)) s += (k.mixed && t == 0) ? (double)nF[x] : mass[x];
+      if (withParticles || !(m & PFLAG)) s += (k.mixed && t == 0) ? (double)nF[x] : mass[x];
     }
   }
   blockAddDouble(s, out);

@@ -1028,8 +1028,9 @@ extern "C" int lbdem_download_walls(lbdem_ctx* ctx, double* FHydro, double* FCon
   return LBDEM_OK;
 }
 
-extern "C" int lbdem_mass_summary(lbdem_ctx* ctx, double* total_mass,
-                                  int64_t* interface_nodes, int64_t* active_nodes) {
+namespace {
+int massSums(lbdem_ctx* ctx, int withParticles, double* total_mass, int64_t* interface_nodes,
+             int64_t* active_nodes) {
   if (!ctx) return LBDEM_ERR_INVALID;
   int rc = lbdem_sync(ctx);
   if (rc) return rc;
@@ -1038,7 +1039,7 @@ extern "C" int lbdem_mass_summary(lbdem_ctx* ctx, double* total_mass,
   CK(cudaMallocAsync(&tmp, 3 * sizeof(double), ctx->stream));
   CK(cudaMemsetAsync(tmp, 0, 3 * sizeof(double), ctx->stream));
   massSummaryKernel<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(
-      ctx->k, ctx->d.mask, ctx->d.mass, ctx->d.nF, tmp, (unsigned long long*)(tmp + 1));
+      ctx->k, ctx->d.mask, ctx->d.mass, ctx->d.nF, tmp, (unsigned long long*)(tmp + 1), withParticles);
   double m = 0;
   unsigned long long c[2] = {0, 0};
   CK(cudaMemcpyAsync(&m, tmp, 8, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1049,4 +1050,14 @@ extern "C" int lbdem_mass_summary(lbdem_ctx* ctx, double* total_mass,
   if (interface_nodes) *interface_nodes = (int64_t)c[0];
   if (active_nodes) *active_nodes = (int64_t)c[1];
   return LBDEM_OK;
+}
+}  // namespace
+
+extern "C" int lbdem_mass_summary(lbdem_ctx* ctx, double* total_mass,
+                                  int64_t* interface_nodes, int64_t* active_nodes) {
+  return massSums(ctx, 0, total_mass, interface_nodes, active_nodes);
+}
+
+extern "C" int lbdem_mass_total(lbdem_ctx* ctx, double* total_mass) {
+  return massSums(ctx, 1, total_mass, nullptr, nullptr);
 }

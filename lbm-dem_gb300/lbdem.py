@@ -162,6 +162,7 @@ def load_library(path: str | None = None) -> C.CDLL:
                                  C.c_int),
         "lbdem_mass_summary": ([c_ctx, C.POINTER(C.c_double), C.POINTER(C.c_int64),
                                 C.POINTER(C.c_int64)], C.c_int),
+        "lbdem_mass_total": ([c_ctx, C.POINTER(C.c_double)], C.c_int),
         "lbdem_profile_enable": ([c_ctx, C.c_int], C.c_int),
         "lbdem_profile_read": ([c_ctx, C.POINTER(Profile), C.c_int], C.c_int),
         "lbdem_estimate_device_bytes": ([C.POINTER(Config), C.c_int32, C.POINTER(C.c_int64)],
@@ -364,6 +365,12 @@ class Solver:
         self._check(self.lib.lbdem_mass_summary(self.ctx, C.byref(m), C.byref(ni), C.byref(na)),
                     "mass_summary")
         return m.value, ni.value, na.value
+
+    def mass_total(self) -> float:
+        """Mass of every active node, those inside particles included."""
+        m = C.c_double()
+        self._check(self.lib.lbdem_mass_total(self.ctx, C.byref(m)), "mass_total")
+        return m.value
 
     def nodes_noalloc(self, first: int, count: int):
         """Populations [19, count] and masses [count] of nodes first ..
