@@ -382,9 +382,12 @@ def serving(args) -> dict:
             raise RuntimeError(f"serving run failed: status {bad[0]['status']}")
         lat = [r["end_time"] - r["submit_time"] for r in res]
         upd = sum(r["active_node_updates"] for r in res)
+        starts = [r["start_time"] for r in res]
         return {"jobs": len(jobs), "jobs_per_hour": round(len(jobs) / wall * 3600.0, 1),
                 "makespan_s": round(wall, 3), "coupled_mlups": round(upd / wall / 1e6, 1),
-                "p50_s": round(pct(lat, 50), 4), "p99_s": round(pct(lat, 99), 4)}
+                "p50_s": round(pct(lat, 50), 4), "p99_s": round(pct(lat, 99), 4),
+                "admission_span_s": round(max(starts) - min(starts), 4),
+                "run_p50_s": round(pct([r["end_time"] - r["start_time"] for r in res], 50), 4)}
 
     batch(lbdem.MIXED, cfgs[:2])  # warm-up (module load, allocator pools)
     mixed = batch(lbdem.MIXED, cfgs)

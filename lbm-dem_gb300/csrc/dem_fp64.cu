@@ -407,11 +407,15 @@ __global__ void nbrPairList(Consts k, DemArgs a) {
     if (pos < cap) a.pairList[pos] = (int)idx;
     else atomicOr(a.iscal + IS_ERROR, ERR_NBR_OVERFLOW);
   }
-}
-
-__global__ void nbrFinish(DemArgs a) {
-  if (!a.iscal[IS_REBUILD]) return;
-  a.iscal[IS_LISTCUR] = 1 - a.iscal[IS_LISTCUR];
+  // the last block to finish makes the new lists current
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(a.iscal + IS_PAIRLIST_DONE, 1) == (int)gridDim.x - 1) {
+      a.iscal[IS_PAIRLIST_DONE] = 0;
+      a.iscal[IS_LISTCUR] = 1 - a.iscal[IS_LISTCUR];
+    }
+  }
 }
 
 // ---- pair forces (owner pass) ------------------------------------------------
@@ -853,6 +857,37 @@ __device__ __forceinline__ void sub3(double* a, const double* b) {
 // per-block shared accumulators for the impactor and wall sums
 enum { GA_OBJ = 0, GA_WALL = GA_OBJ + 12 * MAX_OBJ, GA_N = GA_WALL + 6 * MAX_WALL };
 
+// Impactor totals and integration, wall totals (src/DEM.cpp:773-790,
+// 2742-2760), by the last block of demGather once every block's impactor
+// and wall sums are in.
+__device__ void demObjectsTail(const Consts& k, DemArgs& a) {
+  const int stepNo = a.iscal[IS_DEMSTEP];
+  const int o = threadIdx.x;
+  // volatile: the sums other blocks added must not come from a line this
+  // block's L1 cached earlier in the kernel
+  if (o < k.nObj) {
+    volatile double* ob = a.obj + o * OB_STRIDE;
+    const double dtt = k.dt;
+    for (int c = 0; c < 3; ++c) {
+      ob[OB_FTOTAL + c] =
+          0.0 + ((((ob[OB_FHYDRO + c] + ob[OB_FCONTACT + c]) + ob[OB_FLUB + c]) + ob[OB_FGRAV + c]) +
+                 0.0);
+      ob[OB_MTOTAL + c] = 0.0 + ((ob[OB_MHYDRO + c] + ob[OB_MCONTACT + c]) + ob[OB_MLUB + c]);
+    }
+    if (stepNo >= k.objWaitTime)
+      for (int c = 0; c < 3; ++c) {
+        const double x1 = ob[OB_X1 + c];
+        ob[OB_X0 + c] += dtt * x1 + dtt * dtt * ob[OB_FTOTAL + c] * ob[OB_INVM];
+        ob[OB_X1 + c] = x1 + dtt * ob[OB_FTOTAL + c] * ob[OB_INVM];
+        ob[OB_W1 + c] += dtt * ob[OB_MTOTAL + c] * ob[OB_INVI];
+      }
+  }
+  if (o < k.nWall) {
+    volatile double* w = a.wallF + o * 12;
+    for (int c = 0; c < 3; ++c) w[9 + c] = 0.0 + (((w[c] + w[3 + c]) + w[6 + c]) + 0.0);
+  }
+}
+
 __global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a) {
   const int stepNo = a.iscal[IS_DEMSTEP];
   __shared__ double acc[GA_N];
@@ -1028,33 +1063,19 @@ __global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a) {
       atomicAdd(a.wallF + w * 12 + (c < 3 ? 3 + c : 6 + c - 3), v);
     }
   }
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(a.iscal + IS_GATHER_DONE, 1) == (int)gridDim.x - 1;
+    if (last) a.iscal[IS_GATHER_DONE] = 0;
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    demObjectsTail(k, a);
+  }
 }
 
-// Impactor totals and integration, wall totals (src/DEM.cpp:773-790, 2742-2760).
-__global__ void demObjects(Consts k, DemArgs a) {
-  const int stepNo = a.iscal[IS_DEMSTEP];
-  const int o = threadIdx.x;
-  if (o < k.nObj) {
-    double* ob = a.obj + o * OB_STRIDE;
-    const double dtt = k.dt;
-    for (int c = 0; c < 3; ++c) {
-      ob[OB_FTOTAL + c] =
-          0.0 + ((((ob[OB_FHYDRO + c] + ob[OB_FCONTACT + c]) + ob[OB_FLUB + c]) + ob[OB_FGRAV + c]) +
-                 0.0);
-      ob[OB_MTOTAL + c] = 0.0 + ((ob[OB_MHYDRO + c] + ob[OB_MCONTACT + c]) + ob[OB_MLUB + c]);
-    }
-    if (stepNo >= k.objWaitTime)
-      for (int c = 0; c < 3; ++c) {
-        const double x1 = ob[OB_X1 + c];
-        ob[OB_X0 + c] += dtt * x1 + dtt * dtt * ob[OB_FTOTAL + c] * ob[OB_INVM];
-        ob[OB_X1 + c] = x1 + dtt * ob[OB_FTOTAL + c] * ob[OB_INVM];
-        ob[OB_W1 + c] += dtt * ob[OB_MTOTAL + c] * ob[OB_INVI];
-      }
-  }
-  if (o < k.nWall) {
-    double* w = a.wallF + o * 12;
-    for (int c = 0; c < 3; ++c) w[9 + c] = 0.0 + (((w[c] + w[3 + c]) + w[6 + c]) + 0.0);
-  }
-}
 
 }  // namespace lbdem

@@ -97,22 +97,19 @@ constexpr int MIXED_MAX_MINE = 2048;
 __global__ void lbStepFp64(Consts k, LbArgs a);
 __global__ void lbStepMixed(Consts k, LbArgs a);
 __global__ void lbWallForceMixed(Consts k, LbArgs a);
-__global__ void particleKinematics(Consts k, const double* px0, const double* px1,
-                                   const double* pw1, double* pkd, float* pkf);
-__global__ void lbResetKernel(Consts k, double* pAcc, long long pAccLen, double* obj,
-                              double* wallF, double* scal, int* iscal);
+__global__ void lbPrepare(Consts k, double* pAcc, long long pAccLen, float* pAccF,
+                          long long pAccFLen, double* obj, double* wallF, double* scal,
+                          int* iscal, const double* px0, const double* px1, const double* pw1,
+                          double* pkd, float* pkf);
 __global__ void lbFinalizeKernel(Consts k, double* pF, double* pM, double* pV, double* obj,
                                  double* wallF, double* scal, const int* iscal,
-                                 const float* pAccF, double* pS);
-__global__ void fsResetKernel(double* scal, int* iscal);
-__global__ void lbRedistribute(Consts k, FsArgs a);
+                                 const float* pAccF, double* pS, FsArgs fa, int redistribute);
 __global__ void fsUpdateMass(Consts k, FsArgs a);
 __global__ void fsMutants(Consts k, FsArgs a);
 __global__ void fsSmoothen(Consts k, FsArgs a);
 __global__ void fsMutantsAndFill(Consts k, FsArgs a);
 __global__ void fsEmptyIsolated(Consts k, FsArgs a);
 __global__ void fsRedistribute(Consts k, FsArgs a);
-__global__ void fsClearBulk(Consts k, uint8_t* mask, const int* iscal);
 __global__ void uncoverCollect(Consts k, const uint8_t* mask, const double* obj,
                                uint32_t* list, int* iscal);
 __global__ void uncoverResolve(Consts k, uint8_t* mask, void* f, double* mass, float* nF,
@@ -151,10 +148,8 @@ __global__ void nbrBuildDirect(Consts k, DemArgs a);
 __global__ void nbrDirectHistory(Consts k, DemArgs a);
 __global__ void nbrPartners(Consts k, DemArgs a);
 __global__ void nbrPairList(Consts k, DemArgs a);
-__global__ void nbrFinish(DemArgs a);
 // the DEM step number comes from iscal[IS_DEMSTEP] (advanced by demBegin)
 __global__ void demPairs(Consts k, DemArgs a);
 __global__ void demGather(Consts k, DemArgs a);
-__global__ void demObjects(Consts k, DemArgs a);
 
 }  // namespace lbdem

@@ -219,14 +219,22 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
   }
 }
 
-// Particle kinematics in lattice units, once per LB step: x0/unit.Length and
-// x1/unit.Speed in double (the exact path divides them at every node of the
-// particle in the reference; the quotients are identical), and x0/L, x1/S,
-// w1/unit.AngVel in float for the mixed form.
-__global__ void particleKinematics(Consts k, const double* px0, const double* px1,
-                                   const double* pw1, double* pkd, float* pkf) {
+// Start of the LB step: the per-step reductions are cleared (particle
+// sums, the float sums of the mixed form, impactor and wall hydrodynamic
+// forces, extra mass, interface count and box) and the particle kinematics
+// in lattice units are formed once per particle (x0/L, x1/S, w1/W: the
+// quotients the reference forms at every node).
+__global__ void lbPrepare(Consts k, double* pAcc, long long pAccLen, float* pAccF,
+                          long long pAccFLen, double* obj, double* wallF, double* scal,
+                          int* iscal, const double* px0, const double* px1, const double* pw1,
+                          double* pkd, float* pkf) {
+  const long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = i0; i < pAccLen; i += stride) pAcc[i] = 0.0;
+  if (pAccF)
+    for (long long i = i0; i < pAccFLen; i += stride) pAccF[i] = 0.0f;
   const int P = k.nPart;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * P; i += gridDim.x * blockDim.x) {
+  for (long long i = i0; i < 3LL * P; i += stride) {
     const double xl = px0[i] / k.uLength, vl = px1[i] / k.uSpeed;
     pkd[i] = xl;
     pkd[3 * P + i] = vl;
@@ -236,13 +244,6 @@ __global__ void particleKinematics(Consts k, const double* px0, const double* px
       pkf[6 * P + i] = (float)(pw1[i] / k.uAngVel);
     }
   }
-}
-
-// Reset of the per-step LB reductions (before lbStepFp64).
-__global__ void lbResetKernel(Consts k, double* pAcc, long long pAccLen, double* obj,
-                              double* wallF, double* scal, int* iscal) {
-  const long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  for (long long i = i0; i < pAccLen; i += (long long)gridDim.x * blockDim.x) pAcc[i] = 0.0;
   if (i0 < k.nObj) {
     for (int c = 0; c < 3; ++c) {
       obj[i0 * OB_STRIDE + OB_FHYDRO + c] = 0.0;
@@ -259,11 +260,37 @@ __global__ void lbResetKernel(Consts k, double* pAcc, long long pAccLen, double*
   }
 }
 
+__device__ __forceinline__ bool fsRegion(const Consts& k, const int* iscal, int& x0, int& y0,
+                                         int& z0, int& rx, int& ry, int& rz) {
+  if (iscal[IS_BBOX + 3] < 0) return false;
+  x0 = max(iscal[IS_BBOX + 0] - 1, 0);
+  y0 = max(iscal[IS_BBOX + 1] - 1, 0);
+  z0 = max(iscal[IS_BBOX + 2] - 1, 0);
+  rx = min(iscal[IS_BBOX + 3] + 1, k.X - 1) - x0 + 1;
+  ry = min(iscal[IS_BBOX + 4] + 1, k.Y - 1) - y0 + 1;
+  rz = min(iscal[IS_BBOX + 5] + 1, k.Z - 1) - z0 + 1;
+  return true;
+}
+
+#define FS_LOOP(k, a, ...)                                                               \
+  int _x0, _y0, _z0, _rx, _ry, _rz;                                                      \
+  if (fsRegion(k, a.iscal, _x0, _y0, _z0, _rx, _ry, _rz)) {                              \
+    const long long _vol = (long long)_rx * _ry * _rz;                                   \
+    for (long long _i = blockIdx.x * (long long)blockDim.x + threadIdx.x; _i < _vol;     \
+         _i += (long long)gridDim.x * blockDim.x) {                                      \
+      const int ix = _x0 + (int)(_i % _rx);                                              \
+      const int iy = _y0 + (int)((_i / _rx) % _ry);                                      \
+      const int iz = _z0 + (int)(_i / ((long long)_rx * _ry));                           \
+      const long long x = ix + iy * k.sy + iz * k.sz;                                    \
+      __VA_ARGS__                                                                        \
+    }                                                                                    \
+  }
+
 // Unit conversions at the end of LB::streaming / computeHydroForces and the
 // mass-redistribution amount (src/LB.cpp:1533-1543, 1966-1977, 1844-1847).
 __global__ void lbFinalizeKernel(Consts k, double* pF, double* pM, double* pV, double* obj,
                                  double* wallF, double* scal, const int* iscal,
-                                 const float* pAccF, double* pS) {
+                                 const float* pAccF, double* pS, FsArgs fa, int redistribute) {
   const int P = k.nPart;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
     if (pAccF) {
@@ -296,6 +323,18 @@ __global__ void lbFinalizeKernel(Consts k, double* pF, double* pM, double* pV, d
       }
     scal[SC_ADD_MASS] = scal[SC_EXTRA_MASS] / (double)(unsigned)iscal[IS_NIF];
   }
+  if (redistribute) {
+    // LB::redistributeMass(extraMass) over the interface nodes; every thread
+    // forms the same quotient block 0 stores above
+    const double addMass = scal[SC_EXTRA_MASS] / (double)(unsigned)iscal[IS_NIF];
+    FS_LOOP(k, fa, {
+      if ((fa.mask[x] & TYPE_MASK) == 3) {
+        // the mass the collision used, for fsUpdateMass's recomputation
+        fa.massNew[x] = fa.mass[x];
+        fa.mass[x] += addMass;
+      }
+    })
+  }
 }
 
 // ---- free surface ----------------------------------------------------------
@@ -304,32 +343,6 @@ __global__ void lbFinalizeKernel(Consts k, double* pF, double* pM, double* pV, d
 enum : uint8_t { FS_FILLED = 1, FS_EMPTIED = 2, FS_NEW = 4 };
 
 // Region = interface bounding box of the LB step grown by one node.
-__device__ __forceinline__ bool fsRegion(const Consts& k, const int* iscal, int& x0, int& y0,
-                                         int& z0, int& rx, int& ry, int& rz) {
-  if (iscal[IS_BBOX + 3] < 0) return false;
-  x0 = max(iscal[IS_BBOX + 0] - 1, 0);
-  y0 = max(iscal[IS_BBOX + 1] - 1, 0);
-  z0 = max(iscal[IS_BBOX + 2] - 1, 0);
-  rx = min(iscal[IS_BBOX + 3] + 1, k.X - 1) - x0 + 1;
-  ry = min(iscal[IS_BBOX + 4] + 1, k.Y - 1) - y0 + 1;
-  rz = min(iscal[IS_BBOX + 5] + 1, k.Z - 1) - z0 + 1;
-  return true;
-}
-
-#define FS_LOOP(k, a, ...)                                                               \
-  int _x0, _y0, _z0, _rx, _ry, _rz;                                                      \
-  if (fsRegion(k, a.iscal, _x0, _y0, _z0, _rx, _ry, _rz)) {                              \
-    const long long _vol = (long long)_rx * _ry * _rz;                                   \
-    for (long long _i = blockIdx.x * (long long)blockDim.x + threadIdx.x; _i < _vol;     \
-         _i += (long long)gridDim.x * blockDim.x) {                                      \
-      const int ix = _x0 + (int)(_i % _rx);                                              \
-      const int iy = _y0 + (int)((_i / _rx) % _ry);                                      \
-      const int iz = _z0 + (int)(_i / ((long long)_rx * _ry));                           \
-      const long long x = ix + iy * k.sy + iz * k.sz;                                    \
-      __VA_ARGS__                                                                        \
-    }                                                                                    \
-  }
-
 __device__ __forceinline__ void blockAddDouble(double v, double* dst) {
   __shared__ double red[32];
   const unsigned FULL = 0xffffffffu;
@@ -347,21 +360,15 @@ __device__ __forceinline__ void blockAddDouble(double v, double* dst) {
   __syncthreads();
 }
 
-// LB::redistributeMass(extraMass) at the end of LB::streaming
-// (src/LB.cpp:1533, 1844-1852): every interface node receives an equal share.
-__global__ void lbRedistribute(Consts k, FsArgs a) {
-  const double addMass = a.scal[SC_ADD_MASS];
-  FS_LOOP(k, a, {
-    if ((a.mask[x] & TYPE_MASK) == 3) {
-      // the mass the collision used, for fsUpdateMass's recomputation
-      a.massNew[x] = a.mass[x];
-      a.mass[x] += addMass;
-    }
-  })
-}
 
 // LB::updateMass (interface part).
 __global__ void fsUpdateMass(Consts k, FsArgs a) {
+  // the free-surface step's surplus and interface count start from zero
+  // (fsUpdateMass itself accumulates neither)
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.scal[SC_SURPLUS] = 0.0;
+    a.iscal[IS_NIF2] = 0;
+  }
   FS_LOOP(k, a, {
     const uint8_t m = a.mask[x];
     if ((m & TYPE_MASK) != 3) continue;
@@ -545,23 +552,36 @@ __global__ void fsEmptyIsolated(Consts k, FsArgs a) {
   if (cnt) atomicAdd(a.iscal + IS_NIF2, cnt);
 }
 
-// redistributeMass(massSurplus) + cleanLists of the free-surface step.
+// redistributeMass(massSurplus) + cleanLists of the free-surface step over
+// the interface box grown by 1, and the neighbour-cache upkeep over the box
+// grown by 2: the nodes that left the active types in this step (interface
+// -> gas) lie in the box grown by 1, so their neighbours lie in the box
+// grown by 2. Every thread writes only its own node's mask byte.
 __global__ void fsRedistribute(Consts k, FsArgs a) {
   const double addMass = a.scal[SC_SURPLUS] / (double)(unsigned)a.iscal[IS_NIF2];
-  FS_LOOP(k, a, {
+  int x1, y1, z1, rx1, ry1, rz1;
+  if (!fsRegion(k, a.iscal, x1, y1, z1, rx1, ry1, rz1)) return;
+  const int x0 = max(a.iscal[IS_BBOX + 0] - 2, 0), y0 = max(a.iscal[IS_BBOX + 1] - 2, 0),
+            z0 = max(a.iscal[IS_BBOX + 2] - 2, 0);
+  const long long rx = min(a.iscal[IS_BBOX + 3] + 2, k.X - 1) - x0 + 1,
+                  ry = min(a.iscal[IS_BBOX + 4] + 2, k.Y - 1) - y0 + 1,
+                  rz = min(a.iscal[IS_BBOX + 5] + 2, k.Z - 1) - z0 + 1;
+  const long long vol = rx * ry * rz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int ix = x0 + (int)(i % rx), iy = y0 + (int)((i / rx) % ry),
+              iz = z0 + (int)(i / (rx * ry));
+    const long long x = ix + iy * k.sy + iz * k.sz;
     const uint8_t m = a.mask[x];
-    const int t = m & TYPE_MASK;
-    if (t == 3) a.mass[x] += addMass;
-    const bool act = isActiveT(t);
-    const uint8_t nm = (uint8_t)(act ? (m | ABIT) : (m & ~ABIT));
+    uint8_t nm = (uint8_t)(m & ~BULK);
+    if (ix >= x1 && ix < x1 + rx1 && iy >= y1 && iy < y1 + ry1 && iz >= z1 && iz < z1 + rz1) {
+      const int t = m & TYPE_MASK;
+      if (t == 3) a.mass[x] += addMass;
+      nm = (uint8_t)(isActiveT(t) ? (nm | ABIT) : (nm & ~ABIT));
+      a.fsflag[x] = 0;
+    }
     if (nm != m) a.mask[x] = nm;
-    a.fsflag[x] = 0;
-  })
-}
-
-__global__ void fsResetKernel(double* scal, int* iscal) {
-  scal[SC_SURPLUS] = 0.0;
-  iscal[IS_NIF2] = 0;
+  }
 }
 
 // ---- coupling step -----------------------------------------------------------
@@ -720,25 +740,6 @@ __global__ void __launch_bounds__(1024) uncoverResolve(Consts k, uint8_t* mask, 
     for (int j = 0; j < Q; ++j) fset(k, f, j, x, feqj(j, rho0, ux, uy, uz, usq));
     mass[x] = st == 0 ? rho0 : 0.5 * rho0;
     if (k.mixed && st == 0) nF[x] = (float)rho0;
-  }
-}
-
-// Neighbour-cache upkeep after the free-surface step: the nodes that left
-// the active types (interface -> gas) lie in the interface box grown by 1,
-// so their neighbours lie in the box grown by 2.
-__global__ void fsClearBulk(Consts k, uint8_t* mask, const int* iscal) {
-  if (iscal[IS_BBOX + 3] < 0) return;
-  const int x0 = max(iscal[IS_BBOX + 0] - 2, 0), y0 = max(iscal[IS_BBOX + 1] - 2, 0),
-            z0 = max(iscal[IS_BBOX + 2] - 2, 0);
-  const long long rx = min(iscal[IS_BBOX + 3] + 2, k.X - 1) - x0 + 1,
-                  ry = min(iscal[IS_BBOX + 4] + 2, k.Y - 1) - y0 + 1,
-                  rz = min(iscal[IS_BBOX + 5] + 2, k.Z - 1) - z0 + 1;
-  const long long vol = rx * ry * rz;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long x = (x0 + i % rx) + (y0 + (i / rx) % ry) * k.sy + (z0 + i / (rx * ry)) * k.sz;
-    const uint8_t m = mask[x];
-    if (m & BULK) mask[x] = (uint8_t)(m & ~BULK);
   }
 }
 

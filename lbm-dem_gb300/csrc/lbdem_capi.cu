@@ -191,14 +191,13 @@ int enqueueNeighbourList(lbdem_ctx* ctx) {
   nbrCellAssign<<<pg, 128, 0, s>>>(k, a);
   nbrCellScan<<<1, 1024, 0, s>>>(k, a);
   nbrCellScatter<<<pg, 128, 0, s>>>(k, a);
-  nbrCellSort<<<std::max(1, std::min(MAX_L / 128 + 1, ctx->smCount * 8)), 128, 0, s>>>(k, a);
+  nbrCellSort<<<ctx->gridCells, 128, 0, s>>>(k, a);
   nbrBuildCells<<<pg, 128, 0, s>>>(k, a);
   nbrBuildDirect<<<pg, 128, 0, s>>>(k, a);
   nbrDirectHistory<<<pg, 128, 0, s>>>(k, a);
   nbrPartners<<<pg, 128, 0, s>>>(k, a);
   nbrPairList<<<std::max(1, std::min(ctx->nPart * MAX_N / 256 + 1, ctx->smCount * 8)), 256, 0,
                 s>>>(k, a);
-  nbrFinish<<<1, 1, 0, s>>>(a);
   return launchErr(ctx, "neighbour list");
 }
 
@@ -386,6 +385,25 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   const int direct = std::min(nl[0], nl[1]) < 3 ? 1 : 0;
   if (!direct && (long long)nl[0] * nl[1] * nl[2] > MAX_L)
     return setErr(ctx, LBDEM_ERR_OVERFLOW, "more than 100000 neighbour cells");
+  {
+    auto cap = [&](long long blocks, int most) {
+      return (int)std::max(1LL, std::min<long long>(blocks, most));
+    };
+    const int sm = std::max(1, ctx->smCount);
+    // free surface: the interface box is about the free-surface area deep
+    ctx->gridFs = cap((long long)k.X * k.Z / 32 + 1, sm * 4);
+    const long long shell =
+        2LL * ((long long)k.X * k.Y + (long long)k.Y * k.Z + (long long)k.X * k.Z);
+    ctx->gridShell = cap(shell / 256 + 1, sm * 8);
+    long long box = 0;
+    for (int o = 0; o < cfg->n_objects; ++o) {
+      const long long side = (long long)(2.0 * cfg->objects[o].r / L) + 6;
+      box += side * side * side;
+    }
+    ctx->gridObj = cap(box / 256 + 1, sm * 8);
+    const long long cells = direct ? 1 : (long long)nl[0] * nl[1] * nl[2];
+    ctx->gridCells = cap(cells / 128 + 1, sm * 8);
+  }
 
   // ---- allocation ----
   Device& d = ctx->d;
@@ -576,9 +594,8 @@ extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
   if (rc) return rc;
   demPairs<<<std::max(1, std::min(ctx->nPart * (MAX_N / 2) / 128 + 1, ctx->smCount * 16)), 128, 0,
              s>>>(k, a);
-  demGather<<<partGrid(ctx, 128), 128, 0, s>>>(k, a);
-  demObjects<<<1, 32, 0, s>>>(k, a);
-  ctx->launches += 1 + 10 + 3;
+  demGather<<<partGrid(ctx, 128), 128, 0, s>>>(k, a);  // and the impactor update
+  ctx->launches += 1 + 9 + 2;
   return launchErr(ctx, "dem step");
 }
 
@@ -591,10 +608,10 @@ extern "C" int lbdem_coupling_step(lbdem_ctx* ctx) {
   const int lg = latticeGrid(ctx);
   if (ctx->nObj > 0) {
     cudaMemsetAsync(d.iscal + IS_NUNCOVER, 0, sizeof(int), s);
-    uncoverCollect<<<lg, 256, 0, s>>>(k, d.mask, d.obj, d.uncover, d.iscal);
+    uncoverCollect<<<ctx->gridObj, 256, 0, s>>>(k, d.mask, d.obj, d.uncover, d.iscal);
     uncoverResolve<<<1, 1024, 0, s>>>(k, d.mask, d.f[ctx->cur], d.mass, d.nF, d.uncover,
                                       d.iscal);
-    voxelizeObjects<<<lg, 256, 0, s>>>(k, d.mask, d.solid, d.objIdx, d.mass, d.obj);
+    voxelizeObjects<<<ctx->gridObj, 256, 0, s>>>(k, d.mask, d.solid, d.objIdx, d.mass, d.obj);
     ctx->launches += 3;
   }
   flagClaim<<<partGrid(ctx, 4) , 128, 0, s>>>(k, d.mask, d.claim, d.px0, d.pr, d.iscal, d.uscal);
@@ -616,13 +633,9 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   Device& d = ctx->d;
   cudaStream_t s = ctx->stream;
   const int P1 = std::max(ctx->nPart, 1);
-  lbResetKernel<<<std::max(1, std::min(16 * P1 / 256 + 1, 1024)), 256, 0, s>>>(
-      k, d.pFHydro, 16LL * P1, d.obj, d.wallF, d.scal, d.iscal);
-  if (d.pAccF) cudaMemsetAsync(d.pAccF, 0, ACCF_N * (size_t)P1 * sizeof(float), s);
-  if (ctx->nPart > 0) {
-    particleKinematics<<<partGrid(ctx, 256), 256, 0, s>>>(k, d.px0, d.px1, d.pw1, d.pkd, d.pkf);
-    ctx->launches += 1;
-  }
+  lbPrepare<<<std::max(1, std::min(16 * P1 / 256 + 1, 1024)), 256, 0, s>>>(
+      k, d.pFHydro, 16LL * P1, d.pAccF, (long long)ACCF_N * P1, d.obj, d.wallF, d.scal, d.iscal,
+      d.px0, d.px1, d.pw1, d.pkd, d.pkf);
   LbArgs a = lbArgs(ctx);
   auto* ev = nextLbEvents(ctx);
   if (ev) cudaEventRecord(ev->first, s);
@@ -632,17 +645,15 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   else lbStepFp64<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
   if (ev) cudaEventRecord(ev->second, s);
   if (k.mixed && k.nWall > 0) {
-    lbWallForceMixed<<<ctx->smCount * 8, 256, 0, s>>>(k, a);
+    lbWallForceMixed<<<ctx->gridShell, 256, 0, s>>>(k, a);
     ctx->launches += 1;
   }
-  lbFinalizeKernel<<<std::max(1, std::min(P1 / 256 + 1, 256)), 256, 0, s>>>(
-      k, d.pFHydro, d.pMHydro, d.pFluidVol, d.obj, d.wallF, d.scal, d.iscal, d.pAccF, d.pSHydro);
   ctx->cur = 1 - ctx->cur;
+  // unit conversions, then the extra-mass redistribution (free surface)
+  lbFinalizeKernel<<<std::max(ctx->gridFs, partGrid(ctx, 256)), 256, 0, s>>>(
+      k, d.pFHydro, d.pMHydro, d.pFluidVol, d.obj, d.wallF, d.scal, d.iscal, d.pAccF, d.pSHydro,
+      fsArgs(ctx), ctx->freeSurface ? 1 : 0);
   ctx->launches += 3;
-  if (ctx->freeSurface) {
-    lbRedistribute<<<ctx->smCount * 4, 256, 0, s>>>(k, fsArgs(ctx));
-    ctx->launches += 1;
-  }
   return launchErr(ctx, "lb step");
 }
 
@@ -652,17 +663,15 @@ extern "C" int lbdem_free_surface_step(lbdem_ctx* ctx) {
   const Consts& k = ctx->k;
   Device& d = ctx->d;
   cudaStream_t s = ctx->stream;
-  const int g = ctx->smCount * 4;
+  const int g = ctx->gridFs;
   FsArgs a = fsArgs(ctx);
-  fsResetKernel<<<1, 1, 0, s>>>(d.scal, d.iscal);
   fsUpdateMass<<<g, 256, 0, s>>>(k, a);
   fsMutants<<<g, 256, 0, s>>>(k, a);
   fsSmoothen<<<g, 256, 0, s>>>(k, a);
   fsMutantsAndFill<<<g, 256, 0, s>>>(k, a);
   fsEmptyIsolated<<<g, 256, 0, s>>>(k, a);
   fsRedistribute<<<g, 256, 0, s>>>(k, a);
-  fsClearBulk<<<g, 256, 0, s>>>(k, d.mask, d.iscal);
-  ctx->launches += 8;
+  ctx->launches += 6;
   return launchErr(ctx, "free-surface step");
 }
 

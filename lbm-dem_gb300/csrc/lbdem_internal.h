@@ -147,6 +147,8 @@ enum {
   IS_NPAIRS,                // entries of the owner-pair list
   IS_BLOCKS_DONE,           // demBegin: blocks that have posted their maximum
   IS_DEMSTEP,               // DEM::demTimeStep, advanced by demBegin
+  IS_GATHER_DONE,           // demGather: blocks done (the last one updates the impactors)
+  IS_PAIRLIST_DONE,         // nbrPairList: blocks done (the last one swaps the lists)
   IS_COUNT
 };
 // offsets into Device::uscal
@@ -186,6 +188,10 @@ struct lbdem_ctx {
   long long deviceBytes = 0;
   int smCount = 0;
   int lbMixedBlocks = 0;  // resident blocks of the mixed lattice kernel (one wave)
+  // grids of the per-cycle kernels, sized by their work (fixed per run):
+  // the free-surface area, the wall-adjacent layer, the impactor boxes and
+  // the neighbour cells; grid-stride loops cover any excess
+  int gridFs = 1, gridShell = 1, gridObj = 1, gridCells = 1;
   // measurement
   bool profiling = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> lbEvents;

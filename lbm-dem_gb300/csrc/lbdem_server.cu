@@ -107,9 +107,14 @@ void finishJob(lbdem_server* s, Job* j, int status) {
   releaseJob(s, j);
 }
 
-// Admit queued jobs, in order, while memory and run slots allow.
+// Admit queued jobs, in order, while memory and run slots allow. Creating a
+// run blocks the host for its initialisation, so while runs are in progress
+// only one is admitted per turn and the others keep getting slices.
 void admit(lbdem_server* s) {
-  while (!s->pending.empty() && (int)s->active.size() < s->opt.max_active) {
+  const bool busy = !s->active.empty();
+  int admitted = 0;
+  while (!s->pending.empty() && (int)s->active.size() < s->opt.max_active &&
+         !(busy && admitted >= 1)) {
     Job* j = s->pending.front();
     if (s->used + j->bytes > s->budget && !s->active.empty()) break;
     s->pending.pop_front();
@@ -129,6 +134,7 @@ void admit(lbdem_server* s) {
     s->used += j->bytes;
     j->counted = true;
     s->active.push_back(j);
+    ++admitted;
   }
 }
 
