@@ -20,7 +20,7 @@ struct LbArgs {
   const double* px1;
   const double* pw1;
   const double* pkd;  // [6][P] x0/L, x1/S (double)
-  const float* pkf;   // [9][P] x0/L, x1/S, w1/W (float, mixed form)
+  const float* pkf;   // [P][12]: float4 x0/L, x1/S, w1/W (mixed form)
   double* pFHydro;    // [3][P] lattice-unit sums
   double* pMHydro;    // [3][P]
   double* pSHydro;    // [9][P]

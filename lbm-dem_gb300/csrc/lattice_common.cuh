@@ -333,14 +333,16 @@ __device__ __forceinline__ void collideNodeMixed(const Consts& k, float* g, bool
   float hx = 0.0f, hy = 0.0f, hz = 0.0f;
   s.dx = s.dy = s.dz = s.rx = s.ry = s.rz = 0.0f;
   if (pflag && pid < (uint32_t)P) {
-    // pkf: [9][P] float x0/L, x1/S, w1/W of every particle (particleKinematics)
-    const float rx = (float)ix - pkf[pid];
-    const float ry = (float)iy - pkf[P + pid];
-    const float rz = (float)iz - pkf[2 * P + pid];
-    const float wx = pkf[6 * P + pid], wy = pkf[7 * P + pid], wz = pkf[8 * P + pid];
-    const float lvx = pkf[3 * P + pid] + __fmaf_rn(wy, rz, -wz * ry);
-    const float lvy = pkf[4 * P + pid] + __fmaf_rn(wz, rx, -wx * rz);
-    const float lvz = pkf[5 * P + pid] + __fmaf_rn(wx, ry, -wy * rx);
+    // pkf: per particle three float4: x0/L, x1/S, w1/W (lbPrepare)
+    const float4* q = reinterpret_cast<const float4*>(pkf) + 3 * (size_t)pid;
+    const float4 X0 = __ldg(q), X1 = __ldg(q + 1), W1 = __ldg(q + 2);
+    const float rx = (float)ix - X0.x;
+    const float ry = (float)iy - X0.y;
+    const float rz = (float)iz - X0.z;
+    const float wx = W1.x, wy = W1.y, wz = W1.z;
+    const float lvx = X1.x + __fmaf_rn(wy, rz, -wz * ry);
+    const float lvy = X1.y + __fmaf_rn(wz, rx, -wx * rz);
+    const float lvz = X1.z + __fmaf_rn(wx, ry, -wy * rx);
     const float lf = massOld * inv;
     s.dx = (ux - lvx) * lf;
     s.dy = (uy - lvy) * lf;

@@ -238,10 +238,11 @@ __global__ void lbPrepare(Consts k, double* pAcc, long long pAccLen, float* pAcc
     const double xl = px0[i] / k.uLength, vl = px1[i] / k.uSpeed;
     pkd[i] = xl;
     pkd[3 * P + i] = vl;
-    if (pkf) {
-      pkf[i] = (float)xl;
-      pkf[3 * P + i] = (float)vl;
-      pkf[6 * P + i] = (float)(pw1[i] / k.uAngVel);
+    if (pkf) {  // [P] x (x0/L, x1/S, w1/W) as three float4 (4th lane 0)
+      const long long p = i % P, c = i / P;
+      pkf[12 * p + c] = (float)xl;
+      pkf[12 * p + 4 + c] = (float)vl;
+      pkf[12 * p + 8 + c] = (float)(pw1[i] / k.uAngVel);
     }
   }
   if (i0 < k.nObj) {

@@ -449,7 +449,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   AL(d.pinvm, P1);
   AL(d.pinvI, P1);
   AL(d.pkd, 6 * P1);
-  if (k.mixed) AL(d.pkf, 9 * P1);
+  if (k.mixed) AL(d.pkf, 12 * P1);
   if (k.mixed) AL(d.pAccF, ACCF_N * P1);
   if (k.mixed) {
     AL(d.chunkAct, NP / 256);
@@ -864,7 +864,7 @@ extern "C" int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t prec
   for (int i = 0; i < 3; ++i) add(P1, 8);      // r, invm, invI
   add(6 * P1, 8);                              // pkd
   if (mixed) {
-    add(9 * P1, 4);                            // pkf
+    add(12 * P1, 4);                           // pkf
     add(ACCF_N * P1, 4);                       // pAccF
     add(NP / 256, 4);                          // chunkAct
   }

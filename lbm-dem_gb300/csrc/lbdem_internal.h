@@ -99,7 +99,7 @@ struct Device {
   double *pFRep = nullptr, *pFTotal = nullptr, *pMTotal = nullptr, *pFGrav = nullptr;
   double *pxiw = nullptr, *pxio = nullptr;
   double* pkd = nullptr;                 // [6][P] lattice-unit kinematics
-  float* pkf = nullptr;                  // [9][P] (mixed form)
+  float* pkf = nullptr;                  // [P][12] float4 x0/L, x1/S, w1/W (mixed form)
   float* pAccF = nullptr;                // [ACCF_N][P] particle sums (mixed form)
   uint32_t* chunkAct = nullptr;          // [NP/256] chunk activity (mixed form)
   int* plist[2] = {nullptr, nullptr};    // [P][50]
