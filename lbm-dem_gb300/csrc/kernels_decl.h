@@ -81,12 +81,13 @@ struct DemArgs {
 
 // Mixed lattice step launch shape: chunks of MIXED_CHUNK consecutive nodes
 // (one per thread), staged through MIXED_STAGES shared-memory buffers of 19
-// FP32 planes, the solid indices and the mask bytes that thread 0 fills with
-// bulk copies.
+// FP32 planes, the solid indices, the fluid densities nF and the mask bytes
+// that thread 0 fills with bulk copies.
 constexpr int MIXED_CHUNK = 256;
 constexpr int MIXED_STAGES = 3;
 constexpr int MIXED_STAGE_SOLID = Q * MIXED_CHUNK * 4;                 // byte offsets
-constexpr int MIXED_STAGE_MASK = MIXED_STAGE_SOLID + MIXED_CHUNK * 4;
+constexpr int MIXED_STAGE_NF = MIXED_STAGE_SOLID + MIXED_CHUNK * 4;
+constexpr int MIXED_STAGE_MASK = MIXED_STAGE_NF + MIXED_CHUNK * 4;
 constexpr int MIXED_STAGE_BYTES = MIXED_STAGE_MASK + MIXED_CHUNK;
 constexpr int MIXED_THREADS = MIXED_CHUNK;
 constexpr int MIXED_SMEM = MIXED_STAGES * MIXED_STAGE_BYTES;

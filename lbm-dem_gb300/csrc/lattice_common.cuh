@@ -308,14 +308,25 @@ struct NodeStateF {
   float dx, dy, dz, rx, ry, rz;
 };
 
+// Float kinematics of particle pid (lbPrepare): centre x0/L, velocity x1/S
+// and angular velocity w1/W, three float4 per particle.
+struct KinF {
+  float4 x0, x1, w1;
+};
+__device__ __forceinline__ KinF loadKinF(const float* pkf, uint32_t pid) {
+  const float4* q = reinterpret_cast<const float4*>(pkf) + 3 * (size_t)pid;
+  return KinF{__ldg(q), __ldg(q + 1), __ldg(q + 2)};
+}
+
 // Mixed form of collideNode: BGK + Guo forcing with the particle coupling of
-// LB::computeHydroForces, on float deviations g = f - w (in/out). Explicit
-// fused multiply-adds, so the result is the same in every translation unit
-// whatever its contraction flags.
-__device__ __forceinline__ void collideNodeMixed(const Consts& k, float* g, bool pflag,
-                                                 uint32_t pid, const float* pkf, int P,
-                                                 float massOld, int ix, int iy, int iz,
-                                                 NodeStateF& s) {
+// LB::computeHydroForces, on float deviations g = f - w (in/out). The
+// particle's kinematics kin and the node's old mass are loaded by the caller
+// (ahead of the moment sums, so that their latency overlaps them) and used
+// when coupled is set. Explicit fused multiply-adds, so the result is the
+// same in every translation unit whatever its contraction flags.
+__device__ __forceinline__ void collideNodeMixed(const Consts& k, float* g, bool coupled,
+                                                 const KinF& kin, float massOld, int ix,
+                                                 int iy, int iz, NodeStateF& s) {
   // moments from the sums and differences of opposite pairs (j odd, j + 1)
   float dr = g[0];
   float jx = 0.0f, jy = 0.0f, jz = 0.0f;
@@ -332,10 +343,8 @@ __device__ __forceinline__ void collideNodeMixed(const Consts& k, float* g, bool
   float ux = jx * inv, uy = jy * inv, uz = jz * inv;
   float hx = 0.0f, hy = 0.0f, hz = 0.0f;
   s.dx = s.dy = s.dz = s.rx = s.ry = s.rz = 0.0f;
-  if (pflag && pid < (uint32_t)P) {
-    // pkf: per particle three float4: x0/L, x1/S, w1/W (lbPrepare)
-    const float4* q = reinterpret_cast<const float4*>(pkf) + 3 * (size_t)pid;
-    const float4 X0 = __ldg(q), X1 = __ldg(q + 1), W1 = __ldg(q + 2);
+  if (coupled) {
+    const float4 X0 = kin.x0, X1 = kin.x1, W1 = kin.w1;
     const float rx = (float)ix - X0.x;
     const float ry = (float)iy - X0.y;
     const float rz = (float)iz - X0.z;

@@ -394,8 +394,10 @@ __global__ void fsUpdateMass(Consts k, FsArgs a) {
 #pragma unroll
             for (int q = 0; q < Q; ++q) g[q] = ((const float*)a.fold)[(long long)q * k.NP + x];
             NodeStateF s;
-            collideNodeMixed(k, g, pf, pf ? a.solid[x] : 0u, a.pkf, k.nPart,
-                             (float)a.massNew[x], ix, iy, iz, s);
+            const uint32_t pid = pf ? a.solid[x] : 0u;
+            const bool coupled = pf && pid < (uint32_t)k.nPart;
+            const KinF kin = coupled ? loadKinF(a.pkf, pid) : KinF{};
+            collideNodeMixed(k, g, coupled, kin, (float)a.massNew[x], ix, iy, iz, s);
 #pragma unroll
             for (int q = 0; q < Q; ++q) fsl[q] = (double)g[q];  // deviations
           } else {

@@ -201,6 +201,7 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
   // chunks of this block: blockIdx.x, blockIdx.x + gridDim.x, ...
   const unsigned nMine =
       nChunks > blockIdx.x ? (nChunks - 1u - blockIdx.x) / gridDim.x + 1u : 0u;
+  auto chunkOf = [&](unsigned it) { return blockIdx.x + it * gridDim.x; };
   const int lane = tid & 31;
   const int warp = tid >> 5;
   // Chunks with no active node are skipped: their activity bits (kept by
@@ -209,7 +210,7 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
   const bool useList = k.chunkAct != nullptr && nMine <= (unsigned)MIXED_MAX_MINE;
   if (useList) {
     for (unsigned it = tid; it < nMine; it += blockDim.x)
-      sAct[it] = (uint8_t)k.chunkAct[blockIdx.x + it * gridDim.x];
+      sAct[it] = (uint8_t)k.chunkAct[chunkOf(it)];
     __syncthreads();
     if (warp == 0) {
       unsigned run = 0;
@@ -228,14 +229,14 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
   double extra = 0.0;
   unsigned nact = 0, nif = 0;
   // Thread 0 keeps the stage ring filled: bulk copies of the 19 population
-  // planes and the mask bytes of a chunk, completing on the stage's full
-  // barrier. Iterations 0 .. MIXED_STAGES-1 are issued up front; iteration
+  // planes, solid indices, densities and mask bytes of a chunk, completing
+  // on the stage's full barrier. Iterations 0 .. MIXED_STAGES-1 are issued up front; iteration
   // i + MIXED_STAGES - 1 is issued at iteration i once every warp has
   // released iteration i - 1.
   auto issue = [&](unsigned q) {
     const int st = (int)(q % MIXED_STAGES);
     unsigned char* sb = stageMem + st * MIXED_STAGE_BYTES;
-    const unsigned c = blockIdx.x + (useList ? sList[q] : q) * gridDim.x;
+    const unsigned c = chunkOf(useList ? sList[q] : q);
     const size_t off = (size_t)c * MIXED_CHUNK;
     int cx0, cy0, cz0;
     coords(k, (long long)off, cx0, cy0, cz0);
@@ -245,6 +246,7 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
     for (int j = 0; j < Q; ++j)
       bulkLoad(sb + j * MIXED_CHUNK * 4, gin + j * NP + off, MIXED_CHUNK * 4, &fullBar[st]);
     bulkLoad(sb + MIXED_STAGE_SOLID, a.solid + off, MIXED_CHUNK * 4, &fullBar[st]);
+    bulkLoad(sb + MIXED_STAGE_NF, a.nF + off, MIXED_CHUNK * 4, &fullBar[st]);
     bulkLoad(sb + MIXED_STAGE_MASK, mk + off, MIXED_CHUNK, &fullBar[st]);
   };
   unsigned issued = 0;  // meaningful in thread 0
@@ -281,6 +283,16 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
     for (int j = 0; j < Q; ++j) g[j] = ((const float*)sb)[j * MIXED_CHUNK + tid];
     const uint8_t m = valid ? sb[MIXED_STAGE_MASK + tid] : (uint8_t)2;
     const uint32_t sol = ((const uint32_t*)(sb + MIXED_STAGE_SOLID))[tid];
+    const int t = m & TYPE_MASK;
+    const bool act = valid && isActiveT(t);
+    // particle nodes: their particle's kinematics and old mass, loaded first
+    const bool coupled = act && (m & PFLAG) && sol < (uint32_t)k.nPart;
+    KinF kin{};
+    float massOld = 0.0f;
+    if (coupled) {
+      kin = loadKinF(a.pkf, sol);
+      massOld = t == 3 ? (float)a.mass[x] : ((const float*)(sb + MIXED_STAGE_NF))[tid];
+    }
     __syncwarp();
     if (lane == 0) mbarArrive(&emptyBar[st]);  // this warp is done with the stage
     if (tid == 0 && i >= 1 && issued < nIter) {
@@ -294,15 +306,12 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
         abortFlag = 1;
       }
     }
-    const int t = m & TYPE_MASK;
-    const bool act = valid && isActiveT(t);
     // cleanLists (ABIT) and the neighbour cache (BULK) of this node
     uint8_t nm = (uint8_t)(m & ~(ABIT | BULK));
     if (__any_sync(FULL, act)) {
       unsigned actN = ALL_LINKS, gasN = 0, spcN = 0;
       NodeStateF s;
       s.dx = s.dy = s.dz = s.rx = s.ry = s.rz = 0.0f;
-      float massOld = 0.0f;
       int key = -1;
       if (act) {
         // links into the box's wall layer, known from the coordinates
@@ -313,22 +322,16 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
           actN = 0;
 #pragma unroll
           for (int j = 1; j < Q; ++j) {
-            const int tl = mk[x + (unsigned)(CX(j) + CY(j) * sy + CZ(j) * sz)] & TYPE_MASK;
+            const int tl = mk[x + (unsigned)k.nbOff[j]] & TYPE_MASK;
             actN |= (unsigned)isActiveT(tl) << j;
             gasN |= (unsigned)(tl == 2) << j;
             spcN |= ((PLAIN_TYPES >> tl) & 1u ^ 1u) << j;
           }
         }
         nm |= (uint8_t)(ABIT | ((actN | wallN) == ALL_LINKS ? BULK : 0));
-        const bool pf = (m & PFLAG) != 0;
-        const uint32_t pid = pf ? sol : 0u;
-        if (pf) massOld = t == 3 ? (float)a.mass[x] : a.nF[x];
-        collideNodeMixed(k, g, pf, pid, a.pkf, k.nPart, massOld, ix, iy, iz, s);
-        if (pf) {
-          if (pid < (uint32_t)k.nPart) key = (int)pid;
-          else atomicOr(a.iscal + IS_ERROR, ERR_PARTICLE_INDEX);
-        }
-        if (key < 0) massOld = 0.0f;
+        collideNodeMixed(k, g, coupled, kin, massOld, ix, iy, iz, s);
+        if (coupled) key = (int)sol;
+        else if (m & PFLAG) atomicOr(a.iscal + IS_ERROR, ERR_PARTICLE_INDEX);
       }
       if (__any_sync(FULL, key >= 0))
         particleRunReduce(key, ix, s.dx, s.dy, s.dz, s.rx, s.ry, s.rz, massOld, a.pAccF,
@@ -342,14 +345,13 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
       }
       if (pushAll) {
 #pragma unroll
-        for (int j = 1; j < Q; ++j)
-          __stcs(gout + j * NP + (x + (unsigned)(CX(j) + CY(j) * sy + CZ(j) * sz)), g[j]);
+        for (int j = 1; j < Q; ++j) __stcs(gout + (x + k.pushOff[j]), g[j]);
       } else if (act) {
         const float usq3 = 3.0f * __fmaf_rn(s.ux, s.ux, __fmaf_rn(s.uy, s.uy, s.uz * s.uz));
 #pragma unroll
         for (int j = 1; j < Q; ++j) {
           if ((actN >> j) & 1u) {
-            __stcs(gout + j * NP + (x + (unsigned)(CX(j) + CY(j) * sy + CZ(j) * sz)), g[j]);
+            __stcs(gout + (x + k.pushOff[j]), g[j]);
           } else {
             float out = g[j];
             if ((gasN >> j) & 1u) {

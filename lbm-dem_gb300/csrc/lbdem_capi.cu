@@ -19,6 +19,7 @@
 #include "lbdem_internal.h"
 
 #include "kernels_decl.h"
+#include "lattice_common.cuh"
 
 using namespace lbdem;
 
@@ -276,6 +277,10 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   if (k.NP >= (1ll << 32) / Q) return setErr(ctx, LBDEM_ERR_INVALID, "lattice too large");
   k.sy = k.X;
   k.sz = (long long)k.X * k.Y;
+  for (int j = 0; j < Q; ++j) {
+    k.nbOff[j] = (int)(CX(j) + CY(j) * k.sy + CZ(j) * k.sz);
+    k.pushOff[j] = (unsigned)(j * k.NP + k.nbOff[j]);
+  }
   k.initDensity = 1.0;
   k.initVisc = cfg->initVisc / uDynVisc;
   k.omega = 1.0 / (0.5 + 3.0 * k.initVisc);
@@ -424,7 +429,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
     AL(f1, (size_t)Q * NP);
     d.f[0] = f0;
     d.f[1] = f1;
-    AL(d.nF, N);
+    AL(d.nF, NP);  // padded: the lattice step copies whole chunks
   } else {
     double* f0 = nullptr;
     double* f1 = nullptr;
@@ -852,7 +857,7 @@ extern "C" int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t prec
   add(N, 1);                        // fsflag
   add((long long)Q * NP, mixed ? 4 : 8);
   add((long long)Q * NP, mixed ? 4 : 8);
-  if (mixed) add(N, 4);             // nF
+  if (mixed) add(NP, 4);            // nF
   for (int i = 0; i < 3; ++i) add(N, 8);  // mass, massNew, rhoS
   add(3 * N, 8);                    // uS
   add(3 * N, 8);                    // hS

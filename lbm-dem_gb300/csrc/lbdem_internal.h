@@ -66,6 +66,11 @@ struct Consts {
   // active nodes (the lattice step skips chunks with no bit set); null in
   // the plain form
   uint32_t* chunkAct;
+  // per direction j: neighbour offset cx + cy sy + cz sz, and the push
+  // target of population j relative to a node, j NP + that offset (both in
+  // elements; 19 NP < 2^32 is checked when the run is created)
+  int nbOff[Q];
+  unsigned pushOff[Q];
 };
 
 struct DeviceWall {
