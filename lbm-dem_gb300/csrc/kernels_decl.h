@@ -25,7 +25,7 @@ struct LbArgs {
   double* pMHydro;    // [3][P]
   double* pSHydro;    // [9][P]
   double* pFluidVol;  // [P]
-  float* pAccF;       // [ACCF_N][P] float particle sums (mixed form)
+  float* pAccF;       // [P][ACCF_STRIDE] float particle sums (mixed form)
   double* obj;        // object records
   double* wallF;      // [W][12]
   double* scal;

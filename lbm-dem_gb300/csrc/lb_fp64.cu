@@ -295,18 +295,18 @@ __global__ void lbFinalizeKernel(Consts k, double* pF, double* pM, double* pV, d
   const int P = k.nPart;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
     if (pAccF) {
-      // mixed form: float sums [ACCF_N][P] of d (3), R_ab = sum r_a d_b (9)
-      // and massOld (1); torque = antisymmetric part of R, stresslet = R
+      // mixed form: float sums [P][ACCF_STRIDE] of d (3), R_ab = sum r_a d_b
+      // (9) and massOld (1); torque = antisymmetric part of R, stresslet = R
       // in physical units (src/LB.cpp:1941-1958)
-      const long long PP = P;
+      const float* acc = pAccF + (size_t)i * ACCF_STRIDE;
       double R[9];
-      for (int c = 0; c < 9; ++c) R[c] = (double)pAccF[(3 + c) * PP + i];
-      for (int c = 0; c < 3; ++c) pF[c * P + i] = (double)pAccF[c * PP + i];
+      for (int c = 0; c < 9; ++c) R[c] = (double)acc[3 + c];
+      for (int c = 0; c < 3; ++c) pF[c * P + i] = (double)acc[c];
       pM[i] = R[5] - R[7];
       pM[P + i] = R[6] - R[2];
       pM[2 * P + i] = R[1] - R[3];
       for (int c = 0; c < 9; ++c) pS[c * P + i] = R[c] * k.uLength * k.uForce;
-      pV[i] = (double)pAccF[12 * PP + i];
+      pV[i] = (double)acc[12];
     }
     for (int c = 0; c < 3; ++c) {
       pF[c * P + i] *= k.uForce;

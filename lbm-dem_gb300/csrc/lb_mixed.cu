@@ -100,7 +100,8 @@ __device__ __forceinline__ void bulkLoad(void* dst, const void* src, unsigned by
 
 // Segmented reduction of the particle coupling terms over runs of
 // consecutive lanes that share a particle index and a lattice row, then one
-// set of float atomics per run (issued by the run heads together).
+// set of float atomics per run (issued by the run heads together) into the
+// particle's 64-byte line of sums.
 //
 // Per run only 7 sums are needed: D = sum d, L = sum o d with o the lane's
 // offset from the run head, and V = sum massOld. With r the node position
@@ -113,7 +114,7 @@ __device__ __forceinline__ void bulkLoad(void* dst, const void* src, unsigned by
 // particle in lbFinalizeKernel.
 __device__ __forceinline__ void particleRunReduce(int key, int ix, float dx, float dy, float dz,
                                                   float rx, float ry, float rz, float massOld,
-                                                  float* acc, int P) {
+                                                  float* acc) {
   const int lane = threadIdx.x & 31;
   const unsigned pm = __ballot_sync(FULL, key >= 0);
   const int prevKey = __shfl_up_sync(FULL, key, 1);
@@ -136,18 +137,17 @@ __device__ __forceinline__ void particleRunReduce(int key, int ix, float dx, flo
     }
   }
   if (head) {
-    float* q = acc + key;
-    const long long PP = P;
+    float* q = acc + (size_t)key * ACCF_STRIDE;
     atomicAdd(q, v[0]);
-    atomicAdd(q + PP, v[1]);
-    atomicAdd(q + 2 * PP, v[2]);
+    atomicAdd(q + 1, v[1]);
+    atomicAdd(q + 2, v[2]);
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
-      atomicAdd(q + (3 + b) * PP, __fmaf_rn(rx, v[b], v[3 + b]));
-      atomicAdd(q + (6 + b) * PP, ry * v[b]);
-      atomicAdd(q + (9 + b) * PP, rz * v[b]);
+      atomicAdd(q + 3 + b, __fmaf_rn(rx, v[b], v[3 + b]));
+      atomicAdd(q + 6 + b, ry * v[b]);
+      atomicAdd(q + 9 + b, rz * v[b]);
     }
-    atomicAdd(q + 12 * PP, v[6]);
+    atomicAdd(q + 12, v[6]);
   }
 }
 
@@ -334,8 +334,7 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
         else if (m & PFLAG) atomicOr(a.iscal + IS_ERROR, ERR_PARTICLE_INDEX);
       }
       if (__any_sync(FULL, key >= 0))
-        particleRunReduce(key, ix, s.dx, s.dy, s.dz, s.rx, s.ry, s.rz, massOld, a.pAccF,
-                          k.nPart);
+        particleRunReduce(key, ix, s.dx, s.dy, s.dz, s.rx, s.ry, s.rz, massOld, a.pAccF);
       // warps whose 32 nodes push every population to an active neighbour
       // skip the per-link tests
       const bool pushAll = __all_sync(FULL, act && actN == ALL_LINKS);

@@ -455,7 +455,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   AL(d.pinvI, P1);
   AL(d.pkd, 6 * P1);
   if (k.mixed) AL(d.pkf, 12 * P1);
-  if (k.mixed) AL(d.pAccF, ACCF_N * P1);
+  if (k.mixed) AL(d.pAccF, ACCF_STRIDE * P1);
   if (k.mixed) {
     AL(d.chunkAct, NP / 256);
     // every chunk may hold active nodes until the first lattice step checks
@@ -639,7 +639,7 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   cudaStream_t s = ctx->stream;
   const int P1 = std::max(ctx->nPart, 1);
   lbPrepare<<<std::max(1, std::min(16 * P1 / 256 + 1, 1024)), 256, 0, s>>>(
-      k, d.pFHydro, 16LL * P1, d.pAccF, (long long)ACCF_N * P1, d.obj, d.wallF, d.scal, d.iscal,
+      k, d.pFHydro, 16LL * P1, d.pAccF, (long long)ACCF_STRIDE * P1, d.obj, d.wallF, d.scal, d.iscal,
       d.px0, d.px1, d.pw1, d.pkd, d.pkf);
   LbArgs a = lbArgs(ctx);
   auto* ev = nextLbEvents(ctx);
@@ -870,7 +870,7 @@ extern "C" int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t prec
   add(6 * P1, 8);                              // pkd
   if (mixed) {
     add(12 * P1, 4);                           // pkf
-    add(ACCF_N * P1, 4);                       // pAccF
+    add(ACCF_STRIDE * P1, 4);                  // pAccF
     add(NP / 256, 4);                          // chunkAct
   }
   add(16 * P1, 8);                             // FHydro, MHydro, SHydro, fluidVolume

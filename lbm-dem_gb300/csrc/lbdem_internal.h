@@ -18,6 +18,7 @@ constexpr int MAX_WALL = 6;
 constexpr int PAIR_VALS = 18;    // per neighbour slot: contact(6) lub(9) rep(3)
 constexpr int UNCOVER_CAP = 8192;// uncovered object nodes resolved per step
 constexpr int ACCF_N = 13;       // mixed-form particle sums: d(3), r (x) d (9), mass(1)
+constexpr int ACCF_STRIDE = 16;  // floats per particle: its sums share one 64-byte line
 
 // mask byte layout
 constexpr uint8_t TYPE_MASK = 0x0F;
@@ -105,7 +106,7 @@ struct Device {
   double *pxiw = nullptr, *pxio = nullptr;
   double* pkd = nullptr;                 // [6][P] lattice-unit kinematics
   float* pkf = nullptr;                  // [P][12] float4 x0/L, x1/S, w1/W (mixed form)
-  float* pAccF = nullptr;                // [ACCF_N][P] particle sums (mixed form)
+  float* pAccF = nullptr;                // [P][ACCF_STRIDE] particle sums (mixed form)
   uint32_t* chunkAct = nullptr;          // [NP/256] chunk activity (mixed form)
   int* plist[2] = {nullptr, nullptr};    // [P][50]
   double* pxi[2] = {nullptr, nullptr};   // [P][3][50]
