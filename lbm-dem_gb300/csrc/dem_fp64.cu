@@ -18,6 +18,7 @@
 #include <cfloat>
 #include <climits>
 
+#include "dem_forces.cuh"
 #include "kernels_decl.h"
 
 namespace lbdem {
@@ -420,193 +421,6 @@ __global__ void nbrPairList(Consts k, DemArgs a) {
 
 // ---- pair forces (owner pass) ------------------------------------------------
 
-// DEM::calculateParticleContactForces, one pair (src/DEM.cpp:1506-1700)
-__device__ void pairContact(const Consts& k, double ra, double rb, const double* xa,
-                            const double* xb, const double* va, const double* vb,
-                            const double* wa, const double* wb, double* xi, double* out) {
-  const double rad = 0.5 * (ra + rb);
-  const double x12 = xa[0] - xb[0], y12 = xa[1] - xb[1], z12 = xa[2] - xb[2];
-  const double r12 = sqrt(x12 * x12 + y12 * y12 + z12 * z12);
-  const double urx = va[0] - vb[0], ury = va[1] - vb[1], urz = va[2] - vb[2];
-  const double nx = x12 / r12, ny = y12 / r12, nz = z12 / r12;
-  const double gn = urx * nx + ury * ny + urz * nz;
-  const double mu = k.mu, kk = k.k, c = k.c;
-  const double del = 2 * rad - r12;
-  double fnx, fny, fnz, ftx, fty, ftz;
-  if (del > 0.0) {
-    if (mu != 0.0) {
-      const double ox = ra * wa[0] + rb * wb[0];
-      const double oy = ra * wa[1] + rb * wb[1];
-      const double oz = ra * wa[2] + rb * wb[2];
-      const double vx = urx + ny * oz - nz * oy - gn * nx;
-      const double vy = ury + nz * ox - nx * oz - gn * ny;
-      const double vz = urz + nx * oy - ny * ox - gn * nz;
-      const double xi12 = xi[0] * nx + xi[1] * ny + xi[2] * nz;
-      xi[0] -= xi12 * nx;
-      xi[1] -= xi12 * ny;
-      xi[2] -= xi12 * nz;
-      fnx = kk * del * nx - c * gn * nx;
-      fny = kk * del * ny - c * gn * ny;
-      fnz = kk * del * nz - c * gn * nz;
-      const double kt = 0.2 * kk;
-      const double dct = k.kinVisc == 0.0 ? c : 0.0;
-      ftx = -kt * xi[0] - dct * vx;
-      fty = -kt * xi[1] - dct * vy;
-      ftz = -kt * xi[2] - dct * vz;
-      const double fnn = sqrt(fnx * fnx + fny * fny + fnz * fnz);
-      const double ftt = sqrt(ftx * ftx + fty * fty + ftz * ftz);
-      const double fri = mu * fnn;
-      const double tx = ftx / ftt, ty = fty / ftt, tz = ftz / ftt;
-      xi[0] += vx * k.dt;
-      xi[1] += vy * k.dt;
-      xi[2] += vz * k.dt;
-      if (fri < ftt) {
-        ftx = fri * tx;
-        fty = fri * ty;
-        ftz = fri * tz;
-        xi[0] = -(1 / kt) * (ftx + dct * vx);
-        xi[1] = -(1 / kt) * (fty + dct * vy);
-        xi[2] = -(1 / kt) * (ftz + dct * vz);
-      }
-    } else {
-      fnx = kk * del * nx - c * gn * nx;
-      fny = kk * del * ny - c * gn * ny;
-      fnz = kk * del * nz - c * gn * nz;
-      ftx = fty = ftz = 0.0;
-    }
-  } else {
-    fnx = fny = fnz = ftx = fty = ftz = 0.0;
-    xi[0] = xi[1] = xi[2] = 0.0;
-  }
-  out[0] = fnx + ftx;
-  out[1] = fny + fty;
-  out[2] = fnz + ftz;
-  out[3] = fty * nz - ftz * ny;
-  out[4] = ftz * nx - ftx * nz;
-  out[5] = ftx * ny - fty * nx;
-}
-
-// Nguyen-Ladd lubrication of a sphere pair (src/DEM.cpp:2325-2491) or of a
-// particle and an impactor (:1158-1323; same algebra with the impactor as
-// sphere 2). Returns false outside the cut-off.
-__device__ bool pairLub(const Consts& k, double ra, double rb, const double* xa,
-                        const double* xb, const double* va, const double* vb, const double* wa,
-                        const double* wb, double* out) {
-  const double lub_N = k.lubN, lub_T = k.lubT, lub_R = k.lubR, cut = k.lubCut;
-  const double rad = 0.5 * (ra + rb);
-  double x12 = xa[0] - xb[0], y12 = xa[1] - xb[1], z12 = xa[2] - xb[2];
-  const double r12 = sqrt(x12 * x12 + y12 * y12 + z12 * z12);
-  const double umx = va[0] - vb[0], umy = va[1] - vb[1], umz = va[2] - vb[2];
-  const double w1x = wa[0], w1y = wa[1], w1z = wa[2];
-  const double w2x = wb[0], w2y = wb[1], w2z = wb[2];
-  const double dr = r12 - 2.0 * rad;
-  const double h = dmax(dr, cut);
-  if (!(dr < dmax(cut, dmax(lub_N, dmax(lub_T, lub_R))))) return false;
-  const double alpha = 3.14159265358979323846 * k.kinVisc * rad * k.dt;
-  const double beta1 = rb / ra;
-  const double beta2 = beta1 * beta1;
-  const double beta3 = beta1 * beta2;
-  const double beta4 = pow((1 + beta1), 4.0);
-  double Xa, Ya, Yb1, Yb2, Yc11, Yc12, Yc21, Yc22, h_c, beta;
-  if (dr < dmax(cut, lub_N)) {
-    Xa = 4.0 * beta2 / beta4;
-    h_c = dmax(dr, lub_N);
-    Xa *= rad / h - rad / h_c;
-    Xa *= 6.0 * alpha;
-  } else {
-    Xa = 0.0;
-  }
-  if (dr < dmax(cut, lub_T)) {
-    Ya = 8.0 * beta1 * (2.0 + beta1 + 2.0 * beta2) / (15.0 * beta4);
-    Yb1 = -4.0 * beta1 * (4.0 + beta1) / (5.0 * beta4);
-    Yb2 = 4.0 * beta1 * (4.0 * beta2 + beta1) / (5.0 * beta4);
-    h_c = dmax(dr, lub_T);
-    beta = alpha * log(h_c / h);
-    Ya *= 6.0 * beta;
-    Yb1 *= 4.0 * beta * rad;
-    Yb2 *= 4.0 * beta * rad;
-  } else {
-    Ya = Yb1 = Yb2 = 0.0;
-  }
-  if (dr < dmax(cut, lub_R)) {
-    Yc11 = 16.0 * beta1 / (5.0 * beta4);
-    Yc12 = 4.0 * beta2 / (5.0 * beta4);
-    Yc21 = 4.0 * beta2 / (5.0 * beta4);
-    Yc22 = 16.0 * beta3 / (5.0 * beta4);
-    h_c = dmax(dr, lub_R);
-    beta = alpha * log(h_c / h);
-    Yc11 *= 8.0 * beta * rad * rad;
-    Yc12 *= 8.0 * beta * rad * rad;
-    Yc21 *= 8.0 * beta * rad * rad;
-    Yc22 *= 8.0 * beta * rad * rad;
-  } else {
-    Yc11 = Yc12 = Yc21 = Yc22 = 0.0;
-  }
-  x12 /= r12;
-  y12 /= r12;
-  z12 /= r12;
-  const double um_r = umx * x12 + umy * y12 + umz * z12;
-  const double w1_r = w1x * x12 + w1y * y12 + w1z * z12;
-  const double w2_r = w2x * x12 + w2y * y12 + w2z * z12;
-  const double umxrx = umy * z12 - umz * y12;
-  const double umxry = umz * x12 - umx * z12;
-  const double umxrz = umx * y12 - umy * x12;
-  const double w1xrx = w1y * z12 - w1z * y12;
-  const double w1xry = w1z * x12 - w1x * z12;
-  const double w1xrz = w1x * y12 - w1y * x12;
-  const double w2xrx = w2y * z12 - w2z * y12;
-  const double w2xry = w2z * x12 - w2x * z12;
-  const double w2xrz = w2x * y12 - w2y * x12;
-  double Fx = -Xa * um_r * x12 - Ya * (umx - um_r * x12);
-  double Fy = -Xa * um_r * y12 - Ya * (umy - um_r * y12);
-  double Fz = -Xa * um_r * z12 - Ya * (umz - um_r * z12);
-  Fx += -Yb1 * w1xrx + Yb2 * w2xrx;
-  Fy += -Yb1 * w1xry + Yb2 * w2xry;
-  Fz += -Yb1 * w1xrz + Yb2 * w2xrz;
-  double T1x = Yb1 * umxrx, T1y = Yb1 * umxry, T1z = Yb1 * umxrz;
-  double T2x = -Yb2 * umxrx, T2y = -Yb2 * umxry, T2z = -Yb2 * umxrz;
-  T1x += -Yc11 * (w1x - w1_r * x12) - Yc12 * (w2x - w2_r * x12);
-  T1y += -Yc11 * (w1y - w1_r * y12) - Yc12 * (w2y - w2_r * y12);
-  T1z += -Yc11 * (w1z - w1_r * z12) - Yc12 * (w2z - w2_r * z12);
-  T2x += -Yc21 * (w1x - w1_r * x12) - Yc22 * (w2x - w2_r * x12);
-  T2y += -Yc21 * (w1y - w1_r * y12) - Yc22 * (w2y - w2_r * y12);
-  T2z += -Yc21 * (w1z - w1_r * z12) - Yc22 * (w2z - w2_r * z12);
-  out[0] = Fx;
-  out[1] = Fy;
-  out[2] = Fz;
-  out[3] = T1x;
-  out[4] = T1y;
-  out[5] = T1z;
-  out[6] = T2x;
-  out[7] = T2y;
-  out[8] = T2z;
-  return true;
-}
-
-// DEM::calculateParticleElectroForces, one pair (src/DEM.cpp:1413-1449)
-__device__ void pairRep(const Consts& k, double ra, double rb, const double* xa,
-                        const double* xb, double* out) {
-  const double rad = 0.5 * (ra + rb);
-  const double x12 = xa[0] - xb[0], y12 = xa[1] - xb[1], z12 = xa[2] - xb[2];
-  const double r12 = sqrt(x12 * x12 + y12 * y12 + z12 * z12);
-  const double nx = x12 / r12, ny = y12 / r12, nz = z12 / r12;
-  const double del = 2 * rad - r12;
-  if (del <= 0.0) {
-    out[0] = k.electro * exp(del / k.debye) * nx;
-    out[1] = k.electro * exp(del / k.debye) * ny;
-    out[2] = k.electro * exp(del / k.debye) * nz;
-  } else {
-    out[0] = k.electro * nx;
-    out[1] = k.electro * ny;
-    out[2] = k.electro * nz;
-  }
-}
-
-__device__ __forceinline__ void load3(const double* a, int P, int i, double* v) {
-  v[0] = a[i];
-  v[1] = a[P + i];
-  v[2] = a[2 * P + i];
-}
 
 // Owner pass: every pair (n1 > n2) evaluated once from n1's slot, one
 // thread per entry of the owner-pair list.
@@ -631,264 +445,26 @@ __global__ void demPairs(Consts k, DemArgs a) {
     load3(a.x1, P, j, vb);
     load3(a.w1, P, j, wb);
     const double ra = a.r[i], rb = a.r[j];
+    const PairGeom<double> g = pairGeomD(0.5 * (ra + rb), xa, xb, va, vb);
     double* out = a.pairbuf + (long long)idx * PAIR_VALS;
     uint8_t flag = 0;
-    if (lubOn && pairLub(k, ra, rb, xa, xb, va, vb, wa, wb, out + 6)) flag |= 1;
+    if (lubOn && pairLub(k, ra, rb, g, wa, wb, out + 6)) flag |= 1;
     double xi[3] = {xii[s], xii[MAX_N + s], xii[2 * MAX_N + s]};
-    pairContact(k, ra, rb, xa, xb, va, vb, wa, wb, xi, out);
+    pairContact(k, ra, rb, g, wa, wb, xi, out);
     xii[s] = xi[0];
     xii[MAX_N + s] = xi[1];
     xii[2 * MAX_N + s] = xi[2];
-    pairRep(k, ra, rb, xa, xb, out + 15);
+    pairRep(k, g, out + 15);
     a.pairflag[idx] = flag;
   }
 }
 
 // ---- gather, walls, impactor, integration ------------------------------------
 
-// Particle-wall contact (src/DEM.cpp:1956-2108) or the fictional lid
-// (:2166-2292); returns the force and torque arm; updates xiw.
-__device__ void wallContactOne(const Consts& k, double r, const double* x, const double* v,
-                               const double* w, double* xiw, double x1w, double y1w,
-                               double z1w, double* nstale, double* df, double* dt) {
-  const double r1w = sqrt(x1w * x1w + y1w * y1w + z1w * z1w);
-  const double delw = r - r1w;
-  double fnx, fny, fnz, ftx, fty, ftz;
-  if (delw > 0.0) {
-    nstale[0] = x1w / r1w;
-    nstale[1] = y1w / r1w;
-    nstale[2] = z1w / r1w;
-    const double nx = nstale[0], ny = nstale[1], nz = nstale[2];
-    const double urx = v[0], ury = v[1], urz = v[2];
-    const double gn = urx * nx + ury * ny + urz * nz;
-    if (k.mu != 0.0) {
-      const double ox = r * w[0], oy = r * w[1], oz = r * w[2];
-      const double vx = urx + ny * oz - nz * oy - gn * nx;
-      const double vy = ury + nz * ox - nx * oz - gn * ny;
-      const double vz = urz + nx * oy - ny * ox - gn * nz;
-      const double xi = xiw[0] * nx + xiw[1] * ny + xiw[2] * nz;
-      xiw[0] -= xi * nx;
-      xiw[1] -= xi * ny;
-      xiw[2] -= xi * nz;
-      fnx = k.k * delw * nx - k.c * gn * nx;
-      fny = k.k * delw * ny - k.c * gn * ny;
-      fnz = k.k * delw * nz - k.c * gn * nz;
-      const double kt = 0.2 * k.k;
-      const double dct = k.kinVisc == 0.0 ? k.c : 0.0;
-      ftx = -kt * xiw[0] - dct * vx;
-      fty = -kt * xiw[1] - dct * vy;
-      ftz = -kt * xiw[2] - dct * vz;
-      const double fnn = sqrt(fnx * fnx + fny * fny + fnz * fnz);
-      const double ftt = sqrt(ftx * ftx + fty * fty + ftz * ftz);
-      const double fri = k.mu * fnn;
-      const double tx = ftx / ftt, ty = fty / ftt, tz = ftz / ftt;
-      xiw[0] += vx * k.dt;
-      xiw[1] += vy * k.dt;
-      xiw[2] += vz * k.dt;
-      if (fri < ftt) {
-        ftx = fri * tx;
-        fty = fri * ty;
-        ftz = fri * tz;
-        xiw[0] = -(1 / kt) * (ftx + dct * vx);
-        xiw[1] = -(1 / kt) * (fty + dct * vy);
-        xiw[2] = -(1 / kt) * (ftz + dct * vz);
-      }
-    } else {
-      fnx = k.k * delw * nx - k.c * gn * nx;
-      fny = k.k * delw * ny - k.c * gn * ny;
-      fnz = k.k * delw * nz - k.c * gn * nz;
-      ftx = fty = ftz = 0.0;
-    }
-  } else {
-    fnx = fny = fnz = ftx = fty = ftz = 0.0;
-    xiw[0] = xiw[1] = xiw[2] = 0.0;
-  }
-  df[0] = fnx + ftx;
-  df[1] = fny + fty;
-  df[2] = fnz + ftz;
-  dt[0] = fty * nstale[2] - ftz * nstale[1];
-  dt[1] = ftz * nstale[0] - ftx * nstale[2];
-  dt[2] = ftx * nstale[1] - fty * nstale[0];
-}
 
-// Particle-wall lubrication (src/DEM.cpp:2541-2670)
-__device__ bool wallLubOne(const Consts& k, double rad, const double* v, const double* w,
-                           double x12, double y12, double z12, double* F, double* T) {
-  const double cut = k.lubCut, lub_N = k.lubN, lub_T = k.lubT, lub_R = k.lubR;
-  const double r12 = sqrt(x12 * x12 + y12 * y12 + z12 * z12);
-  const double umx = v[0], umy = v[1], umz = v[2];
-  const double w1x = w[0], w1y = w[1], w1z = w[2];
-  const double dr = r12 - rad;
-  const double h = dmax(dr, cut);
-  if (!(dr < dmax(cut, dmax(lub_N, dmax(lub_T, lub_R))))) return false;
-  const double alpha = 3.14159265358979323846 * k.kinVisc * rad * k.dt;
-  double Xa, Ya, Yb1, Yc11, h_c, beta;
-  if (dr < dmax(cut, lub_N)) {
-    Xa = 1.0;
-    h_c = dmax(dr, lub_N);
-    Xa *= rad / h - rad / h_c;
-    Xa *= 6.0 * alpha;
-  } else {
-    Xa = 0.0;
-  }
-  if (dr < dmax(cut, lub_T)) {
-    Ya = 8.0 / 15.0;
-    Yb1 = -1.0 / 5.0;
-    h_c = dmax(dr, lub_T);
-    beta = alpha * log(h_c / h);
-    Ya *= 6.0 * beta;
-    Yb1 *= 4.0 * beta * rad;
-  } else {
-    Ya = Yb1 = 0.0;
-  }
-  if (dr < dmax(cut, lub_R)) {
-    Yc11 = 2.0 / 5.0;
-    h_c = dmax(dr, lub_R);
-    beta = alpha * log(h_c / h);
-    Yc11 *= 8.0 * beta * rad * rad;
-  } else {
-    Yc11 = 0.0;
-  }
-  x12 /= r12;
-  y12 /= r12;
-  z12 /= r12;
-  const double um_r = umx * x12 + umy * y12 + umz * z12;
-  const double w1_r = w1x * x12 + w1y * y12 + w1z * z12;
-  const double umxrx = umy * z12 - umz * y12;
-  const double umxry = umz * x12 - umx * z12;
-  const double umxrz = umx * y12 - umy * x12;
-  const double w1xrx = w1y * z12 - w1z * y12;
-  const double w1xry = w1z * x12 - w1x * z12;
-  const double w1xrz = w1x * y12 - w1y * x12;
-  F[0] = -Xa * x12 * um_r - Ya * (umx - um_r * x12);
-  F[1] = -Xa * y12 * um_r - Ya * (umy - um_r * y12);
-  F[2] = -Xa * z12 * um_r - Ya * (umz - um_r * z12);
-  F[0] += -Yb1 * w1xrx;
-  F[1] += -Yb1 * w1xry;
-  F[2] += -Yb1 * w1xrz;
-  T[0] = Yb1 * umxrx;
-  T[1] = Yb1 * umxry;
-  T[2] = Yb1 * umxrz;
-  T[0] += -Yc11 * (w1x - w1_r * x12);
-  T[1] += -Yc11 * (w1y - w1_r * y12);
-  T[2] += -Yc11 * (w1z - w1_r * z12);
-  return true;
-}
 
-// Particle-impactor contact (src/DEM.cpp:921-1090); dampCoeffTanw is an
-// uninitialised local in the reference, zero under the pinned build.
-__device__ void objContactOne(const Consts& k, double ra, double ro, const double* xa,
-                              const double* xo, const double* va, const double* vo,
-                              const double* wa, const double* wo, double* xio, double* df,
-                              double* dt) {
-  const double radw = 0.5 * (ra + ro);
-  const double x1w = xa[0] - xo[0], y1w = xa[1] - xo[1], z1w = xa[2] - xo[2];
-  const double r1w = sqrt(x1w * x1w + y1w * y1w + z1w * z1w);
-  const double nx = x1w / r1w, ny = y1w / r1w, nz = z1w / r1w;
-  const double urx = va[0] - vo[0], ury = va[1] - vo[1], urz = va[2] - vo[2];
-  const double delw = (2 * radw) - r1w;
-  const double dampCoeffTanw = 0.0;
-  double fnx, fny, fnz, ftx, fty, ftz;
-  if (delw > 0.0) {
-    const double gn = urx * nx + ury * ny + urz * nz;
-    if (k.mu != 0.0) {
-      const double ox = ra * wa[0] + ro * wo[0];
-      const double oy = ra * wa[1] + ro * wo[1];
-      const double oz = ra * wa[2] + ro * wo[2];
-      const double vx = urx + ny * oz - nz * oy - gn * nx;
-      const double vy = ury + nz * ox - nx * oz - gn * ny;
-      const double vz = urz + nx * oy - ny * ox - gn * nz;
-      const double xi = xio[0] * nx + xio[1] * ny + xio[2] * nz;
-      xio[0] -= xi * nx;
-      xio[1] -= xi * ny;
-      xio[2] -= xi * nz;
-      fnx = k.k * delw * nx - k.c * gn * nx;
-      fny = k.k * delw * ny - k.c * gn * ny;
-      fnz = k.k * delw * nz - k.c * gn * nz;
-      const double kt = 0.2 * k.k;
-      ftx = -kt * xio[0];
-      fty = -kt * xio[1];
-      ftz = -kt * xio[2];
-      const double fnn = sqrt(fnx * fnx + fny * fny + fnz * fnz);
-      const double ftt = sqrt(ftx * ftx + fty * fty + ftz * ftz);
-      const double fri = k.mu * fnn;
-      const double tx = ftx / ftt, ty = fty / ftt, tz = ftz / ftt;
-      if (fri < ftt) {
-        ftx = fri * tx;
-        fty = fri * ty;
-        ftz = fri * tz;
-        xio[0] = -(1 / kt) * (ftx + dampCoeffTanw * vx);
-        xio[1] = -(1 / kt) * (fty + dampCoeffTanw * vy);
-        xio[2] = -(1 / kt) * (ftz + dampCoeffTanw * vz);
-      } else {
-        xio[0] += vx * k.dt;
-        xio[1] += vy * k.dt;
-        xio[2] += vz * k.dt;
-      }
-    } else {
-      fnx = k.k * delw * nx - k.c * gn * nx;
-      fny = k.k * delw * ny - k.c * gn * ny;
-      fnz = k.k * delw * nz - k.c * gn * nz;
-      ftx = fty = ftz = 0.0;
-    }
-  } else {
-    fnx = fny = fnz = ftx = fty = ftz = 0.0;
-    xio[0] = xio[1] = xio[2] = 0.0;
-  }
-  df[0] = fnx + ftx;
-  df[1] = fny + fty;
-  df[2] = fnz + ftz;
-  dt[0] = fty * nz - ftz * ny;
-  dt[1] = ftz * nx - ftx * nz;
-  dt[2] = ftx * ny - fty * nx;
-}
 
-__device__ __forceinline__ void add3(double* a, const double* b) {
-  a[0] += b[0];
-  a[1] += b[1];
-  a[2] += b[2];
-}
-__device__ __forceinline__ void sub3(double* a, const double* b) {
-  a[0] -= b[0];
-  a[1] -= b[1];
-  a[2] -= b[2];
-}
-
-// per-block shared accumulators for the impactor and wall sums
-enum { GA_OBJ = 0, GA_WALL = GA_OBJ + 12 * MAX_OBJ, GA_N = GA_WALL + 6 * MAX_WALL };
-
-// Impactor totals and integration, wall totals (src/DEM.cpp:773-790,
-// 2742-2760), by the last block of demGather once every block's impactor
-// and wall sums are in.
-__device__ void demObjectsTail(const Consts& k, DemArgs& a) {
-  const int stepNo = a.iscal[IS_DEMSTEP];
-  const int o = threadIdx.x;
-  // volatile: the sums other blocks added must not come from a line this
-  // block's L1 cached earlier in the kernel
-  if (o < k.nObj) {
-    volatile double* ob = a.obj + o * OB_STRIDE;
-    const double dtt = k.dt;
-    for (int c = 0; c < 3; ++c) {
-      ob[OB_FTOTAL + c] =
-          0.0 + ((((ob[OB_FHYDRO + c] + ob[OB_FCONTACT + c]) + ob[OB_FLUB + c]) + ob[OB_FGRAV + c]) +
-                 0.0);
-      ob[OB_MTOTAL + c] = 0.0 + ((ob[OB_MHYDRO + c] + ob[OB_MCONTACT + c]) + ob[OB_MLUB + c]);
-    }
-    if (stepNo >= k.objWaitTime)
-      for (int c = 0; c < 3; ++c) {
-        const double x1 = ob[OB_X1 + c];
-        ob[OB_X0 + c] += dtt * x1 + dtt * dtt * ob[OB_FTOTAL + c] * ob[OB_INVM];
-        ob[OB_X1 + c] = x1 + dtt * ob[OB_FTOTAL + c] * ob[OB_INVM];
-        ob[OB_W1 + c] += dtt * ob[OB_MTOTAL + c] * ob[OB_INVI];
-      }
-  }
-  if (o < k.nWall) {
-    volatile double* w = a.wallF + o * 12;
-    for (int c = 0; c < 3; ++c) w[9 + c] = 0.0 + (((w[c] + w[3 + c]) + w[6 + c]) + 0.0);
-  }
-}
-
-__global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a) {
+__global__ void __launch_bounds__(GATHER_THREADS) demGather(Consts k, DemArgs a) {
   const int stepNo = a.iscal[IS_DEMSTEP];
   __shared__ double acc[GA_N];
   for (int t = threadIdx.x; t < GA_N; t += blockDim.x) acc[t] = 0.0;
@@ -938,8 +514,9 @@ __global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a) {
         const double x12 = (xa[0] - W.p[0]) * W.n[0] * W.n[0];
         const double y12 = (xa[1] - W.p[1]) * W.n[1] * W.n[1];
         const double z12 = (xa[2] - W.p[2]) * W.n[2] * W.n[2];
+        const double r12 = sqrt(x12 * x12 + y12 * y12 + z12 * z12);
         double F[3], T[3];
-        if (wallLubOne(k, ra, va, wa, x12, y12, z12, F, T)) {
+        if (wallLubOne(k, ra, va, wa, x12, y12, z12, r12, F, T)) {
           add3(FL, F);
           add3(ML, T);
           for (int c = 0; c < 3; ++c)
@@ -948,8 +525,9 @@ __global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a) {
       }
       for (int o = 0; o < k.nObj; ++o) {
         const double* ob = a.obj + o * OB_STRIDE;
-        objContactOne(k, ra, ob[OB_R], xa, ob + OB_X0, va, ob + OB_X1, wa, ob + OB_W1, xio,
-                      df, dt);
+        const PairGeom<double> g =
+            pairGeomD(0.5 * (ra + ob[OB_R]), xa, ob + OB_X0, va, ob + OB_X1);
+        objContactOne(k, ra, ob[OB_R], g, wa, ob + OB_W1, xio, df, dt);
         add3(FC, df);
         MC[0] += ra * dt[0];
         MC[1] += ra * dt[1];
@@ -963,7 +541,9 @@ __global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a) {
       for (int o = 0; o < k.nObj; ++o) {
         const double* ob = a.obj + o * OB_STRIDE;
         double lo[9];
-        if (pairLub(k, ra, ob[OB_R], xa, ob + OB_X0, va, ob + OB_X1, wa, ob + OB_W1, lo)) {
+        const PairGeom<double> g =
+            pairGeomD(0.5 * (ra + ob[OB_R]), xa, ob + OB_X0, va, ob + OB_X1);
+        if (pairLub(k, ra, ob[OB_R], g, wa, ob + OB_W1, lo)) {
           add3(FL, lo);
           add3(ML, lo + 3);
           for (int c = 0; c < 3; ++c) {
@@ -974,8 +554,8 @@ __global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a) {
       }
     } else {
       double nst[3] = {0.0, 0.0, 0.0};
-      wallContactOne(k, ra, xa, va, wa, xiw, 0.0, xa[1] - (k.demSize[1] - 0.3), 0.0, nst, df,
-                     dt);
+      const double ylid = xa[1] - (k.demSize[1] - 0.3);
+      wallContactOne(k, ra, va, wa, xiw, 0.0, ylid, 0.0, sqrt(ylid * ylid), nst, df, dt);
       add3(FC, df);
       MC[0] += ra * dt[0];
       MC[1] += ra * dt[1];
@@ -1013,7 +593,8 @@ __global__ void __launch_bounds__(128) demGather(Consts k, DemArgs a) {
         const double x1w = (xa[0] - W.p[0]) * W.n[0] * W.n[0];
         const double y1w = (xa[1] - W.p[1]) * W.n[1] * W.n[1];
         const double z1w = (xa[2] - W.p[2]) * W.n[2] * W.n[2];
-        wallContactOne(k, ra, xa, va, wa, xiw, x1w, y1w, z1w, nst, df, dt);
+        const double r1w = sqrt(x1w * x1w + y1w * y1w + z1w * z1w);
+        wallContactOne(k, ra, va, wa, xiw, x1w, y1w, z1w, r1w, nst, df, dt);
         add3(FC, df);
         MC[0] += ra * dt[0];
         MC[1] += ra * dt[1];

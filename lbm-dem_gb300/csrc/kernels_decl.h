@@ -138,6 +138,10 @@ __global__ void nonfiniteCheck(Consts k, const uint8_t* mask, const void* f, int
 __global__ void exportLattice(Consts k, const uint8_t* mask, const void* f, const double* mass,
                               const float* nF, double* fOut, double* massOut);
 
+// threads per block of the gather pass (one thread per particle): small
+// blocks spread a few thousand particles over every SM
+constexpr int GATHER_THREADS = 64;
+
 // dem_fp64.cu
 __global__ void demBegin(Consts k, DemArgs a, int forceRebuild);
 __global__ void nbrCellAssign(Consts k, DemArgs a);
@@ -152,5 +156,8 @@ __global__ void nbrPairList(Consts k, DemArgs a);
 // the DEM step number comes from iscal[IS_DEMSTEP] (advanced by demBegin)
 __global__ void demPairs(Consts k, DemArgs a);
 __global__ void demGather(Consts k, DemArgs a);
+// dem_mixed.cu: the force passes of the mixed form (FP32 force laws)
+__global__ void demPairsMixed(Consts k, DemArgs a);
+__global__ void demGatherMixed(Consts k, DemArgs a);
 
 }  // namespace lbdem

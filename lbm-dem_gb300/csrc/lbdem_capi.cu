@@ -487,7 +487,8 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   AL(d.gorder, P1 * MAX_N);
   // each owner pair is one slot of one list: at most (MAX_N - 1) / 2 per particle
   AL(d.pairList, (size_t)P1 * (MAX_N / 2));
-  AL(d.pairbuf, P1 * MAX_N * PAIR_VALS);
+  // per slot PAIR_VALS doubles (plain form) or floats (mixed form)
+  AL(d.pairbuf, P1 * MAX_N * (k.mixed ? PAIR_VALS / 2 : PAIR_VALS));
   AL(d.pairflag, P1 * MAX_N);
   AL(d.pcell, P1);
   AL(d.ppos, P1);
@@ -597,9 +598,15 @@ extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
   demBegin<<<partGrid(ctx, 256), 256, 0, s>>>(k, a, 0);
   int rc = enqueueNeighbourList(ctx);
   if (rc) return rc;
-  demPairs<<<std::max(1, std::min(ctx->nPart * (MAX_N / 2) / 128 + 1, ctx->smCount * 16)), 128, 0,
-             s>>>(k, a);
-  demGather<<<partGrid(ctx, 128), 128, 0, s>>>(k, a);  // and the impactor update
+  const int pairGrid = std::max(1, std::min(ctx->nPart * (MAX_N / 2) / 128 + 1, ctx->smCount * 16));
+  // the gathers also update the impactor (last block)
+  if (k.mixed) {
+    demPairsMixed<<<pairGrid, 128, 0, s>>>(k, a);
+    demGatherMixed<<<partGrid(ctx, GATHER_THREADS), GATHER_THREADS, 0, s>>>(k, a);
+  } else {
+    demPairs<<<pairGrid, 128, 0, s>>>(k, a);
+    demGather<<<partGrid(ctx, GATHER_THREADS), GATHER_THREADS, 0, s>>>(k, a);
+  }
   ctx->launches += 1 + 9 + 2;
   return launchErr(ctx, "dem step");
 }
@@ -882,7 +889,7 @@ extern "C" int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t prec
   add(P1 * MAX_N, 4);                          // partner
   add(P1 * MAX_N, 4);                          // gorder
   add(P1 * (MAX_N / 2), 4);                    // pairList
-  add(P1 * MAX_N * PAIR_VALS, 8);              // pairbuf
+  add(P1 * MAX_N * (mixed ? PAIR_VALS / 2 : PAIR_VALS), 8);  // pairbuf
   add(P1 * MAX_N, 1);                          // pairflag
   add(P1, 4);
   add(P1, 4);                                  // pcell, ppos
