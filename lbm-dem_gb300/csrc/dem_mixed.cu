@@ -6,7 +6,9 @@
 //   near an impactor,
 // - the particle and impactor integration and the force totals it uses.
 // The per-pair contributions are stored as floats in the pair buffer; the
-// gather sums them in the same order as the plain form.
+// gather visits a particle's neighbour slots in slot order (any fixed order
+// keeps the sums deterministic; the mixed form does not follow the plain
+// form's order of the reference).
 //
 // Reference: DEM::evaluateForces (src/DEM.cpp:655-796) and the force
 // functions it calls; integration src/DEM.cpp:2676-2765.
@@ -56,18 +58,24 @@ __device__ __forceinline__ PairGeom<float> pairGeomM(double rad, const double* d
   return g;
 }
 
-// Offset of particle x from wall W along its normal, and its length; the
-// length in FP64 within NEAR_GAP radii of contact.
+// Offset of particle x from wall W along its normal, and its length: the
+// differences from the wall point in FP64, the rest in FP32 except within
+// NEAR_GAP radii of contact, where the offset is taken in FP64.
 __device__ __forceinline__ float wallGeomM(const DeviceWall& W, const double* x, double r,
                                            float* o) {
-  const double ox = (x[0] - W.p[0]) * W.n[0] * W.n[0];
-  const double oy = (x[1] - W.p[1]) * W.n[1] * W.n[1];
-  const double oz = (x[2] - W.p[2]) * W.n[2] * W.n[2];
-  o[0] = (float)ox;
-  o[1] = (float)oy;
-  o[2] = (float)oz;
+  const double d0 = x[0] - W.p[0], d1 = x[1] - W.p[1], d2 = x[2] - W.p[2];
+  const float n0 = (float)W.n[0], n1 = (float)W.n[1], n2 = (float)W.n[2];
+  o[0] = (float)d0 * n0 * n0;
+  o[1] = (float)d1 * n1 * n1;
+  o[2] = (float)d2 * n2 * n2;
   const float l = sqrtf(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]);
-  if (l < (float)((1.0 + NEAR_GAP) * r)) return (float)sqrt(ox * ox + oy * oy + oz * oz);
+  if (l < (float)((1.0 + NEAR_GAP) * r)) {
+    const double ox = d0 * W.n[0] * W.n[0], oy = d1 * W.n[1] * W.n[1], oz = d2 * W.n[2] * W.n[2];
+    o[0] = (float)ox;
+    o[1] = (float)oy;
+    o[2] = (float)oz;
+    return (float)sqrt(ox * ox + oy * oy + oz * oz);
+  }
   return l;
 }
 
@@ -159,29 +167,38 @@ __global__ void __launch_bounds__(GATHER_THREADS) demGatherMixed(Consts k, DemAr
     load3f(a.xiw, P, i, xiw);
     load3f(a.xio, P, i, xio);
     const int* li = L + (long long)i * MAX_N;
-    const int* go = a.gorder + (long long)i * MAX_N;
     const int* pt = a.partner + (long long)i * MAX_N;
     const int cnt = li[0];
-    float df[3], dt[3];
-    if (afterWait) {
-      for (int u = 0; u < cnt; ++u) {
-        const int s = go[u];
-        const int j = li[s];
-        if (j < i) {
-          if (a.pairflag[(long long)i * MAX_N + s] & 1) {
-            const float* pb = pbuf + ((long long)i * MAX_N + s) * PAIR_VALS;
-            add3f(FL, pb + 6);
-            add3f(ML, pb + 9);
-          }
+    // pairs: contact, electrostatics and (after the wait) lubrication, from
+    // the slot of the pair's owner (the higher index)
+#pragma unroll 4
+    for (int s = 1; s <= cnt; ++s) {
+      const int j = li[s];
+      const bool own = j < i;
+      const long long e = own ? (long long)i * MAX_N + s : (long long)j * MAX_N + pt[s];
+      const float* pb = pbuf + e * PAIR_VALS;
+      if (own) {
+        add3f(FC, pb);
+        add3f(FR, pb + 15);
+      } else {
+        sub3f(FC, pb);
+        sub3f(FR, pb + 15);
+      }
+      MC[0] += ra * pb[3];
+      MC[1] += ra * pb[4];
+      MC[2] += ra * pb[5];
+      if (afterWait && (a.pairflag[e] & 1)) {
+        if (own) {
+          add3f(FL, pb + 6);
+          add3f(ML, pb + 9);
         } else {
-          const long long js = (long long)j * MAX_N + pt[s];
-          if (a.pairflag[js] & 1) {
-            const float* pb = pbuf + js * PAIR_VALS;
-            sub3f(FL, pb + 6);
-            add3f(ML, pb + 12);
-          }
+          sub3f(FL, pb + 6);
+          add3f(ML, pb + 12);
         }
       }
+    }
+    float df[3], dt[3];
+    if (afterWait) {
       for (int w = 0; w < k.nWall; ++w) {
         float o[3];
         const float l = wallGeomM(a.walls[w], xa, raD, o);
@@ -231,24 +248,6 @@ __global__ void __launch_bounds__(GATHER_THREADS) demGatherMixed(Consts k, DemAr
       MC[0] += ra * dt[0];
       MC[1] += ra * dt[1];
       MC[2] += ra * dt[2];
-    }
-    // pair contact and electrostatics in the plain form's order
-    for (int u = 0; u < cnt; ++u) {
-      const int s = go[u];
-      const int j = li[s];
-      const bool own = j < i;
-      const float* pb =
-          pbuf + (own ? (long long)i * MAX_N + s : (long long)j * MAX_N + pt[s]) * PAIR_VALS;
-      if (own) {
-        add3f(FC, pb);
-        add3f(FR, pb + 15);
-      } else {
-        sub3f(FC, pb);
-        sub3f(FR, pb + 15);
-      }
-      MC[0] += ra * pb[3];
-      MC[1] += ra * pb[4];
-      MC[2] += ra * pb[5];
     }
     // walls
     {

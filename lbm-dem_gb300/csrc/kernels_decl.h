@@ -120,7 +120,7 @@ __global__ void voxelizeObjects(Consts k, uint8_t* mask, uint32_t* solid, uint8_
 __global__ void flagClaim(Consts k, const uint8_t* mask, uint32_t* claim, const double* px0,
                           const double* pr, const int* iscal, unsigned long long* uscal);
 __global__ void flagApply(Consts k, uint8_t* mask, uint32_t* solid, uint32_t* claim,
-                          const int* iscal, unsigned long long* uscal);
+                          int* iscal, unsigned long long* uscal);
 __global__ void findNewActiveKernel(Consts k, uint8_t* mask, uint32_t* solid,
                                     const double* px0, const double* pr, int* iscal,
                                     unsigned long long* uscal);

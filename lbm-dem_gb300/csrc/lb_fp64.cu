@@ -819,8 +819,10 @@ __global__ void flagClaim(Consts k, const uint8_t* mask, uint32_t* claim, const 
 // updateIndices, step 2: the flag reset of every node (solid index 0, walls
 // included) and the new flags (src/LB.cpp:689-693).
 __global__ void flagApply(Consts k, uint8_t* mask, uint32_t* solid, uint32_t* claim,
-                          const int* iscal, unsigned long long* uscal) {
+                          int* iscal, unsigned long long* uscal) {
   if (!iscal[IS_NEWNBR]) return;
+  // wall nodes are never claimed: from here on their solid index is 0
+  if (blockIdx.x == 0 && threadIdx.x == 0) iscal[IS_WALLS_RESET] = 1;
   unsigned long long first = ~0ull;
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
        x += (long long)gridDim.x * blockDim.x) {

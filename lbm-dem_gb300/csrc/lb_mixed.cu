@@ -491,66 +491,73 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
 // direction opp(j) of x (bounce-back), so the sums are formed here from the
 // lattice it wrote, before anything else changes it. Walls are the outer
 // node layer of the box (the only wall layout a run accepts), so only the
-// layer inside it is visited: 2 (XY + YZ + XZ) nodes instead of N.
+// layer inside it is visited, one face per blockIdx.y:
+//   0, 1: x = 1, X-2 (all inner y, z)        2, 3: y = 1, Y-2 (x inside them)
+//   4, 5: z = 1, Z-2 (x, y inside them)
+// Each force goes to the wall that the wall node's solid index names, as in
+// the reference: the wall setup gives a node on several faces the last of
+// their walls in face order x0, x1, y0, y1, z0, z1, and the first flag reset
+// (updateIndices) sets every wall node's index to 0 for good.
 __global__ void lbWallForceMixed(Consts k, LbArgs a) {
   __shared__ float accW[3 * MAX_WALL];
   for (int i = threadIdx.x; i < 3 * MAX_WALL; i += blockDim.x) accW[i] = 0.0f;
   __syncthreads();
   const int X = k.X, Y = k.Y, Z = k.Z;
-  const long long nx = X - 2, ny = Y - 2, nz = Z - 2;  // inner box 1..dim-2
+  const int face = blockIdx.y, axis = face >> 1;
+  // the face's node grid (u fastest, then v) and its fixed coordinate
+  const int ux0 = axis == 0 ? 1 : 2, nu = axis == 0 ? Y - 2 : X - 4;
+  const int vx0 = axis == 2 ? 2 : 1, nv = axis == 2 ? Y - 4 : Z - 2;
+  const int fixed = (face & 1) ? (axis == 0 ? X : axis == 1 ? Y : Z) - 2 : 1;
+  const bool reset = a.iscal[IS_WALLS_RESET] != 0;
+  // a lattice 3 nodes wide has one inner layer: its second face is the first
+  const bool dup = (face & 1) && fixed == 1;
   const float* gout = (const float*)a.fout;
-  const size_t NN = (size_t)k.N;
-  if (nx > 0 && ny > 0 && nz > 0) {
-    // faces x = 1, X-2 (all y, z); y = 1, Y-2 (x inside); z = 1, Z-2 (x, y inside)
-    const long long cA = ny * nz, cB = max(nx - 2, 0LL) * nz,
-                    cC = max(nx - 2, 0LL) * max(ny - 2, 0LL);
-    const int fA = nx > 1 ? 2 : 1, fB = ny > 1 ? 2 : 1, fC = nz > 1 ? 2 : 1;
-    const long long total = fA * cA + fB * cB + fC * cC;
-    float fw[3] = {0.0f, 0.0f, 0.0f};
-    int wcur = -1;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
+  const size_t NP = (size_t)k.NP;
+  float fw[3] = {0.0f, 0.0f, 0.0f};
+  int wcur = -1;
+  if (!dup && nu > 0 && nv > 0 && X > 2 && Y > 2 && Z > 2) {
+    const unsigned total = (unsigned)nu * (unsigned)nv;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += gridDim.x * blockDim.x) {
+      const int u = ux0 + (int)(t % (unsigned)nu), v = vx0 + (int)(t / (unsigned)nu);
       int ix, iy, iz;
-      if (i < fA * cA) {
-        const long long r = i % cA;
-        ix = i < cA ? 1 : X - 2;
-        iy = 1 + (int)(r % ny);
-        iz = 1 + (int)(r / ny);
-      } else if (i < fA * cA + fB * cB) {
-        const long long q = i - fA * cA, r = q % cB;
-        iy = q < cB ? 1 : Y - 2;
-        ix = 2 + (int)(r % (nx - 2));
-        iz = 1 + (int)(r / (nx - 2));
-      } else {
-        const long long q = i - fA * cA - fB * cB, r = q % cC;
-        iz = q < cC ? 1 : Z - 2;
-        ix = 2 + (int)(r % (nx - 2));
-        iy = 2 + (int)(r / (nx - 2));
-      }
-      const long long x = ix + iy * k.sy + iz * k.sz;
+      if (axis == 0) { ix = fixed; iy = u; iz = v; }
+      else if (axis == 1) { ix = u; iy = fixed; iz = v; }
+      else { ix = u; iy = v; iz = fixed; }
+      const unsigned x = (unsigned)ix + (unsigned)iy * (unsigned)k.sy + (unsigned)iz * (unsigned)k.sz;
       if (!isActiveT(a.mask[x] & TYPE_MASK)) continue;
-      // the outer layer is all wall nodes: the wall links follow from x
       const unsigned wl = boxWallLinks(k, ix, iy, iz);
 #pragma unroll
       for (int j = 1; j < Q; ++j) {
         if (!((wl >> j) & 1u)) continue;
-        const long long lk = x + nbrOffset(k, j);
-        const uint32_t w = a.solid[lk];
-        if (w >= (uint32_t)k.nWall) continue;
-        if ((int)w != wcur) {
+        const int tx = ix + CX(j), ty = iy + CY(j), tz = iz + CZ(j);
+        const int w = reset ? 0
+                    : tz == Z - 1 ? 5 : tz == 0 ? 4 : ty == Y - 1 ? 3 : ty == 0 ? 2
+                    : tx == X - 1 ? 1 : 0;
+        if (w >= k.nWall) continue;
+        if (w != wcur) {
           if (wcur >= 0)
             for (int c = 0; c < 3; ++c) atomicAdd(&accW[3 * wcur + c], fw[c]);
           fw[0] = fw[1] = fw[2] = 0.0f;
-          wcur = (int)w;
+          wcur = w;
         }
-        const float bb = 2.0f * gout[OPPJ(j) * (size_t)k.NP + x];
+        const float bb = 2.0f * gout[OPPJ(j) * NP + x];
         if (CX(j)) fw[0] += CX(j) > 0 ? bb : -bb;
         if (CY(j)) fw[1] += CY(j) > 0 ? bb : -bb;
         if (CZ(j)) fw[2] += CZ(j) > 0 ? bb : -bb;
       }
     }
-    if (wcur >= 0)
-      for (int c = 0; c < 3; ++c) atomicAdd(&accW[3 * wcur + c], fw[c]);
+  }
+  if (reset) {
+    // one wall: a warp sum, then one shared atomic per component
+    const unsigned FULLM = 0xffffffffu;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      for (int c = 0; c < 3; ++c) fw[c] += __shfl_xor_sync(FULLM, fw[c], o);
+    if ((threadIdx.x & 31) == 0 && k.nWall > 0)
+      for (int c = 0; c < 3; ++c) atomicAdd(&accW[c], fw[c]);
+  } else if (wcur >= 0) {
+    for (int c = 0; c < 3; ++c) atomicAdd(&accW[3 * wcur + c], fw[c]);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < 3 * MAX_WALL; i += blockDim.x)

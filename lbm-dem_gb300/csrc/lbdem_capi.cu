@@ -397,9 +397,10 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
     const int sm = std::max(1, ctx->smCount);
     // free surface: the interface box is about the free-surface area deep
     ctx->gridFs = cap((long long)k.X * k.Z / 32 + 1, sm * 4);
-    const long long shell =
-        2LL * ((long long)k.X * k.Y + (long long)k.Y * k.Z + (long long)k.X * k.Z);
-    ctx->gridShell = cap(shell / 256 + 1, sm * 8);
+    // wall-force sweep: blocks per box face (the largest face's inner nodes)
+    const long long face = std::max({(long long)k.Y * k.Z, (long long)k.X * k.Z,
+                                     (long long)k.X * k.Y});
+    ctx->gridShell = cap(face / 256 + 1, sm * 2);
     long long box = 0;
     for (int o = 0; o < cfg->n_objects; ++o) {
       const long long side = (long long)(2.0 * cfg->objects[o].r / L) + 6;
@@ -657,7 +658,7 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   else lbStepFp64<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
   if (ev) cudaEventRecord(ev->second, s);
   if (k.mixed && k.nWall > 0) {
-    lbWallForceMixed<<<ctx->gridShell, 256, 0, s>>>(k, a);
+    lbWallForceMixed<<<dim3(ctx->gridShell, 6), 256, 0, s>>>(k, a);
     ctx->launches += 1;
   }
   ctx->cur = 1 - ctx->cur;

@@ -155,6 +155,7 @@ enum {
   IS_DEMSTEP,               // DEM::demTimeStep, advanced by demBegin
   IS_GATHER_DONE,           // demGather: blocks done (the last one updates the impactors)
   IS_PAIRLIST_DONE,         // nbrPairList: blocks done (the last one swaps the lists)
+  IS_WALLS_RESET,           // set by the first flag reset: every wall node has solid index 0
   IS_COUNT
 };
 // offsets into Device::uscal
