@@ -113,6 +113,9 @@ __global__ void fsEmptyIsolated(Consts k, FsArgs a);
 __global__ void fsRedistribute(Consts k, FsArgs a);
 __global__ void uncoverCollect(Consts k, const uint8_t* mask, const double* obj,
                                uint32_t* list, int* iscal);
+// dynamic shared memory of uncoverResolve: candidates, their lower-index
+// candidate neighbours and states
+constexpr int UNCOVER_SMEM = UNCOVER_CAP * (4 + 9 * 2 + 1);
 __global__ void uncoverResolve(Consts k, uint8_t* mask, void* f, double* mass, float* nF,
                                uint32_t* list, int* iscal);
 __global__ void voxelizeObjects(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* objIdx,

@@ -362,7 +362,35 @@ __device__ __forceinline__ void blockAddDouble(double v, double* dst) {
 }
 
 
-// LB::updateMass (interface part).
+// Post-collision populations of interface node x (deviations in the mixed
+// form), recomputed from its pre-collision populations for the links into
+// walls and impactors. Kept out of line: few nodes need it, and inlined it
+// would set the register count of the whole mass update.
+__device__ __noinline__ void fsPostCollision(const Consts& k, const FsArgs& a, long long x,
+                                             uint8_t m, int ix, int iy, int iz, double* fsl) {
+  const bool pf = (m & PFLAG) != 0;
+  if (k.mixed) {
+    float g[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) g[q] = ((const float*)a.fold)[(long long)q * k.NP + x];
+    NodeStateF s;
+    const uint32_t pid = pf ? a.solid[x] : 0u;
+    const bool coupled = pf && pid < (uint32_t)k.nPart;
+    const KinF kin = coupled ? loadKinF(a.pkf, pid) : KinF{};
+    collideNodeMixed(k, g, coupled, kin, (float)a.massNew[x], ix, iy, iz, s);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) fsl[q] = (double)g[q];
+  } else {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) fsl[q] = ((const double*)a.fold)[(long long)q * k.NP + x];
+    NodeState s;
+    collideNode(k, fsl, pf, pf ? a.solid[x] : 0u, a.pkd, a.pkd + 3 * k.nPart, a.pw1, k.nPart,
+                a.massNew[x], ix, iy, iz, s);
+  }
+}
+
+// LB::updateMass (interface part). The neighbour types are read first, all
+// links at once; the mass exchange terms are then summed in link order.
 __global__ void fsUpdateMass(Consts k, FsArgs a) {
   // the free-surface step's surplus and interface count start from zero
   // (fsUpdateMass itself accumulates neither)
@@ -374,41 +402,27 @@ __global__ void fsUpdateMass(Consts k, FsArgs a) {
     const uint8_t m = a.mask[x];
     if ((m & TYPE_MASK) != 3) continue;
     const double mx = a.mass[x];
+    // links to fluid or interface nodes, to interface nodes, to walls/impactors
+    unsigned liq = 0, ifc = 0, wal = 0;
+#pragma unroll
+    for (int j = 1; j < Q; ++j) {
+      const int tl = a.mask[x + nbrOffset(k, j)] & TYPE_MASK;
+      liq |= (unsigned)(tl == 3 || tl == 0) << j;
+      ifc |= (unsigned)(tl == 3) << j;
+      wal |= (unsigned)(tl == 8 || tl == 12 || tl == 9) << j;
+    }
     double fsl[Q];
-    bool haveFs = false;
+    if (wal) fsPostCollision(k, a, x, m, ix, iy, iz, fsl);
     double delta = 0.0;
     bool first = true;
-#pragma unroll 1
+#pragma unroll
     for (int j = 1; j < Q; ++j) {
-      const long long lk = x + nbrOffset(k, j);
-      const int tl = a.mask[lk] & TYPE_MASK;
       double term;
-      if (tl == 3 || tl == 0) {
+      if ((liq >> j) & 1u) {
+        const long long lk = x + nbrOffset(k, j);
         const double ms = fdiff(k, a.fcur, OPPJ(j), x, j, lk);
-        term = tl == 3 ? 0.5 * (a.mass[lk] + mx) * ms : 1.0 * ms;
-      } else if (tl == 8 || tl == 12 || tl == 9) {
-        if (!haveFs) {  // post-collision populations of this node, recomputed
-          const bool pf = (m & PFLAG) != 0;
-          if (k.mixed) {
-            float g[Q];
-#pragma unroll
-            for (int q = 0; q < Q; ++q) g[q] = ((const float*)a.fold)[(long long)q * k.NP + x];
-            NodeStateF s;
-            const uint32_t pid = pf ? a.solid[x] : 0u;
-            const bool coupled = pf && pid < (uint32_t)k.nPart;
-            const KinF kin = coupled ? loadKinF(a.pkf, pid) : KinF{};
-            collideNodeMixed(k, g, coupled, kin, (float)a.massNew[x], ix, iy, iz, s);
-#pragma unroll
-            for (int q = 0; q < Q; ++q) fsl[q] = (double)g[q];  // deviations
-          } else {
-#pragma unroll
-            for (int q = 0; q < Q; ++q) fsl[q] = ((const double*)a.fold)[(long long)q * k.NP + x];
-            NodeState s;
-            collideNode(k, fsl, pf, pf ? a.solid[x] : 0u, a.pkd, a.pkd + 3 * k.nPart, a.pw1, k.nPart,
-                        a.massNew[x], ix, iy, iz, s);
-          }
-          haveFs = true;
-        }
+        term = ((ifc >> j) & 1u) ? 0.5 * (a.mass[lk] + mx) * ms : 1.0 * ms;
+      } else if ((wal >> j) & 1u) {
         // f_opp(x) after streaming minus the population x sent into the wall
         const double ms = k.mixed
             ? (double)((const float*)a.fcur)[(long long)OPPJ(j) * k.NP + x] - fsl[j]
@@ -650,12 +664,16 @@ __global__ void uncoverCollect(Consts k, const uint8_t* mask, const double* obj,
 // findNewActiveObject, step 2 (one CTA): resolve the uncovered nodes in the
 // reference's serial order (ascending node index, each node seeing the new
 // types of the lower-index ones) by fixed-point iteration, then initialise
-// them (src/LB.cpp:874-940).
+// them (src/LB.cpp:874-940). Dynamic shared memory (UNCOVER_SMEM bytes):
+// the sorted candidates, for each the indices of its lower-index candidate
+// neighbours (at most the 9 links with a negative node offset), and its state.
 __global__ void __launch_bounds__(1024) uncoverResolve(Consts k, uint8_t* mask, void* f,
                                                        double* mass, float* nF, uint32_t* list,
                                                        int* iscal) {
-  __shared__ uint32_t s_idx[UNCOVER_CAP];
-  __shared__ uint8_t s_st[UNCOVER_CAP];
+  extern __shared__ __align__(16) unsigned char uncoverSmem[];
+  uint32_t* s_idx = reinterpret_cast<uint32_t*>(uncoverSmem);          // [UNCOVER_CAP]
+  int16_t* s_back = reinterpret_cast<int16_t*>(s_idx + UNCOVER_CAP);   // [UNCOVER_CAP][9]
+  uint8_t* s_st = reinterpret_cast<uint8_t*>(s_back + 9 * UNCOVER_CAP);  // [UNCOVER_CAP]
   int n = min(iscal[IS_NUNCOVER], UNCOVER_CAP);
   if (n == 0) return;
   int p2 = 1;
@@ -680,40 +698,71 @@ __global__ void __launch_bounds__(1024) uncoverResolve(Consts k, uint8_t* mask, 
     }
   // the same node can appear once per object box: drop duplicates
   __shared__ int s_n;
-  if (threadIdx.x == 0) {
-    int w = 0;
-    for (int i = 0; i < n; ++i)
-      if (i == 0 || s_idx[i] != s_idx[i - 1]) s_idx[w++] = s_idx[i];
-    s_n = w;
+  if (k.nObj > 1) {
+    if (threadIdx.x == 0) {
+      int w = 0;
+      for (int i = 0; i < n; ++i)
+        if (i == 0 || s_idx[i] != s_idx[i - 1]) s_idx[w++] = s_idx[i];
+      s_n = w;
+    }
+    __syncthreads();
+    n = s_n;
   }
-  __syncthreads();
-  n = s_n;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s_st[i] = 12;
-  __syncthreads();
-  auto typeOf = [&](long long lk, int self) -> int {
-    // binary search among the candidates
+  auto find = [&](uint32_t lk) -> int {  // binary search among the candidates
     int lo = 0, hi = n - 1;
     while (lo <= hi) {
       const int mid = (lo + hi) >> 1;
       const uint32_t v = s_idx[mid];
-      if (v == (uint32_t)lk) return mid < self ? (int)s_st[mid] : 12;
-      if (v < (uint32_t)lk) lo = mid + 1;
+      if (v == lk) return mid;
+      if (v < lk) lo = mid + 1;
       else hi = mid - 1;
     }
-    return mask[lk] & TYPE_MASK;
+    return -1;
   };
+  // One pass over each candidate's links (within the lattice: an impactor
+  // that reaches the outer layer turns wall nodes into impactor nodes):
+  // - a non-candidate neighbour gives a fixed type: s_st bit 4 for a fluid,
+  //   bit 5 for a gas neighbour;
+  // - a lower-index candidate is recorded in s_back;
+  // - a higher-index candidate reads as an impactor node and gives nothing.
+  // s_st bits 0-3 hold the candidate's state, 12 while unresolved.
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const uint32_t x = s_idx[i];
+    int ix, iy, iz;
+    coords(k, (long long)x, ix, iy, iz);
+    uint8_t fix = 0;
+    int nb = 0;
+    for (int j = 1; j < Q; ++j) {
+      const int tx = ix + CX(j), ty = iy + CY(j), tz = iz + CZ(j);
+      if (tx < 0 || tx >= k.X || ty < 0 || ty >= k.Y || tz < 0 || tz >= k.Z) continue;
+      const uint32_t lk = x + (uint32_t)nbrOffset(k, j);
+      const int mid = find(lk);
+      if (mid < 0) {
+        const int tl = mask[lk] & TYPE_MASK;
+        fix |= (uint8_t)((tl == 0 ? 0x10 : 0) | (tl == 2 ? 0x20 : 0));
+      } else if (mid < i && nb < 9) {
+        s_back[9 * i + nb++] = (int16_t)mid;
+      }
+    }
+    for (int b = nb; b < 9; ++b) s_back[9 * i + b] = -1;
+    s_st[i] = (uint8_t)(12 | fix);
+  }
+  __syncthreads();
   for (int iter = 0; iter <= n; ++iter) {
     int changed = 0;
     uint8_t nst[UNCOVER_CAP / 1024];
     for (int i = threadIdx.x, q = 0; i < n; i += blockDim.x, ++q) {
-      const long long x = s_idx[i];
-      bool fluidNb = false, gasNb = false;
-      for (int j = 1; j < Q; ++j) {
-        const int tl = typeOf(x + nbrOffset(k, j), i);
+      const uint8_t me = s_st[i];
+      bool fluidNb = (me & 0x10) != 0, gasNb = (me & 0x20) != 0;
+#pragma unroll
+      for (int b = 0; b < 9; ++b) {
+        const int m = s_back[9 * i + b];
+        if (m < 0) break;
+        const int tl = s_st[m] & 0x0F;
         fluidNb |= tl == 0;
         gasNb |= tl == 2;
       }
-      nst[q] = !fluidNb ? 2 : gasNb ? 3 : 0;
+      nst[q] = (uint8_t)((me & 0x30) | (!fluidNb ? 2 : gasNb ? 3 : 0));
     }
     __syncthreads();
     for (int i = threadIdx.x, q = 0; i < n; i += blockDim.x, ++q)
@@ -726,7 +775,7 @@ __global__ void __launch_bounds__(1024) uncoverResolve(Consts k, uint8_t* mask, 
   const double rho0 = k.initDensity;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const long long x = s_idx[i];
-    const int st = s_st[i];
+    const int st = s_st[i] & 0x0F;
     const uint8_t m = mask[x];
     mask[x] = (uint8_t)((m & ~TYPE_MASK) | st);
     if (st != 2) markActive(k, x);

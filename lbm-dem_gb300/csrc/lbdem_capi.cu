@@ -242,6 +242,8 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
     int perSm = 0;
     CK(cudaFuncSetAttribute(lbStepMixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             MIXED_SMEM));
+    CK(cudaFuncSetAttribute(uncoverResolve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            UNCOVER_SMEM));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, lbStepMixed, MIXED_THREADS,
                                                      MIXED_SMEM));
     ctx->lbMixedBlocks = std::max(1, perSm) * std::max(1, ctx->smCount);
@@ -622,7 +624,7 @@ extern "C" int lbdem_coupling_step(lbdem_ctx* ctx) {
   if (ctx->nObj > 0) {
     cudaMemsetAsync(d.iscal + IS_NUNCOVER, 0, sizeof(int), s);
     uncoverCollect<<<ctx->gridObj, 256, 0, s>>>(k, d.mask, d.obj, d.uncover, d.iscal);
-    uncoverResolve<<<1, 1024, 0, s>>>(k, d.mask, d.f[ctx->cur], d.mass, d.nF, d.uncover,
+    uncoverResolve<<<1, 1024, UNCOVER_SMEM, s>>>(k, d.mask, d.f[ctx->cur], d.mass, d.nF, d.uncover,
                                       d.iscal);
     voxelizeObjects<<<ctx->gridObj, 256, 0, s>>>(k, d.mask, d.solid, d.objIdx, d.mass, d.obj);
     ctx->launches += 3;
