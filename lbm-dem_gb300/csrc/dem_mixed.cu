@@ -144,14 +144,33 @@ __global__ void demPairsMixed(Consts k, DemArgs a) {
 __global__ void __launch_bounds__(GATHER_THREADS) demGatherMixed(Consts k, DemArgs a) {
   const int stepNo = a.iscal[IS_DEMSTEP];
   __shared__ double acc[GA_N];
+  __shared__ DeviceWall sW[MAX_WALL];
+  __shared__ float sWp[MAX_WALL][3], sWn[MAX_WALL][3];
   for (int t = threadIdx.x; t < GA_N; t += blockDim.x) acc[t] = 0.0;
+  if (threadIdx.x < (unsigned)k.nWall) {
+    const DeviceWall W = a.walls[threadIdx.x];
+    sW[threadIdx.x] = W;
+    for (int c = 0; c < 3; ++c) {
+      sWp[threadIdx.x][c] = (float)W.p[c];
+      sWn[threadIdx.x][c] = (float)W.n[c];
+    }
+  }
   __syncthreads();
+  // reach of the wall forces beyond a particle's radius: the largest
+  // lubrication range, plus a margin far above the FP32 error of the test
+  const float wallReach =
+      (float)tmax(k.lubCut, tmax(k.lubN, tmax(k.lubT, k.lubR))) + 0.01f;
   const int cur = a.iscal[IS_LISTCUR];
   const int* L = a.list[cur];
   const float* pbuf = reinterpret_cast<const float*>(a.pairbuf);
   const int P = k.nPart;
   const bool afterWait = stepNo >= k.objWaitTime;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+  // particles in the cell list's order (from the last rebuild), so that a
+  // warp holds neighbours in space and few of its lanes branch into the wall
+  // terms; the particle index order where the direct-sum branch is in use
+  const int* order = a.iscal[IS_DIRECT] ? nullptr : a.cellParts;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P; t += gridDim.x * blockDim.x) {
+    const int i = order ? order[t] : t;
     double xa[3], va[3];
     load3(a.x0, P, i, xa);
     load3(a.x1, P, i, va);
@@ -166,6 +185,12 @@ __global__ void __launch_bounds__(GATHER_THREADS) demGatherMixed(Consts k, DemAr
     float xiw[3], xio[3];
     load3f(a.xiw, P, i, xiw);
     load3f(a.xio, P, i, xio);
+    // the terms of the totals, loaded up front
+    double FH[3], MH[3], FG[3];
+    load3(a.FHydro, P, i, FH);
+    load3(a.MHydro, P, i, MH);
+    load3(a.FGrav, P, i, FG);
+    const double im = a.invm[i], iI = a.invI[i];
     const int* li = L + (long long)i * MAX_N;
     const int* pt = a.partner + (long long)i * MAX_N;
     const int cnt = li[0];
@@ -197,11 +222,28 @@ __global__ void __launch_bounds__(GATHER_THREADS) demGatherMixed(Consts k, DemAr
         }
       }
     }
+    // walls a force can reach (FP32 distance test); the others give no
+    // force and reset the wall spring, as the contact law does out of contact
+    unsigned nearW = 0;
+    {
+      const float xf[3] = {(float)xa[0], (float)xa[1], (float)xa[2]};
+      for (int w = 0; w < k.nWall; ++w) {
+        float l2 = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float oc = (xf[c] - sWp[w][c]) * sWn[w][c] * sWn[w][c];
+          l2 += oc * oc;
+        }
+        const float lim = ra + wallReach;
+        if (l2 < lim * lim) nearW |= 1u << w;
+      }
+    }
     float df[3], dt[3];
     if (afterWait) {
       for (int w = 0; w < k.nWall; ++w) {
+        if (!((nearW >> w) & 1u)) continue;
         float o[3];
-        const float l = wallGeomM(a.walls[w], xa, raD, o);
+        const float l = wallGeomM(sW[w], xa, raD, o);
         float F[3], Tq[3];
         if (wallLubOne(k, ra, vaf, wa, o[0], o[1], o[2], l, F, Tq)) {
           add3f(FL, F);
@@ -253,8 +295,12 @@ __global__ void __launch_bounds__(GATHER_THREADS) demGatherMixed(Consts k, DemAr
     {
       float nst[3] = {0.0f, 0.0f, 0.0f};
       for (int w = 0; w < k.nWall; ++w) {
+        if (!((nearW >> w) & 1u)) {
+          xiw[0] = xiw[1] = xiw[2] = 0.0f;
+          continue;
+        }
         float o[3];
-        const float l = wallGeomM(a.walls[w], xa, raD, o);
+        const float l = wallGeomM(sW[w], xa, raD, o);
         wallContactOne(k, ra, vaf, wa, xiw, o[0], o[1], o[2], l, nst, df, dt);
         add3f(FC, df);
         MC[0] += ra * dt[0];
@@ -265,11 +311,7 @@ __global__ void __launch_bounds__(GATHER_THREADS) demGatherMixed(Consts k, DemAr
       }
     }
     // totals and integration in FP64
-    double FH[3], MH[3], FG[3];
-    load3(a.FHydro, P, i, FH);
-    load3(a.MHydro, P, i, MH);
-    load3(a.FGrav, P, i, FG);
-    const double dtt = k.dt, im = a.invm[i], iI = a.invI[i];
+    const double dtt = k.dt;
     for (int c = 0; c < 3; ++c) {
       const double FT = FH[c] + (double)FC[c] + (double)FL[c] + FG[c] + (double)FR[c];
       const double MT = MH[c] + (double)MC[c] + (double)ML[c];
