@@ -133,7 +133,10 @@ typedef struct lbdem_options {
   int32_t precision;   /* LBDEM_PLAIN_FP64 or LBDEM_MIXED                 */
   int32_t device;      /* CUDA device ordinal                             */
   int32_t check_every; /* NaN/Inf guard cadence in steps (0 = off)        */
-  int32_t reserved[5];
+  int32_t chunks_per_block; /* mixed lattice step: 256-node chunks per block
+                               at least (0: 8); fewer blocks for a small
+                               lattice leave SMs to other runs            */
+  int32_t reserved[4];
 } lbdem_options;
 
 typedef struct lbdem_ctx lbdem_ctx;
@@ -285,7 +288,12 @@ typedef struct lbdem_server_options {
   int32_t max_active;     /* runs resident at once                         */
   int32_t slice_cycles;   /* goCycles enqueued per run per turn            */
   int64_t device_budget_bytes; /* 0: 90 % of the free memory at creation   */
-  int32_t reserved[6];
+  int32_t solo_runs;      /* 1: every run on its own stream only (no launches
+                             shared by several runs)                        */
+  int32_t batch_runs;     /* runs per batch group, each group on its own
+                             stream (0: 6)                                  */
+  int32_t chunks_per_block; /* passed to every run (lbdem_options)         */
+  int32_t reserved[3];
 } lbdem_server_options;
 
 typedef struct lbdem_job_result {
@@ -297,15 +305,21 @@ typedef struct lbdem_job_result {
   double fluid_mass;      /* as lbdem_mass_summary                         */
   int64_t active_node_updates;
   int64_t device_bytes;   /* the run's footprint estimate                  */
+  int32_t batched_cycles; /* cycles run in launches shared with other runs */
+  int32_t reserved;
 } lbdem_job_result;
 
 /* Jobs queue in submission order. A job is admitted when its footprint fits
  * the budget next to the runs in progress and fewer than max_active runs
  * are resident. Each admitted job is a context with its own stream, and
  * lbdem_server_poll advances every resident run by slice_cycles goCycles
- * per turn, so their kernels overlap on the device. A finished run frees
- * its memory for the next job. The server's calls must come from one host
- * thread. */
+ * per turn. Runs in their steady cycle with the same switches (free
+ * surface, impactor, walls) are advanced in batch groups of up to
+ * batch_runs runs: one launch per kernel for all runs of a group (grid
+ * z = run), the pair of cycles captured in a CUDA graph that is rebuilt when
+ * the group's runs change, each group on its own stream; the other runs
+ * advance on their own streams. A finished run frees its memory for the
+ * next job. The server's calls must come from one host thread. */
 int lbdem_server_create(const lbdem_server_options* opt, lbdem_server** out);
 /* Queue a run of `cycles` goCycles; the configuration and its tables are
  * copied. A run larger than the whole budget is refused (LBDEM_ERR_OOM). */

@@ -451,33 +451,54 @@ __device__ __forceinline__ void sub3(double* a, const double* b) {
 enum { GA_OBJ = 0, GA_WALL = GA_OBJ + 12 * MAX_OBJ, GA_N = GA_WALL + 6 * MAX_WALL };
 
 // Impactor totals and integration, wall totals (src/DEM.cpp:773-790,
-// 2742-2760), by the last block of demGather once every block's impactor
-// and wall sums are in.
-__device__ __forceinline__ void demObjectsTail(const Consts& k, DemArgs& a) {
+// 2742-2760), by the last block of the gather once every block's impactor
+// and wall sums are in. The record is read with ld.global.cg (past L1, so
+// no line this block cached earlier in the kernel can be stale) in one batch
+// of independent loads, then written back.
+__device__ __forceinline__ void demObjectsTail(const Consts& k, const DemArgs& a) {
   const int stepNo = a.iscal[IS_DEMSTEP];
   const int o = threadIdx.x;
-  // volatile: the sums other blocks added must not come from a line this
-  // block's L1 cached earlier in the kernel
   if (o < k.nObj) {
-    volatile double* ob = a.obj + o * OB_STRIDE;
-    const double dtt = k.dt;
+    double* ob = a.obj + o * OB_STRIDE;
+    double FH[3], FC[3], FL[3], FG[3], MH[3], MC[3], ML[3], X0[3], X1[3], W1[3];
+#pragma unroll
     for (int c = 0; c < 3; ++c) {
-      ob[OB_FTOTAL + c] =
-          0.0 + ((((ob[OB_FHYDRO + c] + ob[OB_FCONTACT + c]) + ob[OB_FLUB + c]) + ob[OB_FGRAV + c]) +
-                 0.0);
-      ob[OB_MTOTAL + c] = 0.0 + ((ob[OB_MHYDRO + c] + ob[OB_MCONTACT + c]) + ob[OB_MLUB + c]);
+      FH[c] = __ldcg(ob + OB_FHYDRO + c);
+      FC[c] = __ldcg(ob + OB_FCONTACT + c);
+      FL[c] = __ldcg(ob + OB_FLUB + c);
+      FG[c] = __ldcg(ob + OB_FGRAV + c);
+      MH[c] = __ldcg(ob + OB_MHYDRO + c);
+      MC[c] = __ldcg(ob + OB_MCONTACT + c);
+      ML[c] = __ldcg(ob + OB_MLUB + c);
+      X0[c] = __ldcg(ob + OB_X0 + c);
+      X1[c] = __ldcg(ob + OB_X1 + c);
+      W1[c] = __ldcg(ob + OB_W1 + c);
+    }
+    const double invm = __ldcg(ob + OB_INVM), invI = __ldcg(ob + OB_INVI);
+    const double dtt = k.dt;
+    double FT[3], MT[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      FT[c] = 0.0 + ((((FH[c] + FC[c]) + FL[c]) + FG[c]) + 0.0);
+      MT[c] = 0.0 + ((MH[c] + MC[c]) + ML[c]);
+      ob[OB_FTOTAL + c] = FT[c];
+      ob[OB_MTOTAL + c] = MT[c];
     }
     if (stepNo >= k.objWaitTime)
+#pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const double x1 = ob[OB_X1 + c];
-        ob[OB_X0 + c] += dtt * x1 + dtt * dtt * ob[OB_FTOTAL + c] * ob[OB_INVM];
-        ob[OB_X1 + c] = x1 + dtt * ob[OB_FTOTAL + c] * ob[OB_INVM];
-        ob[OB_W1 + c] += dtt * ob[OB_MTOTAL + c] * ob[OB_INVI];
+        ob[OB_X0 + c] = X0[c] + (dtt * X1[c] + dtt * dtt * FT[c] * invm);
+        ob[OB_X1 + c] = X1[c] + dtt * FT[c] * invm;
+        ob[OB_W1 + c] = W1[c] + dtt * MT[c] * invI;
       }
   }
   if (o < k.nWall) {
-    volatile double* w = a.wallF + o * 12;
-    for (int c = 0; c < 3; ++c) w[9 + c] = 0.0 + (((w[c] + w[3 + c]) + w[6 + c]) + 0.0);
+    double* w = a.wallF + o * 12;
+    double v[9];
+#pragma unroll
+    for (int c = 0; c < 9; ++c) v[c] = __ldcg(w + c);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) w[9 + c] = 0.0 + (((v[c] + v[3 + c]) + v[6 + c]) + 0.0);
   }
 }
 

@@ -27,6 +27,11 @@ __device__ __forceinline__ int s_int(double x) { return x >= 0 ? (int)x : (int)(
 __device__ __forceinline__ int n_int(double x) { return x >= 0 ? (int)(x + 0.5) : (int)(x - 0.5); }
 __device__ __forceinline__ double boxf(double a, double b) { return a - s_int(a / b) * b; }
 __device__ __forceinline__ double n_image(double a, double b) { return a - n_int(a / b) * b; }
+// n_image without the division where |a| <= b/4: there a/b rounds into
+// [-0.25, 0.25], n_int gives 0 and the result is a itself
+__device__ __forceinline__ double n_image_near(double a, double b) {
+  return fabs(a) <= 0.25 * b ? a : n_image(a, b);
+}
 __device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
 
 
@@ -36,7 +41,19 @@ __device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : 
 // (src/DEM.cpp:460-470, 368-378): the maximum of |x1|^2 over the particles
 // (exact in any order: atomicMax on the bit patterns of non-negative
 // doubles), then the last block to finish decides on a rebuild.
+__device__ __forceinline__ void demBeginBody(const Consts& k, const DemArgs& a, int forceRebuild);
 __global__ void __launch_bounds__(256) demBegin(Consts k, DemArgs a, int forceRebuild) {
+  demBeginBody(k, a, forceRebuild);
+}
+__global__ void __launch_bounds__(256) demBeginBatch(const JobArgs* jobs) {
+  __shared__ __align__(16) Consts sk;
+  __shared__ __align__(16) DemArgs sa;
+  stageRecord(sk, jobs[blockIdx.z].k);
+  stageRecord(sa, jobs[blockIdx.z].dem);
+  __syncthreads();
+  demBeginBody(sk, sa, 0);
+}
+__device__ __forceinline__ void demBeginBody(const Consts& k, const DemArgs& a, int forceRebuild) {
   __shared__ double red[8];
   __shared__ bool last;
   double m = 0.0;
@@ -93,7 +110,7 @@ __global__ void __launch_bounds__(256) demBegin(Consts k, DemArgs a, int forceRe
 
 // ---- neighbour list ---------------------------------------------------------
 
-__global__ void nbrCellAssign(Consts k, DemArgs a) {
+LBDEM_KERNEL(, nbrCellAssign, DemArgs, dem) {
   if (!a.iscal[IS_REBUILD] || a.iscal[IS_DIRECT]) return;
   const int nlx = a.iscal[IS_NL], nly = a.iscal[IS_NL + 1], nlz = a.iscal[IS_NL + 2];
   const int P = k.nPart;
@@ -115,7 +132,7 @@ __global__ void nbrCellAssign(Consts k, DemArgs a) {
 }
 
 // exclusive scan of the cell counts (one CTA) and the occupancy check
-__global__ void __launch_bounds__(1024) nbrCellScan(Consts k, DemArgs a) {
+LBDEM_KERNEL(__launch_bounds__(1024), nbrCellScan, DemArgs, dem) {
   if (!a.iscal[IS_REBUILD] || a.iscal[IS_DIRECT]) return;
   __shared__ int carry;
   __shared__ int wsum[32];
@@ -154,7 +171,7 @@ __global__ void __launch_bounds__(1024) nbrCellScan(Consts k, DemArgs a) {
   }
 }
 
-__global__ void nbrCellScatter(Consts k, DemArgs a) {
+LBDEM_KERNEL(, nbrCellScatter, DemArgs, dem) {
   if (!a.iscal[IS_REBUILD] || a.iscal[IS_DIRECT]) return;
   const int P = k.nPart;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
@@ -167,7 +184,7 @@ __global__ void nbrCellScatter(Consts k, DemArgs a) {
 
 // particles of a cell in ascending index order (the reference fills cells in
 // particle order, src/DEM.cpp:567-583); positions are 1-based
-__global__ void nbrCellSort(Consts k, DemArgs a) {
+LBDEM_KERNEL(, nbrCellSort, DemArgs, dem) {
   if (!a.iscal[IS_REBUILD] || a.iscal[IS_DIRECT]) return;
   const int ncell = a.iscal[IS_NL] * a.iscal[IS_NL + 1] * a.iscal[IS_NL + 2];
   for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < ncell; l += gridDim.x * blockDim.x) {
@@ -189,9 +206,9 @@ __global__ void nbrCellSort(Consts k, DemArgs a) {
 
 __device__ __forceinline__ bool nbrWithin(const Consts& k, const double* x0, const double* r,
                                           int P, int n1, int n2) {
-  const double x12 = n_image(x0[n1] - x0[n2], k.demSize[0]);
-  const double y12 = n_image(x0[P + n1] - x0[P + n2], k.demSize[1]);
-  const double z12 = n_image(x0[2 * P + n1] - x0[2 * P + n2], k.demSize[2]);
+  const double x12 = n_image_near(x0[n1] - x0[n2], k.demSize[0]);
+  const double y12 = n_image_near(x0[P + n1] - x0[P + n2], k.demSize[1]);
+  const double z12 = n_image_near(x0[2 * P + n1] - x0[2 * P + n2], k.demSize[2]);
   const double r12 = x12 * x12 + y12 * y12 + z12 * z12;
   const double cut = r[n1] + r[n2] + 2.0;
   return r12 <= cut * cut;
@@ -200,7 +217,7 @@ __device__ __forceinline__ bool nbrWithin(const Consts& k, const double* x0, con
 // New list of each particle: the events of the reference's cell sweep that
 // involve it, sorted by (cell l1, neighbour-cell order, position of n1 in
 // l1, position of n2 in l2) - the order in which the reference appends them.
-__global__ void nbrBuildCells(Consts k, DemArgs a) {
+LBDEM_KERNEL(, nbrBuildCells, DemArgs, dem) {
   if (!a.iscal[IS_REBUILD] || a.iscal[IS_DIRECT]) return;
   const int cur = a.iscal[IS_LISTCUR];
   const int* oldList = a.list[cur];
@@ -283,7 +300,7 @@ __global__ void nbrBuildCells(Consts k, DemArgs a) {
 }
 
 // Direct-sum branch (src/DEM.cpp:515-554): lists in (n1, n2) order.
-__global__ void nbrBuildDirect(Consts k, DemArgs a) {
+LBDEM_KERNEL(, nbrBuildDirect, DemArgs, dem) {
   if (!a.iscal[IS_REBUILD] || !a.iscal[IS_DIRECT]) return;
   const int cur = a.iscal[IS_LISTCUR];
   int* newList = a.list[1 - cur];
@@ -306,7 +323,7 @@ __global__ void nbrBuildDirect(Consts k, DemArgs a) {
 
 // Direct-sum history: unmatched slots take the value the reference's
 // cross-copy leaves there (the old spring of n2 at n2's new slot).
-__global__ void nbrDirectHistory(Consts k, DemArgs a) {
+LBDEM_KERNEL(, nbrDirectHistory, DemArgs, dem) {
   if (!a.iscal[IS_REBUILD] || !a.iscal[IS_DIRECT]) return;
   const int cur = a.iscal[IS_LISTCUR];
   const int* oldList = a.list[cur];
@@ -343,7 +360,7 @@ __global__ void nbrDirectHistory(Consts k, DemArgs a) {
 }
 
 // Partner slots and the gather order of every list.
-__global__ void nbrPartners(Consts k, DemArgs a) {
+LBDEM_KERNEL(, nbrPartners, DemArgs, dem) {
   if (!a.iscal[IS_REBUILD]) return;
   const int cur = 1 - a.iscal[IS_LISTCUR];
   const int* L = a.list[cur];
@@ -393,7 +410,7 @@ __global__ void nbrPartners(Consts k, DemArgs a) {
 // Owner slots of the new lists (slot s of particle i with list[i][s] < i),
 // so that the pair pass runs one thread per pair. The order of the entries
 // does not matter: every pair writes only its own slot's outputs.
-__global__ void nbrPairList(Consts k, DemArgs a) {
+LBDEM_KERNEL(, nbrPairList, DemArgs, dem) {
   if (!a.iscal[IS_REBUILD]) return;
   const int* L = a.list[1 - a.iscal[IS_LISTCUR]];
   const long long total = (long long)k.nPart * MAX_N;
@@ -424,7 +441,7 @@ __global__ void nbrPairList(Consts k, DemArgs a) {
 
 // Owner pass: every pair (n1 > n2) evaluated once from n1's slot, one
 // thread per entry of the owner-pair list.
-__global__ void demPairs(Consts k, DemArgs a) {
+LBDEM_KERNEL(, demPairs, DemArgs, dem) {
   // lubrication only after objWaitTime (src/DEM.cpp:716-725)
   const bool lubOn = a.iscal[IS_DEMSTEP] >= k.objWaitTime;
   const int cur = a.iscal[IS_LISTCUR];
@@ -464,7 +481,7 @@ __global__ void demPairs(Consts k, DemArgs a) {
 
 
 
-__global__ void __launch_bounds__(GATHER_THREADS) demGather(Consts k, DemArgs a) {
+LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGather, DemArgs, dem) {
   const int stepNo = a.iscal[IS_DEMSTEP];
   __shared__ double acc[GA_N];
   for (int t = threadIdx.x; t < GA_N; t += blockDim.x) acc[t] = 0.0;

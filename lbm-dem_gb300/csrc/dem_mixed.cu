@@ -94,7 +94,7 @@ __device__ __forceinline__ void sub3f(float* a, const float* b) {
 
 // Owner pass: every pair (n1 > n2) evaluated once from n1's slot, one thread
 // per entry of the owner-pair list; contributions stored as floats.
-__global__ void demPairsMixed(Consts k, DemArgs a) {
+LBDEM_KERNEL(, demPairsMixed, DemArgs, dem) {
   const bool lubOn = a.iscal[IS_DEMSTEP] >= k.objWaitTime;
   const int cur = a.iscal[IS_LISTCUR];
   const int* L = a.list[cur];
@@ -141,7 +141,7 @@ __global__ void demPairsMixed(Consts k, DemArgs a) {
 
 // Gather, wall and impactor terms and integration, one thread per particle:
 // the plain form's demGather with FP32 force sums.
-__global__ void __launch_bounds__(GATHER_THREADS) demGatherMixed(Consts k, DemArgs a) {
+LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGatherMixed, DemArgs, dem) {
   const int stepNo = a.iscal[IS_DEMSTEP];
   __shared__ double acc[GA_N];
   __shared__ DeviceWall sW[MAX_WALL];

@@ -79,6 +79,71 @@ struct DemArgs {
   unsigned long long* uscal;
 };
 
+// Pointers of one run's coupling kernels (impactor uncover and voxelisation,
+// particle flags), of the lattice step's preparation and finalisation.
+struct CoupArgs {
+  uint8_t* mask;
+  uint32_t* solid;
+  uint8_t* objIdx;
+  uint32_t* claim;
+  double* mass;
+  float* nF;
+  void* fcur;  // current lattice (uncovered nodes are initialised in it)
+  uint32_t* uncover;
+  double *px0, *px1, *pw1, *pr;
+  double* obj;
+  double* wallF;
+  double* scal;
+  int* iscal;
+  unsigned long long* uscal;
+  double* pAcc;  // hydrodynamic accumulators, reset by lbPrepare
+  long long pAccLen;
+  float* pAccF;
+  long long pAccFLen;
+  double* pkd;
+  float* pkf;
+  double *pF, *pM, *pV, *pS;  // particle force, torque, volume, stresslet
+  int redistribute;           // free surface on: mass redistribution
+};
+
+// Everything the per-cycle kernels of one run take. Launches that advance
+// many runs at once (blockIdx.z = run) read one record per run; a run has one
+// record per cycle parity (the lattice buffers swap every cycle).
+struct JobArgs {
+  Consts k;
+  DemArgs dem;
+  LbArgs lb;
+  FsArgs fs;
+  CoupArgs cp;
+};
+
+// Copy a record into shared memory; every thread of the block takes part,
+// and a __syncthreads() must follow before it is read.
+template <class T>
+__device__ __forceinline__ void stageRecord(T& dst, const T& src) {
+  static_assert(sizeof(T) % 8 == 0, "records are 8-byte multiples");
+  const unsigned long long* s = reinterpret_cast<const unsigned long long*>(&src);
+  unsigned long long* d = reinterpret_cast<unsigned long long*>(&dst);
+  for (int i = threadIdx.x; i < (int)(sizeof(T) / 8); i += blockDim.x) d[i] = s[i];
+}
+
+// A kernel taking (Consts, ARGT) in two entry points: NAME for one run
+// (arguments by value) and NAME##Batch for many runs at once, which stages
+// run blockIdx.z's record in shared memory. Both run NAME##Body, which
+// follows the macro as the function body.
+#define LBDEM_KERNEL(BOUNDS, NAME, ARGT, FIELD)                                  \
+  __device__ __forceinline__ void NAME##Body(const Consts& k, const ARGT& a);   \
+  __global__ void BOUNDS NAME(Consts k, ARGT a) { NAME##Body(k, a); }           \
+  __global__ void BOUNDS NAME##Batch(const JobArgs* jobs) {                     \
+    __shared__ __align__(16) Consts sk;                                          \
+    __shared__ __align__(16) ARGT sa;                                            \
+    stageRecord(sk, jobs[blockIdx.z].k);                                         \
+    stageRecord(sa, jobs[blockIdx.z].FIELD);                                     \
+    __syncthreads();                                                             \
+    NAME##Body(sk, sa);                                                          \
+  }                                                                              \
+  __device__ __forceinline__ void NAME##Body(const Consts& k, const ARGT& a)
+
 // Mixed lattice step launch shape: chunks of MIXED_CHUNK consecutive nodes
 // (one per thread), staged through MIXED_STAGES shared-memory buffers of 19
 // FP32 planes, the solid indices, the fluid densities nF and the mask bytes
@@ -91,13 +156,17 @@ constexpr int MIXED_STAGE_MASK = MIXED_STAGE_NF + MIXED_CHUNK * 4;
 constexpr int MIXED_STAGE_BYTES = MIXED_STAGE_MASK + MIXED_CHUNK;
 constexpr int MIXED_THREADS = MIXED_CHUNK;
 constexpr int MIXED_SMEM = MIXED_STAGES * MIXED_STAGE_BYTES;
+#define MIXED_BOUNDS __launch_bounds__(MIXED_THREADS, 3)
 // chunks per block up to which inactive chunks are skipped (per-block list)
 constexpr int MIXED_MAX_MINE = 2048;
 
 // lb_fp64.cu / lb_mixed.cu
 __global__ void lbStepFp64(Consts k, LbArgs a);
+__global__ void lbStepFp64Batch(const JobArgs* jobs);
 __global__ void lbStepMixed(Consts k, LbArgs a);
+__global__ void lbStepMixedBatch(const JobArgs* jobs);
 __global__ void lbWallForceMixed(Consts k, LbArgs a);
+__global__ void lbWallForceMixedBatch(const JobArgs* jobs);
 __global__ void lbPrepare(Consts k, double* pAcc, long long pAccLen, float* pAccF,
                           long long pAccFLen, double* obj, double* wallF, double* scal,
                           int* iscal, const double* px0, const double* px1, const double* pw1,
@@ -106,11 +175,17 @@ __global__ void lbFinalizeKernel(Consts k, double* pF, double* pM, double* pV, d
                                  double* wallF, double* scal, const int* iscal,
                                  const float* pAccF, double* pS, FsArgs fa, int redistribute);
 __global__ void fsUpdateMass(Consts k, FsArgs a);
+__global__ void fsUpdateMassBatch(const JobArgs* jobs);
 __global__ void fsMutants(Consts k, FsArgs a);
+__global__ void fsMutantsBatch(const JobArgs* jobs);
 __global__ void fsSmoothen(Consts k, FsArgs a);
+__global__ void fsSmoothenBatch(const JobArgs* jobs);
 __global__ void fsMutantsAndFill(Consts k, FsArgs a);
+__global__ void fsMutantsAndFillBatch(const JobArgs* jobs);
 __global__ void fsEmptyIsolated(Consts k, FsArgs a);
+__global__ void fsEmptyIsolatedBatch(const JobArgs* jobs);
 __global__ void fsRedistribute(Consts k, FsArgs a);
+__global__ void fsRedistributeBatch(const JobArgs* jobs);
 __global__ void uncoverCollect(Consts k, const uint8_t* mask, const double* obj,
                                uint32_t* list, int* iscal);
 // dynamic shared memory of uncoverResolve: candidates, their lower-index
@@ -130,7 +205,8 @@ __global__ void findNewActiveKernel(Consts k, uint8_t* mask, uint32_t* solid,
 __global__ void initTypes(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* objIdx,
                           const int* boundary, const DeviceWall* walls, const int* wallType,
                           const double* obj, double fluidHeightLattice, int freeSurface);
-__global__ void initFields(Consts k, uint8_t* mask, void* f, double* mass, float* nF);
+__global__ void initFields(Consts k, uint8_t* mask, void* f, double* mass, float* nF,
+                           double fluidHeightLattice, int freeSurface);
 // mass of the active nodes (outside particles unless withParticles), counts
 __global__ void massSummaryKernel(Consts k, const uint8_t* mask, const double* mass,
                                   const float* nF, double* out, unsigned long long* cnt,
@@ -148,19 +224,43 @@ constexpr int GATHER_THREADS = 64;
 // dem_fp64.cu
 __global__ void demBegin(Consts k, DemArgs a, int forceRebuild);
 __global__ void nbrCellAssign(Consts k, DemArgs a);
+__global__ void nbrCellAssignBatch(const JobArgs* jobs);
 __global__ void nbrCellScan(Consts k, DemArgs a);
+__global__ void nbrCellScanBatch(const JobArgs* jobs);
 __global__ void nbrCellScatter(Consts k, DemArgs a);
+__global__ void nbrCellScatterBatch(const JobArgs* jobs);
 __global__ void nbrCellSort(Consts k, DemArgs a);
+__global__ void nbrCellSortBatch(const JobArgs* jobs);
 __global__ void nbrBuildCells(Consts k, DemArgs a);
+__global__ void nbrBuildCellsBatch(const JobArgs* jobs);
 __global__ void nbrBuildDirect(Consts k, DemArgs a);
+__global__ void nbrBuildDirectBatch(const JobArgs* jobs);
 __global__ void nbrDirectHistory(Consts k, DemArgs a);
+__global__ void nbrDirectHistoryBatch(const JobArgs* jobs);
 __global__ void nbrPartners(Consts k, DemArgs a);
+__global__ void nbrPartnersBatch(const JobArgs* jobs);
 __global__ void nbrPairList(Consts k, DemArgs a);
+__global__ void nbrPairListBatch(const JobArgs* jobs);
 // the DEM step number comes from iscal[IS_DEMSTEP] (advanced by demBegin)
 __global__ void demPairs(Consts k, DemArgs a);
+__global__ void demPairsBatch(const JobArgs* jobs);
 __global__ void demGather(Consts k, DemArgs a);
+__global__ void demGatherBatch(const JobArgs* jobs);
 // dem_mixed.cu: the force passes of the mixed form (FP32 force laws)
 __global__ void demPairsMixed(Consts k, DemArgs a);
+__global__ void demPairsMixedBatch(const JobArgs* jobs);
 __global__ void demGatherMixed(Consts k, DemArgs a);
+__global__ void demGatherMixedBatch(const JobArgs* jobs);
+
+// many-run entry points of the kernels with their own parameter lists
+__global__ void demBeginBatch(const JobArgs* jobs);
+__global__ void lbPrepareBatch(const JobArgs* jobs);
+__global__ void lbFinalizeKernelBatch(const JobArgs* jobs);
+__global__ void uncoverCollectBatch(const JobArgs* jobs);
+__global__ void uncoverResolveBatch(const JobArgs* jobs);
+__global__ void voxelizeObjectsBatch(const JobArgs* jobs);
+__global__ void flagClaimBatch(const JobArgs* jobs);
+__global__ void flagApplyBatch(const JobArgs* jobs);
+__global__ void findNewActiveKernelBatch(const JobArgs* jobs);
 
 }  // namespace lbdem

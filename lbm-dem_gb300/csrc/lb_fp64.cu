@@ -31,7 +31,7 @@ namespace lbdem {
 // Fused LB step over all nodes: reconstruct, particle forcing, collision,
 // push streaming with the boundary rules of LB::streaming, and the per-node
 // bookkeeping of cleanLists / updateMass (fluid part).
-__global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
+LBDEM_KERNEL(__launch_bounds__(256), lbStepFp64, LbArgs, lb) {
   __shared__ double acc[ACC_N];
   __shared__ int sbox[6];
   __shared__ int snif;
@@ -224,10 +224,11 @@ __global__ void __launch_bounds__(256) lbStepFp64(Consts k, LbArgs a) {
 // forces, extra mass, interface count and box) and the particle kinematics
 // in lattice units are formed once per particle (x0/L, x1/S, w1/W: the
 // quotients the reference forms at every node).
-__global__ void lbPrepare(Consts k, double* pAcc, long long pAccLen, float* pAccF,
-                          long long pAccFLen, double* obj, double* wallF, double* scal,
-                          int* iscal, const double* px0, const double* px1, const double* pw1,
-                          double* pkd, float* pkf) {
+__device__ __forceinline__ void lbPrepareBody(const Consts& k, double* pAcc, long long pAccLen,
+                                              float* pAccF, long long pAccFLen, double* obj,
+                                              double* wallF, double* scal, int* iscal,
+                                              const double* px0, const double* px1,
+                                              const double* pw1, double* pkd, float* pkf) {
   const long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = i0; i < pAccLen; i += stride) pAcc[i] = 0.0;
@@ -289,9 +290,11 @@ __device__ __forceinline__ bool fsRegion(const Consts& k, const int* iscal, int&
 
 // Unit conversions at the end of LB::streaming / computeHydroForces and the
 // mass-redistribution amount (src/LB.cpp:1533-1543, 1966-1977, 1844-1847).
-__global__ void lbFinalizeKernel(Consts k, double* pF, double* pM, double* pV, double* obj,
-                                 double* wallF, double* scal, const int* iscal,
-                                 const float* pAccF, double* pS, FsArgs fa, int redistribute) {
+__device__ __forceinline__ void lbFinalizeBody(const Consts& k, double* pF, double* pM,
+                                               double* pV, double* obj, double* wallF,
+                                               double* scal, const int* iscal,
+                                               const float* pAccF, double* pS,
+                                               const FsArgs& fa, int redistribute) {
   const int P = k.nPart;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
     if (pAccF) {
@@ -391,7 +394,7 @@ __device__ __noinline__ void fsPostCollision(const Consts& k, const FsArgs& a, l
 
 // LB::updateMass (interface part). The neighbour types are read first, all
 // links at once; the mass exchange terms are then summed in link order.
-__global__ void fsUpdateMass(Consts k, FsArgs a) {
+LBDEM_KERNEL(, fsUpdateMass, FsArgs, fs) {
   // the free-surface step's surplus and interface count start from zero
   // (fsUpdateMass itself accumulates neither)
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -439,7 +442,7 @@ __global__ void fsUpdateMass(Consts k, FsArgs a) {
 }
 
 // findInterfaceMutants (src/LB.cpp:1669-1698) after the interface mass copy.
-__global__ void fsMutants(Consts k, FsArgs a) {
+LBDEM_KERNEL(, fsMutants, FsArgs, fs) {
   FS_LOOP(k, a, {
     const uint8_t m = a.mask[x];
     a.fsflag[x] = 0;
@@ -460,7 +463,7 @@ __global__ void fsMutants(Consts k, FsArgs a) {
 // become interface nodes initialised from the first filled neighbour in the
 // reference's order (the highest node index); fluid neighbours of emptied
 // nodes become interface nodes holding 99% of their density.
-__global__ void fsSmoothen(Consts k, FsArgs a) {
+LBDEM_KERNEL(, fsSmoothen, FsArgs, fs) {
   double surplus = 0.0;
   FS_LOOP(k, a, {
     const uint8_t m = a.mask[x];
@@ -512,7 +515,7 @@ __global__ void fsSmoothen(Consts k, FsArgs a) {
 }
 
 // updateMutants + removeIsolated, first pass (src/LB.cpp:1751-1817).
-__global__ void fsMutantsAndFill(Consts k, FsArgs a) {
+LBDEM_KERNEL(, fsMutantsAndFill, FsArgs, fs) {
   double surplus = 0.0;
   FS_LOOP(k, a, {
     const uint8_t fl = a.fsflag[x];
@@ -544,7 +547,7 @@ __global__ void fsMutantsAndFill(Consts k, FsArgs a) {
 }
 
 // removeIsolated, second pass (src/LB.cpp:1819-1841), and the interface count.
-__global__ void fsEmptyIsolated(Consts k, FsArgs a) {
+LBDEM_KERNEL(, fsEmptyIsolated, FsArgs, fs) {
   double surplus = 0.0;
   int cnt = 0;
   FS_LOOP(k, a, {
@@ -574,7 +577,7 @@ __global__ void fsEmptyIsolated(Consts k, FsArgs a) {
 // grown by 2: the nodes that left the active types in this step (interface
 // -> gas) lie in the box grown by 1, so their neighbours lie in the box
 // grown by 2. Every thread writes only its own node's mask byte.
-__global__ void fsRedistribute(Consts k, FsArgs a) {
+LBDEM_KERNEL(, fsRedistribute, FsArgs, fs) {
   const double addMass = a.scal[SC_SURPLUS] / (double)(unsigned)a.iscal[IS_NIF2];
   int x1, y1, z1, rx1, ry1, rz1;
   if (!fsRegion(k, a.iscal, x1, y1, z1, rx1, ry1, rz1)) return;
@@ -635,8 +638,9 @@ __device__ __forceinline__ void loadSpheres(const Consts& k, const double* obj, 
 
 // findNewActiveObject, step 1: collect object nodes that object 0 no longer
 // covers (candidates come from the previous voxelisation boxes).
-__global__ void uncoverCollect(Consts k, const uint8_t* mask, const double* obj,
-                               uint32_t* list, int* iscal) {
+__device__ __forceinline__ void uncoverCollectBody(const Consts& k, const uint8_t* mask,
+                                                   const double* obj, uint32_t* list,
+                                                   int* iscal) {
   __shared__ SphereL cur[MAX_OBJ], prev[MAX_OBJ];
   loadSpheres(k, obj, OB_X0, cur);
   loadSpheres(k, obj, OB_X0PREV, prev);
@@ -667,14 +671,17 @@ __global__ void uncoverCollect(Consts k, const uint8_t* mask, const double* obj,
 // them (src/LB.cpp:874-940). Dynamic shared memory (UNCOVER_SMEM bytes):
 // the sorted candidates, for each the indices of its lower-index candidate
 // neighbours (at most the 9 links with a negative node offset), and its state.
-__global__ void __launch_bounds__(1024) uncoverResolve(Consts k, uint8_t* mask, void* f,
-                                                       double* mass, float* nF, uint32_t* list,
-                                                       int* iscal) {
+__device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mask, void* f,
+                                                   double* mass, float* nF, uint32_t* list,
+                                                   int* iscal) {
   extern __shared__ __align__(16) unsigned char uncoverSmem[];
   uint32_t* s_idx = reinterpret_cast<uint32_t*>(uncoverSmem);          // [UNCOVER_CAP]
   int16_t* s_back = reinterpret_cast<int16_t*>(s_idx + UNCOVER_CAP);   // [UNCOVER_CAP][9]
   uint8_t* s_st = reinterpret_cast<uint8_t*>(s_back + 9 * UNCOVER_CAP);  // [UNCOVER_CAP]
   int n = min(iscal[IS_NUNCOVER], UNCOVER_CAP);
+  // the count is consumed: zero it for the next step's collection
+  __syncthreads();
+  if (threadIdx.x == 0) iscal[IS_NUNCOVER] = 0;
   if (n == 0) return;
   int p2 = 1;
   while (p2 < n) p2 <<= 1;
@@ -796,8 +803,9 @@ __global__ void __launch_bounds__(1024) uncoverResolve(Consts k, uint8_t* mask, 
 }
 
 // Voxelisation of the impactors (updateObjectBoundaries, src/LB.cpp:806-840).
-__global__ void voxelizeObjects(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* objIdx,
-                                double* mass, double* obj) {
+__device__ __forceinline__ void voxelizeObjectsBody(const Consts& k, uint8_t* mask,
+                                                    uint32_t* solid, uint8_t* objIdx,
+                                                    double* mass, double* obj) {
   __shared__ SphereL sph[MAX_OBJ];
   loadSpheres(k, obj, OB_X0, sph);
   __syncthreads();
@@ -839,8 +847,10 @@ __global__ void voxelizeObjects(Consts k, uint8_t* mask, uint32_t* solid, uint8_
 
 // updateIndices, step 1: every particle claims the nodes of the last active
 // list inside it; the highest particle index wins (src/LB.cpp:695-710).
-__global__ void flagClaim(Consts k, const uint8_t* mask, uint32_t* claim, const double* px0,
-                          const double* pr, const int* iscal, unsigned long long* uscal) {
+__device__ __forceinline__ void flagClaimBody(const Consts& k, const uint8_t* mask,
+                                              uint32_t* claim, const double* px0,
+                                              const double* pr, const int* iscal,
+                                              unsigned long long* uscal) {
   if (!iscal[IS_NEWNBR]) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) uscal[US_FIRSTFLAG] = ~0ull;
   const int P = k.nPart;
@@ -867,8 +877,9 @@ __global__ void flagClaim(Consts k, const uint8_t* mask, uint32_t* claim, const 
 
 // updateIndices, step 2: the flag reset of every node (solid index 0, walls
 // included) and the new flags (src/LB.cpp:689-693).
-__global__ void flagApply(Consts k, uint8_t* mask, uint32_t* solid, uint32_t* claim,
-                          int* iscal, unsigned long long* uscal) {
+__device__ __forceinline__ void flagApplyBody(const Consts& k, uint8_t* mask, uint32_t* solid,
+                                              uint32_t* claim, int* iscal,
+                                              unsigned long long* uscal) {
   if (!iscal[IS_NEWNBR]) return;
   // wall nodes are never claimed: from here on their solid index is 0
   if (blockIdx.x == 0 && threadIdx.x == 0) iscal[IS_WALLS_RESET] = 1;
@@ -895,10 +906,10 @@ __global__ void flagApply(Consts k, uint8_t* mask, uint32_t* solid, uint32_t* cl
 // LB::findNewActive (one CTA): walk the flagged nodes in ascending order,
 // un-flag those no longer inside their particle and stop at the first one
 // that still is (the reference's loop-exiting break, src/LB.cpp:2001-2007).
-__global__ void __launch_bounds__(1024) findNewActiveKernel(Consts k, uint8_t* mask,
-                                                            uint32_t* solid, const double* px0,
-                                                            const double* pr, int* iscal,
-                                                            unsigned long long* uscal) {
+__device__ __forceinline__ void findNewActiveBody(const Consts& k, uint8_t* mask,
+                                                  uint32_t* solid, const double* px0,
+                                                  const double* pr, int* iscal,
+                                                  unsigned long long* uscal) {
   __shared__ unsigned long long s_min;
   if (threadIdx.x == 0) iscal[IS_NEWNBR] = 0;
   unsigned long long start = uscal[US_FIRSTFLAG];
@@ -942,11 +953,122 @@ __global__ void __launch_bounds__(1024) findNewActiveKernel(Consts k, uint8_t* m
 
 // ---- initialisation (LB::latticeBolzmannInit) ------------------------------
 
+// ---- entry points of the kernels above with their own parameter lists: one
+// run (arguments by value) and many runs at once (blockIdx.z = run, record
+// staged in shared memory) ----
+
+#define JOB_PROLOGUE                                                  \
+  __shared__ __align__(16) Consts sk;                                 \
+  stageRecord(sk, jobs[blockIdx.z].k);                                \
+  __syncthreads();                                                    \
+  const CoupArgs& c = jobs[blockIdx.z].cp;
+
+__global__ void lbPrepare(Consts k, double* pAcc, long long pAccLen, float* pAccF,
+                          long long pAccFLen, double* obj, double* wallF, double* scal,
+                          int* iscal, const double* px0, const double* px1, const double* pw1,
+                          double* pkd, float* pkf) {
+  lbPrepareBody(k, pAcc, pAccLen, pAccF, pAccFLen, obj, wallF, scal, iscal, px0, px1, pw1, pkd,
+                pkf);
+}
+__global__ void lbPrepareBatch(const JobArgs* jobs) {
+  JOB_PROLOGUE
+  lbPrepareBody(sk, c.pAcc, c.pAccLen, c.pAccF, c.pAccFLen, c.obj, c.wallF, c.scal, c.iscal,
+                c.px0, c.px1, c.pw1, c.pkd, c.pkf);
+}
+
+__global__ void lbFinalizeKernel(Consts k, double* pF, double* pM, double* pV, double* obj,
+                                 double* wallF, double* scal, const int* iscal,
+                                 const float* pAccF, double* pS, FsArgs fa, int redistribute) {
+  lbFinalizeBody(k, pF, pM, pV, obj, wallF, scal, iscal, pAccF, pS, fa, redistribute);
+}
+__global__ void lbFinalizeKernelBatch(const JobArgs* jobs) {
+  JOB_PROLOGUE
+  lbFinalizeBody(sk, c.pF, c.pM, c.pV, c.obj, c.wallF, c.scal, c.iscal, c.pAccF, c.pS,
+                 jobs[blockIdx.z].fs, c.redistribute);
+}
+
+__global__ void uncoverCollect(Consts k, const uint8_t* mask, const double* obj,
+                               uint32_t* list, int* iscal) {
+  uncoverCollectBody(k, mask, obj, list, iscal);
+}
+__global__ void uncoverCollectBatch(const JobArgs* jobs) {
+  JOB_PROLOGUE
+  uncoverCollectBody(sk, c.mask, c.obj, c.uncover, c.iscal);
+}
+
+__global__ void __launch_bounds__(1024) uncoverResolve(Consts k, uint8_t* mask, void* f,
+                                                       double* mass, float* nF, uint32_t* list,
+                                                       int* iscal) {
+  uncoverResolveBody(k, mask, f, mass, nF, list, iscal);
+}
+__global__ void __launch_bounds__(1024) uncoverResolveBatch(const JobArgs* jobs) {
+  JOB_PROLOGUE
+  uncoverResolveBody(sk, c.mask, c.fcur, c.mass, c.nF, c.uncover, c.iscal);
+}
+
+__global__ void voxelizeObjects(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* objIdx,
+                                double* mass, double* obj) {
+  voxelizeObjectsBody(k, mask, solid, objIdx, mass, obj);
+}
+__global__ void voxelizeObjectsBatch(const JobArgs* jobs) {
+  JOB_PROLOGUE
+  voxelizeObjectsBody(sk, c.mask, c.solid, c.objIdx, c.mass, c.obj);
+}
+
+__global__ void flagClaim(Consts k, const uint8_t* mask, uint32_t* claim, const double* px0,
+                          const double* pr, const int* iscal, unsigned long long* uscal) {
+  flagClaimBody(k, mask, claim, px0, pr, iscal, uscal);
+}
+__global__ void flagClaimBatch(const JobArgs* jobs) {
+  JOB_PROLOGUE
+  flagClaimBody(sk, c.mask, c.claim, c.px0, c.pr, c.iscal, c.uscal);
+}
+
+__global__ void flagApply(Consts k, uint8_t* mask, uint32_t* solid, uint32_t* claim,
+                          int* iscal, unsigned long long* uscal) {
+  flagApplyBody(k, mask, solid, claim, iscal, uscal);
+}
+__global__ void flagApplyBatch(const JobArgs* jobs) {
+  JOB_PROLOGUE
+  flagApplyBody(sk, c.mask, c.solid, c.claim, c.iscal, c.uscal);
+}
+
+__global__ void __launch_bounds__(1024) findNewActiveKernel(Consts k, uint8_t* mask,
+                                                            uint32_t* solid, const double* px0,
+                                                            const double* pr, int* iscal,
+                                                            unsigned long long* uscal) {
+  findNewActiveBody(k, mask, solid, px0, pr, iscal, uscal);
+}
+__global__ void __launch_bounds__(1024) findNewActiveKernelBatch(const JobArgs* jobs) {
+  JOB_PROLOGUE
+  findNewActiveBody(sk, c.mask, c.solid, c.px0, c.pr, c.iscal, c.uscal);
+}
+
 // initializeLatticeBoundaries, initializeWallBoundaries,
 // initializeObjectBoundaries and initializeInterface (src/LB.cpp:538-795, 974-992)
 __global__ void initTypes(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* objIdx,
                           const int* boundary, const DeviceWall* walls, const int* wallType,
                           const double* obj, double fluidHeightLattice, int freeSurface) {
+  // the quotients the reference forms at every node, formed once per block
+  // (the same operands give the same double)
+  __shared__ double wp[MAX_WALL][3], wn[MAX_WALL][3], oc[MAX_OBJ][4];
+  __shared__ int wt[MAX_WALL];
+  __shared__ uint32_t oidx[MAX_OBJ];
+  if (threadIdx.x < (unsigned)k.nWall) {
+    const DeviceWall& W = walls[threadIdx.x];
+    for (int c = 0; c < 3; ++c) {
+      wp[threadIdx.x][c] = W.p[c] / k.uLength;
+      wn[threadIdx.x][c] = W.n[c];
+    }
+    wt[threadIdx.x] = wallType[threadIdx.x];
+  }
+  if (threadIdx.x < (unsigned)k.nObj) {
+    const double* ob = obj + threadIdx.x * OB_STRIDE;
+    for (int c = 0; c < 3; ++c) oc[threadIdx.x][c] = ob[OB_X0 + c] / k.uLength;
+    oc[threadIdx.x][3] = ob[OB_R] / k.uLength;
+    oidx[threadIdx.x] = (uint32_t)ob[OB_INDEX];
+  }
+  __syncthreads();
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
        x += (long long)gridDim.x * blockDim.x) {
     int ix, iy, iz;
@@ -961,21 +1083,17 @@ __global__ void initTypes(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* obj
     else if (iz == k.Z - 1) t = boundary[5];
     const double p[3] = {(double)ix, (double)iy, (double)iz};
     for (int w = 0; w < k.nWall; ++w) {
-      const DeviceWall& W = walls[w];
-      const double d = W.n[0] * (p[0] - W.p[0] / k.uLength) +
-                       W.n[1] * (p[1] - W.p[1] / k.uLength) +
-                       W.n[2] * (p[2] - W.p[2] / k.uLength);
+      const double d = wn[w][0] * (p[0] - wp[w][0]) + wn[w][1] * (p[1] - wp[w][1]) +
+                       wn[w][2] * (p[2] - wp[w][2]);
       if (d < 0.0) {
         so = (uint32_t)w;
-        t = wallType[w];
+        t = wt[w];
       }
     }
     uint8_t oi = 0;
     for (int o = 0; o < k.nObj; ++o) {
-      const double* ob = obj + o * OB_STRIDE;
-      if (insideSphere(p[0], p[1], p[2], ob[OB_X0] / k.uLength, ob[OB_X0 + 1] / k.uLength,
-                       ob[OB_X0 + 2] / k.uLength, ob[OB_R] / k.uLength)) {
-        so = (uint32_t)ob[OB_INDEX];
+      if (insideSphere(p[0], p[1], p[2], oc[o][0], oc[o][1], oc[o][2], oc[o][3])) {
+        so = oidx[o];
         t = 12;
         oi = (uint8_t)o;
       }
@@ -991,25 +1109,35 @@ __global__ void initTypes(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* obj
 // interface nodes; active nodes start at equilibrium. Typing in place is safe:
 // a fluid->interface change never alters any node's gas neighbourhood. Also
 // the first cleanLists (active-list bit).
-__global__ void initFields(Consts k, uint8_t* mask, void* f, double* mass, float* nF) {
+__global__ void initFields(Consts k, uint8_t* mask, void* f, double* mass, float* nF,
+                           double fluidHeightLattice, int freeSurface) {
+  // every active node starts at the same equilibrium
+  const double rho0 = k.initDensity;
+  const double ux = k.lbF[0] / 2.0 / rho0 + k.initVel[0];
+  const double uy = k.lbF[1] / 2.0 / rho0 + k.initVel[1];
+  const double uz = k.lbF[2] / 2.0 / rho0 + k.initVel[2];
+  const double usq = ux * ux + uy * uy + uz * uz;
+  double feq[Q];
+#pragma unroll
+  for (int j = 0; j < Q; ++j) feq[j] = feqj(j, rho0, ux, uy, uz, usq);
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
        x += (long long)gridDim.x * blockDim.x) {
     int t = mask[x] & TYPE_MASK;
-    if (t == 0) {
-      for (int j = 1; j < Q; ++j)
-        if ((mask[x + nbrOffset(k, j)] & TYPE_MASK) == 2) {
-          t = 3;
-          break;
-        }
+    if (t == 0 && freeSurface) {
+      // gas is only above the fill height (initTypes): a node whose upper
+      // neighbours are below it has no gas neighbour
+      const int iy = (int)((x / k.sy) % k.Y);
+      if ((double)(unsigned)(iy + 1) > fluidHeightLattice)
+        for (int j = 1; j < Q; ++j)
+          if ((mask[x + nbrOffset(k, j)] & TYPE_MASK) == 2) {
+            t = 3;
+            break;
+          }
     }
     double ms = 0.0;
     if (t == 0 || t == 3) {
-      const double rho0 = k.initDensity;
-      const double ux = k.lbF[0] / 2.0 / rho0 + k.initVel[0];
-      const double uy = k.lbF[1] / 2.0 / rho0 + k.initVel[1];
-      const double uz = k.lbF[2] / 2.0 / rho0 + k.initVel[2];
-      const double usq = ux * ux + uy * uy + uz * uz;
-      for (int j = 0; j < Q; ++j) fset(k, f, j, x, feqj(j, rho0, ux, uy, uz, usq));
+#pragma unroll
+      for (int j = 0; j < Q; ++j) fset(k, f, j, x, feq[j]);
       ms = t == 0 ? rho0 : 0.5 * rho0;
       mask[x] = (uint8_t)((mask[x] & ~TYPE_MASK) | t | ABIT);
       if (k.mixed && t == 0) nF[x] = (float)rho0;

@@ -153,7 +153,7 @@ __device__ __forceinline__ void particleRunReduce(int key, int ix, float dx, flo
 
 }  // namespace
 
-__global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs a) {
+LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
   extern __shared__ __align__(128) unsigned char stageMem[];  // MIXED_STAGES x stage
   __shared__ uint64_t fullBar[MIXED_STAGES], emptyBar[MIXED_STAGES];
   __shared__ int abortFlag;
@@ -498,7 +498,7 @@ __global__ void __launch_bounds__(MIXED_THREADS, 3) lbStepMixed(Consts k, LbArgs
 // the reference: the wall setup gives a node on several faces the last of
 // their walls in face order x0, x1, y0, y1, z0, z1, and the first flag reset
 // (updateIndices) sets every wall node's index to 0 for good.
-__global__ void lbWallForceMixed(Consts k, LbArgs a) {
+LBDEM_KERNEL(, lbWallForceMixed, LbArgs, lb) {
   __shared__ float accW[3 * MAX_WALL];
   for (int i = threadIdx.x; i < 3 * MAX_WALL; i += blockDim.x) accW[i] = 0.0f;
   __syncthreads();

@@ -215,6 +215,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   ctx->precision = precision;
   ctx->device = opt ? opt->device : 0;
   ctx->check_every = opt ? opt->check_every : 0;
+  if (opt && opt->chunks_per_block > 0) ctx->chunksPerBlock = opt->chunks_per_block;
   if (precision != LBDEM_PLAIN_FP64 && precision != LBDEM_MIXED)
     return setErr(ctx, LBDEM_ERR_INVALID, "unknown precision form");
   // ---- validation (the supported subset of the reference's inputs) ----
@@ -243,6 +244,11 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
     CK(cudaFuncSetAttribute(lbStepMixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             MIXED_SMEM));
     CK(cudaFuncSetAttribute(uncoverResolve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            UNCOVER_SMEM));
+    // the many-run entry points of the same kernels
+    CK(cudaFuncSetAttribute(lbStepMixedBatch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            MIXED_SMEM));
+    CK(cudaFuncSetAttribute(uncoverResolveBatch, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             UNCOVER_SMEM));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, lbStepMixed, MIXED_THREADS,
                                                      MIXED_SMEM));
@@ -399,6 +405,9 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
     const int sm = std::max(1, ctx->smCount);
     // free surface: the interface box is about the free-surface area deep
     ctx->gridFs = cap((long long)k.X * k.Z / 32 + 1, sm * 4);
+    // mixed lattice step: one resident wave, but at least chunksPerBlock
+    // chunks per block
+    ctx->gridLattice = cap(k.NP / MIXED_CHUNK / ctx->chunksPerBlock, ctx->lbMixedBlocks);
     // wall-force sweep: blocks per box face (the largest face's inner nodes)
     const long long face = std::max({(long long)k.Y * k.Z, (long long)k.X * k.Z,
                                      (long long)k.X * k.Y});
@@ -534,7 +543,8 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   if (ctx->lbSolve) {
     initTypes<<<lg, 256, 0, st>>>(k, d.mask, d.solid, d.objIdx, dBoundary, d.walls, dWallType,
                                   d.obj, cfg->fluidHeight / L, k.freeSurface);
-    initFields<<<lg, 256, 0, st>>>(k, d.mask, d.f[0], d.mass, d.nF);
+    initFields<<<lg, 256, 0, st>>>(k, d.mask, d.f[0], d.mass, d.nF, cfg->fluidHeight / L,
+                                   k.freeSurface);
     if ((rc = launchErr(ctx, "lattice init")) != LBDEM_OK) return rc;
   }
   // ---- initial neighbour list (DEM::discreteElementInit, :294-296) ----
@@ -622,7 +632,6 @@ extern "C" int lbdem_coupling_step(lbdem_ctx* ctx) {
   cudaStream_t s = ctx->stream;
   const int lg = latticeGrid(ctx);
   if (ctx->nObj > 0) {
-    cudaMemsetAsync(d.iscal + IS_NUNCOVER, 0, sizeof(int), s);
     uncoverCollect<<<ctx->gridObj, 256, 0, s>>>(k, d.mask, d.obj, d.uncover, d.iscal);
     uncoverResolve<<<1, 1024, UNCOVER_SMEM, s>>>(k, d.mask, d.f[ctx->cur], d.mass, d.nF, d.uncover,
                                       d.iscal);
@@ -655,7 +664,7 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   auto* ev = nextLbEvents(ctx);
   if (ev) cudaEventRecord(ev->first, s);
   if (k.mixed)
-    lbStepMixed<<<(int)std::min<long long>(ctx->lbMixedBlocks, k.NP / MIXED_CHUNK),
+    lbStepMixed<<<ctx->gridLattice,
                   MIXED_THREADS, MIXED_SMEM, s>>>(k, a);
   else lbStepFp64<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
   if (ev) cudaEventRecord(ev->second, s);
@@ -786,6 +795,165 @@ int capturePair(lbdem_ctx* ctx, int parity) {
 }
 
 }  // namespace
+
+// ---- many runs advanced by one launch per kernel ----------------------------
+
+// The record of run c for a cycle that starts on lattice buffer cur: the
+// lattice step reads buffer cur, the finalisation and the free-surface step
+// (after the swap) see 1 - cur as current.
+void lbdemJobArgs(lbdem_ctx* c, int cur, JobArgs* j) {
+  std::memset(j, 0, sizeof *j);
+  const int save = c->cur;
+  c->cur = cur;
+  j->k = c->k;
+  j->dem = demArgs(c);
+  j->lb = lbArgs(c);
+  c->cur = 1 - cur;
+  j->fs = fsArgs(c);
+  c->cur = save;
+  Device& d = c->d;
+  CoupArgs& p = j->cp;
+  p.mask = d.mask;
+  p.solid = d.solid;
+  p.objIdx = d.objIdx;
+  p.claim = d.claim;
+  p.mass = d.mass;
+  p.nF = d.nF;
+  p.fcur = d.f[cur];
+  p.uncover = d.uncover;
+  p.px0 = d.px0;
+  p.px1 = d.px1;
+  p.pw1 = d.pw1;
+  p.pr = d.pr;
+  p.obj = d.obj;
+  p.wallF = d.wallF;
+  p.scal = d.scal;
+  p.iscal = d.iscal;
+  p.uscal = d.uscal;
+  const long long P1 = std::max(c->nPart, 1);
+  p.pAcc = d.pFHydro;
+  p.pAccLen = 16LL * P1;
+  p.pAccF = d.pAccF;
+  p.pAccFLen = (long long)ACCF_STRIDE * P1;
+  p.pkd = d.pkd;
+  p.pkf = d.pkf;
+  p.pF = d.pFHydro;
+  p.pM = d.pMHydro;
+  p.pV = d.pFluidVol;
+  p.pS = d.pSHydro;
+  p.redistribute = c->freeSurface ? 1 : 0;
+}
+
+// Runs whose next two cycles are the steady goCycle (the pair-replay
+// conditions) with the DEM, lattice and coupling steps all on; two such runs
+// share a batch when their switches match (batchKey).
+bool lbdemBatchable(const lbdem_ctx* c) {
+  return c->demSolve && c->lbSolve && pairReplayable(c);
+}
+int lbdemBatchKey(const lbdem_ctx* c) {
+  return c->precision | (c->freeSurface ? 2 : 0) | (c->nObj > 0 ? 4 : 0) | (c->nWall > 0 ? 8 : 0);
+}
+
+// One goCycle of every run (DEM, coupling, lattice, free-surface step, as
+// cycleOnce enqueues them) with one launch per kernel: grid z = run, grid
+// x = the largest of the runs' own grids (the kernels loop over their work
+// by grid stride). jobs: the runs' records for this cycle, on the device.
+int lbdemEnqueueBatchCycle(const std::vector<lbdem_ctx*>& runs, const JobArgs* jobs,
+                           cudaStream_t s) {
+  const unsigned n = (unsigned)runs.size();
+  lbdem_ctx* r0 = runs[0];
+  auto gmax = [&](auto grid) {
+    int g = 1;
+    for (lbdem_ctx* c : runs) g = std::max(g, (int)grid(c));
+    return g;
+  };
+  auto G = [&](int gx) { return dim3((unsigned)gx, 1, n); };
+  const bool mixed = r0->k.mixed != 0;
+  // DEM step
+  demBeginBatch<<<G(gmax([](lbdem_ctx* c) { return partGrid(c, 256); })), 256, 0, s>>>(jobs);
+  const int pg = gmax([](lbdem_ctx* c) { return partGrid(c, 128); });
+  nbrCellAssignBatch<<<G(pg), 128, 0, s>>>(jobs);
+  nbrCellScanBatch<<<G(1), 1024, 0, s>>>(jobs);
+  nbrCellScatterBatch<<<G(pg), 128, 0, s>>>(jobs);
+  nbrCellSortBatch<<<G(gmax([](lbdem_ctx* c) { return c->gridCells; })), 128, 0, s>>>(jobs);
+  nbrBuildCellsBatch<<<G(pg), 128, 0, s>>>(jobs);
+  nbrBuildDirectBatch<<<G(pg), 128, 0, s>>>(jobs);
+  nbrDirectHistoryBatch<<<G(pg), 128, 0, s>>>(jobs);
+  nbrPartnersBatch<<<G(pg), 128, 0, s>>>(jobs);
+  nbrPairListBatch<<<G(gmax([](lbdem_ctx* c) {
+                       return std::max(1, std::min(c->nPart * MAX_N / 256 + 1, c->smCount * 8));
+                     })),
+                     256, 0, s>>>(jobs);
+  const int pairG = gmax([](lbdem_ctx* c) {
+    return std::max(1, std::min(c->nPart * (MAX_N / 2) / 128 + 1, c->smCount * 16));
+  });
+  const int gathG = gmax([](lbdem_ctx* c) { return partGrid(c, GATHER_THREADS); });
+  if (mixed) {
+    demPairsMixedBatch<<<G(pairG), 128, 0, s>>>(jobs);
+    demGatherMixedBatch<<<G(gathG), GATHER_THREADS, 0, s>>>(jobs);
+  } else {
+    demPairsBatch<<<G(pairG), 128, 0, s>>>(jobs);
+    demGatherBatch<<<G(gathG), GATHER_THREADS, 0, s>>>(jobs);
+  }
+  // coupling step
+  if (r0->nObj > 0) {
+    const int og = gmax([](lbdem_ctx* c) { return c->gridObj; });
+    uncoverCollectBatch<<<G(og), 256, 0, s>>>(jobs);
+    uncoverResolveBatch<<<G(1), 1024, UNCOVER_SMEM, s>>>(jobs);
+    voxelizeObjectsBatch<<<G(og), 256, 0, s>>>(jobs);
+  }
+  flagClaimBatch<<<G(gmax([](lbdem_ctx* c) { return partGrid(c, 4); })), 128, 0, s>>>(jobs);
+  flagApplyBatch<<<G(gmax([](lbdem_ctx* c) { return latticeGrid(c); })), 256, 0, s>>>(jobs);
+  findNewActiveKernelBatch<<<G(1), 1024, 0, s>>>(jobs);
+  // lattice step
+  lbPrepareBatch<<<G(gmax([](lbdem_ctx* c) {
+                     return std::max(1, std::min(16 * std::max(c->nPart, 1) / 256 + 1, 1024));
+                   })),
+                   256, 0, s>>>(jobs);
+  if (mixed) {
+    lbStepMixedBatch<<<G(gmax([](lbdem_ctx* c) {
+                         return c->gridLattice;
+                       })),
+                       MIXED_THREADS, MIXED_SMEM, s>>>(jobs);
+    if (r0->nWall > 0)
+      lbWallForceMixedBatch<<<dim3((unsigned)gmax([](lbdem_ctx* c) { return c->gridShell; }), 6,
+                                   n),
+                              256, 0, s>>>(jobs);
+  } else {
+    lbStepFp64Batch<<<G(gmax([](lbdem_ctx* c) { return c->smCount * 4; })), 256, 0, s>>>(jobs);
+  }
+  lbFinalizeKernelBatch<<<G(gmax([](lbdem_ctx* c) {
+                            return std::max(c->gridFs, partGrid(c, 256));
+                          })),
+                          256, 0, s>>>(jobs);
+  // free-surface step
+  if (r0->freeSurface) {
+    const int fg = gmax([](lbdem_ctx* c) { return c->gridFs; });
+    fsUpdateMassBatch<<<G(fg), 256, 0, s>>>(jobs);
+    fsMutantsBatch<<<G(fg), 256, 0, s>>>(jobs);
+    fsSmoothenBatch<<<G(fg), 256, 0, s>>>(jobs);
+    fsMutantsAndFillBatch<<<G(fg), 256, 0, s>>>(jobs);
+    fsEmptyIsolatedBatch<<<G(fg), 256, 0, s>>>(jobs);
+    fsRedistributeBatch<<<G(fg), 256, 0, s>>>(jobs);
+  }
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return setErr(r0, LBDEM_ERR_CUDA, std::string("batched cycle: ") +
+                                                          cudaGetErrorString(e));
+  return LBDEM_OK;
+}
+
+// Host counters of a run after `cycles` batched cycles (an even number:
+// the lattice buffer is back where it started).
+void lbdemAdvanceCounters(lbdem_ctx* c, int cycles) {
+  for (int i = 0; i < cycles; ++i) {
+    ++c->lbTime;
+    if (c->demSolve) {
+      ++c->demTimeStep;
+      c->demTime += c->k.dt;
+    }
+  }
+  if (cycles & 1) c->cur = 1 - c->cur;
+}
 
 extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
   if (!ctx) return LBDEM_ERR_INVALID;

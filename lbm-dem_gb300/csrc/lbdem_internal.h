@@ -173,6 +173,17 @@ enum {
 
 }  // namespace lbdem
 
+namespace lbdem {
+struct JobArgs;
+}
+// many runs per launch (lbdem_capi.cu), for the run server
+void lbdemJobArgs(lbdem_ctx* c, int cur, lbdem::JobArgs* j);
+bool lbdemBatchable(const lbdem_ctx* c);
+int lbdemBatchKey(const lbdem_ctx* c);
+int lbdemEnqueueBatchCycle(const std::vector<lbdem_ctx*>& runs, const lbdem::JobArgs* jobs,
+                           cudaStream_t s);
+void lbdemAdvanceCounters(lbdem_ctx* c, int cycles);
+
 struct lbdem_ctx {
   std::string err;
   lbdem::Consts k{};
@@ -195,6 +206,8 @@ struct lbdem_ctx {
   long long deviceBytes = 0;
   int smCount = 0;
   int lbMixedBlocks = 0;  // resident blocks of the mixed lattice kernel (one wave)
+  int chunksPerBlock = 8; // at least this many 256-node chunks per lattice block
+  int gridLattice = 1;    // mixed lattice grid: one wave, or fewer for a small run
   // grids of the per-cycle kernels, sized by their work (fixed per run):
   // the free-surface area, the wall-adjacent layer, the impactor boxes and
   // the neighbour cells; grid-stride loops cover any excess

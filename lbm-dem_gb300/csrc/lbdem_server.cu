@@ -3,13 +3,24 @@
 // Jobs (a configuration and a number of goCycles) queue in submission order
 // and are admitted while their device footprint (lbdem_estimate_device_bytes)
 // fits the memory budget and a run slot is free. Each admitted job is one
-// lbdem context with its own stream; the host advances every job by slices
-// of cycles, so the kernels of different runs overlap on the device, and a
-// job that ends frees its memory (stream-ordered, no device-wide wait) for
-// the next one in the queue. Results carry the submit, start and end times
-// for latency statistics.
+// lbdem context with its own stream; a job that ends frees its memory
+// (stream-ordered, no device-wide wait) for the next one in the queue.
+// Results carry the submit, start and end times for latency statistics.
+//
+// Runs advance by slices of cycles. Runs in their steady cycle with the same
+// switches form batch groups of up to batch_runs runs: one launch per kernel
+// advances all runs of a group (grid z = run, each run's records in a device
+// array), two cycles captured in one CUDA graph, rebuilt whenever the
+// group's members change. Each group has its own stream, so the phases of
+// different groups overlap on the device (a group's latency-bound phases,
+// such as the DEM gather, leave room for another group's lattice step). A
+// run is taken into or out of a group only while neither it nor the group
+// has work in flight, so no cross-stream ordering is needed. Runs outside
+// the groups (their first cycles, an odd last cycle) advance on their own
+// streams.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <deque>
@@ -17,7 +28,7 @@
 #include <thread>
 #include <vector>
 
-#include "lbdem_internal.h"
+#include "kernels_decl.h"
 
 namespace {
 
@@ -36,6 +47,8 @@ struct Job {
   cudaEvent_t sliceDone = nullptr;
   bool inFlight = false;
   bool counted = false;  // its bytes are part of the server's memory in use
+  bool batched = false;  // a member of a batch group
+  int32_t batchedCycles = 0;
 };
 
 }  // namespace
@@ -48,6 +61,18 @@ struct lbdem_server {
   std::deque<Job*> pending;
   std::vector<Job*> active;
   std::deque<lbdem_job_result> finished;
+  // batch groups
+  struct Group {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    lbdem::JobArgs* dJobs = nullptr;  // 2 records per member: cycle 1, cycle 2
+    std::vector<lbdem::JobArgs> hJobs;
+    cudaGraphExec_t graph = nullptr;
+    std::vector<Job*> members;
+    bool inFlight = false;
+  };
+  std::vector<Group> groups;
+  int groupRuns = 0;
   double now() const {
     return std::chrono::duration<double>(Clock::now() - origin).count();
   }
@@ -74,6 +99,7 @@ void finishJob(lbdem_server* s, Job* j, int status) {
   r.job_id = j->id;
   r.status = status;
   r.cycles = j->done;
+  r.batched_cycles = j->batchedCycles;
   r.submit_time = j->submitTime;
   r.start_time = j->startTime;
   r.device_bytes = j->bytes;
@@ -122,6 +148,7 @@ void admit(lbdem_server* s) {
     std::memset(&o, 0, sizeof o);
     o.precision = s->opt.precision;
     o.device = s->opt.device;
+    o.chunks_per_block = s->opt.chunks_per_block;
     j->startTime = s->now();
     int rc = lbdem_create(&j->cfg, &o, &j->ctx);
     if (rc == LBDEM_OK && cudaEventCreateWithFlags(&j->sliceDone, cudaEventDisableTiming) !=
@@ -138,13 +165,129 @@ void admit(lbdem_server* s) {
   }
 }
 
-// One pass over the running jobs: finished slices are noticed, jobs that
-// reached their cycle count end, the others get their next slice. Returns
-// whether anything changed.
+// Capture two batched cycles of group g's members (their records uploaded
+// first) into g.graph.
+int buildGroupGraph(lbdem_server* s, lbdem_server::Group& g) {
+  if (g.graph) {
+    cudaGraphExecDestroy(g.graph);
+    g.graph = nullptr;
+  }
+  const size_t n = g.members.size();
+  g.hJobs.resize(2 * n);
+  std::vector<lbdem_ctx*> runs;
+  for (size_t i = 0; i < n; ++i) {
+    lbdem_ctx* c = g.members[i]->ctx;
+    runs.push_back(c);
+    lbdemJobArgs(c, c->cur, &g.hJobs[i]);
+    lbdemJobArgs(c, 1 - c->cur, &g.hJobs[n + i]);
+  }
+  if (cudaMemcpyAsync(g.dJobs, g.hJobs.data(), 2 * n * sizeof(lbdem::JobArgs),
+                      cudaMemcpyHostToDevice, g.stream) != cudaSuccess)
+    return serverErr(s, LBDEM_ERR_CUDA, "batch records upload");
+  cudaGraph_t graph = nullptr;
+  if (cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return serverErr(s, LBDEM_ERR_CUDA, "batch graph capture");
+  int rc = lbdemEnqueueBatchCycle(runs, g.dJobs, g.stream);
+  if (rc == LBDEM_OK) rc = lbdemEnqueueBatchCycle(runs, g.dJobs + n, g.stream);
+  const cudaError_t e = cudaStreamEndCapture(g.stream, &graph);
+  if (rc != LBDEM_OK || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return serverErr(s, rc ? rc : LBDEM_ERR_CUDA, "batch graph capture");
+  }
+  const cudaError_t ei = cudaGraphInstantiate(&g.graph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) return serverErr(s, LBDEM_ERR_CUDA, "batch graph instantiate");
+  return LBDEM_OK;
+}
+
+void dropJob(lbdem_server* s, Job* j, int status) {
+  j->batched = false;
+  for (size_t q = 0; q < s->active.size(); ++q)
+    if (s->active[q] == j) {
+      s->active.erase(s->active.begin() + q);
+      break;
+    }
+  finishJob(s, j, status);
+}
+
+// A group's turn: when its last slice is done, members that cannot take two
+// more steady cycles leave, idle batchable runs join (up to groupRuns, with
+// the group's switches), and the next slice (an even number of cycles) is
+// enqueued as graph replays on the group's stream.
+bool progressGroup(lbdem_server* s, lbdem_server::Group& g) {
+  if (g.inFlight) {
+    const cudaError_t e = cudaEventQuery(g.done);
+    if (e == cudaErrorNotReady) return false;
+    g.inFlight = false;
+    if (e != cudaSuccess) {
+      for (Job* j : g.members) dropJob(s, j, LBDEM_ERR_CUDA);
+      g.members.clear();
+      return true;
+    }
+  }
+  auto fits = [&](Job* j, int key) {
+    return j->cycles - j->done >= 2 && lbdemBatchable(j->ctx) &&
+           lbdemBatchKey(j->ctx) == key;
+  };
+  std::vector<Job*> next;
+  int key = g.members.empty() ? -1 : lbdemBatchKey(g.members[0]->ctx);
+  for (Job* j : g.members)
+    if (fits(j, key)) next.push_back(j);
+  if (next.empty()) key = -1;
+  for (Job* j : g.members) j->batched = false;
+  for (Job* j : s->active) {
+    if ((int)next.size() >= s->groupRuns) break;
+    if (j->batched || j->inFlight || j->cycles - j->done < 2 || !lbdemBatchable(j->ctx) ||
+        std::find(next.begin(), next.end(), j) != next.end())
+      continue;
+    if (key < 0) key = lbdemBatchKey(j->ctx);
+    if (lbdemBatchKey(j->ctx) == key) next.push_back(j);
+  }
+  const bool changed = next != g.members;
+  g.members = next;
+  for (Job* j : g.members) j->batched = true;
+  if (changed && !g.members.empty() && buildGroupGraph(s, g) != LBDEM_OK) {
+    for (Job* j : g.members) j->batched = false;
+    g.members.clear();
+    return true;
+  }
+  if (g.members.empty()) return changed;
+  int slice = s->opt.slice_cycles & ~1;
+  if (slice < 2) slice = 2;
+  for (Job* j : g.members) slice = std::min(slice, (j->cycles - j->done) & ~1);
+  for (int c = 0; c < slice; c += 2)
+    if (cudaGraphLaunch(g.graph, g.stream) != cudaSuccess) {
+      serverErr(s, LBDEM_ERR_CUDA, "batch graph launch");
+      break;
+    }
+  cudaEventRecord(g.done, g.stream);
+  for (Job* j : g.members) {
+    j->done += slice;
+    j->batchedCycles += slice;
+    lbdemAdvanceCounters(j->ctx, slice);
+  }
+  g.inFlight = true;
+  return true;
+}
+
+// One pass over the running jobs: the groups' turns, then the runs outside
+// them: finished slices are noticed, jobs that reached their cycle count end,
+// the others get their next slice. Returns whether anything changed.
 bool progress(lbdem_server* s) {
   bool changed = false;
+  for (auto& g : s->groups) changed = progressGroup(s, g) || changed;
   for (size_t q = 0; q < s->active.size();) {
     Job* j = s->active[q];
+    if (j->batched) {
+      ++q;
+      continue;
+    }
+    // a run that fits a group waits for a group's next turn
+    if (!s->groups.empty() && !j->inFlight && j->cycles - j->done >= 2 &&
+        lbdemBatchable(j->ctx)) {
+      ++q;
+      continue;
+    }
     if (j->inFlight) {
       const cudaError_t e = cudaEventQuery(j->sliceDone);
       if (e == cudaErrorNotReady) {
@@ -198,6 +341,19 @@ extern "C" int lbdem_server_create(const lbdem_server_options* opt, lbdem_server
   lbdem_server* s = new lbdem_server();
   s->opt = *opt;
   s->origin = Clock::now();
+  if (!opt->solo_runs) {
+    s->groupRuns = opt->batch_runs > 0 ? opt->batch_runs : 6;
+    const int ng = (opt->max_active + s->groupRuns - 1) / s->groupRuns;
+    s->groups.resize(ng);
+    for (auto& g : s->groups)
+      if (cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming) != cudaSuccess ||
+          cudaMalloc(&g.dJobs, 2 * (size_t)s->groupRuns * sizeof(lbdem::JobArgs)) !=
+              cudaSuccess) {
+        lbdem_server_destroy(s);
+        return LBDEM_ERR_CUDA;
+      }
+  }
   s->budget = opt->device_budget_bytes;
   if (s->budget <= 0) {
     size_t freeB = 0, totalB = 0;
@@ -276,6 +432,13 @@ extern "C" const char* lbdem_server_last_error(const lbdem_server* s) {
 extern "C" void lbdem_server_destroy(lbdem_server* s) {
   if (!s) return;
   cudaSetDevice(s->opt.device);
+  for (auto& g : s->groups) {
+    if (g.stream) cudaStreamSynchronize(g.stream);
+    if (g.graph) cudaGraphExecDestroy(g.graph);
+    if (g.done) cudaEventDestroy(g.done);
+    if (g.dJobs) cudaFree(g.dJobs);
+    if (g.stream) cudaStreamDestroy(g.stream);
+  }
   for (Job* j : s->active) releaseJob(s, j);
   for (Job* j : s->pending) delete j;
   delete s;

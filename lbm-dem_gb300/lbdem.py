@@ -74,7 +74,8 @@ class Config(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32),
-                ("check_every", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("check_every", C.c_int32), ("chunks_per_block", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class Info(C.Structure):
@@ -97,7 +98,8 @@ class Profile(C.Structure):
 class ServerOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("max_active", C.c_int32),
                 ("slice_cycles", C.c_int32), ("device_budget_bytes", C.c_int64),
-                ("reserved", C.c_int32 * 6)]
+                ("solo_runs", C.c_int32), ("batch_runs", C.c_int32),
+                ("chunks_per_block", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class JobResult(C.Structure):
@@ -105,7 +107,8 @@ class JobResult(C.Structure):
                 ("submit_time", C.c_double), ("start_time", C.c_double),
                 ("end_time", C.c_double), ("impactor_x0", C.c_double * 3),
                 ("impactor_x1", C.c_double * 3), ("fluid_mass", C.c_double),
-                ("active_node_updates", C.c_int64), ("device_bytes", C.c_int64)]
+                ("active_node_updates", C.c_int64), ("device_bytes", C.c_int64),
+                ("batched_cycles", C.c_int32), ("reserved", C.c_int32)]
 
 
 _P = C.POINTER(C.c_double)
@@ -397,13 +400,16 @@ def estimate_device_bytes(cfg: "LoadedConfig", precision: int = PLAIN_FP64) -> i
 class Server:
     """Many impact runs resident on one GPU (lbdem_server_*): jobs queue in
     submission order, are admitted while their device footprint fits the
-    budget, and advance by slices of goCycles on their own streams."""
+    budget, and advance by slices of goCycles; runs in their steady cycle
+    share one launch per kernel unless solo_runs is set."""
 
     def __init__(self, precision=PLAIN_FP64, device=0, max_active=16, slice_cycles=25,
-                 device_budget_bytes=0):
+                 device_budget_bytes=0, solo_runs=False, batch_runs=0, chunks_per_block=0):
         self.lib = load_library()
         o = ServerOptions(device=device, precision=precision, max_active=max_active,
-                          slice_cycles=slice_cycles, device_budget_bytes=device_budget_bytes)
+                          slice_cycles=slice_cycles, device_budget_bytes=device_budget_bytes,
+                          solo_runs=1 if solo_runs else 0, batch_runs=int(batch_runs),
+                          chunks_per_block=int(chunks_per_block))
         h = C.c_void_p()
         rc = self.lib.lbdem_server_create(C.byref(o), C.byref(h))
         if rc:
@@ -431,7 +437,8 @@ class Server:
                         "end_time": r.end_time, "impactor_x0": list(r.impactor_x0),
                         "impactor_x1": list(r.impactor_x1), "fluid_mass": r.fluid_mass,
                         "active_node_updates": r.active_node_updates,
-                        "device_bytes": r.device_bytes})
+                        "device_bytes": r.device_bytes,
+                        "batched_cycles": r.batched_cycles})
         return out
 
     def status(self) -> dict:

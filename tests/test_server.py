@@ -1,6 +1,8 @@
 """The run server (lbdem_server_*): many impact runs resident on one GPU.
 
-Each run's result must be the same alone and in the mix:
+Each run's result must be the same alone and in the mix, whether the runs
+in the mix share launches (the batch: one launch per kernel for all runs in
+their steady cycle) or advance on their own streams:
 - plain FP64 form: the impactor state to 1e-10 relative, the tolerance of
   the FP64 parity tests;
 - mixed form: the impactor displacement to 1e-3 relative, the mixed form's
@@ -50,11 +52,12 @@ def _solo(name, precision):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("solo", [False, True], ids=["batched", "solo"])
 @pytest.mark.parametrize("prec_name", ["fp64", "mixed"])
-def test_runs_in_the_mix_equal_runs_alone(prec_name, lib):
+def test_runs_in_the_mix_equal_runs_alone(prec_name, solo, lib):
     import lbdem
     prec = lbdem.PLAIN_FP64 if prec_name == "fp64" else lbdem.MIXED
-    srv = lbdem.Server(precision=prec, max_active=len(CASES), slice_cycles=7)
+    srv = lbdem.Server(precision=prec, max_active=len(CASES), slice_cycles=7, solo_runs=solo)
     cfgs = [_cfg(n) for n in CASES]
     ids = {srv.submit(c, CYCLES): n for c, n in zip(cfgs, CASES)}
     res = srv.drain()
@@ -68,6 +71,13 @@ def test_runs_in_the_mix_equal_runs_alone(prec_name, lib):
     for r in res:
         name = ids[r["job_id"]]
         assert r["status"] == 0 and r["cycles"] == CYCLES, name
+        # shared launches carried most of the cycles of the runs that reach
+        # their steady cycle (small_dup spends these cycles in its initial
+        # DEM-only phase, which runs on its own stream)
+        if solo:
+            assert r["batched_cycles"] == 0, name
+        elif name != "small_dup":
+            assert r["batched_cycles"] >= CYCLES // 2, (name, r["batched_cycles"])
         y0, x0, x1 = _solo(name, prec)
         got0, got1 = np.array(r["impactor_x0"]), np.array(r["impactor_x1"])
         if prec == lbdem.PLAIN_FP64:
