@@ -266,7 +266,9 @@ typedef struct lbdem_profile {
   int64_t lb_kernel_launches;   /* profiled launches of that kernel         */
   int64_t kernel_launches;      /* all kernels this context launched        */
   int64_t active_node_updates;  /* active nodes collided and streamed       */
-  int64_t reserved[4];
+  double phase_ms[4];           /* CUDA-event time of the profiled cycles'
+                                   DEM, coupling, lattice and free-surface
+                                   steps (lbdem_cycle only)                 */
 } lbdem_profile;
 /* Record CUDA events around every main lattice kernel launch (on the
  * context's stream) while enabled. */

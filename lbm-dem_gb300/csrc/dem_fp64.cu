@@ -127,6 +127,7 @@ LBDEM_KERNEL(, nbrCellAssign, DemArgs, dem) {
     }
     const int l = lx * nly * nlz + ly * nlz + lz;
     a.pcell[p] = l;
+    a.posf[p] = make_float4((float)x, (float)y, (float)z, (float)a.r[p]);
     atomicAdd(a.cellCount + l, 1);
   }
 }
@@ -205,6 +206,29 @@ LBDEM_KERNEL(, nbrCellSort, DemArgs, dem) {
 }
 
 __device__ __forceinline__ bool nbrWithin(const Consts& k, const double* x0, const double* r,
+                                          int P, int n1, int n2);
+// nbrWithin with an FP32 pre-test on the positions of the last cell
+// assignment: the FP32 squared distance is within about 1e-3 (lu^2) of the
+// FP64 one for lattice-sized boxes, so a pair well inside or well outside
+// the cut-off gets the FP64 answer without FP64 arithmetic. Near the cut-off,
+// or where a periodic image could apply, the FP64 test decides.
+__device__ __forceinline__ bool nbrWithinFast(const Consts& k, const DemArgs& a, int P, int n1,
+                                              int n2) {
+  const float4 p1 = a.posf[n1], p2 = a.posf[n2];
+  const float dx = p1.x - p2.x, dy = p1.y - p2.y, dz = p1.z - p2.z;
+  const float qx = 0.25f * (float)k.demSize[0], qy = 0.25f * (float)k.demSize[1],
+              qz = 0.25f * (float)k.demSize[2];
+  if (fabsf(dx) < 0.99f * qx && fabsf(dy) < 0.99f * qy && fabsf(dz) < 0.99f * qz) {
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    const float cut = p1.w + p2.w + 2.0f;
+    const float c2 = cut * cut;
+    const float band = c2 * 1e-5f + 1e-2f;
+    if (d2 < c2 - band) return true;
+    if (d2 > c2 + band) return false;
+  }
+  return nbrWithin(k, a.x0, a.r, P, n1, n2);
+}
+__device__ __forceinline__ bool nbrWithin(const Consts& k, const double* x0, const double* r,
                                           int P, int n1, int n2) {
   const double x12 = n_image_near(x0[n1] - x0[n2], k.demSize[0]);
   const double y12 = n_image_near(x0[P + n1] - x0[P + n2], k.demSize[1]);
@@ -217,8 +241,18 @@ __device__ __forceinline__ bool nbrWithin(const Consts& k, const double* x0, con
 // New list of each particle: the events of the reference's cell sweep that
 // involve it, sorted by (cell l1, neighbour-cell order, position of n1 in
 // l1, position of n2 in l2) - the order in which the reference appends them.
-LBDEM_KERNEL(, nbrBuildCells, DemArgs, dem) {
+// NBR_GROUP lanes share a particle: they split its 54 cell visits (27
+// neighbour cells, as n1 and as n2), collect the events in shared memory,
+// place each event by its rank among the keys (keys are unique), and copy
+// the tangential history slot by slot.
+constexpr int NBR_GROUP = 8;
+constexpr int NBR_PER_BLOCK = 128 / NBR_GROUP;
+LBDEM_KERNEL(__launch_bounds__(128), nbrBuildCells, DemArgs, dem) {
   if (!a.iscal[IS_REBUILD] || a.iscal[IS_DIRECT]) return;
+  __shared__ unsigned long long sKey[NBR_PER_BLOCK][MAX_N];
+  __shared__ int sNb[NBR_PER_BLOCK][MAX_N];
+  __shared__ int sSorted[NBR_PER_BLOCK][MAX_N];
+  __shared__ int sCnt[NBR_PER_BLOCK];
   const int cur = a.iscal[IS_LISTCUR];
   const int* oldList = a.list[cur];
   const double* oldXi = a.xi[cur];
@@ -226,76 +260,91 @@ LBDEM_KERNEL(, nbrBuildCells, DemArgs, dem) {
   double* newXi = a.xi[1 - cur];
   const int nlx = a.iscal[IS_NL], nly = a.iscal[IS_NL + 1], nlz = a.iscal[IS_NL + 2];
   const int P = k.nPart;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
-    const int cp = a.pcell[p];
-    if (cp < 0) continue;
-    const int cx = cp / (nly * nlz), cy = (cp / nlz) % nly, cz = cp % nlz;
-    const int posp = a.ppos[p];
-    unsigned long long keys[MAX_N];
-    int nb[MAX_N];
+  const int g = threadIdx.x / NBR_GROUP, sub = threadIdx.x % NBR_GROUP;
+  // the loop bound is uniform over the block (it holds __syncthreads)
+  for (int base = blockIdx.x * NBR_PER_BLOCK; base < P; base += gridDim.x * NBR_PER_BLOCK) {
+    const int p = base + g;
+    const int cp = p < P ? a.pcell[p] : -1;
+    const bool valid = cp >= 0;
+    if (sub == 0) sCnt[g] = 0;
+    __syncthreads();
+    if (valid) {
+      const int cx = cp / (nly * nlz), cy = (cp / nlz) % nly, cz = cp % nlz;
+      const int posp = a.ppos[p];
+      for (int v = sub; v < 54; v += NBR_GROUP) {
+        const int kk = v >> 1;
+        const int dx = kk / 9 - 1, dy = (kk / 3) % 3 - 1, dz = kk % 3 - 1;
+        if ((v & 1) == 0) {
+          // p as n1: partner q < p in l2 = l1 + d
+          const int l2 = ((cx + dx + nlx) % nlx) * nly * nlz + ((cy + dy + nly) % nly) * nlz +
+                         (cz + dz + nlz) % nlz;
+          const int s0 = a.cellStart[l2], n = a.cellFill[l2];
+          for (int t = 0; t < n; ++t) {
+            const int q = a.cellParts[s0 + t];
+            if (q >= p || !nbrWithinFast(k, a, P, p, q)) continue;
+            const int e = atomicAdd(&sCnt[g], 1);
+            if (e >= MAX_N - 1) break;
+            sKey[g][e] = ((unsigned long long)cp << 22) | ((unsigned long long)kk << 12) |
+                         ((unsigned long long)posp << 6) | (unsigned long long)(t + 1);
+            sNb[g][e] = q;
+          }
+        } else {
+          // p as n2: partner q > p in l1 = l2 - d
+          const int l1 = ((cx - dx + nlx) % nlx) * nly * nlz + ((cy - dy + nly) % nly) * nlz +
+                         (cz - dz + nlz) % nlz;
+          const int s0 = a.cellStart[l1], n = a.cellFill[l1];
+          for (int t = 0; t < n; ++t) {
+            const int q = a.cellParts[s0 + t];
+            if (q <= p || !nbrWithinFast(k, a, P, q, p)) continue;
+            const int e = atomicAdd(&sCnt[g], 1);
+            if (e >= MAX_N - 1) break;
+            sKey[g][e] = ((unsigned long long)l1 << 22) | ((unsigned long long)kk << 12) |
+                         ((unsigned long long)(t + 1) << 6) | (unsigned long long)posp;
+            sNb[g][e] = q;
+          }
+        }
+      }
+    }
+    __syncthreads();
     int cnt = 0;
-    bool over = false;
-    for (int kk = 0; kk < 27; ++kk) {
-      const int dx = kk / 9 - 1, dy = (kk / 3) % 3 - 1, dz = kk % 3 - 1;
-      // p as n1: partner q < p in l2 = l1 + d
-      {
-        const int l2 = ((cx + dx + nlx) % nlx) * nly * nlz + ((cy + dy + nly) % nly) * nlz +
-                       (cz + dz + nlz) % nlz;
-        const int s = a.cellStart[l2], n = a.cellFill[l2];
-        for (int t = 0; t < n; ++t) {
-          const int q = a.cellParts[s + t];
-          if (q >= p || !nbrWithin(k, a.x0, a.r, P, p, q)) continue;
-          if (cnt >= MAX_N - 1) { over = true; break; }
-          keys[cnt] = ((unsigned long long)cp << 22) | ((unsigned long long)kk << 12) |
-                      ((unsigned long long)posp << 6) | (unsigned long long)(t + 1);
-          nb[cnt++] = q;
+    if (valid) {
+      cnt = sCnt[g];
+      if (cnt > MAX_N - 1) {
+        if (sub == 0) atomicOr(a.iscal + IS_ERROR, ERR_NBR_OVERFLOW);
+        cnt = MAX_N - 1;
+      }
+      for (int e = sub; e < cnt; e += NBR_GROUP) {
+        const unsigned long long key = sKey[g][e];
+        int rank = 0;
+        for (int f = 0; f < cnt; ++f) rank += sKey[g][f] < key ? 1 : 0;
+        sSorted[g][rank] = sNb[g][e];
+      }
+    }
+    __syncthreads();
+    if (valid) {
+      const int* ol = oldList + (long long)p * MAX_N;
+      const double* ox = oldXi + (long long)p * 3 * MAX_N;
+      int* nl = newList + (long long)p * MAX_N;
+      double* nx = newXi + (long long)p * 3 * MAX_N;
+      if (sub == 0) {
+        nl[0] = cnt;
+        for (int c = 0; c < 3; ++c) nx[c * MAX_N] = (double)cnt;
+      }
+      // tangential history: last match in the old list wins; unmatched
+      // slots keep their old value (src/DEM.cpp:633-651)
+      const int ocnt = ol[0];
+      for (int s = 1 + sub; s < MAX_N; s += NBR_GROUP) {
+        int src = s;
+        if (s <= cnt) {
+          const int q = sSorted[g][s - 1];
+          nl[s] = q;
+          for (int l = 1; l <= ocnt; ++l)
+            if (ol[l] == q) src = l;
         }
-      }
-      // p as n2: partner q > p in l1 = l2 - d
-      {
-        const int l1 = ((cx - dx + nlx) % nlx) * nly * nlz + ((cy - dy + nly) % nly) * nlz +
-                       (cz - dz + nlz) % nlz;
-        const int s = a.cellStart[l1], n = a.cellFill[l1];
-        for (int t = 0; t < n; ++t) {
-          const int q = a.cellParts[s + t];
-          if (q <= p || !nbrWithin(k, a.x0, a.r, P, q, p)) continue;
-          if (cnt >= MAX_N - 1) { over = true; break; }
-          keys[cnt] = ((unsigned long long)l1 << 22) | ((unsigned long long)kk << 12) |
-                      ((unsigned long long)(t + 1) << 6) | (unsigned long long)posp;
-          nb[cnt++] = q;
-        }
+        for (int c = 0; c < 3; ++c) nx[c * MAX_N + s] = ox[c * MAX_N + src];
       }
     }
-    if (over) atomicOr(a.iscal + IS_ERROR, ERR_NBR_OVERFLOW);
-    for (int i = 1; i < cnt; ++i) {
-      const unsigned long long kv = keys[i];
-      const int nv = nb[i];
-      int j = i - 1;
-      while (j >= 0 && keys[j] > kv) {
-        keys[j + 1] = keys[j];
-        nb[j + 1] = nb[j];
-        --j;
-      }
-      keys[j + 1] = kv;
-      nb[j + 1] = nv;
-    }
-    const int* ol = oldList + (long long)p * MAX_N;
-    const double* ox = oldXi + (long long)p * 3 * MAX_N;
-    int* nl = newList + (long long)p * MAX_N;
-    double* nx = newXi + (long long)p * 3 * MAX_N;
-    nl[0] = cnt;
-    for (int s = 1; s <= cnt; ++s) nl[s] = nb[s - 1];
-    // tangential history: last match in the old list wins; unmatched slots
-    // keep their old value (src/DEM.cpp:633-651)
-    const int ocnt = ol[0];
-    for (int s = 1; s < MAX_N; ++s) {
-      int src = s;
-      if (s <= cnt)
-        for (int l = 1; l <= ocnt; ++l)
-          if (ol[l] == nl[s]) src = l;
-      for (int c = 0; c < 3; ++c) nx[c * MAX_N + s] = ox[c * MAX_N + src];
-    }
-    for (int c = 0; c < 3; ++c) nx[c * MAX_N] = (double)cnt;
+    __syncthreads();
   }
 }
 
@@ -360,50 +409,63 @@ LBDEM_KERNEL(, nbrDirectHistory, DemArgs, dem) {
 }
 
 // Partner slots and the gather order of every list.
+// One warp per particle: the lanes find the partner slots, lane 0 orders
+// the gather (owner slots in slot order, then the partner slots by (n1,
+// slot in n1's list)).
 LBDEM_KERNEL(, nbrPartners, DemArgs, dem) {
   if (!a.iscal[IS_REBUILD]) return;
   const int cur = 1 - a.iscal[IS_LISTCUR];
   const int* L = a.list[cur];
   const int P = k.nPart;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  for (int i = blockIdx.x * wpb + (int)(threadIdx.x >> 5); i < P; i += gridDim.x * wpb) {
     const int* li = L + (long long)i * MAX_N;
     int* pt = a.partner + (long long)i * MAX_N;
     int* go = a.gorder + (long long)i * MAX_N;
     const int cnt = li[0];
-    int ng = 0;
-    for (int s = 1; s <= cnt; ++s)
-      if (li[s] < i) go[ng++] = s;
-    const int nown = ng;
-    for (int s = 1; s <= cnt; ++s) {
+    // slot s with j = li[s] > i: the occ-th appearance of i in j's list,
+    // occ = the appearances of j in i's slots before s
+    for (int s = 1 + lane; s <= cnt; s += 32) {
       const int j = li[s];
-      pt[s] = 0;
-      if (j <= i) continue;
-      int occ = 0;
-      for (int t = 1; t < s; ++t)
-        if (li[t] == j) ++occ;
-      const int* lj = L + (long long)j * MAX_N;
-      int seen = 0;
-      for (int t = 1; t <= lj[0]; ++t)
-        if (lj[t] == i) {
-          if (seen == occ) {
-            pt[s] = t;
-            break;
+      int found = 0;
+      if (j > i) {
+        int occ = 0;
+        for (int t = 1; t < s; ++t)
+          if (li[t] == j) ++occ;
+        const int* lj = L + (long long)j * MAX_N;
+        int seen = 0;
+        for (int t = 1; t <= lj[0]; ++t)
+          if (lj[t] == i) {
+            if (seen == occ) {
+              found = t;
+              break;
+            }
+            ++seen;
           }
-          ++seen;
-        }
-      go[ng++] = s;
-    }
-    // partner part ordered by (n1, slot in n1's list)
-    for (int u = nown + 1; u < ng; ++u) {
-      const int s = go[u];
-      const long long key = (long long)li[s] * 64 + pt[s];
-      int v = u - 1;
-      while (v >= nown && (long long)li[go[v]] * 64 + pt[go[v]] > key) {
-        go[v + 1] = go[v];
-        --v;
       }
-      go[v + 1] = s;
+      pt[s] = found;
     }
+    __syncwarp();
+    if (lane == 0) {
+      int ng = 0;
+      for (int s = 1; s <= cnt; ++s)
+        if (li[s] < i) go[ng++] = s;
+      const int nown = ng;
+      for (int s = 1; s <= cnt; ++s)
+        if (li[s] > i) go[ng++] = s;
+      // partner part ordered by (n1, slot in n1's list)
+      for (int u = nown + 1; u < ng; ++u) {
+        const int s = go[u];
+        const long long key = (long long)li[s] * 64 + pt[s];
+        int v = u - 1;
+        while (v >= nown && (long long)li[go[v]] * 64 + pt[go[v]] > key) {
+          go[v + 1] = go[v];
+          --v;
+        }
+        go[v + 1] = s;
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -415,15 +477,26 @@ LBDEM_KERNEL(, nbrPairList, DemArgs, dem) {
   const int* L = a.list[1 - a.iscal[IS_LISTCUR]];
   const long long total = (long long)k.nPart * MAX_N;
   const int cap = max(k.nPart, 1) * (MAX_N / 2);
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int s = (int)(idx % MAX_N);
-    if (s == 0) continue;
-    const int i = (int)(idx / MAX_N);
-    if (s > L[(long long)i * MAX_N] || L[idx] >= i) continue;
-    const int pos = atomicAdd(a.iscal + IS_NPAIRS, 1);
-    if (pos < cap) a.pairList[pos] = (int)idx;
-    else atomicOr(a.iscal + IS_ERROR, ERR_NBR_OVERFLOW);
+  // one counter increment per warp (all lanes run the same iterations)
+  const int lane = threadIdx.x & 31;
+  for (long long b0 = blockIdx.x * (long long)blockDim.x; b0 < total;
+       b0 += (long long)gridDim.x * blockDim.x) {
+    const long long idx = b0 + threadIdx.x;
+    bool own = false;
+    if (idx < total) {
+      const int s = (int)(idx % MAX_N);
+      const int i = (int)(idx / MAX_N);
+      own = s != 0 && s <= L[(long long)i * MAX_N] && L[idx] < i;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, own);
+    int first = 0;
+    if (lane == 0 && m) first = atomicAdd(a.iscal + IS_NPAIRS, __popc(m));
+    first = __shfl_sync(0xffffffffu, first, 0);
+    if (own) {
+      const int pos = first + __popc(m & ((1u << lane) - 1u));
+      if (pos < cap) a.pairList[pos] = (int)idx;
+      else atomicOr(a.iscal + IS_ERROR, ERR_NBR_OVERFLOW);
+    }
   }
   // the last block to finish makes the new lists current
   __syncthreads();

@@ -69,6 +69,7 @@ struct DemArgs {
   double* pairbuf;
   uint8_t* pairflag;
   int* pcell;
+  float4* posf;  // [P] FP32 position and radius, written by nbrCellAssign
   int* ppos;
   int *cellCount, *cellStart, *cellFill, *cellParts;
   double* obj;

@@ -91,6 +91,55 @@ __device__ __forceinline__ bool insideSphere(double px, double py, double pz, do
   const double dx = px - cx, dy = py - cy, dz = pz - cz;
   return dx * dx + dy * dy + dz * dz < r * r;
 }
+// insideSphere for the nodes of a box: the centre is kept relative to the
+// box corner lo, where an FP32 squared distance is within about 1e-5 (lu^2)
+// of the FP64 one for spheres of a few lattice units. Outside a band of
+// r^2 * 1e-5 + 3e-5 around r^2 the FP32 comparison gives the FP64 answer;
+// inside it the FP64 test decides.
+struct SphereBoxTest {
+  double cx, cy, cz, r;
+  int lo[3];
+  float fx, fy, fz, r2in, r2out;
+};
+__device__ __forceinline__ SphereBoxTest sphereBoxTest(double cx, double cy, double cz,
+                                                       double r, const int* lo) {
+  SphereBoxTest t;
+  t.cx = cx;
+  t.cy = cy;
+  t.cz = cz;
+  t.r = r;
+  for (int a = 0; a < 3; ++a) t.lo[a] = lo[a];
+  t.fx = (float)(cx - (double)lo[0]);
+  t.fy = (float)(cy - (double)lo[1]);
+  t.fz = (float)(cz - (double)lo[2]);
+  const float r2 = (float)r * (float)r;
+  const float band = r2 * 1e-5f + 3e-5f;
+  t.r2in = r2 - band;
+  t.r2out = r2 + band;
+  return t;
+}
+__device__ __forceinline__ bool insideBox(const SphereBoxTest& t, int ix, int iy, int iz) {
+  const float dx = (float)(ix - t.lo[0]) - t.fx;
+  const float dy = (float)(iy - t.lo[1]) - t.fy;
+  const float dz = (float)(iz - t.lo[2]) - t.fz;
+  const float d2 = dx * dx + dy * dy + dz * dz;
+  if (d2 < t.r2in) return true;
+  if (d2 > t.r2out) return false;
+  return insideSphere((double)ix, (double)iy, (double)iz, t.cx, t.cy, t.cz, t.r);
+}
+// The same answer with FP32 arithmetic where it is clear: the FP32 squared
+// distance is within a few 1e-7 (relative) of the FP64 one, so outside a
+// relative band of 4e-6 around r^2 the comparison cannot differ; inside the
+// band the FP64 test decides.
+__device__ __forceinline__ bool insideSphereFast(double px, double py, double pz, double cx,
+                                                 double cy, double cz, double r) {
+  const float dx = (float)(px - cx), dy = (float)(py - cy), dz = (float)(pz - cz);
+  const float d2 = dx * dx + dy * dy + dz * dz;
+  const float r2 = (float)r * (float)r;
+  if (d2 < r2 * (1.0f - 4e-6f)) return true;
+  if (d2 > r2 * (1.0f + 4e-6f)) return false;
+  return insideSphere(px, py, pz, cx, cy, cz, r);
+}
 
 // node::setEquilibrium / computeEquilibrium for one direction,
 // src/node.cpp:52-73, 100-111

@@ -657,7 +657,7 @@ __device__ __forceinline__ void uncoverCollectBody(const Consts& k, const uint8_
                 iz = lo[2] + (int)(i / (nx * ny));
       const long long x = ix + iy * k.sy + iz * k.sz;
       if ((mask[x] & TYPE_MASK) != 12) continue;
-      if (insideSphere((double)ix, (double)iy, (double)iz, c0x, c0y, c0z, r0)) continue;
+      if (insideSphereFast((double)ix, (double)iy, (double)iz, c0x, c0y, c0z, r0)) continue;
       const int slot = atomicAdd(iscal + IS_NUNCOVER, 1);
       if (slot < UNCOVER_CAP) list[slot] = (uint32_t)x;
       else atomicOr(iscal + IS_ERROR, ERR_UNCOVER_CAP);
@@ -825,7 +825,7 @@ __device__ __forceinline__ void voxelizeObjectsBody(const Consts& k, uint8_t* ma
     const long long x = ix + iy * k.sy + iz * k.sz;
     int last = -1;
     for (int o = 0; o < k.nObj; ++o)
-      if (insideSphere((double)ix, (double)iy, (double)iz, sph[o].c[0], sph[o].c[1],
+      if (insideSphereFast((double)ix, (double)iy, (double)iz, sph[o].c[0], sph[o].c[1],
                        sph[o].c[2], sph[o].r))
         last = o;
     // the box reaches one node past the sphere, so it holds every neighbour
@@ -865,12 +865,12 @@ __device__ __forceinline__ void flagClaimBody(const Consts& k, const uint8_t* ma
     const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
     if (nx <= 0 || ny <= 0 || nz <= 0) continue;
     const int vol = nx * ny * nz;
+    const SphereBoxTest st = sphereBoxTest(cx, cy, cz, r, lo);
     for (int i = lane; i < vol; i += 32) {
       const int ix = lo[0] + i % nx, iy = lo[1] + (i / nx) % ny, iz = lo[2] + i / (nx * ny);
       const long long x = ix + iy * k.sy + iz * k.sz;
       if (!(mask[x] & ABIT)) continue;
-      if (insideSphere((double)ix, (double)iy, (double)iz, cx, cy, cz, r))
-        atomicMax(claim + x, (uint32_t)p + 1u);
+      if (insideBox(st, ix, iy, iz)) atomicMax(claim + x, (uint32_t)p + 1u);
     }
   }
 }
@@ -1092,7 +1092,7 @@ __global__ void initTypes(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* obj
     }
     uint8_t oi = 0;
     for (int o = 0; o < k.nObj; ++o) {
-      if (insideSphere(p[0], p[1], p[2], oc[o][0], oc[o][1], oc[o][2], oc[o][3])) {
+      if (insideSphereFast(p[0], p[1], p[2], oc[o][0], oc[o][1], oc[o][2], oc[o][3])) {
         so = oidx[o];
         t = 12;
         oi = (uint8_t)o;

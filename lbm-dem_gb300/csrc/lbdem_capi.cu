@@ -165,6 +165,7 @@ DemArgs demArgs(lbdem_ctx* c) {
   a.pairbuf = d.pairbuf;
   a.pairflag = d.pairflag;
   a.pcell = d.pcell;
+  a.posf = d.posf;
   a.ppos = d.ppos;
   a.cellCount = d.cellCount;
   a.cellStart = d.cellStart;
@@ -183,6 +184,11 @@ int partGrid(lbdem_ctx* c, int block) {
   return std::max(1, std::min((c->nPart + block - 1) / block, c->smCount * 16));
 }
 
+// nbrBuildCells (16 particles per 128-thread block) and nbrPartners (4)
+int nbrCellsGrid(lbdem_ctx* c) {
+  return std::max(1, std::min((c->nPart + 15) / 16, c->smCount * 16));
+}
+
 // Neighbour-list rebuild kernels (gated on the device-side rebuild flag).
 int enqueueNeighbourList(lbdem_ctx* ctx) {
   const Consts& k = ctx->k;
@@ -193,10 +199,10 @@ int enqueueNeighbourList(lbdem_ctx* ctx) {
   nbrCellScan<<<1, 1024, 0, s>>>(k, a);
   nbrCellScatter<<<pg, 128, 0, s>>>(k, a);
   nbrCellSort<<<ctx->gridCells, 128, 0, s>>>(k, a);
-  nbrBuildCells<<<pg, 128, 0, s>>>(k, a);
+  nbrBuildCells<<<nbrCellsGrid(ctx), 128, 0, s>>>(k, a);
   nbrBuildDirect<<<pg, 128, 0, s>>>(k, a);
   nbrDirectHistory<<<pg, 128, 0, s>>>(k, a);
-  nbrPartners<<<pg, 128, 0, s>>>(k, a);
+  nbrPartners<<<nbrCellsGrid(ctx), 128, 0, s>>>(k, a);  // a warp per particle
   nbrPairList<<<std::max(1, std::min(ctx->nPart * MAX_N / 256 + 1, ctx->smCount * 8)), 256, 0,
                 s>>>(k, a);
   return launchErr(ctx, "neighbour list");
@@ -503,6 +509,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   AL(d.pairbuf, P1 * MAX_N * (k.mixed ? PAIR_VALS / 2 : PAIR_VALS));
   AL(d.pairflag, P1 * MAX_N);
   AL(d.pcell, P1);
+  AL(d.posf, P1);
   AL(d.ppos, P1);
   AL(d.cellCount, (size_t)MAX_L);
   AL(d.cellStart, (size_t)MAX_L);
@@ -571,7 +578,7 @@ extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
                   d.pFLub, d.pMLub, d.pFRep, d.pFTotal, d.pMTotal, d.pFGrav, d.pxiw,
                   d.pxio, d.nF, d.pkd, d.pkf, d.pAccF, d.chunkAct, d.pairList, d.plist[0], d.plist[1], d.pxi[0],
                   d.pxi[1], d.partner, d.gorder,
-                  d.pairbuf, d.pairflag, d.pcell, d.ppos, d.cellCount, d.cellStart,
+                  d.pairbuf, d.pairflag, d.pcell, d.posf, d.ppos, d.cellCount, d.cellStart,
                   d.cellFill, d.cellParts, d.obj, d.wallF, d.walls, d.uncover};
   if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
@@ -581,6 +588,8 @@ extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
     cudaEventDestroy(e.first);
     cudaEventDestroy(e.second);
   }
+  for (auto& e : ctx->phaseEvents)
+    for (cudaEvent_t x : e) cudaEventDestroy(x);
   for (void* p : ptrs)
     if (p) cudaFreeAsync(p, ctx->own_stream);
   if (ctx->own_stream) {
@@ -717,12 +726,19 @@ extern "C" int lbdem_profile_read(lbdem_ctx* ctx, lbdem_profile* out, int reset)
   }
   unsigned long long upd = 0;
   CK(cudaMemcpy(&upd, ctx->d.uscal + US_ACTIVE_UPDATES, sizeof(upd), cudaMemcpyDeviceToHost));
+  for (size_t i = 0; i < ctx->phaseEventsUsed; ++i)
+    for (int p = 0; p < 4; ++p) {
+      float t = 0.0f;
+      CK(cudaEventElapsedTime(&t, ctx->phaseEvents[i][p], ctx->phaseEvents[i][p + 1]));
+      out->phase_ms[p] += t;
+    }
   out->lb_kernel_ms = ms;
   out->lb_kernel_launches = (int64_t)ctx->lbEventsUsed;
   out->kernel_launches = ctx->launches;
   out->active_node_updates = (int64_t)upd;
   if (reset) {
     ctx->lbEventsUsed = 0;
+    ctx->phaseEventsUsed = 0;
     ctx->launches = 0;
     CK(cudaMemsetAsync(ctx->d.uscal + US_ACTIVE_UPDATES, 0, sizeof(upd), ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -734,18 +750,41 @@ extern "C" int lbdem_profile_read(lbdem_ctx* ctx, lbdem_profile* out, int reset)
 namespace {
 
 // One goCycle (src/main.cpp:38-67) without IO.
+// Events at the step boundaries of a profiled cycle (profiling on).
+cudaEvent_t* nextPhaseEvents(lbdem_ctx* c) {
+  if (!c->profiling) return nullptr;
+  if (c->phaseEventsUsed == c->phaseEvents.size()) {
+    std::array<cudaEvent_t, 5> e;
+    for (auto& x : e)
+      if (cudaEventCreate(&x) != cudaSuccess) return nullptr;
+    c->phaseEvents.push_back(e);
+  }
+  return c->phaseEvents[c->phaseEventsUsed++].data();
+}
+
 int cycleOnce(lbdem_ctx* ctx) {
   {
     ++ctx->lbTime;
     int rc = LBDEM_OK;
+    cudaEvent_t* pe = nextPhaseEvents(ctx);
+    int marked = 0;  // events recorded so far; steps not taken get zero time
+    auto mark = [&](int i) {
+      for (; pe && marked <= i; ++marked) cudaEventRecord(pe[marked], ctx->stream);
+    };
+    mark(0);
     if (ctx->demSolve && (rc = lbdem_dem_step(ctx))) return rc;
+    mark(1);
     if (ctx->lbSolve && ctx->demTime >= ctx->demInitialRepeat) {
       if (ctx->demSolve && (rc = lbdem_coupling_step(ctx))) return rc;
+      mark(2);
       if ((rc = lbdem_lb_step(ctx))) return rc;
+      mark(3);
       if (ctx->freeSurface && (rc = lbdem_free_surface_step(ctx))) return rc;
+      mark(4);
     } else if (ctx->lbSolve && ctx->demTime <= ctx->demInitialRepeat) {
       if (ctx->demSolve && (rc = lbdem_coupling_step(ctx))) return rc;
     }
+    mark(4);
     if (ctx->check_every > 0 && ctx->lbTime % ctx->check_every == 0 && ctx->lbSolve) {
       nonfiniteCheck<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(
           ctx->k, ctx->d.mask, ctx->d.f[ctx->cur], ctx->d.iscal);
@@ -876,10 +915,10 @@ int lbdemEnqueueBatchCycle(const std::vector<lbdem_ctx*>& runs, const JobArgs* j
   nbrCellScanBatch<<<G(1), 1024, 0, s>>>(jobs);
   nbrCellScatterBatch<<<G(pg), 128, 0, s>>>(jobs);
   nbrCellSortBatch<<<G(gmax([](lbdem_ctx* c) { return c->gridCells; })), 128, 0, s>>>(jobs);
-  nbrBuildCellsBatch<<<G(pg), 128, 0, s>>>(jobs);
+  nbrBuildCellsBatch<<<G(gmax([](lbdem_ctx* c) { return nbrCellsGrid(c); })), 128, 0, s>>>(jobs);
   nbrBuildDirectBatch<<<G(pg), 128, 0, s>>>(jobs);
   nbrDirectHistoryBatch<<<G(pg), 128, 0, s>>>(jobs);
-  nbrPartnersBatch<<<G(pg), 128, 0, s>>>(jobs);
+  nbrPartnersBatch<<<G(gmax([](lbdem_ctx* c) { return nbrCellsGrid(c); })), 128, 0, s>>>(jobs);
   nbrPairListBatch<<<G(gmax([](lbdem_ctx* c) {
                        return std::max(1, std::min(c->nPart * MAX_N / 256 + 1, c->smCount * 8));
                      })),
@@ -1064,6 +1103,7 @@ extern "C" int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t prec
   add(P1 * MAX_N, 1);                          // pairflag
   add(P1, 4);
   add(P1, 4);                                  // pcell, ppos
+  add(P1, 16);                                 // posf
   for (int i = 0; i < 3; ++i) add(MAX_L, 4);   // cell arrays
   add(P1, 4);                                  // cellParts
   add(O1 * OB_STRIDE, 8);

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <array>
 #include <string>
 #include <vector>
 
@@ -116,6 +117,7 @@ struct Device {
   double* pairbuf = nullptr;             // [P][50][PAIR_VALS]
   uint8_t* pairflag = nullptr;           // [P][50] bit0 = lubrication valid
   int* pcell = nullptr;                  // [P] cell of particle
+  float4* posf = nullptr;                // [P] FP32 position and radius (list rebuilds)
   int* ppos = nullptr;                   // [P] position in its cell (1-based)
   int* cellCount = nullptr;              // [MAX_L]
   int* cellStart = nullptr;              // [MAX_L]
@@ -216,6 +218,10 @@ struct lbdem_ctx {
   bool profiling = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> lbEvents;
   size_t lbEventsUsed = 0;
+  // per profiled cycle: events before the DEM step and after each of the
+  // four steps
+  std::vector<std::array<cudaEvent_t, 5>> phaseEvents;
+  size_t phaseEventsUsed = 0;
   long long launches = 0;
   // two goCycles as one CUDA graph, per starting lattice buffer
   cudaGraphExec_t pairGraph[2] = {nullptr, nullptr};

@@ -92,7 +92,7 @@ class Info(C.Structure):
 class Profile(C.Structure):
     _fields_ = [("lb_kernel_ms", C.c_double), ("lb_kernel_launches", C.c_int64),
                 ("kernel_launches", C.c_int64), ("active_node_updates", C.c_int64),
-                ("reserved", C.c_int64 * 4)]
+                ("phase_ms", C.c_double * 4)]
 
 
 class ServerOptions(C.Structure):
