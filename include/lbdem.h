@@ -290,12 +290,11 @@ typedef struct lbdem_server_options {
   int32_t max_active;     /* runs resident at once                         */
   int32_t slice_cycles;   /* goCycles enqueued per run per turn            */
   int64_t device_budget_bytes; /* 0: 90 % of the free memory at creation   */
-  int32_t solo_runs;      /* 1: every run on its own stream only (no launches
-                             shared by several runs)                        */
-  int32_t batch_runs;     /* runs per batch group, each group on its own
-                             stream (0: 6)                                  */
+  int32_t batch_runs;     /* 0: every run on its own stream; N > 0: runs in
+                             their steady cycle share launches in groups of
+                             up to N, each group on its own stream          */
   int32_t chunks_per_block; /* passed to every run (lbdem_options)         */
-  int32_t reserved[3];
+  int32_t reserved[4];
 } lbdem_server_options;
 
 typedef struct lbdem_job_result {
@@ -315,12 +314,14 @@ typedef struct lbdem_job_result {
  * the budget next to the runs in progress and fewer than max_active runs
  * are resident. Each admitted job is a context with its own stream, and
  * lbdem_server_poll advances every resident run by slice_cycles goCycles
- * per turn. Runs in their steady cycle with the same switches (free
- * surface, impactor, walls) are advanced in batch groups of up to
- * batch_runs runs: one launch per kernel for all runs of a group (grid
- * z = run), the pair of cycles captured in a CUDA graph that is rebuilt when
- * the group's runs change, each group on its own stream; the other runs
- * advance on their own streams. A finished run frees its memory for the
+ * per turn, each run's steady cycles replayed from its own CUDA graphs on its
+ * own stream. With batch_runs > 0, runs in their steady cycle with the same
+ * switches (free surface, impactor, walls) are advanced in batch groups of
+ * up to batch_runs runs instead: one launch per kernel for all runs of a
+ * group (grid z = run), the pair of cycles captured in a CUDA graph that is
+ * rebuilt when the group's runs change, each group on its own stream. Set
+ * CUDA_DEVICE_MAX_CONNECTIONS (for example 32) before the first CUDA call
+ * when more than 8 streams are to run concurrently. A finished run frees its memory for the
  * next job. The server's calls must come from one host thread. */
 int lbdem_server_create(const lbdem_server_options* opt, lbdem_server** out);
 /* Queue a run of `cycles` goCycles; the configuration and its tables are

@@ -7,8 +7,9 @@
 // (stream-ordered, no device-wide wait) for the next one in the queue.
 // Results carry the submit, start and end times for latency statistics.
 //
-// Runs advance by slices of cycles. Runs in their steady cycle with the same
-// switches form batch groups of up to batch_runs runs: one launch per kernel
+// Runs advance by slices of cycles, each on its own stream with its own
+// graphs. On request (batch_runs > 0), runs in their steady cycle with the
+// same switches form batch groups of up to batch_runs runs instead: one launch per kernel
 // advances all runs of a group (grid z = run, each run's records in a device
 // array), two cycles captured in one CUDA graph, rebuilt whenever the
 // group's members change. Each group has its own stream, so the phases of
@@ -341,8 +342,8 @@ extern "C" int lbdem_server_create(const lbdem_server_options* opt, lbdem_server
   lbdem_server* s = new lbdem_server();
   s->opt = *opt;
   s->origin = Clock::now();
-  if (!opt->solo_runs) {
-    s->groupRuns = opt->batch_runs > 0 ? opt->batch_runs : 6;
+  if (opt->batch_runs > 0) {
+    s->groupRuns = opt->batch_runs;
     const int ng = (opt->max_active + s->groupRuns - 1) / s->groupRuns;
     s->groups.resize(ng);
     for (auto& g : s->groups)

@@ -98,8 +98,8 @@ class Profile(C.Structure):
 class ServerOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("max_active", C.c_int32),
                 ("slice_cycles", C.c_int32), ("device_budget_bytes", C.c_int64),
-                ("solo_runs", C.c_int32), ("batch_runs", C.c_int32),
-                ("chunks_per_block", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("batch_runs", C.c_int32), ("chunks_per_block", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class JobResult(C.Structure):
@@ -400,15 +400,15 @@ def estimate_device_bytes(cfg: "LoadedConfig", precision: int = PLAIN_FP64) -> i
 class Server:
     """Many impact runs resident on one GPU (lbdem_server_*): jobs queue in
     submission order, are admitted while their device footprint fits the
-    budget, and advance by slices of goCycles; runs in their steady cycle
-    share one launch per kernel unless solo_runs is set."""
+    budget, and advance by slices of goCycles on their own streams; with
+    batch_runs > 0 runs in their steady cycle share launches in groups."""
 
     def __init__(self, precision=PLAIN_FP64, device=0, max_active=16, slice_cycles=25,
-                 device_budget_bytes=0, solo_runs=False, batch_runs=0, chunks_per_block=0):
+                 device_budget_bytes=0, batch_runs=0, chunks_per_block=0):
         self.lib = load_library()
         o = ServerOptions(device=device, precision=precision, max_active=max_active,
                           slice_cycles=slice_cycles, device_budget_bytes=device_budget_bytes,
-                          solo_runs=1 if solo_runs else 0, batch_runs=int(batch_runs),
+                          batch_runs=int(batch_runs),
                           chunks_per_block=int(chunks_per_block))
         h = C.c_void_p()
         rc = self.lib.lbdem_server_create(C.byref(o), C.byref(h))

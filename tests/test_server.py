@@ -57,7 +57,8 @@ def _solo(name, precision):
 def test_runs_in_the_mix_equal_runs_alone(prec_name, solo, lib):
     import lbdem
     prec = lbdem.PLAIN_FP64 if prec_name == "fp64" else lbdem.MIXED
-    srv = lbdem.Server(precision=prec, max_active=len(CASES), slice_cycles=7, solo_runs=solo)
+    srv = lbdem.Server(precision=prec, max_active=len(CASES), slice_cycles=7,
+                       batch_runs=0 if solo else 2)
     cfgs = [_cfg(n) for n in CASES]
     ids = {srv.submit(c, CYCLES): n for c, n in zip(cfgs, CASES)}
     res = srv.drain()
