@@ -374,8 +374,9 @@ def serving(args) -> dict:
     def pct(v, q):
         return float(np.percentile(np.asarray(v), q)) if len(v) else None
 
-    def batch(prec, jobs):
-        srv = lbdem.Server(precision=prec, max_active=len(jobs), slice_cycles=args.serve_slice)
+    def batch(prec, jobs, **opts):
+        srv = lbdem.Server(precision=prec, max_active=len(jobs), slice_cycles=args.serve_slice,
+                           **opts)
         t0 = time.perf_counter()
         for c in jobs:
             srv.submit(c, C)
@@ -421,6 +422,23 @@ def serving(args) -> dict:
     for c in cfgs:
         c.close()
     lat = [r["end_time"] - r["submit_time"] for r in res]
+    # batched configuration: many runs resident at once, their schedule
+    # (runs per shared launch group, lattice chunks per block) picked by the
+    # autotuner on a sample of them
+    rng64 = np.random.default_rng(args.serve_seed + 1)
+    many = []
+    for i in range(args.serve_batch_jobs):
+        d = os.path.join(CACHE, f"serve{args.serve_seed + 1}", f"j{i:03d}")
+        case = casegen.serving_case(rng64, f"b{i}")
+        if not os.path.exists(os.path.join(d, "parameters.cfg")):
+            case.write(d)
+        many.append(lbdem.LoadedConfig(os.path.join(d, "parameters.cfg")))
+    tb, tc, _ = lbdem.tune_server(many[:8], cycles=40, slice_cycles=args.serve_slice)
+    batched = batch(lbdem.MIXED, many, batch_runs=tb, chunks_per_block=tc)
+    batched["schedule"] = {"batch_runs": tb, "chunks_per_block": tc,
+                           "tuned_on": "the first 8 runs, 40 cycles each"}
+    for c in many:
+        c.close()
     return {
         "sample": f"{len(cfgs)} seeded runs (lattice sides 48-128, vertical 48-160, fluid to "
                   f"60 %, grid-packed phi 0.25-0.30, impactor r 6-16, vy 0.005-0.05), {C} "
@@ -432,6 +450,7 @@ def serving(args) -> dict:
         "poisson_mixed": {"rate_per_min": round(rate * 60.0, 2), "jobs": len(res),
                           "jobs_per_hour": round(len(res) / wall * 3600.0, 1),
                           "p50_s": round(pct(lat, 50), 4), "p99_s": round(pct(lat, 99), 4)},
+        "batched_mixed": batched,
     }
 
 
@@ -452,6 +471,7 @@ def main():
     ap.add_argument("--serve-cycles", type=int, default=200)
     ap.add_argument("--serve-slice", type=int, default=24)
     ap.add_argument("--serve-seed", type=int, default=3)
+    ap.add_argument("--serve-batch-jobs", type=int, default=64)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     os.makedirs(CACHE, exist_ok=True)

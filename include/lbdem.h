@@ -136,7 +136,10 @@ typedef struct lbdem_options {
   int32_t chunks_per_block; /* mixed lattice step: 256-node chunks per block
                                at least (0: 8); fewer blocks for a small
                                lattice leave SMs to other runs            */
-  int32_t reserved[4];
+  int32_t async_init;  /* 1: lbdem_create returns once the device
+                          initialisation is enqueued; its device errors
+                          surface at the next lbdem_sync                  */
+  int32_t reserved[3];
 } lbdem_options;
 
 typedef struct lbdem_ctx lbdem_ctx;
@@ -337,6 +340,13 @@ int lbdem_server_status(const lbdem_server* s, int32_t* queued, int32_t* running
 const char* lbdem_server_last_error(const lbdem_server* s);
 /* Ends the runs still resident (without results) and frees everything. */
 void lbdem_server_destroy(lbdem_server* s);
+/* Autotuner: runs the n sample configurations for `cycles` goCycles under
+ * each candidate schedule (batch_runs 0, 2, 4, 8 x chunks_per_block 8, 32)
+ * with the other fields of *opt, and writes the fastest schedule into
+ * opt->batch_runs and opt->chunks_per_block; *best_seconds (optional) gets
+ * its time. Runs on the device of opt. */
+int lbdem_server_tune(lbdem_server_options* opt, const lbdem_config* const* cfgs, int32_t n,
+                      int32_t cycles, double* best_seconds);
 
 /* ---- readback without device allocation (no counterpart in the
  * reference; a diagnostic of this library) ------------------------------ */

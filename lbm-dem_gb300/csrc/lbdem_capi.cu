@@ -560,9 +560,10 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
     demBegin<<<partGrid(ctx, 256), 256, 0, st>>>(k, a, 1);
     if ((rc = enqueueNeighbourList(ctx)) != LBDEM_OK) return rc;
   }
-  CK(cudaStreamSynchronize(st));
   cudaFreeAsync(dBoundary, st);
   cudaFreeAsync(dWallType, st);
+  if (opt && opt->async_init) return launchErr(ctx, "init");
+  CK(cudaStreamSynchronize(st));
   int e = 0;
   CK(cudaMemcpy(&e, d.iscal + IS_ERROR, sizeof(int), cudaMemcpyDeviceToHost));
   if (e) return setErr(ctx, LBDEM_ERR_DEVICE_STATE, "device error during init: " + std::to_string(e));

@@ -135,13 +135,15 @@ void finishJob(lbdem_server* s, Job* j, int status) {
 }
 
 // Admit queued jobs, in order, while memory and run slots allow. Creating a
-// run blocks the host for its initialisation, so while runs are in progress
-// only one is admitted per turn and the others keep getting slices.
+// run blocks the host for its initialisation (about a millisecond for a
+// small run), so while runs are in progress admission stops after 2 ms of a
+// turn and the resident runs get their next slices.
 void admit(lbdem_server* s) {
   const bool busy = !s->active.empty();
+  const double t0 = s->now();
   int admitted = 0;
   while (!s->pending.empty() && (int)s->active.size() < s->opt.max_active &&
-         !(busy && admitted >= 1)) {
+         !(busy && admitted >= 1 && s->now() - t0 > 2e-3)) {
     Job* j = s->pending.front();
     if (s->used + j->bytes > s->budget && !s->active.empty()) break;
     s->pending.pop_front();
@@ -150,6 +152,9 @@ void admit(lbdem_server* s) {
     o.precision = s->opt.precision;
     o.device = s->opt.device;
     o.chunks_per_block = s->opt.chunks_per_block;
+    // the run's initialisation overlaps the other runs' work; its device
+    // errors surface at the run's end
+    o.async_init = 1;
     j->startTime = s->now();
     int rc = lbdem_create(&j->cfg, &o, &j->ctx);
     if (rc == LBDEM_OK && cudaEventCreateWithFlags(&j->sliceDone, cudaEventDisableTiming) !=
@@ -443,4 +448,47 @@ extern "C" void lbdem_server_destroy(lbdem_server* s) {
   for (Job* j : s->active) releaseJob(s, j);
   for (Job* j : s->pending) delete j;
   delete s;
+}
+
+extern "C" int lbdem_server_tune(lbdem_server_options* opt, const lbdem_config* const* cfgs,
+                                 int32_t n, int32_t cycles, double* best_seconds) {
+  if (!opt || !cfgs || n < 1 || cycles < 1) return LBDEM_ERR_INVALID;
+  const int32_t batchC[] = {0, 2, 4, 8};
+  const int32_t chunkC[] = {8, 32};
+  double best = -1.0;
+  int32_t bestB = 0, bestC = 8;
+  for (int32_t b : batchC)
+    for (int32_t c : chunkC) {
+      lbdem_server_options o = *opt;
+      o.batch_runs = b;
+      o.chunks_per_block = c;
+      if (o.max_active < n) o.max_active = n;
+      lbdem_server* s = nullptr;
+      int rc = lbdem_server_create(&o, &s);
+      if (rc != LBDEM_OK) return rc;
+      const auto t0 = Clock::now();
+      for (int32_t i = 0; i < n && rc == LBDEM_OK; ++i)
+        rc = lbdem_server_submit(s, cfgs[i], cycles, nullptr);
+      int32_t done = 0;
+      std::vector<lbdem_job_result> res(n);
+      while (rc == LBDEM_OK && done < n) {
+        int32_t got = 0;
+        rc = lbdem_server_poll(s, 0.05, res.data() + done, n - done, &got);
+        for (int32_t i = done; i < done + got; ++i)
+          if (res[i].status != LBDEM_OK) rc = res[i].status;
+        done += got;
+      }
+      const double t = std::chrono::duration<double>(Clock::now() - t0).count();
+      lbdem_server_destroy(s);
+      if (rc != LBDEM_OK) return rc;
+      if (best < 0.0 || t < best) {
+        best = t;
+        bestB = b;
+        bestC = c;
+      }
+    }
+  opt->batch_runs = bestB;
+  opt->chunks_per_block = bestC;
+  if (best_seconds) *best_seconds = best;
+  return LBDEM_OK;
 }

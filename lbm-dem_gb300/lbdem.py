@@ -75,7 +75,7 @@ class Config(C.Structure):
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32),
                 ("check_every", C.c_int32), ("chunks_per_block", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("async_init", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class Info(C.Structure):
@@ -179,6 +179,8 @@ def load_library(path: str | None = None) -> C.CDLL:
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int64)], C.c_int),
         "lbdem_server_last_error": ([C.c_void_p], C.c_char_p),
         "lbdem_server_destroy": ([C.c_void_p], None),
+        "lbdem_server_tune": ([C.POINTER(ServerOptions), C.POINTER(C.POINTER(Config)), C.c_int32,
+                               C.c_int32, C.POINTER(C.c_double)], C.c_int),
         "lbdem_download_nodes_noalloc": ([c_ctx, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p],
                                          C.c_int),
     }
@@ -463,6 +465,20 @@ class Server:
         if self.h:
             self.lib.lbdem_server_destroy(self.h)
             self.h = None
+
+
+def tune_server(cfgs, cycles=40, precision=MIXED, device=0, max_active=0, slice_cycles=24):
+    """lbdem_server_tune: the fastest (batch_runs, chunks_per_block) for these
+    sample runs; returns (batch_runs, chunks_per_block, seconds)."""
+    lib = load_library()
+    o = ServerOptions(device=device, precision=precision,
+                      max_active=max_active or len(cfgs), slice_cycles=slice_cycles)
+    arr = (C.POINTER(Config) * len(cfgs))(*[C.pointer(c.cfg) for c in cfgs])
+    t = C.c_double()
+    rc = lib.lbdem_server_tune(C.byref(o), arr, len(cfgs), int(cycles), C.byref(t))
+    if rc:
+        raise RuntimeError(f"lbdem_server_tune: {ERRORS.get(rc, rc)}")
+    return o.batch_runs, o.chunks_per_block, t.value
 
     def __del__(self):
         try:
