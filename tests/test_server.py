@@ -122,3 +122,13 @@ def test_estimate_bounds_the_allocation(lib):
             s.close()
             assert got <= est <= got + 64 * 1024, (name, prec, got, est)
         cfg.close()
+
+
+@pytest.mark.gpu
+def test_tuner_picks_a_candidate_schedule(lib):
+    import lbdem
+    cfgs = [_cfg(n) for n in ("small_cells", "tiny_direct")]
+    b, c, t = lbdem.tune_server(cfgs, cycles=4, precision=lbdem.MIXED, slice_cycles=2)
+    for cf in cfgs:
+        cf.close()
+    assert b in (0, 2, 4, 8) and c in (8, 32) and t > 0.0
