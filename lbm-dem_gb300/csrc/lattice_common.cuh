@@ -85,6 +85,17 @@ __device__ __forceinline__ void coords(const Consts& k, long long x, int& ix, in
   ix = (int)(rem - (unsigned)iy * (unsigned)k.X);
 }
 
+// Compensated accumulation of a mass-budget sum: the atomic addition's
+// rounding error, formed from the value it replaced (TwoSum; exact without
+// contraction), goes to a second accumulator; the budget is acc + lo.
+__device__ __forceinline__ void atomicAddComp(double* acc, double* lo, double v) {
+  const double old = atomicAdd(acc, v);
+  const double s = __dadd_rn(old, v);
+  const double bp = __dsub_rn(s, old);
+  const double err = __dadd_rn(__dsub_rn(old, __dsub_rn(s, bp)), __dsub_rn(v, bp));
+  if (err != 0.0) atomicAdd(lo, err);
+}
+
 // tinyVector::insideSphere, src/myvector.cpp:171-176, on node coordinates
 __device__ __forceinline__ bool insideSphere(double px, double py, double pz, double cx,
                                              double cy, double cz, double r) {

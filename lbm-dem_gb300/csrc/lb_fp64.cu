@@ -202,7 +202,7 @@ LBDEM_KERNEL(__launch_bounds__(256), lbStepFp64, LbArgs, lb) {
       const int o = (i - ACC_OBJ) / 6, c = (i - ACC_OBJ) % 6;
       atomicAdd(a.obj + o * OB_STRIDE + (c < 3 ? OB_FHYDRO + c : OB_MHYDRO + c - 3), v);
     } else {
-      atomicAdd(a.scal + SC_EXTRA_MASS, v);
+      atomicAddComp(a.scal + SC_EXTRA_MASS, a.scal + SC_EXTRA_MASS_LO, v);
     }
   }
   if (threadIdx.x == 0) {
@@ -256,6 +256,7 @@ __device__ __forceinline__ void lbPrepareBody(const Consts& k, double* pAcc, lon
     for (int c = 0; c < 3; ++c) wallF[i0 * 12 + c] = 0.0;
   if (i0 == 0) {
     scal[SC_EXTRA_MASS] = 0.0;
+    scal[SC_EXTRA_MASS_LO] = 0.0;
     iscal[IS_NIF] = 0;
     iscal[IS_BBOX + 0] = iscal[IS_BBOX + 1] = iscal[IS_BBOX + 2] = INT_MAX;
     iscal[IS_BBOX + 3] = iscal[IS_BBOX + 4] = iscal[IS_BBOX + 5] = -1;
@@ -325,12 +326,14 @@ __device__ __forceinline__ void lbFinalizeBody(const Consts& k, double* pF, doub
         obj[o * OB_STRIDE + OB_FHYDRO + c] *= k.uForce;
         obj[o * OB_STRIDE + OB_MHYDRO + c] *= k.uTorque;
       }
-    scal[SC_ADD_MASS] = scal[SC_EXTRA_MASS] / (double)(unsigned)iscal[IS_NIF];
+    scal[SC_ADD_MASS] =
+        (scal[SC_EXTRA_MASS] + scal[SC_EXTRA_MASS_LO]) / (double)(unsigned)iscal[IS_NIF];
   }
   if (redistribute) {
     // LB::redistributeMass(extraMass) over the interface nodes; every thread
     // forms the same quotient block 0 stores above
-    const double addMass = scal[SC_EXTRA_MASS] / (double)(unsigned)iscal[IS_NIF];
+    const double addMass =
+        (scal[SC_EXTRA_MASS] + scal[SC_EXTRA_MASS_LO]) / (double)(unsigned)iscal[IS_NIF];
     FS_LOOP(k, fa, {
       if ((fa.mask[x] & TYPE_MASK) == 3) {
         // the mass the collision used, for fsUpdateMass's recomputation
@@ -347,7 +350,8 @@ __device__ __forceinline__ void lbFinalizeBody(const Consts& k, double* pF, doub
 enum : uint8_t { FS_FILLED = 1, FS_EMPTIED = 2, FS_NEW = 4 };
 
 // Region = interface bounding box of the LB step grown by one node.
-__device__ __forceinline__ void blockAddDouble(double v, double* dst) {
+// dst += the block's sum of v; with lo, compensated (atomicAddComp)
+__device__ __forceinline__ void blockAddDouble(double v, double* dst, double* lo = nullptr) {
   __shared__ double red[32];
   const unsigned FULL = 0xffffffffu;
 #pragma unroll
@@ -359,7 +363,10 @@ __device__ __forceinline__ void blockAddDouble(double v, double* dst) {
     double s = l < (int)(blockDim.x >> 5) ? red[l] : 0.0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
-    if (l == 0 && s != 0.0) atomicAdd(dst, s);
+    if (l == 0 && s != 0.0) {
+      if (lo) atomicAddComp(dst, lo, s);
+      else atomicAdd(dst, s);
+    }
   }
   __syncthreads();
 }
@@ -399,6 +406,7 @@ LBDEM_KERNEL(, fsUpdateMass, FsArgs, fs) {
   // (fsUpdateMass itself accumulates neither)
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.scal[SC_SURPLUS] = 0.0;
+    a.scal[SC_SURPLUS_LO] = 0.0;
     a.iscal[IS_NIF2] = 0;
   }
   FS_LOOP(k, a, {
@@ -511,7 +519,7 @@ LBDEM_KERNEL(, fsSmoothen, FsArgs, fs) {
       }
     }
   })
-  blockAddDouble(surplus, a.scal + SC_SURPLUS);
+  blockAddDouble(surplus, a.scal + SC_SURPLUS, a.scal + SC_SURPLUS_LO);
 }
 
 // updateMutants + removeIsolated, first pass (src/LB.cpp:1751-1817).
@@ -543,7 +551,7 @@ LBDEM_KERNEL(, fsMutantsAndFill, FsArgs, fs) {
       }
     }
   })
-  blockAddDouble(surplus, a.scal + SC_SURPLUS);
+  blockAddDouble(surplus, a.scal + SC_SURPLUS, a.scal + SC_SURPLUS_LO);
 }
 
 // removeIsolated, second pass (src/LB.cpp:1819-1841), and the interface count.
@@ -568,7 +576,7 @@ LBDEM_KERNEL(, fsEmptyIsolated, FsArgs, fs) {
       ++cnt;
     }
   })
-  blockAddDouble(surplus, a.scal + SC_SURPLUS);
+  blockAddDouble(surplus, a.scal + SC_SURPLUS, a.scal + SC_SURPLUS_LO);
   if (cnt) atomicAdd(a.iscal + IS_NIF2, cnt);
 }
 
@@ -578,7 +586,8 @@ LBDEM_KERNEL(, fsEmptyIsolated, FsArgs, fs) {
 // -> gas) lie in the box grown by 1, so their neighbours lie in the box
 // grown by 2. Every thread writes only its own node's mask byte.
 LBDEM_KERNEL(, fsRedistribute, FsArgs, fs) {
-  const double addMass = a.scal[SC_SURPLUS] / (double)(unsigned)a.iscal[IS_NIF2];
+  const double addMass =
+      (a.scal[SC_SURPLUS] + a.scal[SC_SURPLUS_LO]) / (double)(unsigned)a.iscal[IS_NIF2];
   int x1, y1, z1, rx1, ry1, rz1;
   if (!fsRegion(k, a.iscal, x1, y1, z1, rx1, ry1, rz1)) return;
   const int x0 = max(a.iscal[IS_BBOX + 0] - 2, 0), y0 = max(a.iscal[IS_BBOX + 1] - 2, 0),

@@ -470,7 +470,7 @@ LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
               (double)accO[i]);
   }
   if (threadIdx.x == 0) {
-    if (accX != 0.0) atomicAdd(a.scal + SC_EXTRA_MASS, accX);
+    if (accX != 0.0) atomicAddComp(a.scal + SC_EXTRA_MASS, a.scal + SC_EXTRA_MASS_LO, accX);
     if (scnt[0]) atomicAdd(a.uscal + US_ACTIVE_UPDATES, (unsigned long long)scnt[0]);
     if (scnt[1]) atomicAdd(a.iscal + IS_NIF, (int)scnt[1]);
     if (sbox[3] >= 0) {

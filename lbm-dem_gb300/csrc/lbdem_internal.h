@@ -137,6 +137,10 @@ enum {
   SC_SURPLUS,         // free-surface mass surplus
   SC_MAXDISP,         // DEM::maxDisp
   SC_TOTAL_MASS,      // diagnostics
+  // compensation terms of the two mass-budget sums: the rounding error of
+  // every atomic addition to SC_EXTRA_MASS / SC_SURPLUS (atomicAddComp)
+  SC_EXTRA_MASS_LO,
+  SC_SURPLUS_LO,
   SC_COUNT
 };
 // offsets into Device::iscal (ints)
