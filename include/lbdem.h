@@ -261,6 +261,30 @@ int lbdem_mass_summary(lbdem_ctx* ctx, double* total_mass,
  * conserved quantity of the free-surface mass budget). */
 int lbdem_mass_total(lbdem_ctx* ctx, double* total_mass);
 
+/* ---- checkpoint / restore -------------------------------------------- */
+
+/* Write a snapshot of the whole run to `path`: every device buffer at full
+ * precision (lattice, interface masses, particle and impactor state,
+ * neighbour lists, tangential springs, the free-surface budget) and the
+ * step counters. Synchronises the context's stream first, so everything
+ * enqueued before the call is part of the snapshot.
+ * Replaces the reference's resume files IO::exportRecycleFluid
+ * (src/IO.cpp:973-997) and IO::exportRecycleParticles (src/IO.cpp:999),
+ * which keep six significant digits and neither the neighbour lists, the
+ * springs nor the counters. Returns LBDEM_ERR_IO if the file cannot be
+ * written. */
+int lbdem_checkpoint(lbdem_ctx* ctx, const char* path);
+
+/* Load a snapshot written by lbdem_checkpoint into `ctx`, which must have
+ * been created from the same configuration in the same form: the snapshot
+ * replaces its whole state and its step counters, and the next step
+ * continues the snapshotted run. Replaces the reference's restart read
+ * (LB::restartInterface / LB::restartVariables, src/LB.cpp:994-1138, under
+ * lbRestart). A snapshot of another lattice size, particle, impactor or
+ * wall count, form, library build, or a truncated file is refused with
+ * LBDEM_ERR_INVALID or LBDEM_ERR_IO before any state is changed. */
+int lbdem_restore(lbdem_ctx* ctx, const char* path);
+
 /* ---- measurement (no counterpart in the reference) --------------------- */
 
 typedef struct lbdem_profile {

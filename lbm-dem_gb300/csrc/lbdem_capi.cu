@@ -50,8 +50,20 @@ int dalloc(lbdem_ctx* ctx, T** p, size_t count) {
   if (e != cudaSuccess)
     return setErr(ctx, LBDEM_ERR_OOM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
   ctx->deviceBytes += (long long)bytes;
+  ctx->buffers.emplace_back((void*)*p, bytes);
   cudaMemsetAsync(*p, 0, bytes, ctx->stream);
   return LBDEM_OK;
+}
+
+// frees a buffer taken with dalloc that the run does not keep
+void dfree(lbdem_ctx* ctx, void* p) {
+  for (size_t i = 0; i < ctx->buffers.size(); ++i)
+    if (ctx->buffers[i].first == p) {
+      ctx->deviceBytes -= (long long)ctx->buffers[i].second;
+      ctx->buffers.erase(ctx->buffers.begin() + (long)i);
+      break;
+    }
+  cudaFreeAsync(p, ctx->stream);
 }
 
 int launchErr(lbdem_ctx* ctx, const char* what) {
@@ -560,8 +572,8 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
     demBegin<<<partGrid(ctx, 256), 256, 0, st>>>(k, a, 1);
     if ((rc = enqueueNeighbourList(ctx)) != LBDEM_OK) return rc;
   }
-  cudaFreeAsync(dBoundary, st);
-  cudaFreeAsync(dWallType, st);
+  dfree(ctx, dBoundary);
+  dfree(ctx, dWallType);
   if (opt && opt->async_init) return launchErr(ctx, "init");
   CK(cudaStreamSynchronize(st));
   int e = 0;
@@ -572,15 +584,6 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
 
 extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
   if (!ctx) return;
-  Device& d = ctx->d;
-  void* ptrs[] = {d.mask, d.solid, d.objIdx, d.claim, d.fsflag, d.f[0], d.f[1], d.mass,
-                  d.massNew, d.rhoS, d.uS, d.hS, d.scal, d.iscal, d.uscal, d.px0, d.px1,
-                  d.pw1, d.pr, d.pinvm, d.pinvI, d.pFHydro, d.pFContact, d.pMContact,
-                  d.pFLub, d.pMLub, d.pFRep, d.pFTotal, d.pMTotal, d.pFGrav, d.pxiw,
-                  d.pxio, d.nF, d.pkd, d.pkf, d.pAccF, d.chunkAct, d.pairList, d.plist[0], d.plist[1], d.pxi[0],
-                  d.pxi[1], d.partner, d.gorder,
-                  d.pairbuf, d.pairflag, d.pcell, d.posf, d.ppos, d.cellCount, d.cellStart,
-                  d.cellFill, d.cellParts, d.obj, d.wallF, d.walls, d.uncover};
   if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (auto& g : ctx->pairGraph)
@@ -591,8 +594,7 @@ extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
   }
   for (auto& e : ctx->phaseEvents)
     for (cudaEvent_t x : e) cudaEventDestroy(x);
-  for (void* p : ptrs)
-    if (p) cudaFreeAsync(p, ctx->own_stream);
+  for (auto& b : ctx->buffers) cudaFreeAsync(b.first, ctx->own_stream);
   if (ctx->own_stream) {
     cudaStreamSynchronize(ctx->own_stream);
     cudaStreamDestroy(ctx->own_stream);

@@ -5,6 +5,7 @@
 
 #include <array>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "lbdem.h"
@@ -210,6 +211,10 @@ struct lbdem_ctx {
   int nPart = 0, nObj = 0, nWall = 0;
   int objIndexField[lbdem::MAX_OBJ] = {0};
   long long deviceBytes = 0;
+  // every device allocation of the run, in allocation order (the same order
+  // and sizes for every run created from one configuration and form): what
+  // a snapshot holds, and what lbdem_destroy frees
+  std::vector<std::pair<void*, size_t>> buffers;
   int smCount = 0;
   int lbMixedBlocks = 0;  // resident blocks of the mixed lattice kernel (one wave)
   int chunksPerBlock = 8; // at least this many 256-node chunks per lattice block

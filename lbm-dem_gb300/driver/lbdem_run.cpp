@@ -3,7 +3,7 @@
 //
 //   lbdem_run [-c config.cfg] [-i inputDir] [-d dataDir] [-n name]
 //             [-precision fp64|mixed] [-device k] [-steps n] [-every n]
-//             [-key value ...]
+//             [-resume snapshot] [-snapshot snapshot] [-key value ...]
 //
 // As in the reference: the GetPot parameters file is read from -c (default
 // config.cfg); the particles/objects/body tables from input/ relative to the
@@ -17,7 +17,14 @@
 //   mixed form;
 // - every -every cycles (default: every screenExpTime of simulated time, or
 //   only at the end) one line per impactor goes to <data>/impactor.dat and a
-//   summary line to stdout.
+//   summary line to stdout;
+// - -resume loads a snapshot (lbdem_restore) of a run of the same
+//   parameters and form before the first cycle; the run goes on from the
+//   snapshot's cycle count, -steps and maxTime still counting from cycle 0,
+//   and impactor.dat is appended to;
+// - -snapshot writes a snapshot (lbdem_checkpoint) after the last cycle.
+//   Both replace the reference's recycle/restart files (src/IO.cpp:973-997,
+//   src/LB.cpp:353-367) with a bit-exact state.
 #include <sys/stat.h>
 
 #include <cerrno>
@@ -59,7 +66,8 @@ int main(int argc, char** argv) {
   if (hasFlag(argc, argv, "-h") || hasFlag(argc, argv, "--help")) {
     std::printf(
         "Usage: %s [-c configFile] [-i inputDir] [-d dataDir] [-n name] "
-        "[-precision fp64|mixed] [-device k] [-steps n] [-every n] [-key value ...]\n",
+        "[-precision fp64|mixed] [-device k] [-steps n] [-every n] [-resume snapshot] "
+        "[-snapshot snapshot] [-key value ...]\n",
         argv[0]);
     return 0;
   }
@@ -71,6 +79,8 @@ int main(int argc, char** argv) {
   const int device = std::atoi(flagValue(argc, argv, "-device", "0"));
   const long long stepLimit = std::atoll(flagValue(argc, argv, "-steps", "-1"));
   const long long every = std::atoll(flagValue(argc, argv, "-every", "0"));
+  const std::string resume = flagValue(argc, argv, "-resume", "");
+  const std::string snapshot = flagValue(argc, argv, "-snapshot", "");
   if (precision != "fp64" && precision != "mixed") {
     std::fprintf(stderr, "lbdem_run: -precision must be fp64 or mixed\n");
     return 1;
@@ -137,12 +147,20 @@ int main(int argc, char** argv) {
     interval = (long long)(cfg.screenExpTime / cfg.unitTime + 0.5);
   if (interval <= 0) interval = total > 0 ? total : 1;
 
-  std::FILE* out = std::fopen((workDir + "/impactor.dat").c_str(), "w");
+  long long done = 0;
+  if (!resume.empty()) {
+    if ((rc = lbdem_restore(ctx, resume.c_str()))) return fail(ctx, "lbdem_restore", rc);
+    if ((rc = lbdem_get_info(ctx, &info))) return fail(ctx, "lbdem_get_info", rc);
+    done = info.time_step;
+    std::printf("lbdem_run: resumed at cycle %lld from %s\n", done, resume.c_str());
+  }
+  std::FILE* out =
+      std::fopen((workDir + "/impactor.dat").c_str(), resume.empty() ? "w" : "a");
   if (!out) {
     std::fprintf(stderr, "lbdem_run: cannot write %s/impactor.dat\n", workDir.c_str());
     return 1;
   }
-  std::fprintf(out, "# step time object x y z vx vy vz FHx FHy FHz\n");
+  if (resume.empty()) std::fprintf(out, "# step time object x y z vx vy vz FHx FHy FHz\n");
   std::vector<double> x0(3 * (nObj > 0 ? nObj : 1)), x1(x0.size()), fh(x0.size());
   auto report = [&](long long step) -> int {
     lbdem_object_view v;
@@ -167,8 +185,7 @@ int main(int argc, char** argv) {
     return 0;
   };
 
-  if ((rc = report(0))) return fail(ctx, "report", rc);
-  long long done = 0;
+  if (resume.empty() && (rc = report(0))) return fail(ctx, "report", rc);
   while (done < total) {
     const long long n = total - done < interval ? total - done : interval;
     if ((rc = lbdem_cycle(ctx, (int32_t)n))) return fail(ctx, "lbdem_cycle", rc);
@@ -177,6 +194,10 @@ int main(int argc, char** argv) {
     if ((rc = report(done))) return fail(ctx, "report", rc);
   }
   std::fclose(out);
+  if (!snapshot.empty()) {
+    if ((rc = lbdem_checkpoint(ctx, snapshot.c_str()))) return fail(ctx, "lbdem_checkpoint", rc);
+    std::printf("lbdem_run: snapshot of cycle %lld in %s\n", done, snapshot.c_str());
+  }
   lbdem_destroy(ctx);
   lbdem_config_release(&cfg);
   std::printf("lbdem_run: %lld cycles done, results in %s\n", done, workDir.c_str());

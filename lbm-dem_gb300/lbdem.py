@@ -183,6 +183,8 @@ def load_library(path: str | None = None) -> C.CDLL:
                                C.c_int32, C.POINTER(C.c_double)], C.c_int),
         "lbdem_download_nodes_noalloc": ([c_ctx, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p],
                                          C.c_int),
+        "lbdem_checkpoint": ([c_ctx, C.c_char_p], C.c_int),
+        "lbdem_restore": ([c_ctx, C.c_char_p], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)  # a missing entry point is a build error
@@ -376,6 +378,15 @@ class Solver:
         m = C.c_double()
         self._check(self.lib.lbdem_mass_total(self.ctx, C.byref(m)), "mass_total")
         return m.value
+
+    def checkpoint(self, path) -> None:
+        """Write a full-precision snapshot of the run (lbdem_checkpoint)."""
+        self._check(self.lib.lbdem_checkpoint(self.ctx, os.fsencode(path)), "checkpoint")
+
+    def restore(self, path) -> None:
+        """Replace this run's state with a snapshot of a run of the same
+        configuration and form (lbdem_restore)."""
+        self._check(self.lib.lbdem_restore(self.ctx, os.fsencode(path)), "restore")
 
     def nodes_noalloc(self, first: int, count: int):
         """Populations [19, count] and masses [count] of nodes first ..

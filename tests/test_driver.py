@@ -66,3 +66,29 @@ def test_driver_trajectory_matches_oracle(lib, oracle_lib, tmp_path):
         np.testing.assert_allclose(got[k, 3:9], ref, rtol=1e-10, atol=1e-14)
     orc.close()
     cfg.close()
+
+
+@pytest.mark.gpu
+def test_driver_resumes_from_a_snapshot(lib, tmp_path):
+    """Plain FP64 form: 5 cycles with -snapshot, then -resume up to cycle 12,
+    against one uninterrupted 12-cycle run. The resumed run's impactor lines
+    continue the file and agree with the uninterrupted run within 1e-10
+    relative (the order of atomic force sums differs between runs)."""
+    d = _case_dir(tmp_path, "tiny_direct")
+    base = [DRIVER, "-c", "parameters.cfg", "-every", "4"]
+    r = subprocess.run(base + ["-steps", "12", "-d", "whole"], cwd=d, capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run(base + ["-steps", "5", "-d", "split", "-snapshot", "s.lbdemck"], cwd=d,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert (d / "s.lbdemck").exists()
+    r = subprocess.run(base + ["-steps", "12", "-d", "split", "-resume", "s.lbdemck"], cwd=d,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "resumed at cycle 5" in r.stdout
+    whole = _read_impactor(d / "whole" / "impactor.dat")
+    split = _read_impactor(d / "split" / "impactor.dat")
+    assert [int(s) for s in whole[:, 0]] == [0, 4, 8, 12]
+    assert [int(s) for s in split[:, 0]] == [0, 4, 5, 9, 12]
+    np.testing.assert_allclose(split[-1, 1:], whole[-1, 1:], rtol=1e-10, atol=1e-14)
