@@ -137,16 +137,14 @@ __device__ __forceinline__ void particleRunReduce(int key, int ix, float dx, flo
     }
   }
   if (head) {
+    // the particle's line is 64-byte aligned: three 16-byte vector
+    // reductions and one scalar instead of thirteen scalar atomics
     float* q = acc + (size_t)key * ACCF_STRIDE;
-    atomicAdd(q, v[0]);
-    atomicAdd(q + 1, v[1]);
-    atomicAdd(q + 2, v[2]);
-#pragma unroll
-    for (int b = 0; b < 3; ++b) {
-      atomicAdd(q + 3 + b, __fmaf_rn(rx, v[b], v[3 + b]));
-      atomicAdd(q + 6 + b, ry * v[b]);
-      atomicAdd(q + 9 + b, rz * v[b]);
-    }
+    float4* q4 = reinterpret_cast<float4*>(q);
+    atomicAdd(q4, make_float4(v[0], v[1], v[2], __fmaf_rn(rx, v[0], v[3])));
+    atomicAdd(q4 + 1, make_float4(__fmaf_rn(rx, v[1], v[4]), __fmaf_rn(rx, v[2], v[5]),
+                                  ry * v[0], ry * v[1]));
+    atomicAdd(q4 + 2, make_float4(ry * v[2], rz * v[0], rz * v[1], rz * v[2]));
     atomicAdd(q + 12, v[6]);
   }
 }
