@@ -307,13 +307,13 @@ LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
     // cleanLists (ABIT) and the neighbour cache (BULK) of this node
     uint8_t nm = (uint8_t)(m & ~(ABIT | BULK));
     if (__any_sync(FULL, act)) {
-      unsigned actN = ALL_LINKS, gasN = 0, spcN = 0;
+      unsigned actN = ALL_LINKS, gasN = 0, spcN = 0, wallN = 0;
       NodeStateF s;
       s.dx = s.dy = s.dz = s.rx = s.ry = s.rz = 0.0f;
       int key = -1;
       if (act) {
         // links into the box's wall layer, known from the coordinates
-        const unsigned wallN = boxWallLinks(k, ix, iy, iz);
+        wallN = boxWallLinks(k, ix, iy, iz);
         if (m & BULK) {
           actN = ALL_LINKS & ~wallN;
         } else {
@@ -333,16 +333,26 @@ LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
       }
       if (__any_sync(FULL, key >= 0))
         particleRunReduce(key, ix, s.dx, s.dy, s.dz, s.rx, s.ry, s.rz, massOld, a.pAccF);
-      // warps whose 32 nodes push every population to an active neighbour
-      // skip the per-link tests
-      const bool pushAll = __all_sync(FULL, act && actN == ALL_LINKS);
+      // Warps whose active nodes link only to active nodes and to the box's
+      // wall layer skip the per-link tests: every population is pushed (a
+      // push into the wall layer lands in a wall node's slot, which no step
+      // reads and no other node writes), then the wall links bounce back.
+      // The first and last warps of every lattice row are of this kind.
+      const bool pushAll = __all_sync(FULL, !act || (actN | wallN) == ALL_LINKS);
       if (act) {
         ++nact;
         __stcs(gout + x, g[0]);
       }
       if (pushAll) {
+        if (act) {
 #pragma unroll
-        for (int j = 1; j < Q; ++j) __stcs(gout + (x + k.pushOff[j]), g[j]);
+          for (int j = 1; j < Q; ++j) __stcs(gout + (x + k.pushOff[j]), g[j]);
+          if (wallN) {
+#pragma unroll
+            for (int j = 1; j < Q; ++j)
+              if ((wallN >> j) & 1u) gout[OPPJ(j) * NP + x] = g[j];
+          }
+        }
       } else if (act) {
         const float usq3 = 3.0f * __fmaf_rn(s.ux, s.ux, __fmaf_rn(s.uy, s.uy, s.uz * s.uz));
 #pragma unroll
