@@ -31,6 +31,7 @@ struct LbArgs {
   double* scal;
   int* iscal;
   unsigned long long* uscal;
+  uint32_t* ifList;   // interface nodes of this step, appended (IS_IFLIST entries)
 };
 
 struct FsArgs {
@@ -54,6 +55,7 @@ struct FsArgs {
   const double* obj;
   double* scal;
   int* iscal;
+  const uint32_t* ifList;  // interface nodes after the lattice step (IS_IFLIST entries)
 };
 
 struct DemArgs {

@@ -77,6 +77,18 @@ __device__ __forceinline__ long long nbrOffset(const Consts& k, int j) {
   return (long long)CX(j) + (long long)CY(j) * k.sy + (long long)CZ(j) * k.sz;
 }
 
+// Appends node x to the interface list. Called only by the lanes that hold
+// an interface node; the lanes executing together share one atomic and
+// write their entries in lane order.
+__device__ __forceinline__ void appendInterface(uint32_t x, uint32_t* list, int* iscal) {
+  const unsigned am = __activemask();
+  const int lane = threadIdx.x & 31, first = __ffs(am) - 1;
+  int base = 0;
+  if (lane == first) base = atomicAdd(iscal + IS_IFLIST, __popc(am));
+  base = __shfl_sync(am, base, first);
+  list[base + __popc(am & ((1u << lane) - 1u))] = x;
+}
+
 __device__ __forceinline__ void coords(const Consts& k, long long x, int& ix, int& iy, int& iz) {
   const unsigned ux = (unsigned)x;
   iz = (int)(ux / (unsigned)k.sz);

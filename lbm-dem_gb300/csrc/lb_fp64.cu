@@ -167,6 +167,7 @@ LBDEM_KERNEL(__launch_bounds__(256), lbStepFp64, LbArgs, lb) {
         }
       }
       if (t == 3) {
+        appendInterface((uint32_t)x, a.ifList, a.iscal);
         a.rhoS[x] = s.n;
         a.uS[x] = s.ux;
         a.uS[N + x] = s.uy;
@@ -258,6 +259,7 @@ __device__ __forceinline__ void lbPrepareBody(const Consts& k, double* pAcc, lon
     scal[SC_EXTRA_MASS] = 0.0;
     scal[SC_EXTRA_MASS_LO] = 0.0;
     iscal[IS_NIF] = 0;
+    iscal[IS_IFLIST] = 0;
     iscal[IS_BBOX + 0] = iscal[IS_BBOX + 1] = iscal[IS_BBOX + 2] = INT_MAX;
     iscal[IS_BBOX + 3] = iscal[IS_BBOX + 4] = iscal[IS_BBOX + 5] = -1;
   }
@@ -334,13 +336,13 @@ __device__ __forceinline__ void lbFinalizeBody(const Consts& k, double* pF, doub
     // forms the same quotient block 0 stores above
     const double addMass =
         (scal[SC_EXTRA_MASS] + scal[SC_EXTRA_MASS_LO]) / (double)(unsigned)iscal[IS_NIF];
-    FS_LOOP(k, fa, {
-      if ((fa.mask[x] & TYPE_MASK) == 3) {
-        // the mass the collision used, for fsUpdateMass's recomputation
-        fa.massNew[x] = fa.mass[x];
-        fa.mass[x] += addMass;
-      }
-    })
+    const int nl = fa.iscal[IS_IFLIST];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nl; i += gridDim.x * blockDim.x) {
+      const uint32_t x = fa.ifList[i];
+      // the mass the collision used, for fsUpdateMass's recomputation
+      fa.massNew[x] = fa.mass[x];
+      fa.mass[x] += addMass;
+    }
   }
 }
 
@@ -401,7 +403,7 @@ __device__ __noinline__ void fsPostCollision(const Consts& k, const FsArgs& a, l
 
 // LB::updateMass (interface part). The neighbour types are read first, all
 // links at once; the mass exchange terms are then summed in link order.
-LBDEM_KERNEL(, fsUpdateMass, FsArgs, fs) {
+LBDEM_KERNEL(__launch_bounds__(256, 2), fsUpdateMass, FsArgs, fs) {
   // the free-surface step's surplus and interface count start from zero
   // (fsUpdateMass itself accumulates neither)
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -409,9 +411,14 @@ LBDEM_KERNEL(, fsUpdateMass, FsArgs, fs) {
     a.scal[SC_SURPLUS_LO] = 0.0;
     a.iscal[IS_NIF2] = 0;
   }
-  FS_LOOP(k, a, {
+  // over the interface nodes the lattice step listed (none has changed
+  // type since)
+  const int nl = a.iscal[IS_IFLIST];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nl; i += gridDim.x * blockDim.x) {
+    const long long x = a.ifList[i];
     const uint8_t m = a.mask[x];
-    if ((m & TYPE_MASK) != 3) continue;
+    int ix, iy, iz;
+    coords(k, x, ix, iy, iz);
     const double mx = a.mass[x];
     // links to fluid or interface nodes, to interface nodes, to walls/impactors
     unsigned liq = 0, ifc = 0, wal = 0;
@@ -446,7 +453,7 @@ LBDEM_KERNEL(, fsUpdateMass, FsArgs, fs) {
       first = false;
     }
     a.massNew[x] = mx + delta;
-  })
+  }
 }
 
 // findInterfaceMutants (src/LB.cpp:1669-1698) after the interface mass copy.

@@ -425,6 +425,7 @@ LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
       if (act) {
         if (t == 3) {
           ++nif;
+          appendInterface(x, a.ifList, a.iscal);
           a.rhoS[x] = s.n;
           a.uS[x] = s.ux;
           a.uS[NN + x] = s.uy;

@@ -104,6 +104,7 @@ LbArgs lbArgs(lbdem_ctx* c) {
   a.scal = d.scal;
   a.iscal = d.iscal;
   a.uscal = d.uscal;
+  a.ifList = d.ifList;
   (void)P;
   return a;
 }
@@ -143,6 +144,7 @@ FsArgs fsArgs(lbdem_ctx* c) {
   a.obj = d.obj;
   a.scal = d.scal;
   a.iscal = d.iscal;
+  a.ifList = d.ifList;
   return a;
 }
 
@@ -531,6 +533,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   AL(d.wallF, (size_t)MAX_WALL * 12);
   AL(d.walls, (size_t)MAX_WALL);
   AL(d.uncover, (size_t)UNCOVER_CAP);
+  AL(d.ifList, N);
   int* dBoundary = nullptr;
   int* dWallType = nullptr;
   AL(dBoundary, 6);
@@ -1113,6 +1116,7 @@ extern "C" int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t prec
   add(MAX_WALL * 12, 8);
   add(MAX_WALL, (long long)sizeof(DeviceWall));
   add(UNCOVER_CAP, 4);
+  add(N, 4);                                   // interface list
   *bytes = total;
   return LBDEM_OK;
 }

@@ -129,6 +129,7 @@ struct Device {
   double* wallF = nullptr;               // [W][12]: FHydro FContact FLub FTotal
   DeviceWall* walls = nullptr;
   uint32_t* uncover = nullptr;           // [UNCOVER_CAP] candidate list
+  uint32_t* ifList = nullptr;            // [N] interface nodes of the lattice step, any order
 };
 
 // offsets into Device::scal (doubles)
@@ -163,6 +164,7 @@ enum {
   IS_GATHER_DONE,           // demGather: blocks done (the last one updates the impactors)
   IS_PAIRLIST_DONE,         // nbrPairList: blocks done (the last one swaps the lists)
   IS_WALLS_RESET,           // set by the first flag reset: every wall node has solid index 0
+  IS_IFLIST,                // entries of Device::ifList written by this lattice step
   IS_COUNT
 };
 // offsets into Device::uscal
