@@ -285,6 +285,30 @@ int lbdem_checkpoint(lbdem_ctx* ctx, const char* path);
  * LBDEM_ERR_INVALID or LBDEM_ERR_IO before any state is changed. */
 int lbdem_restore(lbdem_ctx* ctx, const char* path);
 
+/* ---- the reference's screen-phase output files ------------------------ */
+
+/* Open the reference's screen-phase files in directory `dir` (which must
+ * exist) and append their header lines as IO::initialize does
+ * (src/IO.cpp:43-94): export.dat and, with the DEM on, objPosition.dat,
+ * objForce.dat, wallForce.dat, bodyPosition.dat and the three stress files.
+ * From then on lbdem_cycle appends the lines IO::outputStep writes
+ * (src/IO.cpp:113-158) at every cycle where the reference's screen counter
+ * (unsigned)(realTime / screen_exp_time) + 1 advances, realTime being the
+ * sum of unitTime over the cycles; a run opened before its first cycle
+ * also gets the line the reference writes before the first goCycle
+ * (src/main.cpp:286). Same numbers and layout as the reference: "%g",
+ * vectors as "x y z ", tab-separated groups. Lines are formatted from
+ * copies taken on the context's stream into pinned memory, without
+ * synchronising it; lbdem_sync and lbdem_output_close write all pending
+ * lines. The stress files keep their header lines only: this library does
+ * not form the DEM stress sums. screen_exp_time 0 writes headers only.
+ * Only lbdem_cycle advances the output clock; the four single-step entry
+ * points do not. */
+int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_exp_time);
+/* Write every pending line and close the files (also done by
+ * lbdem_destroy). */
+int lbdem_output_close(lbdem_ctx* ctx);
+
 /* ---- measurement (no counterpart in the reference) --------------------- */
 
 typedef struct lbdem_profile {

@@ -281,6 +281,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   ctx->lbSolve = cfg->lbSolve != 0;
   ctx->freeSurface = cfg->freeSurfaceSolve != 0;
   ctx->demInitialRepeat = cfg->demInitialRepeat;
+  ctx->fluidHeight = cfg->fluidHeight;
   k.freeSurface = ctx->freeSurface ? 1 : 0;
   k.forceField = cfg->forceFieldSolve != 0;
   // measureUnits::setComposite
@@ -597,6 +598,8 @@ extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
   }
   for (auto& e : ctx->phaseEvents)
     for (cudaEvent_t x : e) cudaEventDestroy(x);
+  lbdemOutputDrain(ctx, true);
+  lbdemOutputFree(ctx);
   for (auto& b : ctx->buffers) cudaFreeAsync(b.first, ctx->own_stream);
   if (ctx->own_stream) {
     cudaStreamSynchronize(ctx->own_stream);
@@ -1005,7 +1008,9 @@ extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
   int32_t i = 0;
   while (i < n) {
     int rc = LBDEM_OK;
-    if (n - i >= 2 && pairReplayable(ctx)) {
+    // a pair replays two cycles; an output line due after the first of them
+    // needs that cycle on its own
+    if (n - i >= 2 && pairReplayable(ctx) && !lbdemOutputDueNext(ctx)) {
       const int parity = ctx->cur;
       if (!ctx->pairGraph[parity]) {
         if ((rc = capturePair(ctx, parity))) return rc;
@@ -1021,18 +1026,22 @@ extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
         }
         ctx->launches += ctx->pairKernels;
       }
+      for (int c = 0; c < 2; ++c)
+        if ((rc = lbdemOutputAfterCycle(ctx))) return rc;
       i += 2;
       continue;
     }
     if ((rc = cycleOnce(ctx))) return rc;
+    if ((rc = lbdemOutputAfterCycle(ctx))) return rc;
     ++i;
   }
-  return LBDEM_OK;
+  return lbdemOutputDrain(ctx, false);
 }
 
 extern "C" int lbdem_sync(lbdem_ctx* ctx) {
   if (!ctx) return LBDEM_ERR_INVALID;
   CK(cudaStreamSynchronize(ctx->stream));
+  if (int rc = lbdemOutputDrain(ctx, true)) return rc;
   int e = 0;
   CK(cudaMemcpy(&e, ctx->d.iscal + IS_ERROR, sizeof(int), cudaMemcpyDeviceToHost));
   if (e) {

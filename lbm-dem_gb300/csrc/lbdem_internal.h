@@ -185,6 +185,15 @@ enum {
 namespace lbdem {
 struct JobArgs;
 }
+struct lbdem_output;  // screen-phase output files (output.cu)
+// after each goCycle of lbdem_cycle: advance the output clock one cycle and
+// enqueue the copy of the state if a line is due
+int lbdemOutputAfterCycle(lbdem_ctx* c);
+// whether the next cycle is an output cycle
+bool lbdemOutputDueNext(const lbdem_ctx* c);
+// write the lines whose copies have completed (all of them, waiting, if wait)
+int lbdemOutputDrain(lbdem_ctx* c, bool wait);
+void lbdemOutputFree(lbdem_ctx* c);
 // many runs per launch (lbdem_capi.cu), for the run server
 void lbdemJobArgs(lbdem_ctx* c, int cur, lbdem::JobArgs* j);
 bool lbdemBatchable(const lbdem_ctx* c);
@@ -211,6 +220,8 @@ struct lbdem_ctx {
   bool lbFReset = false;  // lbF reset by the first collision when !forceField
   double lbFConfig[3] = {0, 0, 0};
   int nPart = 0, nObj = 0, nWall = 0;
+  double fluidHeight = 0.0;     // physical, as the configuration gives it
+  lbdem_output* out = nullptr;  // open screen-phase output files, if any
   int objIndexField[lbdem::MAX_OBJ] = {0};
   long long deviceBytes = 0;
   // every device allocation of the run, in allocation order (the same order

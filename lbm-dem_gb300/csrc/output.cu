@@ -1,0 +1,280 @@
+// The reference's screen-phase output files, written from the run's device
+// state without synchronising its stream.
+//
+// Reference: IO::initialize (src/IO.cpp:8-94) creates the files and their
+// header lines; IO::outputStep (src/IO.cpp:113-158) runs once before the
+// first goCycle and after every goCycle (src/main.cpp:66, 286), and when
+// the screen counter (unsigned)(realTime / screenExpTime) + 1 has advanced
+// it appends one line to export.dat and, with the DEM on, the impactor
+// lines (IO::exportObjectPosition / exportObjectForce, src/IO.cpp:1239-1353)
+// and the wall line (IO::exportWallForce, src/IO.cpp:1295-1314). realTime is
+// the sum of unitTime over the cycles, added one cycle at a time as goCycle
+// does, so the same cycles are picked. Numbers are printed as the
+// reference's streams print them: six significant digits ("%g"), each
+// vector as "x y z ", groups separated by tabs.
+//
+// At an output cycle the impactor records and the wall-force records are
+// copied on the run's stream into a slot of a pinned ring, followed by an
+// event; the lines are formatted once the event has completed (checked
+// after each lbdem_cycle call, waited for by lbdem_sync and
+// lbdem_output_close). A full ring waits for its oldest slot.
+//
+// Not written: the stress files (stressTensor.dat, normalStressCont.dat,
+// shearStressCont.dat) receive their header lines only, as this library
+// does not form the DEM stress sums; bodyPosition.dat has only its header,
+// as in the reference for a run without bodies.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "kernels_decl.h"
+#include "lbdem_internal.h"
+
+using namespace lbdem;
+
+struct lbdem_output {
+  double screenExp = 0.0, unitTime = 0.0, fluidHeight = 0.0;
+  double realTime = 0.0;   // IO::realTime
+  unsigned lastScreen = 0; // IO::lastScreenExp
+  bool dem = false;
+  std::FILE* fExport = nullptr;
+  std::FILE* fPos = nullptr;
+  std::FILE* fForce = nullptr;
+  std::FILE* fWall = nullptr;
+  int nObj = 0, nWall = 0;
+  size_t slotDoubles = 0;  // nObj * OB_STRIDE + nWall * 12
+  double* pinned = nullptr;
+  struct Slot {
+    cudaEvent_t ev = nullptr;
+    unsigned long long step = 0;
+    double realTime = 0.0;
+  };
+  std::vector<Slot> slots;
+  size_t head = 0, count = 0;  // FIFO of slots whose copy is in flight
+};
+
+namespace {
+
+constexpr int kSlots = 64;
+
+int fail(lbdem_ctx* ctx, int code, const std::string& msg) {
+  ctx->err = msg;
+  return code;
+}
+
+unsigned screenCounter(const lbdem_output* o, double t) {
+  return o->screenExp > 0.0 ? static_cast<unsigned>(t / o->screenExp) + 1u : 0u;
+}
+
+void vec(std::FILE* f, const double* v) { std::fprintf(f, "%g %g %g ", v[0], v[1], v[2]); }
+
+// the lines of one captured cycle
+void writeSlot(lbdem_output* o, const lbdem_output::Slot& s, const double* rec) {
+  std::fprintf(o->fExport, "%llu; time=%g\t\n", s.step, s.realTime);
+  if (o->dem && o->nObj > 0) {
+    for (int i = 0; i < o->nObj; ++i) {
+      const double* ob = rec + (size_t)i * OB_STRIDE;
+      const double r = ob[OB_R];
+      const double depth = (o->fluidHeight + r) - ob[OB_X0 + 1];
+      vec(o->fPos, ob + OB_X0);
+      std::fputs("\t", o->fPos);
+      vec(o->fPos, ob + OB_X1);
+      std::fprintf(o->fPos, "\t%g\n", depth);
+    }
+    for (int i = 0; i < o->nObj; ++i) {
+      const double* ob = rec + (size_t)i * OB_STRIDE;
+      const double r = ob[OB_R];
+      const double depth = (o->fluidHeight + r) - ob[OB_X0 + 1];
+      double fe[3], se[3] = {0.0, 0.0, 0.0};
+      for (int c = 0; c < 3; ++c) fe[c] = ob[OB_FTOTAL + c] - ob[OB_FGRAV + c];
+      if (depth > 0) {
+        const double area = 4.0 * M_PI * r * r * (depth / (2.0 * r));
+        for (int c = 0; c < 3; ++c) se[c] = fe[c] / area;
+      }
+      const double zero[3] = {0.0, 0.0, 0.0};  // an impactor's FRep is never set
+      const double* groups[7] = {fe, se, ob + OB_FTOTAL, ob + OB_FCONTACT, ob + OB_FHYDRO,
+                                 ob + OB_FLUB, zero};
+      for (int g = 0; g < 7; ++g) {
+        vec(o->fForce, groups[g]);
+        std::fputs(g < 6 ? "\t" : "\n", o->fForce);
+      }
+    }
+  }
+  if (o->dem && o->nWall > 0) {
+    const double* wf = rec + (size_t)o->nObj * OB_STRIDE;
+    for (int w = 0; w < o->nWall; ++w) {
+      vec(o->fWall, wf + 12 * w + 9);  // FTotal
+      std::fputs("\t", o->fWall);
+      vec(o->fWall, wf + 12 * w + 3);  // FContact
+      std::fputs("\t", o->fWall);
+    }
+    std::fputs("\n", o->fWall);
+  }
+}
+
+// writes the oldest pending slot; waits for its copy if `wait`
+int writeOldest(lbdem_ctx* ctx, bool wait, bool* wrote) {
+  lbdem_output* o = ctx->out;
+  *wrote = false;
+  if (!o->count) return LBDEM_OK;
+  lbdem_output::Slot& s = o->slots[o->head];
+  cudaError_t e = wait ? cudaEventSynchronize(s.ev) : cudaEventQuery(s.ev);
+  if (e == cudaErrorNotReady) return LBDEM_OK;
+  if (e != cudaSuccess)
+    return fail(ctx, LBDEM_ERR_CUDA, std::string("output copy: ") + cudaGetErrorString(e));
+  writeSlot(o, s, o->pinned + o->head * o->slotDoubles);
+  o->head = (o->head + 1) % o->slots.size();
+  --o->count;
+  *wrote = true;
+  return LBDEM_OK;
+}
+
+// enqueues the copy of this cycle's impactor and wall records
+int capture(lbdem_ctx* ctx) {
+  lbdem_output* o = ctx->out;
+  bool wrote = false;
+  int rc;
+  if (o->count == o->slots.size() && (rc = writeOldest(ctx, true, &wrote))) return rc;
+  const size_t k = (o->head + o->count) % o->slots.size();
+  double* dst = o->pinned + k * o->slotDoubles;
+  cudaError_t e = cudaSuccess;
+  if (o->nObj > 0)
+    e = cudaMemcpyAsync(dst, ctx->d.obj, (size_t)o->nObj * OB_STRIDE * sizeof(double),
+                        cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess && o->nWall > 0)
+    e = cudaMemcpyAsync(dst + (size_t)o->nObj * OB_STRIDE, ctx->d.wallF,
+                        (size_t)o->nWall * 12 * sizeof(double), cudaMemcpyDeviceToHost,
+                        ctx->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(o->slots[k].ev, ctx->stream);
+  if (e != cudaSuccess)
+    return fail(ctx, LBDEM_ERR_CUDA, std::string("output copy: ") + cudaGetErrorString(e));
+  o->slots[k].step = (unsigned long long)ctx->lbTime;
+  o->slots[k].realTime = o->realTime;
+  ++o->count;
+  return LBDEM_OK;
+}
+
+std::FILE* openWithHeader(const std::string& path, const char* header) {
+  std::FILE* f = std::fopen(path.c_str(), "a");
+  if (f && header) std::fputs(header, f);
+  return f;
+}
+
+}  // namespace
+
+bool lbdemOutputDueNext(const lbdem_ctx* ctx) {
+  const lbdem_output* o = ctx->out;
+  return o && screenCounter(o, o->realTime + o->unitTime) > o->lastScreen;
+}
+
+int lbdemOutputAfterCycle(lbdem_ctx* ctx) {
+  lbdem_output* o = ctx->out;
+  if (!o) return LBDEM_OK;
+  o->realTime += o->unitTime;
+  const unsigned c = screenCounter(o, o->realTime);
+  if (c <= o->lastScreen) return LBDEM_OK;
+  o->lastScreen = c;
+  return capture(ctx);
+}
+
+int lbdemOutputDrain(lbdem_ctx* ctx, bool wait) {
+  if (!ctx->out) return LBDEM_OK;
+  bool wrote = true;
+  while (wrote) {
+    const int rc = writeOldest(ctx, wait, &wrote);
+    if (rc) return rc;
+  }
+  std::fflush(ctx->out->fExport);
+  return LBDEM_OK;
+}
+
+void lbdemOutputFree(lbdem_ctx* ctx) {
+  lbdem_output* o = ctx->out;
+  if (!o) return;
+  for (auto& s : o->slots)
+    if (s.ev) cudaEventDestroy(s.ev);
+  if (o->pinned) cudaFreeHost(o->pinned);
+  for (std::FILE* f : {o->fExport, o->fPos, o->fForce, o->fWall})
+    if (f) std::fclose(f);
+  delete o;
+  ctx->out = nullptr;
+}
+
+extern "C" int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_exp_time) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  if (!dir || !(screen_exp_time >= 0.0))
+    return fail(ctx, LBDEM_ERR_INVALID, "output_open: null directory or negative screenExpTime");
+  if (ctx->out) return fail(ctx, LBDEM_ERR_INVALID, "output_open: output already open");
+  lbdem_output* o = new lbdem_output;
+  ctx->out = o;
+  o->screenExp = screen_exp_time;
+  o->unitTime = ctx->k.uTime;
+  o->fluidHeight = ctx->fluidHeight;
+  o->dem = ctx->demSolve;
+  o->nObj = ctx->nObj;
+  o->nWall = ctx->nWall;
+  o->slotDoubles = std::max<size_t>((size_t)o->nObj * OB_STRIDE + (size_t)o->nWall * 12, 1);
+  // realTime of the cycles already run, summed as goCycle sums it
+  for (long long i = 0; i < ctx->lbTime; ++i) o->realTime += o->unitTime;
+  const std::string d(dir);
+  // IO::initialize, src/IO.cpp:43-94 (headers appended, as its ios::app opens)
+  o->fExport = openWithHeader(d + "/export.dat", nullptr);
+  bool ok = o->fExport != nullptr;
+  if (o->dem) {
+    o->fPos = openWithHeader(d + "/objPosition.dat",
+                             "position(x) position(y) position(z) velocity(x) velocity(y) "
+                             "velocity(z) depth(y)  \n");
+    std::FILE* body = openWithHeader(d + "/bodyPosition.dat",
+                                     "position(x) position(y) position(z) velocity(x) "
+                                     "velocity(y) velocity(z) Length Delta  \n");
+    o->fForce = openWithHeader(
+        d + "/objForce.dat",
+        "FExerted(x) FExerted(y) FExerted(z) SExerted(x) SExerted(y) SExerted(z) FTotal(x) "
+        "FTotal(y) FTotal(z) FContact(x) FContact(y) FContact(z) FHydro(x) FHydro(y) "
+        "FHydro(z) FLub(x) FLub(y) FLub(z) FRep(x) FRep(y) FRep(z) FGrav(x) FGrav(y) "
+        "FGrav(z) \n");
+    o->fWall = openWithHeader(
+        d + "/wallForce.dat",
+        "0-FTotal(x) 0-FTotal(y) 0-FTotal(z) 1-FTotal(x) 1-FTotal(y) 1-FTotal(z) 2-FTotal(x) "
+        "2-FTotal(y) 2-FTotal(z) 3-FTotal(x) 3-FTotal(y) 3-FTotal(z) 4-FTotal(x) 4-FTotal(y) "
+        "4-FTotal(z) 5-FTotal(x) 5-FTotal(y) 5-FTotal(z) \n");
+    std::FILE* st = openWithHeader(d + "/stressTensor.dat", "xx yy zz xy yz zx \n");
+    std::FILE* sn = openWithHeader(d + "/normalStressCont.dat",
+                                   "hydro-xx hydro-yy hydro-zz lub-xx lub-yy lub-zz contact-xx "
+                                   "contact-yy contact-zz rep-xx rep-yy rep-zz \n");
+    std::FILE* ss = openWithHeader(d + "/shearStressCont.dat",
+                                   "hydro-xy hydro-yz hydro-zx lub-xy lub-yz lub-zx contact-xy "
+                                   "contact-yz contact-zx rep-xy rep-yz rep-zx \n");
+    ok = ok && o->fPos && body && o->fForce && o->fWall && st && sn && ss;
+    for (std::FILE* f : {body, st, sn, ss})
+      if (f) std::fclose(f);
+  }
+  if (!ok) {
+    lbdemOutputFree(ctx);
+    return fail(ctx, LBDEM_ERR_IO, std::string("output_open: cannot write files in ") + d);
+  }
+  o->slots.resize(kSlots);
+  cudaError_t e = cudaMallocHost((void**)&o->pinned, kSlots * o->slotDoubles * sizeof(double));
+  for (auto& s : o->slots)
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    lbdemOutputFree(ctx);
+    return fail(ctx, LBDEM_ERR_CUDA, std::string("output_open: ") + cudaGetErrorString(e));
+  }
+  // IO::outputStep before the first goCycle (src/main.cpp:286); a run that
+  // has already cycled continues the schedule from its current time
+  o->lastScreen = screenCounter(o, o->realTime);
+  if (ctx->lbTime == 0 && o->lastScreen > 0) return capture(ctx);
+  return LBDEM_OK;
+}
+
+extern "C" int lbdem_output_close(lbdem_ctx* ctx) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  if (!ctx->out) return LBDEM_OK;
+  const int rc = lbdemOutputDrain(ctx, true);
+  lbdemOutputFree(ctx);
+  return rc;
+}

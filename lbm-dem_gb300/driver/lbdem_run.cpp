@@ -25,6 +25,9 @@
 // - -snapshot writes a snapshot (lbdem_checkpoint) after the last cycle.
 //   Both replace the reference's recycle/restart files (src/IO.cpp:973-997,
 //   src/LB.cpp:353-367) with a bit-exact state.
+// With screenExpTime > 0 the reference's own screen-phase files (export.dat,
+// objPosition.dat, objForce.dat, wallForce.dat, ...) are written into the
+// data directory as IO::outputStep writes them (lbdem_output_open).
 #include <sys/stat.h>
 
 #include <cerrno>
@@ -185,6 +188,9 @@ int main(int argc, char** argv) {
     return 0;
   };
 
+  if (cfg.screenExpTime > 0.0 &&
+      (rc = lbdem_output_open(ctx, workDir.c_str(), cfg.screenExpTime)))
+    return fail(ctx, "lbdem_output_open", rc);
   if (resume.empty() && (rc = report(0))) return fail(ctx, "report", rc);
   while (done < total) {
     const long long n = total - done < interval ? total - done : interval;
@@ -194,6 +200,7 @@ int main(int argc, char** argv) {
     if ((rc = report(done))) return fail(ctx, "report", rc);
   }
   std::fclose(out);
+  if ((rc = lbdem_output_close(ctx))) return fail(ctx, "lbdem_output_close", rc);
   if (!snapshot.empty()) {
     if ((rc = lbdem_checkpoint(ctx, snapshot.c_str()))) return fail(ctx, "lbdem_checkpoint", rc);
     std::printf("lbdem_run: snapshot of cycle %lld in %s\n", done, snapshot.c_str());

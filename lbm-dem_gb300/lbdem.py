@@ -184,6 +184,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "lbdem_download_nodes_noalloc": ([c_ctx, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p],
                                          C.c_int),
         "lbdem_checkpoint": ([c_ctx, C.c_char_p], C.c_int),
+        "lbdem_output_open": ([c_ctx, C.c_char_p, C.c_double], C.c_int),
+        "lbdem_output_close": ([c_ctx], C.c_int),
         "lbdem_restore": ([c_ctx, C.c_char_p], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -387,6 +389,15 @@ class Solver:
         """Replace this run's state with a snapshot of a run of the same
         configuration and form (lbdem_restore)."""
         self._check(self.lib.lbdem_restore(self.ctx, os.fsencode(path)), "restore")
+
+    def output_open(self, directory, screen_exp_time: float) -> None:
+        """Write the reference's screen-phase files into `directory` from now
+        on (lbdem_output_open)."""
+        self._check(self.lib.lbdem_output_open(self.ctx, os.fsencode(directory),
+                                               float(screen_exp_time)), "output_open")
+
+    def output_close(self) -> None:
+        self._check(self.lib.lbdem_output_close(self.ctx), "output_close")
 
     def nodes_noalloc(self, first: int, count: int):
         """Populations [19, count] and masses [count] of nodes first ..

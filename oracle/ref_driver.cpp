@@ -5,7 +5,11 @@
 // time loop:
 //   init sequence   = src/main.cpp:239-286 (parseConfigFile, latticeDefinition,
 //                     discreteElementInit, latticeBolzmannInit, time reset)
-//   one step        = goCycle, src/main.cpp:38-67 (IO::outputStep omitted)
+//   one step        = goCycle, src/main.cpp:38-67; IO::outputStep only with
+//                     -io DIR (the reference's own IO code, src/IO.cpp, with
+//                     every VTK/recycle export time 0: the screen-phase
+//                     files export.dat, objPosition.dat, objForce.dat,
+//                     wallForce.dat and the stress files, in DIR)
 // Defined-behaviour pins applied here, at the public-member level, without
 // touching the reference sources:
 //   * particle::list/_list/xix/xiy/xiz/_xix/_xiy/_xiz (src/elmt.h:44-51) are
@@ -18,7 +22,7 @@
 // Output: full-precision state dumps (oracle/statedump.h) and a timing line.
 //
 // usage: lbdem_ref -c parameters.cfg -steps N [-dump DIR] [-every K]
-//                  [-time] [-anyReferenceKey value ...]
+//                  [-io DIR] [-time] [-anyReferenceKey value ...]
 // Inputs particles.dat / objects.dat / body.dat are read from ./input/ under
 // the working directory, exactly as the reference does (src/DEM.cpp:81,138,169).
 #include <sys/stat.h>
@@ -30,6 +34,7 @@
 #include <vector>
 
 #include "DEM.h"
+#include "IO.h"
 #include "LB.h"
 #include "getpot.h"
 #include "statedump.h"
@@ -184,6 +189,8 @@ int main(int argc, char** argv) {
   int every = 1;
   if (commandLine.search("-every")) every = commandLine.next(1);
   const bool timing = commandLine.search("-time");
+  std::string ioDir;
+  if (commandLine.search("-io")) ioDir = commandLine.next("");
 
   GetPot configFile(cfg.c_str());
   DEM dem;
@@ -223,6 +230,27 @@ int main(int argc, char** argv) {
   dem.demTime = 0.0;
   dem.demTimeStep = 0;
 
+  // IO as src/main.cpp:75-120, 128-185 and 282-286 set it up, screen phase only
+  IO io;
+  if (!ioDir.empty()) {
+    io.workDirectory = ioDir;
+    ::mkdir(ioDir.c_str(), 0777);
+    io.demSolve = run.demSolve;
+    io.lbmSolve = run.lbSolve;
+    PARSE_CLASS_MEMBER(configFile, io.screenExpTime, "screenExpTime", 0.0);
+    io.stateExpTime = io.fluidExpTime = io.fluidLagrangianExpTime = io.fluid2DExpTime = 0.0;
+    io.partExpTime = io.boundExpTime = io.objectExpTime = io.bodyExpTime = 0.0;
+    io.springExpTime = io.objectExpTime2 = io.chainExpTime = io.velExpTime = 0.0;
+    io.dispExpTime = io.stressExpTime = io.part_yDispExpTime = io.part_rDispExpTime = 0.0;
+    io.part_n1ExpTime = io.part_n2ExpTime = io.part_pressureExpTime = 0.0;
+    io.part_yyStressExpTime = io.fluidRecycleExpTime = io.partRecycleExpTime = 0.0;
+    io.outputExpTime = io.simComplexExpTime = 0.0;
+    io.initialize();
+    io.currentTimeStep = 0;
+    io.realTime = 0.0;
+    io.outputStep(lb, dem);
+  }
+
   auto dumpName = [&](int s) {
     char buf[64];
     std::snprintf(buf, sizeof buf, "/dump_%06d.bin", s);
@@ -237,6 +265,8 @@ int main(int argc, char** argv) {
   for (int s = 1; s <= steps; ++s) {
     const auto t0 = std::chrono::steady_clock::now();
     // goCycle, src/main.cpp:38-67
+    io.realTime += lb.unit.Time;
+    ++io.currentTimeStep;
     ++lb.time;
     if (run.demSolve) dem.discreteElementStep(lb.boundary);
     if (run.lbSolve && dem.demTime >= dem.demInitialRepeat) {
@@ -252,6 +282,7 @@ int main(int argc, char** argv) {
     }
     const auto t1 = std::chrono::steady_clock::now();
     seconds += std::chrono::duration<double>(t1 - t0).count();
+    if (!ioDir.empty()) io.outputStep(lb, dem);
     if (!dumpDir.empty() && (s % every == 0 || s == steps))
       dumpState(dumpName(s), s, lb, dem);
   }

@@ -1,0 +1,63 @@
+"""Generate the golden screen-phase output files from the pinned reference
+build.
+
+Run here (where the reference tree exists):
+    make -C oracle ref && python tests/golden/make_io_golden.py
+
+For every case below it runs the reference's own IO code (oracle/_ref/lbdem_ref
+with -io, which calls IO::initialize and IO::outputStep of src/IO.cpp) on the
+committed inputs of tests/golden/<case>/ with the screenExpTime given here,
+and keeps the files it writes (export.dat, objPosition.dat, objForce.dat,
+wallForce.dat, bodyPosition.dat and the three stress files) in
+tests/golden/io/<case>/, with a cases.json of the steps and screenExpTime.
+"""
+from __future__ import annotations
+
+import json
+import os
+import shutil
+import subprocess
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = os.path.join(REPO, "oracle", "_ref", "lbdem_ref")
+
+# case -> (cycles, screenExpTime); unitTime is 1.0 in every case, so the
+# reference writes a line at cycle 0 and whenever floor(t / screenExpTime)
+# advances
+CASES = {
+    "tiny_direct": (12, 3.5),
+    "small_cells": (24, 5.5),
+    "c1": (30, 7.5),
+}
+FILES = ("export.dat", "objPosition.dat", "objForce.dat", "wallForce.dat", "bodyPosition.dat",
+         "stressTensor.dat", "normalStressCont.dat", "shearStressCont.dat")
+
+
+def make(name: str, steps: int, screen: float) -> None:
+    out = os.path.join(HERE, "io", name)
+    if os.path.isdir(out):
+        shutil.rmtree(out)
+    os.makedirs(out)
+    with tempfile.TemporaryDirectory() as tmp:
+        case = os.path.join(tmp, name)
+        shutil.copytree(os.path.join(HERE, name), case)
+        subprocess.run([REF, "-c", "parameters.cfg", "-steps", str(steps), "-io", "ioout",
+                        "-screenExpTime", repr(screen)], cwd=case, check=True,
+                       stdout=subprocess.DEVNULL)
+        for f in FILES:
+            shutil.copy(os.path.join(case, "ioout", f), os.path.join(out, f))
+
+
+def main() -> None:
+    for name, (steps, screen) in CASES.items():
+        make(name, steps, screen)
+        print("wrote", name)
+    with open(os.path.join(HERE, "io", "cases.json"), "w") as fh:
+        json.dump({k: {"steps": s, "screenExpTime": e} for k, (s, e) in CASES.items()}, fh,
+                  indent=1)
+
+
+if __name__ == "__main__":
+    main()
