@@ -84,7 +84,7 @@ typedef struct lbdem_object_in {
 
 /* Every configuration key of parameters.cfg the step depends on, with the
  * reference's names (src/main.cpp:128-185, src/LB.cpp:128-338,
- * src/DEM.cpp:17-78). Unsupported keys (restart, topography, rotation,
+ * src/DEM.cpp:17-78). Unsupported keys (topography, rotation,
  * non-Newtonian rheology, bodies) are accepted only at their inert values. */
 typedef struct lbdem_config {
   /* switches and time integration */
@@ -126,6 +126,9 @@ typedef struct lbdem_config {
   int32_t n_objects;
   const lbdem_object_in* objects;
   int32_t n_bodies;
+  /* lbRestartFile (src/LB.cpp:139): the fluid recycle file read under
+   * lbRestart, as given (relative to the working directory) */
+  const char* lbRestartFile;
 } lbdem_config;
 
 /* Run options that are not part of the reference's configuration. */
@@ -284,6 +287,21 @@ int lbdem_checkpoint(lbdem_ctx* ctx, const char* path);
  * wall count, form, library build, or a truncated file is refused with
  * LBDEM_ERR_INVALID or LBDEM_ERR_IO before any state is changed. */
 int lbdem_restore(lbdem_ctx* ctx, const char* path);
+
+/* ---- the reference's fluid recycle file ------------------------------- */
+
+/* Write the reference's fluid recycle file (IO::exportRecycleFluid,
+ * src/IO.cpp:973-997) of the run's current state: the lattice size, the
+ * type of every node, and per fluid or interface node in index order its
+ * density and mass less the initial density, velocity, viscosity and 19
+ * populations, with the reference's six significant digits. The density
+ * and velocity are those of the current populations (the reference writes
+ * the values of the last collision, with the force shift); restarts read
+ * neither. Synchronises
+ * the context's stream. A run created with lbRestart = 1 and
+ * lbRestartFile = this file starts from it as the reference's restart does
+ * (LB::restartInterface / restartVariables, src/LB.cpp:994-1138). */
+int lbdem_export_recycle_fluid(lbdem_ctx* ctx, const char* path);
 
 /* ---- the reference's screen-phase output files ------------------------ */
 

@@ -172,6 +172,14 @@ extern "C" int lbdem_config_load(const char* cfg_path, const char* input_dir,
   c->forceFieldSolve = ks.i("forceFieldSolve", 0);
 
   c->lbRestart = ks.b("lbRestart", false);
+  {
+    const std::string f = ks.s("lbRestartFile", "");
+    if (!f.empty()) {
+      char* p = new char[f.size() + 1];
+      std::memcpy(p, f.c_str(), f.size() + 1);
+      c->lbRestartFile = p;
+    }
+  }
   c->lbTopography = ks.b("lbTopography", false);
   c->unitLength = ks.d("unitLength", 1.0);
   c->unitTime = ks.d("unitTime", 1.0);
@@ -310,7 +318,9 @@ extern "C" void lbdem_config_release(lbdem_config* c) {
   if (!c) return;
   delete[] c->particles;
   delete[] c->objects;
+  delete[] c->lbRestartFile;
   c->particles = nullptr;
   c->objects = nullptr;
+  c->lbRestartFile = nullptr;
   c->n_particles = c->n_objects = 0;
 }

@@ -189,7 +189,8 @@ __global__ void fsEmptyIsolated(Consts k, FsArgs a);
 __global__ void fsEmptyIsolatedBatch(const JobArgs* jobs);
 __global__ void fsRedistribute(Consts k, FsArgs a);
 __global__ void fsRedistributeBatch(const JobArgs* jobs);
-__global__ void uncoverCollect(Consts k, const uint8_t* mask, const double* obj,
+__global__ void uncoverCollect(Consts k, const uint8_t* mask, const uint32_t* solid,
+                               const double* obj,
                                uint32_t* list, int* iscal);
 // dynamic shared memory of uncoverResolve: candidates, their lower-index
 // candidate neighbours and states

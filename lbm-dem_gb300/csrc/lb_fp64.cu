@@ -138,8 +138,10 @@ LBDEM_KERNEL(__launch_bounds__(256), lbStepFp64, LbArgs, lb) {
         } else if (tl == 12) {
           const int ov = a.objIdx[lk];
           const double* ob = a.obj + ov * OB_STRIDE;
-          const double vx = ob[OB_X1] / k.uSpeed, vy = ob[OB_X1 + 1] / k.uSpeed,
-                       vz = ob[OB_X1 + 2] / k.uSpeed;
+          const bool stale = (a.mask[lk] & OSTALE) != 0;
+          const double vx = stale ? 0.0 : ob[OB_X1] / k.uSpeed,
+                       vy = stale ? 0.0 : ob[OB_X1 + 1] / k.uSpeed,
+                       vz = stale ? 0.0 : ob[OB_X1 + 2] / k.uSpeed;
           const double BBi = 2.0 * 3.0 * s.n * WJ(j) * dotc(j, vx, vy, vz);
           const double bb = 2.0 * (fs - sp[j]) - BBi;
           const uint32_t so = a.solid[lk];
@@ -652,11 +654,14 @@ __device__ __forceinline__ void loadSpheres(const Consts& k, const double* obj, 
   }
 }
 
-// findNewActiveObject, step 1: collect object nodes that object 0 no longer
-// covers (candidates come from the previous voxelisation boxes).
+// findNewActiveObject, step 1: collect the nodes of LB::objectNodes that
+// object 0 no longer covers. objectNodes (src/LB.cpp:770-789, 822-839) holds
+// the object nodes that lay inside the sphere of the object their solid
+// index names, at that object's position of the previous voxelisation; an
+// object node outside it (one a restart file typed) is never uncovered.
 __device__ __forceinline__ void uncoverCollectBody(const Consts& k, const uint8_t* mask,
-                                                   const double* obj, uint32_t* list,
-                                                   int* iscal) {
+                                                   const uint32_t* solid, const double* obj,
+                                                   uint32_t* list, int* iscal) {
   __shared__ SphereL cur[MAX_OBJ], prev[MAX_OBJ];
   loadSpheres(k, obj, OB_X0, cur);
   loadSpheres(k, obj, OB_X0PREV, prev);
@@ -673,6 +678,11 @@ __device__ __forceinline__ void uncoverCollectBody(const Consts& k, const uint8_
                 iz = lo[2] + (int)(i / (nx * ny));
       const long long x = ix + iy * k.sy + iz * k.sz;
       if ((mask[x] & TYPE_MASK) != 12) continue;
+      // member of objectNodes: inside its own object's previous sphere
+      if (solid[x] != (uint32_t)o ||
+          !insideSphereFast((double)ix, (double)iy, (double)iz, prev[o].c[0], prev[o].c[1],
+                            prev[o].c[2], prev[o].r))
+        continue;
       if (insideSphereFast((double)ix, (double)iy, (double)iz, c0x, c0y, c0z, r0)) continue;
       const int slot = atomicAdd(iscal + IS_NUNCOVER, 1);
       if (slot < UNCOVER_CAP) list[slot] = (uint32_t)x;
@@ -851,7 +861,7 @@ __device__ __forceinline__ void voxelizeObjectsBody(const Consts& k, uint8_t* ma
       if (m0 & BULK) mask[x] = (uint8_t)(m0 & ~BULK);
       continue;
     }
-    mask[x] = (uint8_t)((m0 & ~(TYPE_MASK | BULK)) | 12);
+    mask[x] = (uint8_t)((m0 & ~(TYPE_MASK | BULK | OSTALE)) | 12);
     solid[x] = (uint32_t)obj[last * OB_STRIDE + OB_INDEX];
     objIdx[x] = (uint8_t)last;
     mass[x] = 0.0;
@@ -1003,13 +1013,13 @@ __global__ void lbFinalizeKernelBatch(const JobArgs* jobs) {
                  jobs[blockIdx.z].fs, c.redistribute);
 }
 
-__global__ void uncoverCollect(Consts k, const uint8_t* mask, const double* obj,
-                               uint32_t* list, int* iscal) {
-  uncoverCollectBody(k, mask, obj, list, iscal);
+__global__ void uncoverCollect(Consts k, const uint8_t* mask, const uint32_t* solid,
+                               const double* obj, uint32_t* list, int* iscal) {
+  uncoverCollectBody(k, mask, solid, obj, list, iscal);
 }
 __global__ void uncoverCollectBatch(const JobArgs* jobs) {
   JOB_PROLOGUE
-  uncoverCollectBody(sk, c.mask, c.obj, c.uncover, c.iscal);
+  uncoverCollectBody(sk, c.mask, c.solid, c.obj, c.uncover, c.iscal);
 }
 
 __global__ void __launch_bounds__(1024) uncoverResolve(Consts k, uint8_t* mask, void* f,

@@ -381,7 +381,8 @@ LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
             const int dj = c_dir[j];
             const int cx = (dj & 3) - 1, cy = ((dj >> 2) & 3) - 1, cz = ((dj >> 4) & 3) - 1;
             const unsigned lk = x + (unsigned)(cx + cy * sy + cz * sz);
-            const int tl = mk[lk] & TYPE_MASK;
+            const uint8_t mlk = mk[lk];
+            const int tl = mlk & TYPE_MASK;
             const int oi = a.objIdx[lk];
             if (tl != 12 || oi >= k.nObj) {
               atomicOr(a.iscal + IS_ERROR, ERR_TYPE);
@@ -391,7 +392,8 @@ LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
             const float gj = *dst;
             const float* ov = sObj + 6 * oi;
             const float wj = j <= 6 ? (float)WJ(1) : (float)WJ(7);
-            const float cv = __fmaf_rn((float)cx, ov[3], __fmaf_rn((float)cy, ov[4], (float)cz * ov[5]));
+            const float cv = (mlk & OSTALE) ? 0.0f
+                : __fmaf_rn((float)cx, ov[3], __fmaf_rn((float)cy, ov[4], (float)cz * ov[5]));
             const float BBi = 6.0f * s.n * wj * cv;
             const uint32_t so = a.solid[lk];
             if (so < (uint32_t)k.nObj) {

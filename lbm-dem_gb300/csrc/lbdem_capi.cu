@@ -239,9 +239,9 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   if (precision != LBDEM_PLAIN_FP64 && precision != LBDEM_MIXED)
     return setErr(ctx, LBDEM_ERR_INVALID, "unknown precision form");
   // ---- validation (the supported subset of the reference's inputs) ----
-  if (!cfg->rheologyNewtonian || cfg->turbulenceSolve || cfg->lbRestart || cfg->lbTopography)
+  if (!cfg->rheologyNewtonian || cfg->turbulenceSolve || cfg->lbTopography)
     return setErr(ctx, LBDEM_ERR_INVALID,
-                  "only NEWTONIAN rheology without turbulence, restart or topography");
+                  "only NEWTONIAN rheology without turbulence or topography");
   if (cfg->n_bodies != 0) return setErr(ctx, LBDEM_ERR_INVALID, "bodies are not supported");
   for (int i = 0; i < 6; ++i)
     if (cfg->boundary[i] != 7 && cfg->boundary[i] != 8)
@@ -564,11 +564,17 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   // ---- LB::latticeBolzmannInit on the device ----
   const int lg = latticeGrid(ctx);
   if (ctx->lbSolve) {
+    // under lbRestart, LB::initializeTypes without the free-surface
+    // interface, then the recycle file (src/LB.cpp:353-367)
+    const int fsInit = cfg->lbRestart ? 0 : k.freeSurface;
     initTypes<<<lg, 256, 0, st>>>(k, d.mask, d.solid, d.objIdx, dBoundary, d.walls, dWallType,
-                                  d.obj, cfg->fluidHeight / L, k.freeSurface);
-    initFields<<<lg, 256, 0, st>>>(k, d.mask, d.f[0], d.mass, d.nF, cfg->fluidHeight / L,
-                                   k.freeSurface);
+                                  d.obj, cfg->fluidHeight / L, fsInit);
+    if (!cfg->lbRestart)
+      initFields<<<lg, 256, 0, st>>>(k, d.mask, d.f[0], d.mass, d.nF, cfg->fluidHeight / L,
+                                     k.freeSurface);
     if ((rc = launchErr(ctx, "lattice init")) != LBDEM_OK) return rc;
+    if (cfg->lbRestart && (rc = lbdemRestartFluid(ctx, cfg->lbRestartFile)) != LBDEM_OK)
+      return rc;
   }
   // ---- initial neighbour list (DEM::discreteElementInit, :294-296) ----
   {
@@ -650,7 +656,7 @@ extern "C" int lbdem_coupling_step(lbdem_ctx* ctx) {
   cudaStream_t s = ctx->stream;
   const int lg = latticeGrid(ctx);
   if (ctx->nObj > 0) {
-    uncoverCollect<<<ctx->gridObj, 256, 0, s>>>(k, d.mask, d.obj, d.uncover, d.iscal);
+    uncoverCollect<<<ctx->gridObj, 256, 0, s>>>(k, d.mask, d.solid, d.obj, d.uncover, d.iscal);
     uncoverResolve<<<1, 1024, UNCOVER_SMEM, s>>>(k, d.mask, d.f[ctx->cur], d.mass, d.nF, d.uncover,
                                       d.iscal);
     voxelizeObjects<<<ctx->gridObj, 256, 0, s>>>(k, d.mask, d.solid, d.objIdx, d.mass, d.obj);

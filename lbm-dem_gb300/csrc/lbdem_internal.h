@@ -31,6 +31,12 @@ constexpr uint8_t ABIT = 0x20;    // member of the last active list (cleanLists)
 // step; cleared around every node that leaves the active types
 // (free-surface emptying, impactor voxelisation); box walls never change.
 constexpr uint8_t BULK = 0x40;
+// An impactor node outside every impactor, which only a restart file makes
+// (its type comes from the file): in the reference it is in no object's
+// node list, so it is never uncovered, and its node is recreated every
+// step without the impactor's velocity (src/LB.cpp:822-839): links into it
+// bounce back with zero wall velocity. Cleared when an impactor covers it.
+constexpr uint8_t OSTALE = 0x80;
 
 // device error bits
 enum : int {
@@ -189,6 +195,8 @@ struct lbdem_output;  // screen-phase output files (output.cu)
 // after each goCycle of lbdem_cycle: advance the output clock one cycle and
 // enqueue the copy of the state if a line is due
 int lbdemOutputAfterCycle(lbdem_ctx* c);
+// lbdem_create under lbRestart: types and fields from the fluid recycle file
+int lbdemRestartFluid(lbdem_ctx* c, const char* path);
 // whether the next cycle is an output cycle
 bool lbdemOutputDueNext(const lbdem_ctx* c);
 // write the lines whose copies have completed (all of them, waiting, if wait)

@@ -40,6 +40,7 @@ struct Job {
   lbdem_config cfg{};
   std::vector<lbdem_particle_in> parts;
   std::vector<lbdem_object_in> objs;
+  std::string restartFile;
   int32_t cycles = 0;
   int32_t done = 0;
   int64_t bytes = 0;
@@ -393,6 +394,8 @@ extern "C" int lbdem_server_submit(lbdem_server* s, const lbdem_config* cfg, int
   j->objs.assign(cfg->objects, cfg->objects + cfg->n_objects);
   j->cfg.particles = j->parts.empty() ? nullptr : j->parts.data();
   j->cfg.objects = j->objs.empty() ? nullptr : j->objs.data();
+  j->restartFile = cfg->lbRestartFile ? cfg->lbRestartFile : "";
+  j->cfg.lbRestartFile = cfg->lbRestartFile ? j->restartFile.c_str() : nullptr;
   j->cycles = cycles;
   j->bytes = bytes;
   j->submitTime = s->now();

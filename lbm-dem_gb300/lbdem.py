@@ -68,7 +68,7 @@ class Config(C.Structure):
         ("nonLinType", C.c_int32), ("k13", C.c_double), ("scale", C.c_double),
         ("n_particles", C.c_int32), ("particles", C.POINTER(ParticleIn)),
         ("n_objects", C.c_int32), ("objects", C.POINTER(ObjectIn)),
-        ("n_bodies", C.c_int32),
+        ("n_bodies", C.c_int32), ("lbRestartFile", C.c_char_p),
     ]
 
 
@@ -184,6 +184,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "lbdem_download_nodes_noalloc": ([c_ctx, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p],
                                          C.c_int),
         "lbdem_checkpoint": ([c_ctx, C.c_char_p], C.c_int),
+        "lbdem_export_recycle_fluid": ([c_ctx, C.c_char_p], C.c_int),
         "lbdem_output_open": ([c_ctx, C.c_char_p, C.c_double], C.c_int),
         "lbdem_output_close": ([c_ctx], C.c_int),
         "lbdem_restore": ([c_ctx, C.c_char_p], C.c_int),
@@ -389,6 +390,11 @@ class Solver:
         """Replace this run's state with a snapshot of a run of the same
         configuration and form (lbdem_restore)."""
         self._check(self.lib.lbdem_restore(self.ctx, os.fsencode(path)), "restore")
+
+    def export_recycle_fluid(self, path) -> None:
+        """Write the reference's fluid recycle file of the current state."""
+        self._check(self.lib.lbdem_export_recycle_fluid(self.ctx, os.fsencode(path)),
+                    "export_recycle_fluid")
 
     def output_open(self, directory, screen_exp_time: float) -> None:
         """Write the reference's screen-phase files into `directory` from now
