@@ -323,6 +323,13 @@ int lbdem_export_recycle_fluid(lbdem_ctx* ctx, const char* path);
  * Only lbdem_cycle advances the output clock; the four single-step entry
  * points do not. */
 int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_exp_time);
+/* With output open, also write the reference's fluid recycle files
+ * (IO::createFiles, src/IO.cpp:201-210): dir/fluidData/fluidRecycle%010u.dat
+ * named by the cycle, at every cycle where (unsigned)(realTime /
+ * fluid_recycle_exp_time) + 1 advances, and now for a run that has not
+ * cycled yet; each is lbdem_export_recycle_fluid and synchronises the
+ * stream. 0 turns them off. */
+int lbdem_output_recycle(lbdem_ctx* ctx, double fluid_recycle_exp_time);
 /* Write every pending line and close the files (also done by
  * lbdem_destroy). */
 int lbdem_output_close(lbdem_ctx* ctx);

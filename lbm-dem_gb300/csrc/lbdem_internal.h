@@ -202,6 +202,7 @@ bool lbdemOutputDueNext(const lbdem_ctx* c);
 // write the lines whose copies have completed (all of them, waiting, if wait)
 int lbdemOutputDrain(lbdem_ctx* c, bool wait);
 void lbdemOutputFree(lbdem_ctx* c);
+extern "C" int lbdem_export_recycle_fluid(lbdem_ctx* c, const char* path);
 // many runs per launch (lbdem_capi.cu), for the run server
 void lbdemJobArgs(lbdem_ctx* c, int cur, lbdem::JobArgs* j);
 bool lbdemBatchable(const lbdem_ctx* c);

@@ -19,11 +19,18 @@
 // after each lbdem_cycle call, waited for by lbdem_sync and
 // lbdem_output_close). A full ring waits for its oldest slot.
 //
+// With lbdem_output_recycle the fluid recycle files of IO::createFiles
+// (src/IO.cpp:201-210) are written as well: dir/fluidData/
+// fluidRecycle%010u.dat, named by the cycle, whenever the counter
+// (unsigned)(realTime / fluidRecycleExpTime) + 1 advances (at the first
+// cycle too). Each one is a full lattice export and synchronises the stream.
+//
 // Not written: the stress files (stressTensor.dat, normalStressCont.dat,
 // shearStressCont.dat) receive their header lines only, as this library
 // does not form the DEM stress sums; bodyPosition.dat has only its header,
 // as in the reference for a run without bodies.
 #include <cuda_runtime.h>
+#include <sys/stat.h>
 
 #include <cmath>
 #include <cstdio>
@@ -36,9 +43,12 @@
 using namespace lbdem;
 
 struct lbdem_output {
+  std::string dir;
   double screenExp = 0.0, unitTime = 0.0, fluidHeight = 0.0;
   double realTime = 0.0;   // IO::realTime
   unsigned lastScreen = 0; // IO::lastScreenExp
+  double recycleExp = 0.0;  // IO::fluidRecycleExpTime (0: off)
+  unsigned lastRecycle = 0; // IO::lastFluidRecycleExp
   bool dem = false;
   std::FILE* fExport = nullptr;
   std::FILE* fPos = nullptr;
@@ -67,6 +77,16 @@ int fail(lbdem_ctx* ctx, int code, const std::string& msg) {
 
 unsigned screenCounter(const lbdem_output* o, double t) {
   return o->screenExp > 0.0 ? static_cast<unsigned>(t / o->screenExp) + 1u : 0u;
+}
+unsigned recycleCounter(const lbdem_output* o, double t) {
+  return o->recycleExp > 0.0 ? static_cast<unsigned>(t / o->recycleExp) + 1u : 0u;
+}
+
+// IO::exportRecycleFluid at this cycle (waits for the run's work)
+int writeRecycle(lbdem_ctx* ctx) {
+  char name[64];
+  std::snprintf(name, sizeof name, "/fluidData/fluidRecycle%010u.dat", (unsigned)ctx->lbTime);
+  return lbdem_export_recycle_fluid(ctx, (ctx->out->dir + name).c_str());
 }
 
 void vec(std::FILE* f, const double* v) { std::fprintf(f, "%g %g %g ", v[0], v[1], v[2]); }
@@ -167,7 +187,9 @@ std::FILE* openWithHeader(const std::string& path, const char* header) {
 
 bool lbdemOutputDueNext(const lbdem_ctx* ctx) {
   const lbdem_output* o = ctx->out;
-  return o && screenCounter(o, o->realTime + o->unitTime) > o->lastScreen;
+  if (!o) return false;
+  const double t = o->realTime + o->unitTime;
+  return screenCounter(o, t) > o->lastScreen || recycleCounter(o, t) > o->lastRecycle;
 }
 
 int lbdemOutputAfterCycle(lbdem_ctx* ctx) {
@@ -175,9 +197,16 @@ int lbdemOutputAfterCycle(lbdem_ctx* ctx) {
   if (!o) return LBDEM_OK;
   o->realTime += o->unitTime;
   const unsigned c = screenCounter(o, o->realTime);
-  if (c <= o->lastScreen) return LBDEM_OK;
-  o->lastScreen = c;
-  return capture(ctx);
+  if (c > o->lastScreen) {
+    o->lastScreen = c;
+    if (int rc = capture(ctx)) return rc;
+  }
+  const unsigned r = recycleCounter(o, o->realTime);
+  if (r > o->lastRecycle) {
+    o->lastRecycle = r;
+    return writeRecycle(ctx);
+  }
+  return LBDEM_OK;
 }
 
 int lbdemOutputDrain(lbdem_ctx* ctx, bool wait) {
@@ -210,6 +239,7 @@ extern "C" int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_
   if (ctx->out) return fail(ctx, LBDEM_ERR_INVALID, "output_open: output already open");
   lbdem_output* o = new lbdem_output;
   ctx->out = o;
+  o->dir = dir;
   o->screenExp = screen_exp_time;
   o->unitTime = ctx->k.uTime;
   o->fluidHeight = ctx->fluidHeight;
@@ -220,7 +250,10 @@ extern "C" int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_
   // realTime of the cycles already run, summed as goCycle sums it
   for (long long i = 0; i < ctx->lbTime; ++i) o->realTime += o->unitTime;
   const std::string d(dir);
-  // IO::initialize, src/IO.cpp:43-94 (headers appended, as its ios::app opens)
+  // IO::initialize, src/IO.cpp:8-94: its two data folders, then the files
+  // (headers appended, as its ios::app opens)
+  if (ctx->demSolve) ::mkdir((d + "/particleData").c_str(), 0777);
+  if (ctx->lbSolve) ::mkdir((d + "/fluidData").c_str(), 0777);
   o->fExport = openWithHeader(d + "/export.dat", nullptr);
   bool ok = o->fExport != nullptr;
   if (o->dem) {
@@ -268,6 +301,19 @@ extern "C" int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_
   // has already cycled continues the schedule from its current time
   o->lastScreen = screenCounter(o, o->realTime);
   if (ctx->lbTime == 0 && o->lastScreen > 0) return capture(ctx);
+  return LBDEM_OK;
+}
+
+extern "C" int lbdem_output_recycle(lbdem_ctx* ctx, double fluid_recycle_exp_time) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  lbdem_output* o = ctx->out;
+  if (!o) return fail(ctx, LBDEM_ERR_INVALID, "output_recycle: output not open");
+  if (!(fluid_recycle_exp_time >= 0.0))
+    return fail(ctx, LBDEM_ERR_INVALID, "output_recycle: negative fluidRecycleExpTime");
+  o->recycleExp = ctx->lbSolve ? fluid_recycle_exp_time : 0.0;
+  o->lastRecycle = recycleCounter(o, o->realTime);
+  // the file IO::outputStep writes before the first goCycle
+  if (ctx->lbTime == 0 && o->lastRecycle > 0) return writeRecycle(ctx);
   return LBDEM_OK;
 }
 

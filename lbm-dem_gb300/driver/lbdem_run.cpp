@@ -27,7 +27,9 @@
 //   src/LB.cpp:353-367) with a bit-exact state.
 // With screenExpTime > 0 the reference's own screen-phase files (export.dat,
 // objPosition.dat, objForce.dat, wallForce.dat, ...) are written into the
-// data directory as IO::outputStep writes them (lbdem_output_open).
+// data directory as IO::outputStep writes them (lbdem_output_open), and with
+// fluidRecycleExpTime > 0 its fluid recycle files into data/fluidData
+// (lbdem_output_recycle).
 #include <sys/stat.h>
 
 #include <cerrno>
@@ -188,9 +190,12 @@ int main(int argc, char** argv) {
     return 0;
   };
 
-  if (cfg.screenExpTime > 0.0 &&
-      (rc = lbdem_output_open(ctx, workDir.c_str(), cfg.screenExpTime)))
-    return fail(ctx, "lbdem_output_open", rc);
+  if (cfg.screenExpTime > 0.0 || cfg.fluidRecycleExpTime > 0.0) {
+    if ((rc = lbdem_output_open(ctx, workDir.c_str(), cfg.screenExpTime)))
+      return fail(ctx, "lbdem_output_open", rc);
+    if ((rc = lbdem_output_recycle(ctx, cfg.fluidRecycleExpTime)))
+      return fail(ctx, "lbdem_output_recycle", rc);
+  }
   if (resume.empty() && (rc = report(0))) return fail(ctx, "report", rc);
   while (done < total) {
     const long long n = total - done < interval ? total - done : interval;

@@ -22,14 +22,18 @@ tests/golden/make_recycle_golden.py).
     largest value (the order of atomic force sums differs), node type
     counts are equal and the total mass agrees within 1e-12.
 - GPU, mixed form: the same start (populations within FP32 rounding).
+- GPU, driver with fluidRecycleExpTime 8: the recycle files of cycles 0 and
+  8 in data/fluidData, the one of cycle 8 equal to the reference's as above.
 """
 import gzip
 import os
+import shutil
+import subprocess
 
 import numpy as np
 import pytest
 
-from conftest import GOLDEN
+from conftest import GOLDEN, REPO
 
 REC = os.path.join(GOLDEN, "recycle")
 CASE = "tiny_direct"
@@ -65,18 +69,8 @@ def test_restart_file_key_is_parsed(lib):
         c.close()
 
 
-@pytest.mark.gpu
-def test_export_matches_the_reference_recycle_file(lib, tmp_path):
-    import lbdem
-    cfg = _cfg()
-    s = lbdem.Solver(cfg, precision=lbdem.PLAIN_FP64)
-    try:
-        s.cycle(8)
-        s.export_recycle_fluid(tmp_path / "mine.dat")
-    finally:
-        s.close()
-        cfg.close()
-    size_m, types_m, recs_m = _records(tmp_path / "mine.dat")
+def _compare_recycle(mine, tmp_path):
+    size_m, types_m, recs_m = _records(mine)
     size_r, types_r, recs_r = _records(_reference_file(tmp_path))
     assert size_m == size_r
     assert types_m == types_r
@@ -95,6 +89,33 @@ def test_export_matches_the_reference_recycle_file(lib, tmp_path):
     np.testing.assert_allclose(a[:, 0], n - 1.0, rtol=0, atol=ATOL_MOMENTS)
     for col, c in ((1, cx), (2, cy), (3, cz)):
         np.testing.assert_allclose(a[:, col], (f * c).sum(axis=1) / n, rtol=0, atol=ATOL_MOMENTS)
+
+
+@pytest.mark.gpu
+def test_export_matches_the_reference_recycle_file(lib, tmp_path):
+    import lbdem
+    cfg = _cfg()
+    s = lbdem.Solver(cfg, precision=lbdem.PLAIN_FP64)
+    try:
+        s.cycle(8)
+        s.export_recycle_fluid(tmp_path / "mine.dat")
+    finally:
+        s.close()
+        cfg.close()
+    _compare_recycle(tmp_path / "mine.dat", tmp_path)
+
+
+@pytest.mark.gpu
+def test_driver_writes_recycle_files_at_the_reference_cycles(lib, tmp_path):
+    d = tmp_path / CASE
+    shutil.copytree(os.path.join(GOLDEN, CASE), d)
+    driver = os.path.join(REPO, "lbm-dem_gb300", "lbdem_run")
+    r = subprocess.run([driver, "-c", "parameters.cfg", "-steps", "8", "-fluidRecycleExpTime",
+                        "8", "-d", "out"], cwd=d, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    names = sorted(os.listdir(d / "out" / "fluidData"))
+    assert names == ["fluidRecycle0000000000.dat", "fluidRecycle0000000008.dat"]
+    _compare_recycle(d / "out" / "fluidData" / "fluidRecycle0000000008.dat", tmp_path)
 
 
 @pytest.mark.gpu
