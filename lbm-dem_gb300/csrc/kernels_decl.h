@@ -224,6 +224,9 @@ __global__ void exportLattice(Consts k, const uint8_t* mask, const void* f, cons
 // threads per block of the gather pass (one thread per particle): small
 // blocks spread a few thousand particles over every SM
 constexpr int GATHER_THREADS = 64;
+// DEM stress sums: contact, lubrication, electrostatic, hydrodynamic (3x3 each)
+constexpr int STRESS_N = 36;
+__global__ void demStress(Consts k, DemArgs a, const double* SHydro, double* out);
 
 // dem_fp64.cu
 __global__ void demBegin(Consts k, DemArgs a, int forceRebuild);

@@ -535,6 +535,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   AL(d.walls, (size_t)MAX_WALL);
   AL(d.uncover, (size_t)UNCOVER_CAP);
   AL(d.ifList, N);
+  AL(d.stress, (size_t)STRESS_N);
   int* dBoundary = nullptr;
   int* dWallType = nullptr;
   AL(dBoundary, 6);
@@ -624,6 +625,19 @@ extern "C" int lbdem_set_stream(lbdem_ctx* ctx, void* stream) {
   return LBDEM_OK;
 }
 
+// the stress sums of DEM::evaluateForces, on cycles whose stress-file line
+// is due: after the pair pass, before the gather moves the particles
+static int enqueueStress(lbdem_ctx* ctx, const DemArgs& a) {
+  if (!ctx->stressNext) return LBDEM_OK;
+  CK(cudaMemsetAsync(ctx->d.stress, 0, STRESS_N * sizeof(double), ctx->stream));
+  if (ctx->nPart > 0) {
+    demStress<<<partGrid(ctx, 128), 128, 0, ctx->stream>>>(ctx->k, a, ctx->d.pSHydro,
+                                                           ctx->d.stress);
+    ++ctx->launches;
+  }
+  return LBDEM_OK;
+}
+
 // DEM::discreteElementStep (multiStep = 1)
 extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
   if (!ctx) return LBDEM_ERR_INVALID;
@@ -639,9 +653,11 @@ extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
   // the gathers also update the impactor (last block)
   if (k.mixed) {
     demPairsMixed<<<pairGrid, 128, 0, s>>>(k, a);
+    if ((rc = enqueueStress(ctx, a))) return rc;
     demGatherMixed<<<partGrid(ctx, GATHER_THREADS), GATHER_THREADS, 0, s>>>(k, a);
   } else {
     demPairs<<<pairGrid, 128, 0, s>>>(k, a);
+    if ((rc = enqueueStress(ctx, a))) return rc;
     demGather<<<partGrid(ctx, GATHER_THREADS), GATHER_THREADS, 0, s>>>(k, a);
   }
   ctx->launches += 1 + 9 + 2;
@@ -1016,7 +1032,7 @@ extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
     int rc = LBDEM_OK;
     // a pair replays two cycles; an output line due after the first of them
     // needs that cycle on its own
-    if (n - i >= 2 && pairReplayable(ctx) && !lbdemOutputDueNext(ctx)) {
+    if (n - i >= 2 && pairReplayable(ctx) && !lbdemOutputBlocksPair(ctx)) {
       const int parity = ctx->cur;
       if (!ctx->pairGraph[parity]) {
         if ((rc = capturePair(ctx, parity))) return rc;
@@ -1037,7 +1053,10 @@ extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
       i += 2;
       continue;
     }
-    if ((rc = cycleOnce(ctx))) return rc;
+    ctx->stressNext = lbdemOutputStressNext(ctx);
+    rc = cycleOnce(ctx);
+    ctx->stressNext = false;
+    if (rc) return rc;
     if ((rc = lbdemOutputAfterCycle(ctx))) return rc;
     ++i;
   }
@@ -1132,6 +1151,7 @@ extern "C" int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t prec
   add(MAX_WALL, (long long)sizeof(DeviceWall));
   add(UNCOVER_CAP, 4);
   add(N, 4);                                   // interface list
+  add(STRESS_N, 8);                            // stress sums
   *bytes = total;
   return LBDEM_OK;
 }

@@ -136,6 +136,7 @@ struct Device {
   DeviceWall* walls = nullptr;
   uint32_t* uncover = nullptr;           // [UNCOVER_CAP] candidate list
   uint32_t* ifList = nullptr;            // [N] interface nodes of the lattice step, any order
+  double* stress = nullptr;              // [36] DEM stress sums of an output cycle (demStress)
 };
 
 // offsets into Device::scal (doubles)
@@ -199,6 +200,12 @@ int lbdemOutputAfterCycle(lbdem_ctx* c);
 int lbdemRestartFluid(lbdem_ctx* c, const char* path);
 // whether the next cycle is an output cycle
 bool lbdemOutputDueNext(const lbdem_ctx* c);
+// whether the next cycle's DEM step forms the stress sums (a stress-file line
+// follows it)
+bool lbdemOutputStressNext(const lbdem_ctx* c);
+// whether two cycles cannot run as one replayed pair: an output is due after
+// the first, or the stress sums are due in the second
+bool lbdemOutputBlocksPair(const lbdem_ctx* c);
 // write the lines whose copies have completed (all of them, waiting, if wait)
 int lbdemOutputDrain(lbdem_ctx* c, bool wait);
 void lbdemOutputFree(lbdem_ctx* c);
@@ -231,6 +238,7 @@ struct lbdem_ctx {
   int nPart = 0, nObj = 0, nWall = 0;
   double fluidHeight = 0.0;     // physical, as the configuration gives it
   lbdem_output* out = nullptr;  // open screen-phase output files, if any
+  bool stressNext = false;      // the next DEM step forms the stress sums
   int objIndexField[lbdem::MAX_OBJ] = {0};
   long long deviceBytes = 0;
   // every device allocation of the run, in allocation order (the same order

@@ -25,10 +25,14 @@
 // (unsigned)(realTime / fluidRecycleExpTime) + 1 advances (at the first
 // cycle too). Each one is a full lattice export and synchronises the stream.
 //
-// Not written: the stress files (stressTensor.dat, normalStressCont.dat,
-// shearStressCont.dat) receive their header lines only, as this library
-// does not form the DEM stress sums; bodyPosition.dat has only its header,
-// as in the reference for a run without bodies.
+// The stress files (IO::exportStressTensor and the two contribution files,
+// src/IO.cpp:1355-1409) take the DEM stress sums of the cycle's DEM step
+// (demStress, launched on the cycles whose line is due), each divided by
+// the DEM volume: the total as xx yy zz and the mean off-diagonal pairs
+// (tinyMatrix::print, src/myvector.cpp:382-392), the hydrodynamic,
+// lubrication, contact and electrostatic parts as their normal and shear
+// triples. bodyPosition.dat has only its header, as in the reference for a
+// run without bodies.
 #include <cuda_runtime.h>
 #include <sys/stat.h>
 
@@ -54,8 +58,12 @@ struct lbdem_output {
   std::FILE* fPos = nullptr;
   std::FILE* fForce = nullptr;
   std::FILE* fWall = nullptr;
+  std::FILE* fStress = nullptr;
+  std::FILE* fNormal = nullptr;
+  std::FILE* fShear = nullptr;
+  double vol = 1.0;  // DEM::vol, src/DEM.cpp:211-215
   int nObj = 0, nWall = 0;
-  size_t slotDoubles = 0;  // nObj * OB_STRIDE + nWall * 12
+  size_t slotDoubles = 0;  // nObj * OB_STRIDE + nWall * 12 + STRESS_N
   double* pinned = nullptr;
   struct Slot {
     cudaEvent_t ev = nullptr;
@@ -90,6 +98,11 @@ int writeRecycle(lbdem_ctx* ctx) {
 }
 
 void vec(std::FILE* f, const double* v) { std::fprintf(f, "%g %g %g ", v[0], v[1], v[2]); }
+// tinyMatrix::printNormal / printShear of a row-major 3x3
+void normal3(std::FILE* f, const double* m) { std::fprintf(f, "%g %g %g ", m[0], m[4], m[8]); }
+void shear3(std::FILE* f, const double* m) {
+  std::fprintf(f, "%g %g %g ", (m[1] + m[3]) / 2.0, (m[5] + m[7]) / 2.0, (m[2] + m[6]) / 2.0);
+}
 
 // the lines of one captured cycle
 void writeSlot(lbdem_output* o, const lbdem_output::Slot& s, const double* rec) {
@@ -133,6 +146,28 @@ void writeSlot(lbdem_output* o, const lbdem_output::Slot& s, const double* rec) 
     }
     std::fputs("\n", o->fWall);
   }
+  if (o->dem) {
+    // DEM::evaluateForces: each part over the volume, then the total
+    const double* raw = rec + (size_t)o->nObj * OB_STRIDE + (size_t)o->nWall * 12;
+    double part[4][9], total[9];
+    for (int p = 0; p < 4; ++p)
+      for (int c = 0; c < 9; ++c) part[p][c] = raw[9 * p + c] / o->vol;
+    const double* contact = part[0];
+    const double* lub = part[1];
+    const double* electro = part[2];
+    const double* hydro = part[3];
+    for (int c = 0; c < 9; ++c) total[c] = 0.0 + (((contact[c] + lub[c]) + electro[c]) + hydro[c]);
+    normal3(o->fStress, total);
+    shear3(o->fStress, total);
+    std::fputs("\n", o->fStress);
+    const double* order[4] = {hydro, lub, contact, electro};
+    for (int p = 0; p < 4; ++p) {
+      normal3(o->fNormal, order[p]);
+      std::fputs(p < 3 ? "\t" : "\n", o->fNormal);
+      shear3(o->fShear, order[p]);
+      std::fputs(p < 3 ? "\t" : "\n", o->fShear);
+    }
+  }
 }
 
 // writes the oldest pending slot; waits for its copy if `wait`
@@ -168,6 +203,10 @@ int capture(lbdem_ctx* ctx) {
     e = cudaMemcpyAsync(dst + (size_t)o->nObj * OB_STRIDE, ctx->d.wallF,
                         (size_t)o->nWall * 12 * sizeof(double), cudaMemcpyDeviceToHost,
                         ctx->stream);
+  if (e == cudaSuccess && o->dem)
+    e = cudaMemcpyAsync(dst + (size_t)o->nObj * OB_STRIDE + (size_t)o->nWall * 12,
+                        ctx->d.stress, STRESS_N * sizeof(double), cudaMemcpyDeviceToHost,
+                        ctx->stream);
   if (e == cudaSuccess) e = cudaEventRecord(o->slots[k].ev, ctx->stream);
   if (e != cudaSuccess)
     return fail(ctx, LBDEM_ERR_CUDA, std::string("output copy: ") + cudaGetErrorString(e));
@@ -190,6 +229,18 @@ bool lbdemOutputDueNext(const lbdem_ctx* ctx) {
   if (!o) return false;
   const double t = o->realTime + o->unitTime;
   return screenCounter(o, t) > o->lastScreen || recycleCounter(o, t) > o->lastRecycle;
+}
+
+bool lbdemOutputStressNext(const lbdem_ctx* ctx) {
+  const lbdem_output* o = ctx->out;
+  return o && o->dem && screenCounter(o, o->realTime + o->unitTime) > o->lastScreen;
+}
+
+bool lbdemOutputBlocksPair(const lbdem_ctx* ctx) {
+  const lbdem_output* o = ctx->out;
+  if (!o) return false;
+  if (lbdemOutputDueNext(ctx)) return true;
+  return o->dem && screenCounter(o, (o->realTime + o->unitTime) + o->unitTime) > o->lastScreen;
 }
 
 int lbdemOutputAfterCycle(lbdem_ctx* ctx) {
@@ -226,7 +277,8 @@ void lbdemOutputFree(lbdem_ctx* ctx) {
   for (auto& s : o->slots)
     if (s.ev) cudaEventDestroy(s.ev);
   if (o->pinned) cudaFreeHost(o->pinned);
-  for (std::FILE* f : {o->fExport, o->fPos, o->fForce, o->fWall})
+  for (std::FILE* f : {o->fExport, o->fPos, o->fForce, o->fWall, o->fStress, o->fNormal,
+                       o->fShear})
     if (f) std::fclose(f);
   delete o;
   ctx->out = nullptr;
@@ -246,7 +298,8 @@ extern "C" int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_
   o->dem = ctx->demSolve;
   o->nObj = ctx->nObj;
   o->nWall = ctx->nWall;
-  o->slotDoubles = std::max<size_t>((size_t)o->nObj * OB_STRIDE + (size_t)o->nWall * 12, 1);
+  o->slotDoubles = (size_t)o->nObj * OB_STRIDE + (size_t)o->nWall * 12 + STRESS_N;
+  o->vol = ctx->k.demSize[0] * ctx->k.demSize[1] * ctx->k.demSize[2];
   // realTime of the cycles already run, summed as goCycle sums it
   for (long long i = 0; i < ctx->lbTime; ++i) o->realTime += o->unitTime;
   const std::string d(dir);
@@ -274,16 +327,15 @@ extern "C" int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_
         "0-FTotal(x) 0-FTotal(y) 0-FTotal(z) 1-FTotal(x) 1-FTotal(y) 1-FTotal(z) 2-FTotal(x) "
         "2-FTotal(y) 2-FTotal(z) 3-FTotal(x) 3-FTotal(y) 3-FTotal(z) 4-FTotal(x) 4-FTotal(y) "
         "4-FTotal(z) 5-FTotal(x) 5-FTotal(y) 5-FTotal(z) \n");
-    std::FILE* st = openWithHeader(d + "/stressTensor.dat", "xx yy zz xy yz zx \n");
-    std::FILE* sn = openWithHeader(d + "/normalStressCont.dat",
-                                   "hydro-xx hydro-yy hydro-zz lub-xx lub-yy lub-zz contact-xx "
-                                   "contact-yy contact-zz rep-xx rep-yy rep-zz \n");
-    std::FILE* ss = openWithHeader(d + "/shearStressCont.dat",
-                                   "hydro-xy hydro-yz hydro-zx lub-xy lub-yz lub-zx contact-xy "
-                                   "contact-yz contact-zx rep-xy rep-yz rep-zx \n");
-    ok = ok && o->fPos && body && o->fForce && o->fWall && st && sn && ss;
-    for (std::FILE* f : {body, st, sn, ss})
-      if (f) std::fclose(f);
+    o->fStress = openWithHeader(d + "/stressTensor.dat", "xx yy zz xy yz zx \n");
+    o->fNormal = openWithHeader(d + "/normalStressCont.dat",
+                                "hydro-xx hydro-yy hydro-zz lub-xx lub-yy lub-zz contact-xx "
+                                "contact-yy contact-zz rep-xx rep-yy rep-zz \n");
+    o->fShear = openWithHeader(d + "/shearStressCont.dat",
+                               "hydro-xy hydro-yz hydro-zx lub-xy lub-yz lub-zx contact-xy "
+                               "contact-yz contact-zx rep-xy rep-yz rep-zx \n");
+    ok = ok && o->fPos && body && o->fForce && o->fWall && o->fStress && o->fNormal && o->fShear;
+    if (body) std::fclose(body);
   }
   if (!ok) {
     lbdemOutputFree(ctx);

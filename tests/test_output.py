@@ -14,8 +14,8 @@ the reference's own IO code wrote for the same inputs
   cancel to near zero.
 - GPU, mixed form through the Python API: the same layout, numbers within
   MIXED_FRAC of each file's largest value.
-- The stress files keep the reference's header line only (the library does
-  not form the DEM stress sums); bodyPosition.dat is header-only in both.
+- The stress files (the DEM stress sums over the DEM volume) are compared
+  the same way; bodyPosition.dat is header-only in both.
 """
 import json
 import os
@@ -29,8 +29,9 @@ from conftest import GOLDEN, REPO
 
 DRIVER = os.path.join(REPO, "lbm-dem_gb300", "lbdem_run")
 IO = os.path.join(GOLDEN, "io")
-FILLED = ("export.dat", "objPosition.dat", "objForce.dat", "wallForce.dat", "bodyPosition.dat")
 STRESS = ("stressTensor.dat", "normalStressCont.dat", "shearStressCont.dat")
+FILLED = ("export.dat", "objPosition.dat", "objForce.dat", "wallForce.dat",
+          "bodyPosition.dat") + STRESS
 RTOL_PRINT = 2e-5
 ATOL_FRAC = 1e-9
 MIXED_FRAC = 1e-3
@@ -106,8 +107,6 @@ def test_driver_writes_the_reference_files(name, lib, tmp_path):
     assert r.returncode == 0, r.stderr
     for f in FILLED:
         _compare(d / "out" / f, os.path.join(IO, name, f), RTOL_PRINT, ATOL_FRAC)
-    for f in STRESS:
-        assert _lines(d / "out" / f)[0] == _lines(os.path.join(IO, name, f))[0]
 
 
 @pytest.mark.gpu
