@@ -323,13 +323,18 @@ int lbdem_export_recycle_fluid(lbdem_ctx* ctx, const char* path);
  * Only lbdem_cycle advances the output clock; the four single-step entry
  * points do not. */
 int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_exp_time);
-/* With output open, also write the reference's fluid recycle files
- * (IO::createFiles, src/IO.cpp:201-210): dir/fluidData/fluidRecycle%010u.dat
- * named by the cycle, at every cycle where (unsigned)(realTime /
- * fluid_recycle_exp_time) + 1 advances, and now for a run that has not
- * cycled yet; each is lbdem_export_recycle_fluid and synchronises the
- * stream. 0 turns them off. */
-int lbdem_output_recycle(lbdem_ctx* ctx, double fluid_recycle_exp_time);
+/* With output open, also write the reference's recycle files
+ * (IO::createFiles, src/IO.cpp:201-210, 268-274): dir/fluidData/
+ * fluidRecycle%010u.dat named by the cycle, at every cycle where
+ * (unsigned)(realTime / fluid_recycle_exp_time) + 1 advances (each is
+ * lbdem_export_recycle_fluid), and dir/particleData/partRecycle%04u.dat
+ * named by its counter, at every cycle where the part_recycle_exp_time
+ * counter advances (IO::exportRecycleParticles: radius, position,
+ * velocity, negated total stresslet and vertical displacement); both also
+ * now for a run that has not cycled yet. Each file synchronises the
+ * stream. 0 turns either off. */
+int lbdem_output_recycle(lbdem_ctx* ctx, double fluid_recycle_exp_time,
+                         double part_recycle_exp_time);
 /* Write every pending line and close the files (also done by
  * lbdem_destroy). */
 int lbdem_output_close(lbdem_ctx* ctx);

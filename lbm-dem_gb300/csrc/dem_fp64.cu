@@ -705,7 +705,12 @@ LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGather, DemArgs, dem) {
     }
     const double dtt = k.dt, im = a.invm[i], iI = a.invI[i];
     for (int c = 0; c < 3; ++c) {
-      a.x0[c * P + i] = xa[c] + (dtt * va[c] + dtt * dtt * FT[c] * im);
+      const double xn = xa[c] + (dtt * va[c] + dtt * dtt * FT[c] * im);
+      a.x0[c * P + i] = xn;
+      if (c == 1) {
+        a.dispY[i] = a.xinitY[i] - xn;
+        if (stepNo == k.objWaitTime) a.xinitY[i] = xn;
+      }
       a.x1[c * P + i] = va[c] + dtt * FT[c] * im;
       a.w1[c * P + i] = wa[c] + dtt * MT[c] * iI;
       a.FContact[c * P + i] = FC[c];

@@ -315,7 +315,12 @@ LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGatherMixed, DemArgs, dem) {
     for (int c = 0; c < 3; ++c) {
       const double FT = FH[c] + (double)FC[c] + (double)FL[c] + FG[c] + (double)FR[c];
       const double MT = MH[c] + (double)MC[c] + (double)ML[c];
-      a.x0[c * P + i] = xa[c] + (dtt * va[c] + dtt * dtt * FT * im);
+      const double xn = xa[c] + (dtt * va[c] + dtt * dtt * FT * im);
+      a.x0[c * P + i] = xn;
+      if (c == 1) {  // particle::disp.y and x_i.y (src/DEM.cpp:2705, 2721-2724)
+        a.dispY[i] = a.xinitY[i] - xn;
+        if (stepNo == k.objWaitTime) a.xinitY[i] = xn;
+      }
       a.x1[c * P + i] = va[c] + dtt * FT * im;
       a.w1[c * P + i] = waD[c] + dtt * MT * iI;
       a.FContact[c * P + i] = FC[c];

@@ -18,6 +18,10 @@
 // the particles' tangential springs before the gather advances them (the
 // same law on the same inputs, including the fictional lid before
 // objWaitTime); the stresslets are formed here in FP64 for both forms.
+// With perParticle, also each particle's STotal = SHydro + SLub + SContact
+// + SRep (src/DEM.cpp:748), for the particle recycle file: a pair's contact
+// and electrostatic tensors go to both particles, its stresslets to each
+// side.
 #include "dem_forces.cuh"
 
 namespace lbdem {
@@ -96,11 +100,18 @@ __device__ void addOuter(const double* r, const double* f, double* S) {
     for (int b = 0; b < 3; ++b) S[3 * a + b] -= r[a] * f[b];
 }
 
+// perParticle[c][P] += T[c] for particle p
+__device__ void scatter9(double* perParticle, int P, int p, const double* T) {
+  for (int c = 0; c < 9; ++c)
+    if (T[c] != 0.0) atomicAdd(perParticle + (long long)c * P + p, T[c]);
+}
+
 }  // namespace
 
 // One thread per particle; out[36] += contact, lub, electro, hydro (3x3
 // row-major each). Launched between the pair pass and the gather.
-__global__ void demStress(Consts k, DemArgs a, const double* SHydro, double* out) {
+__global__ void demStress(Consts k, DemArgs a, const double* SHydro, double* out,
+                          double* perParticle) {
   __shared__ double acc[STRESS_N];
   for (int t = threadIdx.x; t < STRESS_N; t += blockDim.x) acc[t] = 0.0;
   __syncthreads();
@@ -109,6 +120,8 @@ __global__ void demStress(Consts k, DemArgs a, const double* SHydro, double* out
   const int* L = a.list[a.iscal[IS_LISTCUR]];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
     double C[9] = {0}, Lb[9] = {0}, E[9] = {0}, H[9];
+    double Ti[9] = {0};  // this particle's share of the pair terms
+    double Cown[9] = {0}, Lown[9] = {0};  // its wall and impactor terms
     double xa[3], va[3], wa[3];
     load3(a.x0, P, i, xa);
     load3(a.x1, P, i, va);
@@ -131,19 +144,37 @@ __global__ void demStress(Consts k, DemArgs a, const double* SHydro, double* out
         fr[c] = k.mixed ? (double)((const float*)a.pairbuf)[e * PAIR_VALS + 15 + c]
                         : a.pairbuf[e * PAIR_VALS + 15 + c];
       }
+      double T[9] = {0};  // contact + electrostatic of the pair, for both particles
       addOuter(r12v, fc, C);
       addOuter(r12v, fr, E);
-      if (!afterWait) continue;
-      const double rb = a.r[j];
-      const double r12 = sqrt(r12v[0] * r12v[0] + r12v[1] * r12v[1] + r12v[2] * r12v[2]);
-      LubStress ls;
-      if (!lubStressSpheres(k, ra, rb, r12 - (ra + rb), ls)) continue;
-      load3(a.x1, P, j, vb);
-      load3(a.w1, P, j, wb);
-      const double n[3] = {r12v[0] / r12, r12v[1] / r12, r12v[2] / r12};
-      const double um[3] = {va[0] - vb[0], va[1] - vb[1], va[2] - vb[2]};
-      addStresslet(1.0, ls.Xg1, ls.Yg1, ls.Yh11, ls.Yh12, n, um, wa, wb, Lb);
-      addStresslet(-1.0, ls.Xg2, ls.Yg2, ls.Yh21, ls.Yh22, n, um, wa, wb, Lb);
+      if (perParticle) {
+        addOuter(r12v, fc, T);
+        addOuter(r12v, fr, T);
+        for (int c = 0; c < 9; ++c) Ti[c] += T[c];
+      }
+      double S2[9] = {0};
+      if (afterWait) {
+        const double rb = a.r[j];
+        const double r12 = sqrt(r12v[0] * r12v[0] + r12v[1] * r12v[1] + r12v[2] * r12v[2]);
+        LubStress ls;
+        if (lubStressSpheres(k, ra, rb, r12 - (ra + rb), ls)) {
+          load3(a.x1, P, j, vb);
+          load3(a.w1, P, j, wb);
+          const double n[3] = {r12v[0] / r12, r12v[1] / r12, r12v[2] / r12};
+          const double um[3] = {va[0] - vb[0], va[1] - vb[1], va[2] - vb[2]};
+          double S1[9] = {0};
+          addStresslet(1.0, ls.Xg1, ls.Yg1, ls.Yh11, ls.Yh12, n, um, wa, wb, S1);
+          addStresslet(-1.0, ls.Xg2, ls.Yg2, ls.Yh21, ls.Yh22, n, um, wa, wb, S2);
+          for (int c = 0; c < 9; ++c) {
+            Lb[c] += S1[c] + S2[c];
+            Ti[c] += S1[c];
+          }
+        }
+      }
+      if (perParticle) {
+        for (int c = 0; c < 9; ++c) T[c] += S2[c];
+        scatter9(perParticle, P, j, T);
+      }
     }
     double xiw[3], xio[3], df[3], dt[3];
     load3(a.xiw, P, i, xiw);
@@ -158,14 +189,14 @@ __global__ void demStress(Consts k, DemArgs a, const double* SHydro, double* out
         LubStress ls;
         if (!lubStressWall(k, ra, r12 - ra, ls)) continue;
         const double n[3] = {o[0] / r12, o[1] / r12, o[2] / r12};
-        addStresslet(1.0, ls.Xg1, ls.Yg1, ls.Yh11, 0.0, n, va, wa, zero3, Lb);
+        addStresslet(1.0, ls.Xg1, ls.Yg1, ls.Yh11, 0.0, n, va, wa, zero3, Lown);
       }
       for (int ob = 0; ob < k.nObj; ++ob) {
         const double* B = a.obj + ob * OB_STRIDE;
         const PairGeom<double> g = pairGeomD(0.5 * (ra + B[OB_R]), xa, B + OB_X0, va, B + OB_X1);
         objContactOne(k, ra, B[OB_R], g, wa, B + OB_W1, xio, df, dt);
         const double r[3] = {xa[0] - B[OB_X0], xa[1] - B[OB_X0 + 1], xa[2] - B[OB_X0 + 2]};
-        addOuter(r, df, C);
+        addOuter(r, df, Cown);
       }
       for (int ob = 0; ob < k.nObj; ++ob) {
         const double* B = a.obj + ob * OB_STRIDE;
@@ -175,7 +206,7 @@ __global__ void demStress(Consts k, DemArgs a, const double* SHydro, double* out
         if (!lubStressSpheres(k, ra, B[OB_R], r12 - (ra + B[OB_R]), ls)) continue;
         const double n[3] = {r[0] / r12, r[1] / r12, r[2] / r12};
         const double um[3] = {va[0] - B[OB_X1], va[1] - B[OB_X1 + 1], va[2] - B[OB_X1 + 2]};
-        addStresslet(1.0, ls.Xg1, ls.Yg1, ls.Yh11, ls.Yh12, n, um, wa, B + OB_W1, Lb);
+        addStresslet(1.0, ls.Xg1, ls.Yg1, ls.Yh11, ls.Yh12, n, um, wa, B + OB_W1, Lown);
       }
     } else {
       // the fictional lid advances the wall spring before the walls do
@@ -191,10 +222,18 @@ __global__ void demStress(Consts k, DemArgs a, const double* SHydro, double* out
         for (int c = 0; c < 3; ++c) o[c] = (xa[c] - W.p[c]) * W.n[c] * W.n[c];
         const double r1w = sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]);
         wallContactOne(k, ra, va, wa, xiw, o[0], o[1], o[2], r1w, nst, df, dt);
-        addOuter(o, df, C);
+        addOuter(o, df, Cown);
       }
     }
+    if (perParticle) {
+      // pair terms (Ti), then its own walls, impactor and hydrodynamics
+      double T[9];
+      for (int c = 0; c < 9; ++c) T[c] = Ti[c] + (Cown[c] + Lown[c]) + H[c];
+      scatter9(perParticle, P, i, T);
+    }
     for (int c = 0; c < 9; ++c) {
+      C[c] += Cown[c];
+      Lb[c] += Lown[c];
       if (C[c] != 0.0) atomicAdd(&acc[c], C[c]);
       if (Lb[c] != 0.0) atomicAdd(&acc[9 + c], Lb[c]);
       if (E[c] != 0.0) atomicAdd(&acc[18 + c], E[c]);

@@ -72,6 +72,11 @@ struct DemArgs {
   uint8_t* pairflag;
   int* pcell;
   float4* posf;  // [P] FP32 position and radius, written by nbrCellAssign
+  // particle::x_i.y (position at the start, again after the objWaitTime
+  // step) and disp.y = x_i.y - x0.y after each integration (src/DEM.cpp:288,
+  // 2705, 2721-2724); read only by the particle recycle file
+  double* xinitY;
+  double* dispY;
   int* ppos;
   int *cellCount, *cellStart, *cellFill, *cellParts;
   double* obj;
@@ -226,7 +231,8 @@ __global__ void exportLattice(Consts k, const uint8_t* mask, const void* f, cons
 constexpr int GATHER_THREADS = 64;
 // DEM stress sums: contact, lubrication, electrostatic, hydrodynamic (3x3 each)
 constexpr int STRESS_N = 36;
-__global__ void demStress(Consts k, DemArgs a, const double* SHydro, double* out);
+__global__ void demStress(Consts k, DemArgs a, const double* SHydro, double* out,
+                          double* perParticle);
 
 // dem_fp64.cu
 __global__ void demBegin(Consts k, DemArgs a, int forceRebuild);

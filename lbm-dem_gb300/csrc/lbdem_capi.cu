@@ -154,6 +154,8 @@ DemArgs demArgs(lbdem_ctx* c) {
   a.x0 = d.px0;
   a.x1 = d.px1;
   a.w1 = d.pw1;
+  a.xinitY = d.xinitY;
+  a.dispY = d.dispY;
   a.r = d.pr;
   a.invm = d.pinvm;
   a.invI = d.pinvI;
@@ -536,6 +538,9 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   AL(d.uncover, (size_t)UNCOVER_CAP);
   AL(d.ifList, N);
   AL(d.stress, (size_t)STRESS_N);
+  AL(d.pStress, 9 * P1);
+  AL(d.xinitY, P1);
+  AL(d.dispY, P1);
   int* dBoundary = nullptr;
   int* dWallType = nullptr;
   AL(dBoundary, 6);
@@ -544,6 +549,8 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   cudaStream_t st = ctx->stream;
   // ---- uploads ----
   CK(cudaMemcpyAsync(d.px0, hx0.data(), 3 * P * sizeof(double), cudaMemcpyHostToDevice, st));
+  // particle::x_i = x0 at the start (src/DEM.cpp:288)
+  CK(cudaMemcpyAsync(d.xinitY, d.px0 + P, P * sizeof(double), cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(d.pr, hr.data(), P * sizeof(double), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d.pinvm, hinvm.data(), P * sizeof(double), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d.pinvI, hinvI.data(), P * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -630,9 +637,13 @@ extern "C" int lbdem_set_stream(lbdem_ctx* ctx, void* stream) {
 static int enqueueStress(lbdem_ctx* ctx, const DemArgs& a) {
   if (!ctx->stressNext) return LBDEM_OK;
   CK(cudaMemsetAsync(ctx->d.stress, 0, STRESS_N * sizeof(double), ctx->stream));
+  double* per = ctx->pStressNext ? ctx->d.pStress : nullptr;
+  if (per)
+    CK(cudaMemsetAsync(per, 0, 9 * (size_t)std::max(ctx->nPart, 1) * sizeof(double),
+                       ctx->stream));
   if (ctx->nPart > 0) {
     demStress<<<partGrid(ctx, 128), 128, 0, ctx->stream>>>(ctx->k, a, ctx->d.pSHydro,
-                                                           ctx->d.stress);
+                                                           ctx->d.stress, per);
     ++ctx->launches;
   }
   return LBDEM_OK;
@@ -1054,8 +1065,9 @@ extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
       continue;
     }
     ctx->stressNext = lbdemOutputStressNext(ctx);
+    ctx->pStressNext = lbdemOutputParticleStressNext(ctx);
     rc = cycleOnce(ctx);
-    ctx->stressNext = false;
+    ctx->stressNext = ctx->pStressNext = false;
     if (rc) return rc;
     if ((rc = lbdemOutputAfterCycle(ctx))) return rc;
     ++i;
@@ -1152,6 +1164,8 @@ extern "C" int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t prec
   add(UNCOVER_CAP, 4);
   add(N, 4);                                   // interface list
   add(STRESS_N, 8);                            // stress sums
+  add(9 * P1, 8);                              // per-particle stresslets
+  add(2 * P1, 8);                              // x_i.y, disp.y
   *bytes = total;
   return LBDEM_OK;
 }

@@ -137,6 +137,9 @@ struct Device {
   uint32_t* uncover = nullptr;           // [UNCOVER_CAP] candidate list
   uint32_t* ifList = nullptr;            // [N] interface nodes of the lattice step, any order
   double* stress = nullptr;              // [36] DEM stress sums of an output cycle (demStress)
+  double* pStress = nullptr;             // [9][P] per-particle total stresslet (same cycles)
+  double* xinitY = nullptr;              // [P] particle::x_i.y
+  double* dispY = nullptr;               // [P] particle::disp.y
 };
 
 // offsets into Device::scal (doubles)
@@ -203,6 +206,9 @@ bool lbdemOutputDueNext(const lbdem_ctx* c);
 // whether the next cycle's DEM step forms the stress sums (a stress-file line
 // follows it)
 bool lbdemOutputStressNext(const lbdem_ctx* c);
+// whether it also forms the per-particle totals (a particle recycle file
+// follows it)
+bool lbdemOutputParticleStressNext(const lbdem_ctx* c);
 // whether two cycles cannot run as one replayed pair: an output is due after
 // the first, or the stress sums are due in the second
 bool lbdemOutputBlocksPair(const lbdem_ctx* c);
@@ -239,6 +245,7 @@ struct lbdem_ctx {
   double fluidHeight = 0.0;     // physical, as the configuration gives it
   lbdem_output* out = nullptr;  // open screen-phase output files, if any
   bool stressNext = false;      // the next DEM step forms the stress sums
+  bool pStressNext = false;     // ... and the per-particle totals
   int objIndexField[lbdem::MAX_OBJ] = {0};
   long long deviceBytes = 0;
   // every device allocation of the run, in allocation order (the same order

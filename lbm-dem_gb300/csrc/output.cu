@@ -19,11 +19,17 @@
 // after each lbdem_cycle call, waited for by lbdem_sync and
 // lbdem_output_close). A full ring waits for its oldest slot.
 //
-// With lbdem_output_recycle the fluid recycle files of IO::createFiles
-// (src/IO.cpp:201-210) are written as well: dir/fluidData/
+// With lbdem_output_recycle the recycle files of IO::createFiles
+// (src/IO.cpp:201-210, 268-274) are written as well: dir/fluidData/
 // fluidRecycle%010u.dat, named by the cycle, whenever the counter
-// (unsigned)(realTime / fluidRecycleExpTime) + 1 advances (at the first
-// cycle too). Each one is a full lattice export and synchronises the stream.
+// (unsigned)(realTime / fluidRecycleExpTime) + 1 advances, and
+// dir/particleData/partRecycle%04u.dat, named by its counter, whenever the
+// partRecycleExpTime counter does (both at the first cycle too).
+// IO::exportRecycleParticles (src/IO.cpp:999-1030) writes per particle the
+// radius, position and velocity, then the negated total stresslet (xx, yy,
+// zz and the three mean off-diagonal pairs) and the negated vertical
+// displacement since the start, tab-separated. Each file synchronises the
+// stream.
 //
 // The stress files (IO::exportStressTensor and the two contribution files,
 // src/IO.cpp:1355-1409) take the DEM stress sums of the cycle's DEM step
@@ -53,6 +59,8 @@ struct lbdem_output {
   unsigned lastScreen = 0; // IO::lastScreenExp
   double recycleExp = 0.0;  // IO::fluidRecycleExpTime (0: off)
   unsigned lastRecycle = 0; // IO::lastFluidRecycleExp
+  double partExp = 0.0;     // IO::partRecycleExpTime (0: off)
+  unsigned lastPart = 0;    // IO::lastPartRecycleExp
   bool dem = false;
   std::FILE* fExport = nullptr;
   std::FILE* fPos = nullptr;
@@ -88,6 +96,46 @@ unsigned screenCounter(const lbdem_output* o, double t) {
 }
 unsigned recycleCounter(const lbdem_output* o, double t) {
   return o->recycleExp > 0.0 ? static_cast<unsigned>(t / o->recycleExp) + 1u : 0u;
+}
+unsigned partCounter(const lbdem_output* o, double t) {
+  return o->partExp > 0.0 ? static_cast<unsigned>(t / o->partExp) + 1u : 0u;
+}
+
+// IO::exportRecycleParticles, named by the counter (waits for the run's work)
+int writePartRecycle(lbdem_ctx* ctx, unsigned counter) {
+  int rc = lbdem_sync(ctx);
+  if (rc) return rc;
+  const int P = ctx->nPart;
+  std::vector<double> r(P), x0(3 * (size_t)P), x1(3 * (size_t)P), S(9 * (size_t)P), dy(P);
+  const Device& d = ctx->d;
+  cudaError_t e = cudaSuccess;
+  if (P > 0) {
+    e = cudaMemcpy(r.data(), d.pr, P * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(x0.data(), d.px0, 3 * P * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(x1.data(), d.px1, 3 * P * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(S.data(), d.pStress, 9 * P * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(dy.data(), d.dispY, P * sizeof(double), cudaMemcpyDeviceToHost);
+  }
+  if (e != cudaSuccess)
+    return fail(ctx, LBDEM_ERR_CUDA, std::string("particle recycle: ") + cudaGetErrorString(e));
+  char name[64];
+  std::snprintf(name, sizeof name, "/particleData/partRecycle%04u.dat", counter);
+  std::FILE* f = std::fopen((ctx->out->dir + name).c_str(), "w");
+  if (!f) return fail(ctx, LBDEM_ERR_IO, std::string("cannot write ") + ctx->out->dir + name);
+  for (int i = 0; i < P; ++i) {
+    auto m = [&](int c) { return S[(size_t)c * P + i]; };
+    std::fprintf(f, "%g ", r[i]);
+    std::fprintf(f, "%g %g %g ", x0[i], x0[P + i], x0[2 * (size_t)P + i]);
+    std::fprintf(f, "%g %g %g ", x1[i], x1[P + i], x1[2 * (size_t)P + i]);
+    std::fprintf(f, "%g\t%g\t%g\t%g\t%g\t%g\t%g\n", -m(0), -m(4), -m(8), -(m(1) + m(3)) * 0.5,
+                 -(m(5) + m(7)) * 0.5, -(m(2) + m(6)) * 0.5, -dy[i]);
+  }
+  if (std::fclose(f) != 0) return fail(ctx, LBDEM_ERR_IO, std::string("write failed: ") + name);
+  return LBDEM_OK;
 }
 
 // IO::exportRecycleFluid at this cycle (waits for the run's work)
@@ -228,19 +276,27 @@ bool lbdemOutputDueNext(const lbdem_ctx* ctx) {
   const lbdem_output* o = ctx->out;
   if (!o) return false;
   const double t = o->realTime + o->unitTime;
-  return screenCounter(o, t) > o->lastScreen || recycleCounter(o, t) > o->lastRecycle;
+  return screenCounter(o, t) > o->lastScreen || recycleCounter(o, t) > o->lastRecycle ||
+         partCounter(o, t) > o->lastPart;
+}
+
+bool lbdemOutputParticleStressNext(const lbdem_ctx* ctx) {
+  const lbdem_output* o = ctx->out;
+  return o && o->dem && partCounter(o, o->realTime + o->unitTime) > o->lastPart;
 }
 
 bool lbdemOutputStressNext(const lbdem_ctx* ctx) {
   const lbdem_output* o = ctx->out;
-  return o && o->dem && screenCounter(o, o->realTime + o->unitTime) > o->lastScreen;
+  return o && o->dem && (screenCounter(o, o->realTime + o->unitTime) > o->lastScreen ||
+                         partCounter(o, o->realTime + o->unitTime) > o->lastPart);
 }
 
 bool lbdemOutputBlocksPair(const lbdem_ctx* ctx) {
   const lbdem_output* o = ctx->out;
   if (!o) return false;
   if (lbdemOutputDueNext(ctx)) return true;
-  return o->dem && screenCounter(o, (o->realTime + o->unitTime) + o->unitTime) > o->lastScreen;
+  const double t2 = (o->realTime + o->unitTime) + o->unitTime;
+  return o->dem && (screenCounter(o, t2) > o->lastScreen || partCounter(o, t2) > o->lastPart);
 }
 
 int lbdemOutputAfterCycle(lbdem_ctx* ctx) {
@@ -255,7 +311,12 @@ int lbdemOutputAfterCycle(lbdem_ctx* ctx) {
   const unsigned r = recycleCounter(o, o->realTime);
   if (r > o->lastRecycle) {
     o->lastRecycle = r;
-    return writeRecycle(ctx);
+    if (int rc = writeRecycle(ctx)) return rc;
+  }
+  const unsigned p = partCounter(o, o->realTime);
+  if (p > o->lastPart) {
+    o->lastPart = p;
+    return writePartRecycle(ctx, p);
   }
   return LBDEM_OK;
 }
@@ -356,16 +417,22 @@ extern "C" int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_
   return LBDEM_OK;
 }
 
-extern "C" int lbdem_output_recycle(lbdem_ctx* ctx, double fluid_recycle_exp_time) {
+extern "C" int lbdem_output_recycle(lbdem_ctx* ctx, double fluid_recycle_exp_time,
+                                    double part_recycle_exp_time) {
   if (!ctx) return LBDEM_ERR_INVALID;
   lbdem_output* o = ctx->out;
   if (!o) return fail(ctx, LBDEM_ERR_INVALID, "output_recycle: output not open");
-  if (!(fluid_recycle_exp_time >= 0.0))
-    return fail(ctx, LBDEM_ERR_INVALID, "output_recycle: negative fluidRecycleExpTime");
+  if (!(fluid_recycle_exp_time >= 0.0) || !(part_recycle_exp_time >= 0.0))
+    return fail(ctx, LBDEM_ERR_INVALID, "output_recycle: negative export time");
   o->recycleExp = ctx->lbSolve ? fluid_recycle_exp_time : 0.0;
+  o->partExp = ctx->demSolve ? part_recycle_exp_time : 0.0;
   o->lastRecycle = recycleCounter(o, o->realTime);
-  // the file IO::outputStep writes before the first goCycle
-  if (ctx->lbTime == 0 && o->lastRecycle > 0) return writeRecycle(ctx);
+  o->lastPart = partCounter(o, o->realTime);
+  // the files IO::outputStep writes before the first goCycle
+  if (ctx->lbTime != 0) return LBDEM_OK;
+  if (o->lastRecycle > 0)
+    if (int rc = writeRecycle(ctx)) return rc;
+  if (o->lastPart > 0) return writePartRecycle(ctx, o->lastPart);
   return LBDEM_OK;
 }
 

@@ -28,8 +28,8 @@
 // With screenExpTime > 0 the reference's own screen-phase files (export.dat,
 // objPosition.dat, objForce.dat, wallForce.dat, ...) are written into the
 // data directory as IO::outputStep writes them (lbdem_output_open), and with
-// fluidRecycleExpTime > 0 its fluid recycle files into data/fluidData
-// (lbdem_output_recycle).
+// fluidRecycleExpTime / partRecycleExpTime > 0 its recycle files into
+// data/fluidData and data/particleData (lbdem_output_recycle).
 #include <sys/stat.h>
 
 #include <cerrno>
@@ -190,10 +190,11 @@ int main(int argc, char** argv) {
     return 0;
   };
 
-  if (cfg.screenExpTime > 0.0 || cfg.fluidRecycleExpTime > 0.0) {
+  if (cfg.screenExpTime > 0.0 || cfg.fluidRecycleExpTime > 0.0 ||
+      cfg.partRecycleExpTime > 0.0) {
     if ((rc = lbdem_output_open(ctx, workDir.c_str(), cfg.screenExpTime)))
       return fail(ctx, "lbdem_output_open", rc);
-    if ((rc = lbdem_output_recycle(ctx, cfg.fluidRecycleExpTime)))
+    if ((rc = lbdem_output_recycle(ctx, cfg.fluidRecycleExpTime, cfg.partRecycleExpTime)))
       return fail(ctx, "lbdem_output_recycle", rc);
   }
   if (resume.empty() && (rc = report(0))) return fail(ctx, "report", rc);

@@ -187,7 +187,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "lbdem_export_recycle_fluid": ([c_ctx, C.c_char_p], C.c_int),
         "lbdem_output_open": ([c_ctx, C.c_char_p, C.c_double], C.c_int),
         "lbdem_output_close": ([c_ctx], C.c_int),
-        "lbdem_output_recycle": ([c_ctx, C.c_double], C.c_int),
+        "lbdem_output_recycle": ([c_ctx, C.c_double, C.c_double], C.c_int),
         "lbdem_restore": ([c_ctx, C.c_char_p], C.c_int),
     }
     for name, (args, res) in sig.items():

@@ -9,9 +9,10 @@
 //                     -io DIR (the reference's own IO code, src/IO.cpp, with
 //                     every VTK export time 0: the screen-phase files
 //                     export.dat, objPosition.dat, objForce.dat,
-//                     wallForce.dat and the stress files, in DIR, and the
+//                     wallForce.dat and the stress files, in DIR, the
 //                     fluid recycle files in DIR/fluidData at
-//                     fluidRecycleExpTime)
+//                     fluidRecycleExpTime and the particle recycle files in
+//                     DIR/particleData at partRecycleExpTime)
 // Defined-behaviour pins applied here, at the public-member level, without
 // touching the reference sources:
 //   * particle::list/_list/xix/xiy/xiz/_xix/_xiy/_xiz (src/elmt.h:44-51) are
@@ -245,7 +246,8 @@ int main(int argc, char** argv) {
     io.springExpTime = io.objectExpTime2 = io.chainExpTime = io.velExpTime = 0.0;
     io.dispExpTime = io.stressExpTime = io.part_yDispExpTime = io.part_rDispExpTime = 0.0;
     io.part_n1ExpTime = io.part_n2ExpTime = io.part_pressureExpTime = 0.0;
-    io.part_yyStressExpTime = io.partRecycleExpTime = 0.0;
+    io.part_yyStressExpTime = 0.0;
+    PARSE_CLASS_MEMBER(configFile, io.partRecycleExpTime, "partRecycleExpTime", 0.0);
     PARSE_CLASS_MEMBER(configFile, io.fluidRecycleExpTime, "fluidRecycleExpTime", 0.0);
     io.outputExpTime = io.simComplexExpTime = 0.0;
     io.initialize();

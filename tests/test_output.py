@@ -14,8 +14,10 @@ the reference's own IO code wrote for the same inputs
   cancel to near zero.
 - GPU, mixed form through the Python API: the same layout, numbers within
   MIXED_FRAC of each file's largest value.
-- The stress files (the DEM stress sums over the DEM volume) are compared
-  the same way; bodyPosition.dat is header-only in both.
+- The stress files (the DEM stress sums over the DEM volume) and the
+  particle recycle files (particleData/partRecycle*.dat, the driver with
+  partRecycleExpTime: per-particle total stresslets and displacements) are
+  compared the same way; bodyPosition.dat is header-only in both.
 """
 import json
 import os
@@ -66,10 +68,11 @@ def _compare(got_path, ref_path, rtol, atol_frac):
     atol = atol_frac * _scale(ref)
     for n, (lg, lr) in enumerate(zip(got, ref)):
         assert lg.count("\t") == lr.count("\t"), (name, n, lg, lr)
-        tg, tr = lg.split(" "), lr.split(" ")
+        assert lg.count(" ") == lr.count(" "), (name, n, lg, lr)
+        tg, tr = lg.split(), lr.split()
         assert len(tg) == len(tr), (name, n, lg, lr)
         for a, b in zip(tg, tr):
-            fa, fb = _num(a.strip("\t")), _num(b.strip("\t"))
+            fa, fb = _num(a), _num(b)
             if fa is None or fb is None:
                 assert a == b, (name, n, a, b)
             else:
@@ -102,11 +105,17 @@ def test_driver_writes_the_reference_files(name, lib, tmp_path):
     d = tmp_path / name
     shutil.copytree(os.path.join(GOLDEN, name), d)
     r = subprocess.run([DRIVER, "-c", "parameters.cfg", "-steps", str(c["steps"]),
-                        "-screenExpTime", repr(c["screenExpTime"]), "-d", "out"], cwd=d,
+                        "-screenExpTime", repr(c["screenExpTime"]), "-partRecycleExpTime",
+                        repr(c["partRecycleExpTime"]), "-d", "out"], cwd=d,
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     for f in FILLED:
         _compare(d / "out" / f, os.path.join(IO, name, f), RTOL_PRINT, ATOL_FRAC)
+    want = sorted(os.listdir(os.path.join(IO, name, "particleData")))
+    assert sorted(os.listdir(d / "out" / "particleData")) == want
+    for f in want:
+        _compare(d / "out" / "particleData" / f, os.path.join(IO, name, "particleData", f),
+                 RTOL_PRINT, ATOL_FRAC)
 
 
 @pytest.mark.gpu
