@@ -892,8 +892,27 @@ __device__ __forceinline__ void flagClaimBody(const Consts& k, const uint8_t* ma
     if (nx <= 0 || ny <= 0 || nz <= 0) continue;
     const int vol = nx * ny * nz;
     const SphereBoxTest st = sphereBoxTest(cx, cy, cz, r, lo);
+    // lane l visits box nodes l, l + 32, ...: its box coordinates advance by
+    // the decomposition of 32 with carries (no division per node), and nodes
+    // clearly outside the sphere are dropped before their mask is read
+    int bx = lane % nx, by = (lane / nx) % ny, bz = lane / (nx * ny);
+    const int sx = 32 % nx, sy = (32 / nx) % ny, sz = 32 / (nx * ny);
     for (int i = lane; i < vol; i += 32) {
-      const int ix = lo[0] + i % nx, iy = lo[1] + (i / nx) % ny, iz = lo[2] + i / (nx * ny);
+      const int ix = lo[0] + bx, iy = lo[1] + by, iz = lo[2] + bz;
+      bx += sx;
+      by += sy;
+      bz += sz;
+      if (bx >= nx) {
+        bx -= nx;
+        ++by;
+      }
+      if (by >= ny) {
+        by -= ny;
+        ++bz;
+      }
+      const float dx = (float)(ix - lo[0]) - st.fx, dy = (float)(iy - lo[1]) - st.fy,
+                  dz = (float)(iz - lo[2]) - st.fz;
+      if (dx * dx + dy * dy + dz * dz > st.r2out) continue;
       const long long x = ix + iy * k.sy + iz * k.sz;
       if (!(mask[x] & ABIT)) continue;
       if (insideBox(st, ix, iy, iz)) atomicMax(claim + x, (uint32_t)p + 1u);
