@@ -252,6 +252,7 @@ LBDEM_KERNEL(__launch_bounds__(128), nbrBuildCells, DemArgs, dem) {
   __shared__ unsigned long long sKey[NBR_PER_BLOCK][MAX_N];
   __shared__ int sNb[NBR_PER_BLOCK][MAX_N];
   __shared__ int sSorted[NBR_PER_BLOCK][MAX_N];
+  __shared__ int sOld[NBR_PER_BLOCK][MAX_N];
   __shared__ int sCnt[NBR_PER_BLOCK];
   const int cur = a.iscal[IS_LISTCUR];
   const int* oldList = a.list[cur];
@@ -268,16 +269,21 @@ LBDEM_KERNEL(__launch_bounds__(128), nbrBuildCells, DemArgs, dem) {
     const bool valid = cp >= 0;
     if (sub == 0) sCnt[g] = 0;
     __syncthreads();
+    // a cell coordinate shifted by -1, 0 or +1 wrapped into [0, n): the
+    // reference's (c + d + n) % n for |d| <= 1
+    auto wrap = [](int c, int n) { return c < 0 ? c + n : (c >= n ? c - n : c); };
     if (valid) {
       const int cx = cp / (nly * nlz), cy = (cp / nlz) % nly, cz = cp % nlz;
       const int posp = a.ppos[p];
+      // the old list of p, for the history copy below
+      for (int l = sub; l < MAX_N; l += NBR_GROUP) sOld[g][l] = oldList[(long long)p * MAX_N + l];
       for (int v = sub; v < 54; v += NBR_GROUP) {
         const int kk = v >> 1;
         const int dx = kk / 9 - 1, dy = (kk / 3) % 3 - 1, dz = kk % 3 - 1;
         if ((v & 1) == 0) {
           // p as n1: partner q < p in l2 = l1 + d
-          const int l2 = ((cx + dx + nlx) % nlx) * nly * nlz + ((cy + dy + nly) % nly) * nlz +
-                         (cz + dz + nlz) % nlz;
+          const int l2 = wrap(cx + dx, nlx) * nly * nlz + wrap(cy + dy, nly) * nlz +
+                         wrap(cz + dz, nlz);
           const int s0 = a.cellStart[l2], n = a.cellFill[l2];
           for (int t = 0; t < n; ++t) {
             const int q = a.cellParts[s0 + t];
@@ -290,8 +296,8 @@ LBDEM_KERNEL(__launch_bounds__(128), nbrBuildCells, DemArgs, dem) {
           }
         } else {
           // p as n2: partner q > p in l1 = l2 - d
-          const int l1 = ((cx - dx + nlx) % nlx) * nly * nlz + ((cy - dy + nly) % nly) * nlz +
-                         (cz - dz + nlz) % nlz;
+          const int l1 = wrap(cx - dx, nlx) * nly * nlz + wrap(cy - dy, nly) * nlz +
+                         wrap(cz - dz, nlz);
           const int s0 = a.cellStart[l1], n = a.cellFill[l1];
           for (int t = 0; t < n; ++t) {
             const int q = a.cellParts[s0 + t];
@@ -322,7 +328,7 @@ LBDEM_KERNEL(__launch_bounds__(128), nbrBuildCells, DemArgs, dem) {
     }
     __syncthreads();
     if (valid) {
-      const int* ol = oldList + (long long)p * MAX_N;
+      const int* ol = sOld[g];
       const double* ox = oldXi + (long long)p * 3 * MAX_N;
       int* nl = newList + (long long)p * MAX_N;
       double* nx = newXi + (long long)p * 3 * MAX_N;
