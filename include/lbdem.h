@@ -306,7 +306,8 @@ int lbdem_export_recycle_fluid(lbdem_ctx* ctx, const char* path);
 /* ---- the reference's screen-phase output files ------------------------ */
 
 /* Open the reference's screen-phase files in directory `dir` (which must
- * exist) and append their header lines as IO::initialize does
+ * exist; its particleData and fluidData folders are created) and append
+ * their header lines as IO::initialize does
  * (src/IO.cpp:43-94): export.dat and, with the DEM on, objPosition.dat,
  * objForce.dat, wallForce.dat, bodyPosition.dat and the three stress files.
  * From then on lbdem_cycle appends the lines IO::outputStep writes
@@ -318,8 +319,9 @@ int lbdem_export_recycle_fluid(lbdem_ctx* ctx, const char* path);
  * vectors as "x y z ", tab-separated groups. Lines are formatted from
  * copies taken on the context's stream into pinned memory, without
  * synchronising it; lbdem_sync and lbdem_output_close write all pending
- * lines. The stress files keep their header lines only: this library does
- * not form the DEM stress sums. screen_exp_time 0 writes headers only.
+ * lines. The stress files carry DEM::evaluateForces' stress sums of the
+ * cycle, formed on the output cycles only. screen_exp_time 0 writes headers
+ * only.
  * Only lbdem_cycle advances the output clock; the four single-step entry
  * points do not. */
 int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_exp_time);
