@@ -189,6 +189,7 @@ extern "C" int lbdem_restore(lbdem_ctx* ctx, const char* path) {
     return fail(ctx, LBDEM_ERR_IO, "restore: cannot seek in the snapshot");
 
   CKC(cudaStreamSynchronize(ctx->stream));
+  if (int rc = lbdemOutputDrain(ctx, true)) return rc;  // lines of the run being replaced
   Pinned stage;
   CKC(cudaMallocHost(&stage.p, kStageBytes));
   for (const auto& b : ctx->buffers) {
@@ -210,6 +211,8 @@ extern "C" int lbdem_restore(lbdem_ctx* ctx, const char* path) {
   ctx->lbTime = h.lbTime;
   ctx->demTimeStep = h.demTimeStep;
   ctx->demTime = h.demTime;
+  // open output files continue from the restored cycle count
+  lbdemOutputResync(ctx);
   // captured cycles hold the old constants by value: capture again
   for (auto& g : ctx->pairGraph)
     if (g) {

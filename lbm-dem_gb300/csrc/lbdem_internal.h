@@ -215,6 +215,9 @@ bool lbdemOutputBlocksPair(const lbdem_ctx* c);
 // write the lines whose copies have completed (all of them, waiting, if wait)
 int lbdemOutputDrain(lbdem_ctx* c, bool wait);
 void lbdemOutputFree(lbdem_ctx* c);
+// after a restore: the output clock of the restored cycle count (pending
+// lines are written first; no line for the current cycle)
+void lbdemOutputResync(lbdem_ctx* c);
 extern "C" int lbdem_export_recycle_fluid(lbdem_ctx* c, const char* path);
 // many runs per launch (lbdem_capi.cu), for the run server
 void lbdemJobArgs(lbdem_ctx* c, int cur, lbdem::JobArgs* j);

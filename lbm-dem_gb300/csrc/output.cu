@@ -332,6 +332,16 @@ int lbdemOutputDrain(lbdem_ctx* ctx, bool wait) {
   return LBDEM_OK;
 }
 
+void lbdemOutputResync(lbdem_ctx* ctx) {
+  lbdem_output* o = ctx->out;
+  if (!o) return;
+  o->realTime = 0.0;
+  for (long long i = 0; i < ctx->lbTime; ++i) o->realTime += o->unitTime;
+  o->lastScreen = screenCounter(o, o->realTime);
+  o->lastRecycle = recycleCounter(o, o->realTime);
+  o->lastPart = partCounter(o, o->realTime);
+}
+
 void lbdemOutputFree(lbdem_ctx* ctx) {
   lbdem_output* o = ctx->out;
   if (!o) return;

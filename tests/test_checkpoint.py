@@ -131,3 +131,28 @@ def test_snapshot_of_another_run_or_a_truncated_file_is_refused(tmp_path, lib):
         other_cfg.close()
         small.close()
         tiny.close()
+
+
+def test_output_continues_from_the_restored_cycle(tmp_path, lib):
+    """Output open on the target run: after a restore to cycle 5 its lines
+    continue with the reference's output cycles after 5 (screenExpTime 3.5:
+    7 and 11), numbered by the restored cycle count."""
+    import lbdem
+    cfg = _cfg("tiny_direct")
+    a = lbdem.Solver(cfg, precision=lbdem.PLAIN_FP64)
+    b = lbdem.Solver(cfg, precision=lbdem.PLAIN_FP64)
+    try:
+        a.cycle(5)
+        a.checkpoint(tmp_path / "run.lbdemck")
+        out = tmp_path / "out"
+        out.mkdir()
+        b.output_open(out, 3.5)  # writes the line of cycle 0
+        b.restore(tmp_path / "run.lbdemck")
+        b.cycle(7)
+        b.output_close()
+        steps = [int(l.split(";")[0]) for l in (out / "export.dat").read_text().splitlines()]
+        assert steps == [0, 7, 11]
+    finally:
+        a.close()
+        b.close()
+        cfg.close()
