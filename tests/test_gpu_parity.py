@@ -58,7 +58,7 @@ def test_fp64_phase_by_phase(lib, oracle_lib):
 
 
 def test_fp64_config1_100_steps(lib, oracle_lib):
-    """BASELINE config 1 (64x80x64, 376 spheres): 100-step horizon."""
+    """The c1 case (64x80x64 lattice, 376 spheres): 100-step horizon."""
     cfg, gpu, orc = _pair("c1")
     with tempfile.TemporaryDirectory() as tmp:
         for s in range(10, 101, 10):

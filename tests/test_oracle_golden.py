@@ -54,7 +54,7 @@ def test_oracle_bitwise_equal_to_reference(name, lib, oracle_lib, tmp_path):
 
 
 def test_oracle_bitwise_equal_to_reference_config1(lib, oracle_lib, tmp_path):
-    """BASELINE config 1 (64x80x64, 376 spheres), 100 steps, every 10th."""
+    """The c1 case (64x80x64 lattice, 376 spheres), 100 steps, every 10th."""
     _run("c1", lib, oracle_lib, tmp_path)
 
 
