@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -153,49 +154,161 @@ def allsum(world, v: float) -> float:
 
 
 def upload_bytes(cfg) -> int:
+    """Bytes lbdem_create copies from the host: the particle and impactor
+    tables and the small run records (the lattice itself is initialised on the
+    device from the configuration)."""
     c = cfg.cfg
     P, O = c.n_particles, c.n_objects
     return int(P * 8 * (3 + 1 + 1 + 1 + 3) + max(O, 1) * 44 * 8 + 6 * 48 + 6 * 4 + 6 * 4 + 8
                + 32 * 4)
 
 
-def cpu_baseline(cfg, workload, warm=1, steps=2, budget_s=60.0) -> dict:
-    """Oracle (CPU restatement of the reference algorithm) on a bounded sample."""
+def bench_config(args, cfg, world) -> dict:
+    """The ``config`` of both arms' lines, from the case itself (identical for
+    the GPU arm and the reference arm)."""
+    c = cfg.cfg
+    L = float(c.unitLength)
+    lattice = [int(math.floor(v / L + 0.5)) for v in (c.lbSizeX, c.lbSizeY, c.lbSizeZ)]
+    nodes = lattice[0] * lattice[1] * lattice[2]
+    gb = nodes * 19 * 4 / 1e9  # one FP32 population lattice
+    l2 = (f"one population lattice is {gb:.2f} GB, larger than the 129 MB L2: no flush"
+          if gb > 0.129 else
+          f"one population lattice is {gb * 1e3:.0f} MB, within the 129 MB L2: "
+          f"kernel times are L2-assisted")
+    return {"workload": args.workload, "description": WORKLOADS[args.workload],
+            "lattice": lattice, "particles": int(c.n_particles),
+            "parallelism": f"replicas{world}", "l2": l2}
+
+
+PORT_KIND = ("port: the oracle, a dense-array restatement of the reference's step "
+             "(bit-exact against the compiled reference); faster than the reference's own "
+             "node-list code, so the ratio against it understates the speed-up over the "
+             "reference itself")
+
+
+def cpu_baseline(cfg, workload, steps, warm=1, budget_s=75.0, single_s=30.0) -> dict:
+    """The oracle (CPU restatement of the reference algorithm, OpenMP on its
+    per-node loops) on a bounded sample of the workload: up to ``steps``
+    coupled steps on all host threads within ``budget_s``, then a one-thread
+    figure on up to ``single_s`` of further steps."""
     import oracle_ffi
     oracle_ffi.build_oracle()
+    cores = oracle_ffi.max_threads()
     orc = oracle_ffi.Oracle(cfg)
     orc.cycle(warm)
-    done, upd, t0 = 0, 0, time.perf_counter()
-    while done < steps and time.perf_counter() - t0 < budget_s:
-        orc.cycle(1)
-        upd += orc.counters()[3]
-        done += 1
-    dt = time.perf_counter() - t0
+
+    def timed(limit_steps, limit_s):
+        done, upd, t0 = 0, 0, time.perf_counter()
+        while done < limit_steps and (done == 0 or time.perf_counter() - t0 < limit_s):
+            orc.cycle(1)
+            upd += orc.counters()[3]
+            done += 1
+        return done, upd, time.perf_counter() - t0
+
+    done, upd, dt = timed(steps, budget_s)
+    oracle_ffi.set_threads(1)
+    d1, u1, t1 = timed(steps, single_s)
+    oracle_ffi.set_threads(cores)
     orc.close()
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": round(upd / dt / 1e6, 4), "unit": "MLUPS", "cores": cores, "kind": "port",
-            "sample": f"{done} coupled steps of workload {workload} after {warm} warm-up step(s), "
-                      f"CPU restatement (oracle) with OpenMP on reconstruction/collision"}
+    return {"value": round(upd / dt / 1e6, 4), "unit": "MLUPS", "cores": cores,
+            "kind": "port",
+            "sample": f"{done} coupled steps of workload {workload} (of {steps} asked, "
+                      f"{budget_s:.0f} s budget) after {warm} warm-up step(s), {cores} threads; "
+                      + PORT_KIND,
+            "single_thread": {"value": round(u1 / t1 / 1e6, 4), "unit": "MLUPS",
+                              "steps": d1, "cores": 1}}
 
 
 def run_reference(args, world, rank):
     """Reference arm: the CPU restatement of the reference's algorithm (the
-    reference itself cannot be built on the GPU host), timed on the host."""
+    oracle; the reference itself cannot be built on the GPU host), timed on
+    the host's cores. Reads the case with the pure-Python reader, so nothing
+    but the oracle's library is loaded."""
     if rank != 0:
         return
-    import lbdem
-    cfg = lbdem.LoadedConfig(case_path(args.workload))
-    cb = cpu_baseline(cfg, args.workload, warm=min(args.warmup, 1), steps=args.steps,
+    import caseio
+    cfg = caseio.CaseConfig(case_path(args.workload))
+    cb = cpu_baseline(cfg, args.workload, steps=args.steps, warm=min(args.warmup, 1),
                       budget_s=150.0)
     line = {"impl": "reference", "metric": "coupled MLUPS", "value": cb["value"],
             "unit": "MLUPS", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": args.workload,
-                                            "description": WORKLOADS[args.workload]},
+            "data": "synthetic", "config": bench_config(args, cfg, world),
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def kernel_roofline(prof, precision: str) -> dict:
+    """The lattice kernel's own figure from its CUDA-event time per launch."""
+    peak, peak_kind = peaks()
+    bpn = BYTES_PER_NODE[precision]
+    achieved = bpn * prof.active_node_updates / (prof.lb_kernel_ms * 1e-3) / 1e9 \
+        if prof.lb_kernel_ms > 0 else 0.0
+    return {"achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind,
+            "frac": round(achieved / peak, 4), "bytes_per_active_node": bpn,
+            "kernel_ms_per_launch": round(prof.lb_kernel_ms / max(prof.lb_kernel_launches, 1), 4)}
+
+
+def timed_cycles(solver, n: int, torch, stream) -> tuple[float, object]:
+    """n goCycles between CUDA events on the run's stream; (ms, counters)."""
+    solver.sync()
+    solver.profile_read(reset=True)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    solver.cycle(n)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    solver.sync()
+    return ev0.elapsed_time(ev1), solver.profile_read(reset=True)
+
+
+def late_window(args, cfg, local, torch) -> dict:
+    """The mixed form after the impact: a fresh run advanced to cycle
+    ``--late-start``, then ``--late-steps`` cycles timed (neighbour-list
+    rebuilds nearly every step, impactor coupled to the suspension)."""
+    import lbdem
+    sv = lbdem.Solver(cfg, precision=lbdem.MIXED, device=local)
+    st = torch.cuda.Stream(device=local)
+    sv.set_stream(st.cuda_stream)
+    sv.cycle(args.late_start)
+    r0 = sv.get_info().neighbour_rebuilds
+    ms, p = timed_cycles(sv, args.late_steps, torch, st)
+    r1 = sv.get_info().neighbour_rebuilds
+    sv.profile_enable(True)
+    sv.cycle(args.late_steps)
+    sv.sync()
+    prof = sv.profile_read(reset=True)
+    sv.close()
+    return {"cycles": [args.late_start + 1, args.late_start + args.late_steps],
+            "value": round(p.active_node_updates / (ms * 1e-3) / 1e6, 2), "unit": "MLUPS",
+            "ms_per_step": round(ms / args.late_steps, 4),
+            "neighbour_rebuilds": int(r1 - r0),
+            "lattice_kernel": kernel_roofline(prof, "mixed")}
+
+
+def fp64_form(args, cfg, local, torch) -> dict:
+    """The plain FP64 form (the parity form) on the same workload."""
+    import lbdem
+    sv = lbdem.Solver(cfg, precision=lbdem.PLAIN_FP64, device=local)
+    st = torch.cuda.Stream(device=local)
+    sv.set_stream(st.cuda_stream)
+    sv.cycle(max(args.warmup, 3))
+    ms, p = timed_cycles(sv, args.fp64_steps, torch, st)
+    sv.profile_enable(True)
+    sv.cycle(min(args.fp64_steps, 10))
+    sv.sync()
+    prof = sv.profile_read(reset=True)
+    sv.close()
+    k = kernel_roofline(prof, "fp64")
+    k["bound"] = ("FP64 pipe: about 600 FP64 operations per node with the reference's "
+                  "divides; the HBM fraction above is not its limit")
+    return {"steps": args.fp64_steps, "value": round(p.active_node_updates / (ms * 1e-3) / 1e6, 2),
+            "unit": "MLUPS", "ms_per_step": round(ms / args.fp64_steps, 4),
+            "lattice_kernel": k}
 
 
 def run_ours(args, world, rank, local):
@@ -238,10 +351,9 @@ def run_ours(args, world, rank, local):
     solver.sync()
     prof = solver.profile_read(reset=True)
     solver.profile_enable(False)
-    info = solver.get_info()
     solver.close()
 
-    # ---- end to end through the C ABI: upload, K cycles, per-step read-back ----
+    # ---- end to end through the C ABI: case upload, K cycles, per-step read-back ----
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     s2 = lbdem.Solver(cfg, precision=prec, device=local)
@@ -251,13 +363,11 @@ def run_ours(args, world, rank, local):
         s2.objects()  # impactor state back to the host every step
     p2 = s2.profile_read(reset=True)
     t_e2e = time.perf_counter() - t0
+    n_obj = int(s2.get_info().n_objects)
     s2.close()
     e2e_val = allsum(world, float(p2.active_node_updates)) / allmax(world, t_e2e) / 1e6
 
-    peak, peak_kind = peaks()
-    bpn = BYTES_PER_NODE[args.precision]
-    achieved = bpn * prof.active_node_updates / (prof.lb_kernel_ms * 1e-3) / 1e9 \
-        if prof.lb_kernel_ms > 0 else 0.0
+    kr = kernel_roofline(prof, args.precision)
     traffic = None
     tr = os.path.join(REPO, "profiles", f"traffic_{args.precision}.json")
     if os.path.exists(tr):
@@ -269,33 +379,39 @@ def run_ours(args, world, rank, local):
                 prof.lb_kernel_launches
     if rank != 0:
         return
-    cb = None
-    if world == 1 and not args.no_cpu_baseline:
-        cb = cpu_baseline(cfg, args.workload)
+    up = upload_bytes(cfg)
+    extra = world == 1
     line = {
         "metric": "coupled MLUPS", "value": round(value, 2), "unit": "MLUPS",
         "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": round(ms_max / K, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "description": WORKLOADS[args.workload],
-                   "precision": args.precision, "lattice": list(info.lb_size),
-                   "particles": int(info.n_particles), "parallelism": f"replicas{world}",
-                   "l2": "state (lattice > 1 GB) exceeds the 129 MB L2; no flush"},
+        "precision": args.precision,
+        "config": bench_config(args, cfg, world),
         "e2e": {"value": round(e2e_val, 2), "unit": "MLUPS",
-                "h2d_bytes_per_step": upload_bytes(cfg) // max(K, 1),
-                "d2h_bytes_per_step": int(info.n_objects) * 10 * 3 * 8},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "traffic": traffic, "peak_kind": peak_kind,
+                "h2d_bytes_per_step": up // max(K, 1),
+                "d2h_bytes_per_step": n_obj * 10 * 3 * 8,
+                "note": f"timed region: lbdem_create from the host tables ({up} B copied once, "
+                        f"shown amortised over the {K} steps; the lattice is initialised on "
+                        f"the device from the configuration), then every step lbdem_cycle(1) "
+                        f"and a read-back of the impactor record to host memory"},
+        "roofline": {"bound": "hbm", "achieved": kr["achieved"], "peak": kr["peak"],
+                     "unit": "GB/s", "frac": kr["frac"], "traffic": traffic,
+                     "peak_kind": kr["peak_kind"],
                      "kernel": "lbStep (fused reconstruct/collide/stream)",
-                     "bytes_per_active_node": bpn,
-                     "kernel_ms_per_launch": round(prof.lb_kernel_ms / max(prof.lb_kernel_launches, 1), 4)},
-        "cpu_baseline": cb,
-        "serving": None if (args.no_serving or world > 1) else serving(args),
-        "accuracy": None if (args.no_accuracy or world > 1) else accuracy(args, cfg),
+                     "bytes_per_active_node": kr["bytes_per_active_node"],
+                     "kernel_ms_per_launch": kr["kernel_ms_per_launch"]},
         "clocks": clk,
         "gpu_launches": int(timed.kernel_launches),
     }
+    if extra and not args.no_late and args.precision == "mixed":
+        line["late"] = late_window(args, cfg, local, torch)
+    if extra and not args.no_fp64:
+        line["fp64"] = fp64_form(args, cfg, local, torch)
+    line["cpu_baseline"] = None if (not extra or args.no_cpu_baseline) else \
+        cpu_baseline(cfg, args.workload, steps=K, budget_s=60.0, single_s=25.0)
+    line["serving"] = None if (args.no_serving or not extra) else serving(args)
+    line["accuracy"] = None if (args.no_accuracy or not extra) else accuracy(args, cfg)
     print(json.dumps(line), flush=True)
 
 
@@ -465,6 +581,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-late", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--late-start", type=int, default=600)
+    ap.add_argument("--late-steps", type=int, default=100)
+    ap.add_argument("--fp64-steps", type=int, default=30)
     ap.add_argument("--accuracy-steps", type=int, default=300)
     ap.add_argument("--serve-jobs", type=int, default=24)
     ap.add_argument("--serve-fp64-jobs", type=int, default=8)

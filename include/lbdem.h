@@ -19,6 +19,8 @@
  *  - Plain pointers and sizes only; caller-owned host buffers; the context
  *    owns all device memory. One context is one impact run on one GPU.
  *  - Calls on one context are not thread-safe; distinct contexts are.
+ *  - Every call on a context makes the context's device current for its
+ *    own duration and restores the calling thread's device on return.
  *  - Download calls synchronise the context's stream; step calls only
  *    enqueue work (no host synchronisation inside a step).
  */
@@ -451,7 +453,11 @@ int lbdem_server_tune(lbdem_server_options* opt, const lbdem_config* const* cfgs
  * The buffer is shared by every context on a device: calls that overlap in
  * time on one device race on it; serialise them. The first call on each
  * device looks up the buffer's address (cudaGetSymbolAddress); make that
- * first call before any stream capture. Synchronises the context's stream. */
+ * first call before any stream capture. Synchronises the context's stream
+ * and makes the context's device current for the call. Unlike
+ * lbdem_download_lattice it does not return the run's device error: after a
+ * step reported a fault (LBDEM_ERR_NONFINITE, LBDEM_ERR_OVERFLOW, ...) the
+ * nodes can still be read, to inspect the state at the fault. */
 int lbdem_download_nodes_noalloc(lbdem_ctx* ctx, int64_t first, int64_t count,
                                  double* f, double* mass);
 

@@ -289,6 +289,41 @@ def serving_case(rng: np.random.Generator, name: str = "job") -> Case:
     return Case(params=p, particles=parts, objects=objs, name=name)
 
 
+def to_physical(case: Case, length: float, time: float, density: float) -> Case:
+    """The same run in physical units: unitLength/unitTime/unitDensity set to
+    ``length``/``time``/``density`` and every dimensional input scaled so that
+    the lattice run is unchanged (LB::latticeBoltzmannGet divides by the
+    composite units, src/node.cpp:512-525, src/LB.cpp:153-326; the DEM works in
+    physical units). The lubrication viscosity kinVisc is scaled with the
+    density as well, so that its coefficient pi nu a dt (src/DEM.cpp:2354)
+    keeps its ratio to the particle masses."""
+    L, T, D = float(length), float(time), float(density)
+    p = dict(case.params)
+    scale = {
+        "lbSizeX": L, "lbSizeY": L, "lbSizeZ": L, "fluidHeight": L,
+        "initVisc": D * L * L / T,
+        "lbFX": L / T / T, "lbFY": L / T / T, "lbFZ": L / T / T,
+        "initVelocityX": L / T, "initVelocityY": L / T, "initVelocityZ": L / T,
+        "density": D, "objectDensity": D, "bodyDensity": D,
+        "linearStiff": D * L ** 3 / T / T,
+        "kinVisc": D * L * L / T,
+        "electroForce": D * L ** 4 / T / T,
+        "debyeLength": L, "lubCutoff": L, "lubNormal": L, "lubTangential": L,
+        "lubRotation": L,
+    }
+    for k, f in scale.items():
+        p[k] = repr(float(p[k]) * f)
+    p["unitLength"], p["unitTime"], p["unitDensity"] = repr(L), repr(T), repr(D)
+    parts = case.particles.copy()
+    parts[:, 0:4] *= L          # r, x, y, z
+    parts[:, 4:7] *= L / T      # v
+    parts[:, 7:10] /= T         # w
+    objs = case.objects.copy()
+    objs[:, 0:4] *= L
+    objs[:, 4:7] *= L / T
+    return Case(params=p, particles=parts, objects=objs, name=case.name)
+
+
 def volume_fraction(case: Case) -> float:
     nx, ny, nz = case.lattice
     fill = float(case.params["fluidHeight"])
@@ -321,4 +356,13 @@ def named_case(name: str, seed: int = 1) -> Case:
         return impact_case((18, 28, 18), 16.0, 5, (3.0, 3.4), 4.0, 20.5,
                            -0.05, 5.0, 0.8, 1.0e-4, seed,
                            overrides={"objWaitTime": "2"}, name=name)
+    if name == "units_dyn":
+        # a cell-list case in physical units (unitLength 0.5, unitTime 0.02,
+        # unitDensity 1000), with boundary0 = 8: every wall is a moving
+        # no-slip wall (type 8), as DEM::initializeWalls takes the moving flag
+        # of boundary0 for all walls (src/DEM.cpp:430-447)
+        lat = impact_case((30, 40, 30), 27.0, 18, (3.0, 3.4), 5.0, 32.0,
+                          -0.08, 5.0, 0.8, 1.0e-4, seed,
+                          overrides={"objWaitTime": "3", "boundary0": "8"}, name=name)
+        return to_physical(lat, 0.5, 0.02, 1000.0)
     raise KeyError(name)

@@ -86,6 +86,7 @@ struct Pinned {
 
 extern "C" int lbdem_checkpoint(lbdem_ctx* ctx, const char* path) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   if (!path) return fail(ctx, LBDEM_ERR_INVALID, "checkpoint: null path");
   // everything enqueued so far is part of the state
   CKC(cudaStreamSynchronize(ctx->stream));
@@ -140,6 +141,7 @@ extern "C" int lbdem_checkpoint(lbdem_ctx* ctx, const char* path) {
 
 extern "C" int lbdem_restore(lbdem_ctx* ctx, const char* path) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   if (!path) return fail(ctx, LBDEM_ERR_INVALID, "restore: null path");
   File in;
   in.f = fopen(path, "rb");

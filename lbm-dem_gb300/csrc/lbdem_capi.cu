@@ -257,7 +257,11 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return setErr(ctx, LBDEM_ERR_NO_DEVICE, "no CUDA device");
-  CK(cudaSetDevice(ctx->device));
+  if (ctx->device < 0 || ctx->device >= ndev)
+    return setErr(ctx, LBDEM_ERR_INVALID, "device ordinal " + std::to_string(ctx->device) +
+                                              " out of range (" + std::to_string(ndev) + " devices)");
+  // the caller's current device is put back on return
+  DeviceScope devScope(ctx->device);
   CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
   ctx->stream = ctx->own_stream;
   CK(cudaDeviceGetAttribute(&ctx->smCount, cudaDevAttrMultiProcessorCount, ctx->device));
@@ -602,6 +606,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
 
 extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
   if (!ctx) return;
+  DeviceScope devScope(ctx->device);
   if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (auto& g : ctx->pairGraph)
@@ -652,6 +657,7 @@ static int enqueueStress(lbdem_ctx* ctx, const DemArgs& a) {
 // DEM::discreteElementStep (multiStep = 1)
 extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   ++ctx->demTimeStep;
   ctx->demTime += ctx->k.dt;
   const Consts& k = ctx->k;
@@ -678,6 +684,7 @@ extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
 // LB::latticeBoltzmannCouplingStep
 extern "C" int lbdem_coupling_step(lbdem_ctx* ctx) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   const Consts& k = ctx->k;
   Device& d = ctx->d;
   cudaStream_t s = ctx->stream;
@@ -699,6 +706,7 @@ extern "C" int lbdem_coupling_step(lbdem_ctx* ctx) {
 // LB::latticeBolzmannStep
 extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   if (!ctx->k.forceField && !ctx->lbFReset) {  // LB::collision, src/LB.cpp:1303-1305
     ctx->lbFReset = true;
     ctx->k.lbF[0] = ctx->k.lbF[1] = ctx->k.lbF[2] = 0.0;
@@ -735,6 +743,7 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
 // LB::latticeBoltzmannFreeSurfaceStep
 extern "C" int lbdem_free_surface_step(lbdem_ctx* ctx) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   const Consts& k = ctx->k;
   Device& d = ctx->d;
   cudaStream_t s = ctx->stream;
@@ -758,6 +767,7 @@ extern "C" int lbdem_profile_enable(lbdem_ctx* ctx, int enable) {
 
 extern "C" int lbdem_profile_read(lbdem_ctx* ctx, lbdem_profile* out, int reset) {
   if (!ctx || !out) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   std::memset(out, 0, sizeof(*out));
   CK(cudaStreamSynchronize(ctx->stream));
   double ms = 0.0;
@@ -1038,6 +1048,7 @@ void lbdemAdvanceCounters(lbdem_ctx* c, int cycles) {
 
 extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   int32_t i = 0;
   while (i < n) {
     int rc = LBDEM_OK;
@@ -1077,6 +1088,7 @@ extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
 
 extern "C" int lbdem_sync(lbdem_ctx* ctx) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   CK(cudaStreamSynchronize(ctx->stream));
   if (int rc = lbdemOutputDrain(ctx, true)) return rc;
   int e = 0;
@@ -1195,6 +1207,17 @@ extern "C" int lbdem_get_info(lbdem_ctx* ctx, lbdem_info* info) {
 }
 
 namespace {
+// a download temporary, freed on every return path
+struct DeviceTemp {
+  double* p = nullptr;
+  DeviceTemp() = default;
+  DeviceTemp(const DeviceTemp&) = delete;
+  DeviceTemp& operator=(const DeviceTemp&) = delete;
+  ~DeviceTemp() {
+    if (p) cudaFree(p);
+  }
+};
+
 int d2h(lbdem_ctx* ctx, void* dst, const void* src, size_t bytes) {
   if (!dst) return LBDEM_OK;
   CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
@@ -1215,6 +1238,7 @@ extern "C" int lbdem_download_lattice(lbdem_ctx* ctx, uint8_t* type, uint8_t* pf
                                       int32_t* solid, double* n, double* u, double* mass,
                                       double* f) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   int rc = lbdem_sync(ctx);
   if (rc) return rc;
   const size_t N = (size_t)ctx->k.N;
@@ -1229,31 +1253,32 @@ extern "C" int lbdem_download_lattice(lbdem_ctx* ctx, uint8_t* type, uint8_t* pf
   }
   if ((rc = d2h(ctx, solid, d.solid, N * 4))) return rc;
   if (mass || f) {
-    double* tmp = nullptr;
-    CK(cudaMalloc(&tmp, (size_t)(Q + 1) * N * sizeof(double)));
+    DeviceTemp t;
+    CK(cudaMalloc(&t.p, (size_t)(Q + 1) * N * sizeof(double)));
+    double* tmp = t.p;
     exportLattice<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(ctx->k, d.mask, d.f[ctx->cur], d.mass,
                                                              d.nF, tmp, tmp + (size_t)Q * N);
     CK(cudaStreamSynchronize(ctx->stream));
     if (f) CK(cudaMemcpy(f, tmp, (size_t)Q * N * 8, cudaMemcpyDeviceToHost));
     if (mass) CK(cudaMemcpy(mass, tmp + (size_t)Q * N, N * 8, cudaMemcpyDeviceToHost));
-    cudaFree(tmp);
   }
   if (n || u) {
-    double* tmp = nullptr;
-    CK(cudaMalloc(&tmp, 4 * N * sizeof(double)));
+    DeviceTemp t;
+    CK(cudaMalloc(&t.p, 4 * N * sizeof(double)));
+    double* tmp = t.p;
     momentsKernel<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(ctx->k, d.mask,
                                                              d.f[ctx->cur], tmp,
                                                              tmp + N);
     CK(cudaStreamSynchronize(ctx->stream));
     if (n) CK(cudaMemcpy(n, tmp, N * 8, cudaMemcpyDeviceToHost));
     if (u) CK(cudaMemcpy(u, tmp + N, 3 * N * 8, cudaMemcpyDeviceToHost));
-    cudaFree(tmp);
   }
   return LBDEM_OK;
 }
 
 extern "C" int lbdem_download_particles(lbdem_ctx* ctx, const lbdem_particle_view* v) {
   if (!ctx || !v) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   int rc = lbdem_sync(ctx);
   if (rc) return rc;
   Device& d = ctx->d;
@@ -1283,6 +1308,7 @@ extern "C" int lbdem_download_particles(lbdem_ctx* ctx, const lbdem_particle_vie
 
 extern "C" int lbdem_download_objects(lbdem_ctx* ctx, const lbdem_object_view* v) {
   if (!ctx || !v) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   int rc = lbdem_sync(ctx);
   if (rc) return rc;
   const int O = ctx->nObj;
@@ -1303,6 +1329,7 @@ extern "C" int lbdem_download_objects(lbdem_ctx* ctx, const lbdem_object_view* v
 extern "C" int lbdem_download_walls(lbdem_ctx* ctx, double* FHydro, double* FContact,
                                     double* FLub, double* FTotal) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   int rc = lbdem_sync(ctx);
   if (rc) return rc;
   const int W = ctx->nWall;
@@ -1320,6 +1347,7 @@ namespace {
 int massSums(lbdem_ctx* ctx, int withParticles, double* total_mass, int64_t* interface_nodes,
              int64_t* active_nodes) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   int rc = lbdem_sync(ctx);
   if (rc) return rc;
   // stream-ordered temporary: no device-wide synchronisation

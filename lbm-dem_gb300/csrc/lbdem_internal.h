@@ -227,6 +227,26 @@ int lbdemEnqueueBatchCycle(const std::vector<lbdem_ctx*>& runs, const lbdem::Job
                            cudaStream_t s);
 void lbdemAdvanceCounters(lbdem_ctx* c, int cycles);
 
+// Makes a device current for the length of one entry point and puts the
+// calling thread's previous device back on exit, so that contexts on
+// different devices can be driven from one host thread.
+struct DeviceScope {
+  int prev = -1;
+  int dev;
+  explicit DeviceScope(int d) : dev(d) {
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+      prev = -1;
+      return;
+    }
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceScope() {
+    if (prev >= 0 && prev != dev) cudaSetDevice(prev);
+  }
+  DeviceScope(const DeviceScope&) = delete;
+  DeviceScope& operator=(const DeviceScope&) = delete;
+};
+
 struct lbdem_ctx {
   std::string err;
   lbdem::Consts k{};

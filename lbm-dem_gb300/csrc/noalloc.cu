@@ -15,7 +15,12 @@
 // contexts) race on it and must be serialised by the caller. Its device
 // address is looked up (cudaGetSymbolAddress) by the first call on each
 // device, which also loads this module's device code if that has not
-// happened yet; make that first call before any stream capture.
+// happened yet; make that first call before any stream capture. Each call
+// makes the context's device current for its own duration.
+//
+// The call waits for the context's stream but does not read the run's
+// device error bits, so it returns the nodes also after a step reported a
+// fault (where lbdem_sync and lbdem_download_lattice return that fault).
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -83,6 +88,7 @@ __global__ void exportNodeRange(Consts k, const uint8_t* mask, const void* f, co
 extern "C" int lbdem_download_nodes_noalloc(lbdem_ctx* ctx, int64_t first, int64_t count,
                                             double* f, double* mass) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   if (count > kMaxNodes)
     return fail(ctx, LBDEM_ERR_INVALID,
                 "lbdem_download_nodes_noalloc: count " + std::to_string(count) +
@@ -96,15 +102,20 @@ extern "C" int lbdem_download_nodes_noalloc(lbdem_ctx* ctx, int64_t first, int64
   double* stage = nullptr;
   int rc = stageAddress(ctx, &stage);
   if (rc) return rc;
-  rc = lbdem_sync(ctx);
-  if (rc) return rc;
+  // Waits for the work enqueued so far without reading the run's device
+  // error bits: the nodes can still be read after a step reported a fault
+  // (non-finite values, list overflow), which is when a monitor wants them.
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess)
+    return fail(ctx, LBDEM_ERR_CUDA,
+                std::string("lbdem_download_nodes_noalloc: ") + cudaGetErrorString(e));
   if (count == 0 || (!f && !mass)) return LBDEM_OK;
   const int n = (int)count;
   const int block = 256;
   const int grid = (n + block - 1) / block;
   exportNodeRange<<<grid, block, 0, ctx->stream>>>(ctx->k, ctx->d.mask, ctx->d.f[ctx->cur],
                                                    ctx->d.mass, ctx->d.nF, first, n, stage);
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   if (e == cudaSuccess && f)
     e = cudaMemcpyAsync(f, stage, (size_t)Q * n * sizeof(double), cudaMemcpyDeviceToHost,
                         ctx->stream);

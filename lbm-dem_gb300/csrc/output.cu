@@ -357,6 +357,7 @@ void lbdemOutputFree(lbdem_ctx* ctx) {
 
 extern "C" int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_exp_time) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   if (!dir || !(screen_exp_time >= 0.0))
     return fail(ctx, LBDEM_ERR_INVALID, "output_open: null directory or negative screenExpTime");
   if (ctx->out) return fail(ctx, LBDEM_ERR_INVALID, "output_open: output already open");
@@ -430,6 +431,7 @@ extern "C" int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_
 extern "C" int lbdem_output_recycle(lbdem_ctx* ctx, double fluid_recycle_exp_time,
                                     double part_recycle_exp_time) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   lbdem_output* o = ctx->out;
   if (!o) return fail(ctx, LBDEM_ERR_INVALID, "output_recycle: output not open");
   if (!(fluid_recycle_exp_time >= 0.0) || !(part_recycle_exp_time >= 0.0))
@@ -448,6 +450,7 @@ extern "C" int lbdem_output_recycle(lbdem_ctx* ctx, double fluid_recycle_exp_tim
 
 extern "C" int lbdem_output_close(lbdem_ctx* ctx) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   if (!ctx->out) return LBDEM_OK;
   const int rc = lbdemOutputDrain(ctx, true);
   lbdemOutputFree(ctx);

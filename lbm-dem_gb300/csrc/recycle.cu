@@ -162,6 +162,7 @@ int lbdemRestartFluid(lbdem_ctx* ctx, const char* path) {
 
 extern "C" int lbdem_export_recycle_fluid(lbdem_ctx* ctx, const char* path) {
   if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
   if (!path) return fail(ctx, LBDEM_ERR_INVALID, "export_recycle_fluid: null path");
   const Consts& k = ctx->k;
   const size_t N = (size_t)k.N;

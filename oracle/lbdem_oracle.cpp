@@ -32,6 +32,8 @@
 #include <string>
 #include <vector>
 
+#include <omp.h>
+
 #include "statedump.h"
 
 namespace {
@@ -2002,6 +2004,12 @@ int oracle_counters(oracle_ctx* c, int64_t* o) {
   return LBDEM_OK;
 }
 double oracle_dem_time(oracle_ctx* c) { return c->demTime; }
+int oracle_set_threads(int32_t n) {
+  if (n < 1) return LBDEM_ERR_INVALID;
+  omp_set_num_threads(n);
+  return LBDEM_OK;
+}
+int oracle_max_threads(void) { return omp_get_max_threads(); }
 int oracle_object0(oracle_ctx* c, double* o) {
   if (c->objects.empty()) return LBDEM_ERR_INVALID;
   const Object& ob = c->objects[0];

@@ -36,6 +36,10 @@ int oracle_dump(oracle_ctx* ctx, const char* path);
  * [3] active nodes, [4] interface nodes */
 int oracle_counters(oracle_ctx* ctx, int64_t* out5);
 double oracle_dem_time(oracle_ctx* ctx);
+/* OpenMP threads of the per-node loops (reconstruction, collision); the
+ * results do not depend on it (every node is updated on its own) */
+int oracle_set_threads(int32_t n);
+int oracle_max_threads(void);
 /* impactor 0 position/velocity, 6 doubles */
 int oracle_object0(oracle_ctx* ctx, double* out6);
 

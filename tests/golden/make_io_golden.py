@@ -2,7 +2,7 @@
 build.
 
 Run here (where the reference tree exists):
-    make -C oracle ref && python tests/golden/make_io_golden.py
+    make -C oracle ref REF=<reference>/src && python tests/golden/make_io_golden.py
 
 For every case below it runs the reference's own IO code (oracle/_ref/lbdem_ref
 with -io, which calls IO::initialize and IO::outputStep of src/IO.cpp) on the

@@ -1,7 +1,7 @@
 """Generate the golden fluid recycle files from the pinned reference build.
 
 Run here (where the reference tree exists):
-    make -C oracle ref && python tests/golden/make_recycle_golden.py
+    make -C oracle ref REF=<reference>/src && python tests/golden/make_recycle_golden.py
 
 For the tiny_direct case (tests/golden/tiny_direct/) it
 1. runs the reference with its own IO code (oracle/_ref/lbdem_ref -io) for
@@ -40,7 +40,7 @@ SMALL_KEYS = ("p_", "o_", "w_", "step", "demTime", "demTimeStep")
 
 def main() -> None:
     if not os.path.exists(REF):
-        sys.exit("oracle/_ref/lbdem_ref missing: run `make -C oracle ref` first")
+        sys.exit("oracle/_ref/lbdem_ref missing: run `make -C oracle ref REF=<reference>/src` first")
     out = os.path.join(HERE, "recycle")
     os.makedirs(out, exist_ok=True)
     with tempfile.TemporaryDirectory() as tmp:

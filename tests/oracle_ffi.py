@@ -40,13 +40,25 @@ def load() -> C.CDLL:
         lib.oracle_dem_time.argtypes = [v]
         lib.oracle_dem_time.restype = C.c_double
         lib.oracle_object0.argtypes = [v, C.POINTER(C.c_double)]
+        lib.oracle_set_threads.argtypes = [C.c_int32]
+        lib.oracle_max_threads.argtypes = []
         _lib = lib
     return _lib
 
 
+def set_threads(n: int) -> None:
+    """OpenMP threads of the oracle's per-node loops (results do not change)."""
+    load().oracle_set_threads(int(n))
+
+
+def max_threads() -> int:
+    return int(load().oracle_max_threads())
+
+
 class Oracle:
     def __init__(self, config):
-        """config: lbdem.LoadedConfig (the product's parsed case)."""
+        """config: a parsed case with a ``cfg`` lbdem_config structure
+        (caseio.CaseConfig, or lbdem.LoadedConfig)."""
         self.lib = load()
         self.ctx = C.c_void_p()
         rc = self.lib.oracle_create(C.byref(config.cfg), C.byref(self.ctx))

@@ -42,7 +42,8 @@ def _run(name, steps, every):
     return y0, np.array(traj_m), np.array(traj_o), np.array(mass_m), np.array(mass_o)
 
 
-@pytest.mark.parametrize("name,steps,every", [("small_cells", 60, 5), ("c1", 100, 10)])
+@pytest.mark.parametrize("name,steps,every", [("small_cells", 60, 5), ("c1", 100, 10),
+                                              ("units_dyn", 60, 5), ("example", 20, 5)])
 def test_mixed_impactor_trajectory_within_1e3(name, steps, every, lib, oracle_lib):
     y0, tm, to, mm, mo = _run(name, steps, every)
     disp_o = to[:, 1] - y0

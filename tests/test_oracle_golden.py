@@ -48,7 +48,7 @@ def _run(name, lib, oracle_lib, tmp_path):
     cfg.close()
 
 
-@pytest.mark.parametrize("name", ["tiny_direct", "small_cells", "small_dup"])
+@pytest.mark.parametrize("name", ["tiny_direct", "small_cells", "small_dup", "units_dyn"])
 def test_oracle_bitwise_equal_to_reference(name, lib, oracle_lib, tmp_path):
     _run(name, lib, oracle_lib, tmp_path)
 
@@ -56,6 +56,12 @@ def test_oracle_bitwise_equal_to_reference(name, lib, oracle_lib, tmp_path):
 def test_oracle_bitwise_equal_to_reference_config1(lib, oracle_lib, tmp_path):
     """The c1 case (64x80x64 lattice, 376 spheres), 100 steps, every 10th."""
     _run("c1", lib, oracle_lib, tmp_path)
+
+
+def test_oracle_bitwise_equal_to_reference_example(lib, oracle_lib, tmp_path):
+    """The reference's own example input in physical units (unitLength 0.2,
+    unitTime 1e-3, 123x200x123 lattice, 962 spheres), 20 steps."""
+    _run("example", lib, oracle_lib, tmp_path)
 
 
 def test_golden_cases_exercise_every_branch():
