@@ -37,11 +37,16 @@ sys.path.insert(0, os.path.join(REPO, "tests"))
 CACHE = os.path.join(REPO, "bench_cache")
 WORKLOADS = {
     "c2": "256x320x256 lattice (y vertical) filled to y=240, 25000 bidisperse spheres "
-          "(r 3.0/4.2, seeded RSA), impactor r=20 density 5 vy=-0.02, tau=0.6",
+          "(r 3.0/4.2) randomly inserted and compressed into a bed of volume fraction 0.50 "
+          "(164 high), impactor r=20 density 5 vy=-0.02, tau=0.6",
     "c1": "64x80x64 lattice filled to y=60, 400 bidisperse spheres (r 3.0/4.2, seeded RSA), "
           "impactor r=8 density 5 vy=-0.01, tau=0.8",
-    "c2s": "160x200x160 lattice filled to y=150, 6100 bidisperse spheres (r 3.0/4.2, seeded "
-           "RSA), impactor r=14 density 5 vy=-0.02, tau=0.6 (profiling size of c2)",
+    "c2s": "160x200x160 lattice filled to y=150, 6100 bidisperse spheres (r 3.0/4.2) in a "
+           "compressed bed of volume fraction 0.50, impactor r=14 density 5 vy=-0.02, tau=0.6 "
+           "(profiling size of c2)",
+    "c5": "512x384x512 lattice filled to y=300, 200000 bidisperse spheres (r 3.0/4.2) "
+          "randomly inserted and compressed into a bed of volume fraction 0.55 (296 high), "
+          "impactor r=32 density 8 vy=-0.03, tau=0.6",
 }
 # Algorithmic bytes per active-node update of the lattice kernel: 19
 # populations read + 19 written, 8 B (plain FP64) or 4 B (FP32 storage).
@@ -464,38 +469,48 @@ def accuracy(args, cfg) -> dict:
 def serving(args) -> dict:
     """Many impact runs on the GPU at once through the run server.
 
-    A seeded stream of varied runs (lattice sides 48-128, vertical up to 160,
-    grid-packed suspensions, impactor radius 6-16 falling at 0.005-0.05),
-    each ``--serve-cycles`` goCycles:
-    - batch: all runs submitted at once (jobs/h, makespan);
+    Seeded streams of varied runs (lattice sides 48-128, vertical up to 160,
+    fluid to 60 %, a compressed bed of volume fraction 0.40-0.55 over 80 % of
+    the fluid depth, impactor radius 6-16 falling at 0.005-0.05):
+    - batch: ``--serve-jobs`` runs of ``--serve-cycles`` goCycles submitted at
+      once (jobs/h, makespan, p50/p99);
     - the same first runs in the plain FP64 form and in the mixed form
       (jobs/h of each);
-    - a Poisson arrival stream at 80 % of the batch throughput (p50/p99
-      completion latency from submission).
+    - Poisson arrivals at each rate of ``--serve-rates`` (jobs per minute):
+      ``--sweep-jobs`` runs of ``--sweep-cycles`` goCycles, the same arrival
+      times and runs for the mixed and the plain FP64 form; p50/p99
+      completion latency from arrival, jobs/h over the stream;
+    - batched: ``--serve-batch-jobs`` runs resident at once under the
+      schedule the autotuner picks.
     """
     import random
     import casegen
     import lbdem
     import numpy as np
-    rng = np.random.default_rng(args.serve_seed)
-    cfgs = []
-    for i in range(args.serve_jobs):
-        d = os.path.join(CACHE, f"serve{args.serve_seed}", f"j{i:03d}")
-        case = casegen.serving_case(rng, f"j{i}")
-        if not os.path.exists(os.path.join(d, "parameters.cfg")):
-            case.write(d)
-        cfgs.append(lbdem.LoadedConfig(os.path.join(d, "parameters.cfg")))
+
+    def job_set(seed, n, tag):
+        rng = np.random.default_rng(seed)
+        out = []
+        for i in range(n):
+            d = os.path.join(CACHE, f"serve{seed}bed", f"j{i:03d}")
+            case = casegen.serving_case(rng, f"{tag}{i}")
+            if not os.path.exists(os.path.join(d, "parameters.cfg")):
+                case.write(d)
+            out.append(lbdem.LoadedConfig(os.path.join(d, "parameters.cfg")))
+        return out
+
+    cfgs = job_set(args.serve_seed, args.serve_jobs, "j")
     C = args.serve_cycles
 
     def pct(v, q):
         return float(np.percentile(np.asarray(v), q)) if len(v) else None
 
-    def batch(prec, jobs, **opts):
+    def batch(prec, jobs, cycles=C, **opts):
         srv = lbdem.Server(precision=prec, max_active=len(jobs), slice_cycles=args.serve_slice,
                            **opts)
         t0 = time.perf_counter()
         for c in jobs:
-            srv.submit(c, C)
+            srv.submit(c, cycles)
         res = srv.drain()
         wall = time.perf_counter() - t0
         srv.close()
@@ -511,44 +526,52 @@ def serving(args) -> dict:
                 "admission_span_s": round(max(starts) - min(starts), 4),
                 "run_p50_s": round(pct([r["end_time"] - r["start_time"] for r in res], 50), 4)}
 
+    def poisson(prec, jobs, arrivals, cycles):
+        srv = lbdem.Server(precision=prec, max_active=len(jobs), slice_cycles=args.serve_slice)
+        res, k, t0 = [], 0, time.perf_counter()
+        while len(res) < len(jobs):
+            now = time.perf_counter() - t0
+            while k < len(jobs) and arrivals[k] <= now:
+                srv.submit(jobs[k], cycles)
+                k += 1
+            wait = min(0.01, arrivals[k] - now) if k < len(jobs) else 0.05
+            res += srv.poll(max(wait, 0.0))
+        wall = time.perf_counter() - t0
+        srv.close()
+        bad = [r for r in res if r["status"] != 0]
+        if bad:
+            raise RuntimeError(f"serving run failed: status {bad[0]['status']}")
+        lat = [r["end_time"] - r["submit_time"] for r in res]
+        span = max(r["end_time"] for r in res) - min(r["submit_time"] for r in res)
+        return {"p50_s": round(pct(lat, 50), 3), "p99_s": round(pct(lat, 99), 3),
+                "jobs_per_hour": round(len(res) / span * 3600.0, 1),
+                "wall_s": round(wall, 2)}
+
     batch(lbdem.MIXED, cfgs[:2])  # warm-up (module load, allocator pools)
     mixed = batch(lbdem.MIXED, cfgs)
     sub = cfgs[:args.serve_fp64_jobs]
     mixed_sub = batch(lbdem.MIXED, sub)
     fp64_sub = batch(lbdem.PLAIN_FP64, sub)
-    # Poisson arrivals at 80 % of the mixed batch throughput
-    rate = 0.8 * mixed["jobs_per_hour"] / 3600.0
-    r2 = random.Random(args.serve_seed)
-    arrivals, t = [], 0.0
-    for _ in cfgs:
-        t += r2.expovariate(rate)
-        arrivals.append(t)
-    srv = lbdem.Server(precision=lbdem.MIXED, max_active=len(cfgs),
-                       slice_cycles=args.serve_slice)
-    res, k, t0 = [], 0, time.perf_counter()
-    while len(res) < len(cfgs):
-        now = time.perf_counter() - t0
-        while k < len(cfgs) and arrivals[k] <= now:
-            srv.submit(cfgs[k], C)
-            k += 1
-        wait = min(0.01, arrivals[k] - now) if k < len(cfgs) else 0.05
-        res += srv.poll(max(wait, 0.0))
-    wall = time.perf_counter() - t0
-    srv.close()
+    # Poisson sweep: the same runs and arrival times for both forms
+    rates = [float(v) for v in args.serve_rates.split(",") if v]
+    sweep = []
+    for rate in rates:
+        r2 = random.Random(int(args.serve_seed * 1000 + rate * 10))
+        arrivals, t = [], 0.0
+        for _ in range(args.sweep_jobs):
+            t += r2.expovariate(rate / 60.0)
+            arrivals.append(t)
+        jobs = [cfgs[(i + int(rate)) % len(cfgs)] for i in range(args.sweep_jobs)]
+        row = {"rate_per_min": rate, "jobs": args.sweep_jobs, "cycles": args.sweep_cycles}
+        row["mixed"] = poisson(lbdem.MIXED, jobs, arrivals, args.sweep_cycles)
+        row["fp64"] = poisson(lbdem.PLAIN_FP64, jobs, arrivals, args.sweep_cycles)
+        sweep.append(row)
     for c in cfgs:
         c.close()
-    lat = [r["end_time"] - r["submit_time"] for r in res]
     # batched configuration: many runs resident at once, their schedule
     # (runs per shared launch group, lattice chunks per block) picked by the
     # autotuner on a sample of them
-    rng64 = np.random.default_rng(args.serve_seed + 1)
-    many = []
-    for i in range(args.serve_batch_jobs):
-        d = os.path.join(CACHE, f"serve{args.serve_seed + 1}", f"j{i:03d}")
-        case = casegen.serving_case(rng64, f"b{i}")
-        if not os.path.exists(os.path.join(d, "parameters.cfg")):
-            case.write(d)
-        many.append(lbdem.LoadedConfig(os.path.join(d, "parameters.cfg")))
+    many = job_set(args.serve_seed + 1, args.serve_batch_jobs, "b")
     tb, tc, _ = lbdem.tune_server(many[:8], cycles=40, slice_cycles=args.serve_slice)
     batched = batch(lbdem.MIXED, many, batch_runs=tb, chunks_per_block=tc)
     batched["schedule"] = {"batch_runs": tb, "chunks_per_block": tc,
@@ -556,17 +579,15 @@ def serving(args) -> dict:
     for c in many:
         c.close()
     return {
-        "sample": f"{len(cfgs)} seeded runs (lattice sides 48-128, vertical 48-160, fluid to "
-                  f"60 %, grid-packed phi 0.25-0.30, impactor r 6-16, vy 0.005-0.05), {C} "
-                  f"goCycles each, {args.serve_slice}-cycle slices, all resident at once",
-        "batch_mixed": mixed,
-        "same_runs": {"runs": len(sub), "mixed": mixed_sub, "fp64": fp64_sub,
+        "sample": f"seeded runs: lattice sides 48-128, vertical 48-160, fluid to 60 %, a "
+                  f"compressed bed of volume fraction 0.40-0.55 over 80 % of the fluid depth, "
+                  f"impactor r 6-16, vy 0.005-0.05; {args.serve_slice}-cycle slices",
+        "batch_mixed": dict(mixed, cycles=C),
+        "same_runs": {"runs": len(sub), "cycles": C, "mixed": mixed_sub, "fp64": fp64_sub,
                       "jobs_per_hour_ratio_mixed_over_fp64":
                           round(mixed_sub["jobs_per_hour"] / fp64_sub["jobs_per_hour"], 2)},
-        "poisson_mixed": {"rate_per_min": round(rate * 60.0, 2), "jobs": len(res),
-                          "jobs_per_hour": round(len(res) / wall * 3600.0, 1),
-                          "p50_s": round(pct(lat, 50), 4), "p99_s": round(pct(lat, 99), 4)},
-        "batched_mixed": batched,
+        "poisson_sweep": sweep,
+        "batched_mixed": dict(batched, cycles=C),
     }
 
 
@@ -593,6 +614,10 @@ def main():
     ap.add_argument("--serve-slice", type=int, default=24)
     ap.add_argument("--serve-seed", type=int, default=3)
     ap.add_argument("--serve-batch-jobs", type=int, default=64)
+    ap.add_argument("--serve-rates", default="10,20,50",
+                    help="Poisson arrival rates (jobs per minute), comma-separated")
+    ap.add_argument("--sweep-jobs", type=int, default=4)
+    ap.add_argument("--sweep-cycles", type=int, default=5000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     os.makedirs(CACHE, exist_ok=True)

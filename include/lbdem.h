@@ -144,8 +144,15 @@ typedef struct lbdem_options {
   int32_t async_init;  /* 1: lbdem_create returns once the device
                           initialisation is enqueued; its device errors
                           surface at the next lbdem_sync                  */
-  int32_t reserved[3];
+  int32_t debug_flags; /* tests of the failure paths only; 0 otherwise    */
+  int32_t reserved[2];
 } lbdem_options;
+
+/* debug_flags: the mixed form's lattice step issues none of its bulk copies
+ * into shared memory, so its bounded waits for them run out (after a short
+ * limit; nothing is in flight) and the step reports
+ * LBDEM_ERR_DEVICE_STATE at the next lbdem_sync. For tests of that path. */
+#define LBDEM_DEBUG_NO_LATTICE_COPIES 1
 
 typedef struct lbdem_ctx lbdem_ctx;
 

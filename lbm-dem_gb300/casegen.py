@@ -187,13 +187,15 @@ def impact_case(lattice=(64, 80, 64), fill=60.0, n_particles=400,
                 radii=(3.0, 4.2), impactor_r=8.0, impactor_y=70.0,
                 impactor_vy=-0.01, impactor_density=5.0, tau=0.8,
                 gravity=1.0e-5, seed=1, gap=0.05, overrides=None,
-                name="case") -> Case:
+                name="case", bed_phi=None) -> Case:
     """Bidisperse suspension under a falling impactor (reference axes).
 
     Lattice sides are in lattice units (unitLength = unitTime = 1), the walls
     are the outermost node layers (wall planes at 0.5 and side-1.5, as set by
-    src/LB.cpp:186-193). Particles are RSA-placed below ``fill``; half the
-    spheres (by number) take each radius.
+    src/LB.cpp:186-193). Half the spheres (by number) take each radius. They
+    are RSA-placed below ``fill``, or, with ``bed_phi``, randomly inserted and
+    compressed into a bed of that volume fraction on the floor
+    (``compress_pack``; the bed must fit below ``fill``).
     """
     rng = np.random.default_rng(seed)
     p = dict(DEFAULT_PARAMS)
@@ -219,7 +221,10 @@ def impact_case(lattice=(64, 80, 64), fill=60.0, n_particles=400,
     rs = np.array([radii[1]] * (n_particles - half) + [radii[0]] * half)
     lo = (0.5, 0.5, 0.5)
     hi = (nx - 1.5, float(fill), nz - 1.5)
-    pk = rsa_pack(rng, lo, hi, rs, gap=gap)
+    if bed_phi is None:
+        pk = rsa_pack(rng, lo, hi, rs, gap=gap)
+    else:
+        pk, _ = compress_pack(rng, lo, hi, rs, bed_phi)
     order = rng.permutation(len(pk))
     pk = pk[order]
     parts = np.zeros((len(pk), 10))
@@ -228,6 +233,102 @@ def impact_case(lattice=(64, 80, 64), fill=60.0, n_particles=400,
     objs[0] = (impactor_r, 0.5 * (nx - 1), impactor_y, 0.5 * (nz - 1),
                0.0, impactor_vy, 0.0)
     return Case(params=p, particles=parts, objects=objs, name=name)
+
+
+def _relax(x, r, lo, hi, gap, tol, max_iter, skin, state):
+    """Remove overlaps (surfaces closer than ``gap``) by Jacobi position
+    projection with heavy-ball momentum: every overlapping pair moves apart
+    by half its overlap along the line of centres, the step keeps a fraction
+    of the previous one (reset whenever the largest overlap grows), and every
+    sphere is clipped into the box. Candidate pairs come from a Verlet list
+    (centres within r_i + r_j + gap + skin) rebuilt whenever a sphere has
+    moved more than skin / 2 since the last build; the pairs are sorted, so
+    the sums (numpy bincount, in order) and the result are the same on every
+    machine. Returns the largest remaining overlap."""
+    from scipy.spatial import cKDTree
+    n = len(r)
+    rmax = float(r.max())
+    worst = np.inf
+    last = np.inf
+    v = state.setdefault("v", np.zeros_like(x))
+    lo_r = lo + r[:, None]
+    hi_r = hi - r[:, None]
+    for _ in range(max_iter):
+        if state.get("pairs") is None or \
+                np.max(np.abs(x - state["xref"])) > 0.5 * skin:
+            p = cKDTree(x).query_pairs(2.0 * rmax + gap + skin, output_type="ndarray")
+            p = p[np.lexsort((p[:, 1], p[:, 0]))] if len(p) else p.reshape(0, 2)
+            i, j = p[:, 0], p[:, 1]
+            contact = r[i] + r[j] + gap
+            d = np.sqrt(np.sum((x[j] - x[i]) ** 2, axis=1))
+            keep = d < contact + skin
+            state["pairs"] = (i[keep].copy(), j[keep].copy(), contact[keep].copy())
+            state["xref"] = x.copy()
+        i, j, contact = state["pairs"]
+        d = x[j] - x[i]
+        dist = np.sqrt(np.einsum("ij,ij->i", d, d))
+        ov = contact - dist
+        m = ov > 0.0
+        worst = float(ov[m].max()) if m.any() else 0.0
+        if worst < tol:
+            break
+        if worst > last:
+            v[:] = 0.0
+        last = worst
+        im, jm = i[m], j[m]
+        s = 0.5 * ov[m] / np.maximum(dist[m], 1e-12)
+        dm = d[m] * s[:, None]
+        disp = np.empty_like(x)
+        for a in range(3):
+            disp[:, a] = np.bincount(jm, dm[:, a], n) - np.bincount(im, dm[:, a], n)
+        v *= 0.5
+        v += 0.6 * disp
+        x += v
+        np.clip(x, lo_r, hi_r, out=x)
+    return worst
+
+
+def compress_pack(rng: np.random.Generator, lo, hi, radii: np.ndarray, phi: float,
+                  phi0: float = 0.30, gap: float = 0.02, step: float = 0.01,
+                  tol: float = 1e-3) -> tuple[np.ndarray, float]:
+    """Seeded random packing compressed into a bed of volume fraction ``phi``.
+
+    The spheres are inserted at random (volume fraction ``phi0`` of a box as
+    wide as [lo, hi] in x and z, as tall in y as that takes), their overlaps
+    are relaxed away, and the box is then compressed along y towards the
+    bed height H = V_spheres / (phi * width_x * width_z): every stage
+    rescales the heights by (1 - ``step``) towards the floor lo[1] and relaxes
+    the overlaps again (``_relax``), until the bed is H high. Surfaces end at
+    least ``gap`` - ``tol`` apart and inside the box, so no two spheres and no
+    sphere and wall touch.
+
+    Returns (rows of r, x, y, z in the order of ``radii``, H).
+    """
+    lo = np.asarray(lo, float)
+    hi = np.asarray(hi, float)
+    r = np.asarray(radii, float)
+    area = (hi[0] - lo[0]) * (hi[2] - lo[2])
+    vol = float(np.sum(4.0 / 3.0 * math.pi * r ** 3))
+    H = vol / (phi * area)
+    if H > hi[1] - lo[1]:
+        raise ValueError(f"a bed at volume fraction {phi} is {H:.1f} high, above the box")
+    h = max(vol / (phi0 * area), H)
+    top = lo.copy()
+    top[0], top[2] = hi[0], hi[2]
+    top[1] = lo[1] + h
+    x = lo + r[:, None] + (top - lo - 2.0 * r[:, None]) * rng.random((len(r), 3))
+    state: dict = {}
+    skin = 0.6
+    _relax(x, r, lo, top, gap, 0.05, 2000, skin, state)
+    while top[1] > lo[1] + H:
+        new = max(lo[1] + H, lo[1] + (top[1] - lo[1]) * (1.0 - step))
+        x[:, 1] = lo[1] + (x[:, 1] - lo[1]) * ((new - lo[1]) / (top[1] - lo[1]))
+        top[1] = new
+        _relax(x, r, lo, top, gap, 0.05, 400, skin, state)
+    worst = _relax(x, r, lo, top, gap, tol, 20000, skin, state)
+    if worst >= tol:
+        raise RuntimeError(f"packing did not relax: overlap {worst:.3g} left at phi {phi}")
+    return np.column_stack([r, x]), float(H)
 
 
 def grid_pack(rng: np.random.Generator, lo, hi, radii=(3.0, 4.2), phi=0.3,
@@ -258,11 +359,15 @@ def grid_pack(rng: np.random.Generator, lo, hi, radii=(3.0, 4.2), phi=0.3,
     return np.column_stack([r, pos])
 
 
-def serving_case(rng: np.random.Generator, name: str = "job") -> Case:
+def serving_case(rng: np.random.Generator, name: str = "job", bed: bool = True) -> Case:
     """One impact run of a varied job stream: lattice sides 48-128 (vertical
-    up to 160), fluid to 60 % of the height, a grid-packed bidisperse
-    suspension (phi 0.25-0.30), an impactor of radius 6-16 (at most what the
-    gas layer holds) falling at 0.005-0.05 just above the surface."""
+    up to 160), fluid to 60 % of the height, an impactor of radius 6-16 (at
+    most what the gas layer holds) falling at 0.005-0.05 just above the
+    surface, and a bidisperse suspension (radii 3.0 / 4.2, half each):
+    with ``bed``, spheres compressed into a bed of volume fraction drawn from
+    0.40-0.55 that fills 80 % of the fluid depth (``compress_pack``);
+    otherwise a grid-packed suspension of volume fraction 0.25-0.30 through
+    the whole fluid."""
     nx, nz = (int(v) for v in rng.integers(48, 129, size=2))
     ny = int(rng.integers(48, 161))
     fill = 0.6 * ny
@@ -281,8 +386,16 @@ def serving_case(rng: np.random.Generator, name: str = "job") -> Case:
     p["lubNormal"] = p["lubTangential"] = p["lubRotation"] = repr(0.5 * amean)
     p["debyeLength"] = repr(0.05 * amean)
     p["lubCutoff"] = repr(0.1 * amean)
-    pk = grid_pack(rng, (0.5, 0.5, 0.5), (nx - 1.5, fill, nz - 1.5),
-                   phi=float(rng.uniform(0.25, 0.30)))
+    if bed:
+        phi = float(rng.uniform(0.40, 0.55))
+        depth = 0.8 * (fill - 0.5)
+        vmean = 0.5 * 4.0 / 3.0 * math.pi * (3.0 ** 3 + 4.2 ** 3)
+        n = int(phi * (nx - 2) * (nz - 2) * depth / vmean)
+        rs = np.array([4.2] * (n - n // 2) + [3.0] * (n // 2))
+        pk, _ = compress_pack(rng, (0.5, 0.5, 0.5), (nx - 1.5, fill, nz - 1.5), rs, phi)
+    else:
+        pk = grid_pack(rng, (0.5, 0.5, 0.5), (nx - 1.5, fill, nz - 1.5),
+                       phi=float(rng.uniform(0.25, 0.30)))
     parts = np.zeros((len(pk), 10))
     parts[:, :4] = pk[rng.permutation(len(pk))]
     objs = np.array([[r_imp, 0.5 * (nx - 1), fill + r_imp + 1.0, 0.5 * (nz - 1), 0.0, vy, 0.0]])
@@ -325,10 +438,20 @@ def to_physical(case: Case, length: float, time: float, density: float) -> Case:
 
 
 def volume_fraction(case: Case) -> float:
+    """Spheres' volume over the fluid column below fluidHeight."""
     nx, ny, nz = case.lattice
     fill = float(case.params["fluidHeight"])
     vol = (nx - 2) * (fill - 0.5) * (nz - 2)
     return float(np.sum(4.0 / 3.0 * math.pi * case.particles[:, 0] ** 3) / vol)
+
+
+def bed_fraction(case: Case) -> float:
+    """Spheres' volume over the bed they fill: the box floor (y = 0.5) up to
+    the top of the highest sphere, across the inner width of the box."""
+    nx, ny, nz = case.lattice
+    p = case.particles
+    top = float(np.max(p[:, 2] + p[:, 0]))
+    return float(np.sum(4.0 / 3.0 * math.pi * p[:, 0] ** 3) / ((nx - 2) * (top - 0.5) * (nz - 2)))
 
 
 # Named workloads. Sizes follow the benchmark configurations of this project
@@ -338,11 +461,19 @@ def named_case(name: str, seed: int = 1) -> Case:
         return impact_case((64, 80, 64), 60.0, 400, (3.0, 4.2), 8.0, 70.0,
                            -0.01, 5.0, 0.8, 1.0e-5, seed, name=name)
     if name == "c2":
+        # 25 000 spheres compressed into a bed of volume fraction 0.50 on the
+        # floor (about 164 lattice units high), clear fluid above it to 240
         return impact_case((256, 320, 256), 240.0, 25000, (3.0, 4.2), 20.0,
-                           262.0, -0.02, 5.0, 0.6, 1.0e-5, seed, name=name)
+                           262.0, -0.02, 5.0, 0.6, 1.0e-5, seed, name=name, bed_phi=0.50)
     if name == "c2s":  # config-2 physics on a 160x200x160 lattice (profiling size)
         return impact_case((160, 200, 160), 150.0, 6100, (3.0, 4.2), 14.0, 166.0,
-                           -0.02, 5.0, 0.6, 1.0e-5, seed, name=name)
+                           -0.02, 5.0, 0.6, 1.0e-5, seed, name=name, bed_phi=0.50)
+    if name == "c5":
+        # 512x384x512, 200 000 spheres compressed into a bed of volume
+        # fraction 0.55 (about 296 high, the fluid is filled to 300); impactor
+        # of radius 32, density 8, falling at 0.03 from just above the surface
+        return impact_case((512, 384, 512), 300.0, 200000, (3.0, 4.2), 32.0, 334.0,
+                           -0.03, 8.0, 0.6, 1.0e-5, seed, name=name, bed_phi=0.55)
     if name == "small_cells":
         return impact_case((28, 40, 28), 27.0, 16, (3.0, 3.4), 5.0, 32.0,
                            -0.08, 5.0, 0.8, 1.0e-4, seed,

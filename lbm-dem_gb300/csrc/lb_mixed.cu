@@ -77,6 +77,9 @@ __device__ __forceinline__ bool mbarTryWait(uint64_t* bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
+// with LBDEM_DEBUG_NO_LATTICE_COPIES no copy is ever issued, so nothing can
+// be in flight when a wait gives up and a short limit is safe
+constexpr int WAIT_LIMIT_NO_COPIES = 1 << 14;
 // one thread waits for the phase of the given parity to complete
 __device__ __forceinline__ bool mbarWait(uint64_t* bar, unsigned parity) {
   for (int it = 0; it < WAIT_LIMIT; ++it)
@@ -84,8 +87,8 @@ __device__ __forceinline__ bool mbarWait(uint64_t* bar, unsigned parity) {
   return false;
 }
 // all lanes of a warp wait together; the result is warp-uniform
-__device__ __forceinline__ bool warpWait(uint64_t* bar, unsigned parity) {
-  for (int it = 0; it < WAIT_LIMIT; ++it)
+__device__ __forceinline__ bool warpWait(uint64_t* bar, unsigned parity, int limit) {
+  for (int it = 0; it < limit; ++it)
     if (__all_sync(0xffffffffu, mbarTryWait(bar, parity))) return true;
   return false;
 }
@@ -248,14 +251,17 @@ LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
     bulkLoad(sb + MIXED_STAGE_MASK, mk + off, MIXED_CHUNK, &fullBar[st]);
   };
   unsigned issued = 0;  // meaningful in thread 0
-  if (tid == 0)
+  // test of the timeout path: no copy is issued, every wait runs out
+  const bool noCopies = (k.debugFlags & LBDEM_DEBUG_NO_LATTICE_COPIES) != 0;
+  const int waitLimit = noCopies ? WAIT_LIMIT_NO_COPIES : WAIT_LIMIT;
+  if (tid == 0 && !noCopies)
     for (; issued < nIter && issued < (unsigned)MIXED_STAGES; ++issued) issue(issued);
   const int X = k.X, Y = k.Y, sy = (int)k.sy, sz = (int)k.sz;
   unsigned i = 0;
   for (; i < nIter; ++i) {
     const int st = (int)(i % MIXED_STAGES);
     const unsigned ph = (i / MIXED_STAGES) & 1u;
-    if (__any_sync(FULL, *(volatile int*)&abortFlag != 0) || !warpWait(&fullBar[st], ph)) {
+    if (__any_sync(FULL, *(volatile int*)&abortFlag != 0) || !warpWait(&fullBar[st], ph, waitLimit)) {
       if (lane == 0) {
         atomicOr(a.iscal + IS_ERROR, ERR_PIPELINE);
         abortFlag = 1;
@@ -293,7 +299,7 @@ LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
     }
     __syncwarp();
     if (lane == 0) mbarArrive(&emptyBar[st]);  // this warp is done with the stage
-    if (tid == 0 && i >= 1 && issued < nIter) {
+    if (tid == 0 && i >= 1 && issued < nIter && !noCopies) {
       // refill the stage of iteration i - 1 with iteration i - 1 + MIXED_STAGES
       const unsigned pi = i - 1u;
       if (mbarWait(&emptyBar[pi % MIXED_STAGES], (pi / MIXED_STAGES) & 1u)) {

@@ -75,6 +75,25 @@ int launchErr(lbdem_ctx* ctx, const char* what) {
 
 int latticeGrid(lbdem_ctx* ctx) { return std::max(1, ctx->smCount) * 8; }
 
+// The status of a run's device error bits (0: LBDEM_OK), with a message.
+int deviceError(lbdem_ctx* ctx, int e, const char* when) {
+  if (!e) return LBDEM_OK;
+  std::string m = std::string("device error bits") + when + " " + std::to_string(e) + ":";
+  if (e & ERR_TYPE) m += " streaming-type";
+  if (e & ERR_NBR_OVERFLOW) m += " neighbour-list-overflow";
+  if (e & ERR_CELL_OVERFLOW) m += " cell-overflow";
+  if (e & ERR_UNCOVER_CAP) m += " uncover-capacity";
+  if (e & ERR_PARTICLE_INDEX) m += " particle-index";
+  if (e & ERR_NONFINITE) m += " non-finite";
+  if (e & ERR_GRID) m += " particle-outside-grid";
+  if (e & ERR_PIPELINE) m += " lattice-copy-pipeline-timeout";
+  const int code = (e & ERR_NONFINITE) ? LBDEM_ERR_NONFINITE
+                 : (e & (ERR_NBR_OVERFLOW | ERR_CELL_OVERFLOW | ERR_UNCOVER_CAP))
+                     ? LBDEM_ERR_OVERFLOW
+                     : LBDEM_ERR_DEVICE_STATE;
+  return setErr(ctx, code, m);
+}
+
 LbArgs lbArgs(lbdem_ctx* c) {
   Device& d = c->d;
   const int P = std::max(c->nPart, 1);
@@ -283,6 +302,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
 
   Consts& k = ctx->k;
   std::memset(&k, 0, sizeof(k));
+  k.debugFlags = opt ? opt->debug_flags : 0;
   ctx->demSolve = cfg->demSolve != 0;
   ctx->lbSolve = cfg->lbSolve != 0;
   ctx->freeSurface = cfg->freeSurfaceSolve != 0;
@@ -600,8 +620,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   CK(cudaStreamSynchronize(st));
   int e = 0;
   CK(cudaMemcpy(&e, d.iscal + IS_ERROR, sizeof(int), cudaMemcpyDeviceToHost));
-  if (e) return setErr(ctx, LBDEM_ERR_DEVICE_STATE, "device error during init: " + std::to_string(e));
-  return LBDEM_OK;
+  return deviceError(ctx, e, " during init");
 }
 
 extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
@@ -1093,23 +1112,7 @@ extern "C" int lbdem_sync(lbdem_ctx* ctx) {
   if (int rc = lbdemOutputDrain(ctx, true)) return rc;
   int e = 0;
   CK(cudaMemcpy(&e, ctx->d.iscal + IS_ERROR, sizeof(int), cudaMemcpyDeviceToHost));
-  if (e) {
-    std::string m = "device error bits " + std::to_string(e) + ":";
-    if (e & ERR_TYPE) m += " streaming-type";
-    if (e & ERR_NBR_OVERFLOW) m += " neighbour-list-overflow";
-    if (e & ERR_CELL_OVERFLOW) m += " cell-overflow";
-    if (e & ERR_UNCOVER_CAP) m += " uncover-capacity";
-    if (e & ERR_PARTICLE_INDEX) m += " particle-index";
-    if (e & ERR_NONFINITE) m += " non-finite";
-    if (e & ERR_GRID) m += " particle-outside-grid";
-    if (e & ERR_PIPELINE) m += " lattice-copy-pipeline-timeout";
-    const int code = (e & ERR_NONFINITE) ? LBDEM_ERR_NONFINITE
-                   : (e & (ERR_NBR_OVERFLOW | ERR_CELL_OVERFLOW | ERR_UNCOVER_CAP))
-                       ? LBDEM_ERR_OVERFLOW
-                       : LBDEM_ERR_DEVICE_STATE;
-    return setErr(ctx, code, m);
-  }
-  return LBDEM_OK;
+  return deviceError(ctx, e, "");
 }
 
 // Device bytes lbdem_create allocates for cfg, array by array as it does

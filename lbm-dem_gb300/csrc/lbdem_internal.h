@@ -80,6 +80,7 @@ struct Consts {
   // elements; 19 NP < 2^32 is checked when the run is created)
   int nbOff[Q];
   unsigned pushOff[Q];
+  int debugFlags;  // lbdem_options::debug_flags (failure-path tests only)
 };
 
 struct DeviceWall {

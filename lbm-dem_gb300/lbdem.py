@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(HERE, "liblbdem.so")
 PLAIN_FP64 = 0
 MIXED = 1
 NOALLOC_MAX_NODES = 16384  # LBDEM_NOALLOC_MAX_NODES in include/lbdem.h
+DEBUG_NO_LATTICE_COPIES = 1  # LBDEM_DEBUG_NO_LATTICE_COPIES
 
 ERRORS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
@@ -142,10 +143,12 @@ class Solver:
     """One impact run on the GPU (wraps an lbdem_ctx)."""
 
     def __init__(self, config: LoadedConfig, precision: int = PLAIN_FP64,
-                 device: int = 0, check_every: int = 0):
+                 device: int = 0, check_every: int = 0, async_init: bool = False,
+                 debug_flags: int = 0):
         self.lib = load_library()
         self.ctx = C.c_void_p()
-        opt = Options(precision=precision, device=device, check_every=check_every)
+        opt = Options(precision=precision, device=device, check_every=check_every,
+                      async_init=1 if async_init else 0, debug_flags=debug_flags)
         rc = self.lib.lbdem_create(C.byref(config.cfg), C.byref(opt), C.byref(self.ctx))
         if rc != 0:
             msg = self.lib.lbdem_last_error(self.ctx).decode() if self.ctx else ""

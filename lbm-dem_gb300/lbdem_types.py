@@ -59,7 +59,8 @@ class Config(C.Structure):
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32),
                 ("check_every", C.c_int32), ("chunks_per_block", C.c_int32),
-                ("async_init", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("async_init", C.c_int32), ("debug_flags", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class Info(C.Structure):
