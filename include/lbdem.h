@@ -60,6 +60,12 @@ extern "C" {
 #define LBDEM_TOPOGRAPHY 11
 #define LBDEM_OBJECT 12
 
+/* rheology models (enum Rheology, src/node.h:17) */
+#define LBDEM_NEWTONIAN 0
+#define LBDEM_BINGHAM 1
+#define LBDEM_FRICTIONAL 2
+#define LBDEM_VOELLMY 3
+
 /* precision forms */
 #define LBDEM_PLAIN_FP64 0 /* FP64 throughout, reproduces the reference    */
 #define LBDEM_MIXED 1      /* FP32 deviation storage, FP64 islands         */
@@ -131,6 +137,14 @@ typedef struct lbdem_config {
   /* lbRestartFile (src/LB.cpp:139): the fluid recycle file read under
    * lbRestart, as given (relative to the working directory) */
   const char* lbRestartFile;
+  /* rheology (src/LB.cpp:196-242): the model (LBDEM_NEWTONIAN ...) and its
+   * parameters in physical units; a key the model does not read keeps its
+   * default, as in the reference (BINGHAM reads no initVisc: initVisc is
+   * then the default 1/6 of the reference's FluidMaterial). Apparent
+   * viscosity and the Smagorinsky term (turbulenceSolve, turbConst) follow
+   * node::computeApparentViscosity (src/node.cpp:113-168). */
+  int32_t rheologyModel;
+  double plasticVisc, yieldStress, frictionCoefFluid, voellmyConstant;
 } lbdem_config;
 
 /* Run options that are not part of the reference's configuration. */
@@ -224,6 +238,13 @@ int lbdem_get_info(lbdem_ctx* ctx, lbdem_info* info);
 int lbdem_download_lattice(lbdem_ctx* ctx, uint8_t* type, uint8_t* pflag,
                            int32_t* solid, double* n, double* u, double* mass,
                            double* f);
+
+/* Viscosity of every node in lattice units, visc[N]: node::visc
+ * (src/node.h:54-114), which LB::collision updates per node for
+ * non-Newtonian rheology and the Smagorinsky term (src/LB.cpp:1322-1325,
+ * src/node.cpp:113-168); initVisc at every active node of a Newtonian run;
+ * 0 at non-active nodes. */
+int lbdem_download_viscosity(lbdem_ctx* ctx, double* visc);
 
 /* Particle state, row-major [P][3]; any pointer may be NULL. */
 typedef struct lbdem_particle_view {

@@ -487,6 +487,23 @@ def named_case(name: str, seed: int = 1) -> Case:
         return impact_case((18, 28, 18), 16.0, 5, (3.0, 3.4), 4.0, 20.5,
                            -0.05, 5.0, 0.8, 1.0e-4, seed,
                            overrides={"objWaitTime": "2"}, name=name)
+    rheo = {
+        # the rheology models of node::computeApparentViscosity
+        # (src/node.cpp:113-168) on the small_cells geometry; lattice units
+        "rheo_bingham": {"rheologyModel": "BINGHAM", "plasticVisc": "0.1",
+                         "yieldStress": "2.0e-6"},
+        "rheo_frictional": {"rheologyModel": "FRICTIONAL", "initVisc": "0.1",
+                            "frictionCoefFluid": "0.4"},
+        "rheo_voellmy": {"rheologyModel": "VOELLMY", "initVisc": "0.1",
+                         "frictionCoefFluid": "0.4", "voellmyConstant": "2.0e-4"},
+        "rheo_turbulent": {"rheologyModel": "NEWTONIAN", "initVisc": "0.1",
+                           "turbulenceSolve": "1", "turbConst": "5.0"},
+    }
+    if name in rheo:
+        ov = {"objWaitTime": "3"}
+        ov.update(rheo[name])
+        return impact_case((28, 40, 28), 27.0, 16, (3.0, 3.4), 5.0, 32.0,
+                           -0.08, 5.0, 0.8, 1.0e-4, seed, overrides=ov, name=name)
     if name == "units_dyn":
         # a cell-list case in physical units (unitLength 0.5, unitTime 0.02,
         # unitDensity 1000), with boundary0 = 8: every wall is a moving

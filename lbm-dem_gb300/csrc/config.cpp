@@ -187,9 +187,23 @@ extern "C" int lbdem_config_load(const char* cfg_path, const char* input_dir,
   c->lbSizeX = ks.d("lbSizeX", 0.0);
   c->lbSizeY = ks.d("lbSizeY", 0.0);
   c->lbSizeZ = ks.d("lbSizeZ", 0.0);
+  // src/LB.cpp:196-242: each model reads its own keys; the others keep
+  // FluidMaterial's defaults (src/node.h:41-50), initVisc 1/6 included
   const std::string rheo = ks.s("rheologyModel", "none");
-  c->rheologyNewtonian = (rheo == "NEWTONIAN" || rheo == "none") ? 1 : 0;
-  c->initVisc = ks.d("initVisc", 1.0);
+  c->rheologyModel = rheo == "BINGHAM" ? LBDEM_BINGHAM
+                   : rheo == "FRICTIONAL" ? LBDEM_FRICTIONAL
+                   : rheo == "VOELLMY" ? LBDEM_VOELLMY : LBDEM_NEWTONIAN;
+  c->rheologyNewtonian = c->rheologyModel == LBDEM_NEWTONIAN ? 1 : 0;
+  c->initVisc = (1.0 - 0.5) / 3.0;
+  c->voellmyConstant = 0.0;
+  if (c->rheologyModel != LBDEM_BINGHAM) c->initVisc = ks.d("initVisc", 1.0);
+  if (c->rheologyModel == LBDEM_BINGHAM) {
+    c->plasticVisc = ks.d("plasticVisc", 0.0);
+    c->yieldStress = ks.d("yieldStress", 0.0);
+  }
+  if (c->rheologyModel == LBDEM_FRICTIONAL || c->rheologyModel == LBDEM_VOELLMY)
+    c->frictionCoefFluid = ks.d("frictionCoefFluid", 0.0);
+  if (c->rheologyModel == LBDEM_VOELLMY) c->voellmyConstant = ks.d("voellmyConstant", 1.0);
   c->turbulenceSolve = ks.i("turbulenceSolve", 0);
   c->turbConst = ks.d("turbConst", 0.0);
   c->initVelocity[0] = ks.d("initVelocityX", 0.0);

@@ -153,24 +153,59 @@ __device__ __forceinline__ void stageRecord(T& dst, const T& src) {
   __device__ __forceinline__ void NAME##Body(const Consts& k, const ARGT& a)
 
 // Mixed lattice step launch shape: chunks of MIXED_CHUNK consecutive nodes
-// (one per thread), staged through MIXED_STAGES shared-memory buffers of 19
-// FP32 planes, the solid indices, the fluid densities nF and the mask bytes
-// that thread 0 fills with bulk copies.
+// (one consumer thread per node), staged through MIXED_STAGES shared-memory
+// buffers of 19 FP32 planes, the solid indices, the fluid densities nF and
+// the mask bytes, which a producer warp of each block fills with bulk
+// copies. Measured on GB300 (256x320x256 lattice, 15.4 M active nodes):
+//   producer warp, 2 blocks/SM, 3 stages      0.507 ms  (the default)
+//   thread 0 of warp 0 issuing, 3 blocks/SM   0.543 ms
+//   thread 0 issuing, 2 blocks/SM             0.686 ms
+//   producer, 3 blocks/SM                     0.538 ms
+//   producer, 2 blocks/SM, 2 or 4 stages      0.509-0.510 ms
+//   solid indices and nF read from global memory by particle nodes instead of
+//   staged: 0.579 ms at 2 blocks/SM, 0.509 ms at 3
+// The knobs stay compile-time options (-D) for re-measurement.
 constexpr int MIXED_CHUNK = 256;
-constexpr int MIXED_STAGES = 3;
+#ifndef LBDEM_MIXED_STAGES
+#define LBDEM_MIXED_STAGES 3
+#endif
+#ifndef LBDEM_MIXED_MIN_BLOCKS
+#define LBDEM_MIXED_MIN_BLOCKS 2
+#endif
+// resident lattice blocks per SM at most (the grid is one resident wave)
+#ifndef LBDEM_MIXED_MAX_PER_SM
+#define LBDEM_MIXED_MAX_PER_SM 2
+#endif
+constexpr int MIXED_STAGES = LBDEM_MIXED_STAGES;
+// LBDEM_MIXED_STAGE_SIDE 1: the solid indices and fluid densities of a chunk
+// are staged with its populations; 0: particle nodes (the only readers) load
+// theirs from global memory, and a stage holds the populations and mask bytes
+#ifndef LBDEM_MIXED_STAGE_SIDE
+#define LBDEM_MIXED_STAGE_SIDE 1
+#endif
 constexpr int MIXED_STAGE_SOLID = Q * MIXED_CHUNK * 4;                 // byte offsets
 constexpr int MIXED_STAGE_NF = MIXED_STAGE_SOLID + MIXED_CHUNK * 4;
-constexpr int MIXED_STAGE_MASK = MIXED_STAGE_NF + MIXED_CHUNK * 4;
+constexpr int MIXED_STAGE_MASK =
+    LBDEM_MIXED_STAGE_SIDE ? MIXED_STAGE_NF + MIXED_CHUNK * 4 : Q * MIXED_CHUNK * 4;
 constexpr int MIXED_STAGE_BYTES = MIXED_STAGE_MASK + MIXED_CHUNK;
-constexpr int MIXED_THREADS = MIXED_CHUNK;
+// LBDEM_MIXED_PRODUCER 1: an extra warp of each block issues the bulk copies
+// (iteration q once every consumer warp has released iteration
+// q - MIXED_STAGES); 0: thread 0 issues them between its own nodes
+#ifndef LBDEM_MIXED_PRODUCER
+#define LBDEM_MIXED_PRODUCER 1
+#endif
+constexpr int MIXED_CONSUMERS = MIXED_CHUNK;
+constexpr int MIXED_THREADS = MIXED_CONSUMERS + 32 * LBDEM_MIXED_PRODUCER;
 constexpr int MIXED_SMEM = MIXED_STAGES * MIXED_STAGE_BYTES;
-#define MIXED_BOUNDS __launch_bounds__(MIXED_THREADS, 3)
+#define MIXED_BOUNDS __launch_bounds__(MIXED_THREADS, LBDEM_MIXED_MIN_BLOCKS)
 // chunks per block up to which inactive chunks are skipped (per-block list)
 constexpr int MIXED_MAX_MINE = 2048;
 
 // lb_fp64.cu / lb_mixed.cu
 __global__ void lbStepFp64(Consts k, LbArgs a);
 __global__ void lbStepFp64Batch(const JobArgs* jobs);
+__global__ void lbStepFp64Rheo(Consts k, LbArgs a);
+__global__ void lbStepFp64RheoBatch(const JobArgs* jobs);
 __global__ void lbStepMixed(Consts k, LbArgs a);
 __global__ void lbStepMixedBatch(const JobArgs* jobs);
 __global__ void lbWallForceMixed(Consts k, LbArgs a);
@@ -214,6 +249,7 @@ __global__ void findNewActiveKernel(Consts k, uint8_t* mask, uint32_t* solid,
 __global__ void initTypes(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* objIdx,
                           const int* boundary, const DeviceWall* walls, const int* wallType,
                           const double* obj, double fluidHeightLattice, int freeSurface);
+__global__ void fillDouble(double* v, long long n, double value);
 __global__ void initFields(Consts k, uint8_t* mask, void* f, double* mass, float* nF,
                            double fluidHeightLattice, int freeSurface);
 // mass of the active nodes (outside particles unless withParticles), counts

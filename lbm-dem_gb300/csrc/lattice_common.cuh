@@ -29,7 +29,7 @@ __host__ __device__ constexpr double WJ(int j) {
   return j == 0 ? 12.0 / 36.0 : j <= 6 ? 2.0 / 36.0 : 1.0 / 36.0;
 }
 
-__device__ __forceinline__ bool isActiveT(int t) { return t == 0 || t == 3; }
+__host__ __device__ __forceinline__ bool isActiveT(int t) { return t == 0 || t == 3; }
 
 // bits j = 1..18 of the links whose lattice velocity has the given component sign
 __host__ __device__ constexpr unsigned linksWith(int axis, int sign) {
@@ -181,11 +181,74 @@ struct NodeState {
   double dx, dy, dz, rx, ry, rz;
 };
 
+// node::computeApparentViscosity (src/node.cpp:113-168) on the node's
+// pre-collision populations f, its equilibrium feq, density n and shifted
+// velocity; visc is the node's viscosity of the last step (tau) and gets the
+// new one. Same operations and order as the reference (this is compiled
+// without FMA contraction); terms with c_a c_b = 0 are skipped (they add an
+// exact +-0), c_a c_b = -1 subtracts.
+__device__ __forceinline__ void apparentViscosity(const Consts& k, const double* f,
+                                                  const double* feq, double n, double ux,
+                                                  double uy, double uz, double& visc) {
+  const double minVisc = (0.500001 - 0.5) / 3.0;  // minTau, src/lattice.h:26
+  const double maxVisc = (1.8 - 0.5) / 3.0;       // maxTau, src/lattice.h:27
+  const double tau = 0.5 + 3.0 * visc;
+  double g[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+  for (int j = 0; j < Q; ++j) {
+    const double d = f[j] - feq[j];
+    const int c[3] = {CX(j), CY(j), CZ(j)};
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const int cc = c[p] * c[q];
+        if (cc > 0) g[3 * p + q] += d;
+        else if (cc < 0) g[3 * p + q] += -d;
+      }
+  }
+  const double sc = 1.5 / (tau * n);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) g[i] *= sc;
+  // tinyMatrix::magnitude, src/myvector.cpp:546-550
+  const double mag = sqrt(0.5 * (g[0] * g[0] + g[4] * g[4] + g[8] * g[8] +
+                                 2.0 * (g[1] * g[3] + g[6] * g[2] + g[5] * g[7])));
+  const double shearRate = 2.0 * mag;
+  double nuApp;
+  if (k.rheo == LBDEM_BINGHAM) {
+    nuApp = k.plasticVisc + k.yieldStress / shearRate;
+  } else if (k.rheo == LBDEM_FRICTIONAL) {
+    const double pr = 0.33333333 * (n - 1.0);
+    const double pressure = pr > 0.0 ? pr : 0.0;  // std::max(0.0, pr)
+    nuApp = k.initVisc + k.frictionCoef * pressure / shearRate;
+  } else if (k.rheo == LBDEM_VOELLMY) {
+    const double pr = 0.33333333 * (n - 1.0);
+    const double pressure = pr > 0.0 ? pr : 0.0;
+    nuApp = (k.frictionCoef * pressure + (ux * ux + uy * uy + uz * uz) / k.voellmyCoef) /
+            shearRate;
+  } else {
+    nuApp = k.initVisc;
+  }
+  if (k.turbulence) {
+    const double nuTurb = k.turbConst * shearRate;
+    nuApp += nuTurb;
+  }
+  // std::max(minVisc, std::min(maxVisc, nuApp)), NaN handling included
+  const double lo = nuApp < maxVisc ? nuApp : maxVisc;
+  visc = minVisc < lo ? lo : minVisc;
+}
+
+// RHEO: the node's viscosity comes from viscp (k.visc + x) instead of the
+// run's single value; with update, the apparent viscosity is evaluated
+// first and stored there (LB::collision, src/LB.cpp:1322-1325), otherwise
+// the stored one is used (a recomputation of the same collision).
+template <bool RHEO = false>
 __device__ __forceinline__ void collideNode(const Consts& k, double* f, bool pflag,
                                             uint32_t pid, const double* px0,
                                             const double* px1, const double* pw1,
                                             int P, double massOld, int ix, int iy, int iz,
-                                            NodeState& s) {
+                                            NodeState& s, double* viscp = nullptr,
+                                            bool update = false) {
   // node::reconstruct
   double n = 0.0;
 #pragma unroll
@@ -235,12 +298,28 @@ __device__ __forceinline__ void collideNode(const Consts& k, double* f, bool pfl
   uy = uy + Ty * 0.5 / n;
   uz = uz + Tz * 0.5 / n;
   const double usq = ux * ux + uy * uy + uz * uz;
+  double omega = k.omega, omegaf = k.omegaf;
+  if (RHEO) {
+    double visc = *viscp;
+    if (update) {
+      double feqa[Q];
+#pragma unroll
+      for (int j = 0; j < Q; ++j) {
+        const double vu = dotc(j, ux, uy, uz);
+        feqa[j] = WJ(j) * n * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
+      }
+      apparentViscosity(k, f, feqa, n, ux, uy, uz, visc);
+      *viscp = visc;
+    }
+    omega = 1.0 / (0.5 + 3.0 * visc);          // node::solveCollision
+    omegaf = 1.0 - 1.0 / (1.0 + 6.0 * visc);   // node::addForce
+  }
   // node::solveCollision + node::addForce
 #pragma unroll
   for (int j = 0; j < Q; ++j) {
     const double vu = dotc(j, ux, uy, uz);
     const double feq = WJ(j) * n * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
-    double fj = f[j] + k.omega * (feq - f[j]);
+    double fj = f[j] + omega * (feq - f[j]);
     const double v9 = 9.0 * vu;
     const double fpx = CX(j) == 0 ? (-ux) * 3.0 : CX(j) > 0 ? v9 + (1.0 - ux) * 3.0
                                                              : -v9 + (-1.0 - ux) * 3.0;
@@ -248,7 +327,7 @@ __device__ __forceinline__ void collideNode(const Consts& k, double* f, bool pfl
                                                              : -v9 + (-1.0 - uy) * 3.0;
     const double fpz = CZ(j) == 0 ? (-uz) * 3.0 : CZ(j) > 0 ? v9 + (1.0 - uz) * 3.0
                                                              : -v9 + (-1.0 - uz) * 3.0;
-    fj += k.omegaf * WJ(j) * (fpx * Tx + fpy * Ty + fpz * Tz);
+    fj += omegaf * WJ(j) * (fpx * Tx + fpy * Ty + fpz * Tz);
     f[j] = fj;
   }
   s.n = n;

@@ -31,7 +31,8 @@ namespace lbdem {
 // Fused LB step over all nodes: reconstruct, particle forcing, collision,
 // push streaming with the boundary rules of LB::streaming, and the per-node
 // bookkeeping of cleanLists / updateMass (fluid part).
-LBDEM_KERNEL(__launch_bounds__(256), lbStepFp64, LbArgs, lb) {
+template <bool RHEO>
+__device__ __forceinline__ void lbStepFp64Impl(const Consts& k, const LbArgs& a) {
   __shared__ double acc[ACC_N];
   __shared__ int sbox[6];
   __shared__ int snif;
@@ -83,8 +84,8 @@ LBDEM_KERNEL(__launch_bounds__(256), lbStepFp64, LbArgs, lb) {
       const uint32_t pid = pf ? a.solid[x] : 0u;
       const double massOld = a.mass[x];
       NodeState s;
-      collideNode(k, f, pf, pid, a.pkd, a.pkd + 3 * k.nPart, a.pw1, k.nPart, massOld, ix, iy, iz,
-                  s);
+      collideNode<RHEO>(k, f, pf, pid, a.pkd, a.pkd + 3 * k.nPart, a.pw1, k.nPart, massOld, ix,
+                        iy, iz, s, RHEO ? k.visc + x : nullptr, true);
       if (pf && pid < (uint32_t)k.nPart) {
         key = (int)pid;
         pv[0] = s.dx * 1.0;
@@ -221,6 +222,11 @@ LBDEM_KERNEL(__launch_bounds__(256), lbStepFp64, LbArgs, lb) {
     }
   }
 }
+
+LBDEM_KERNEL(__launch_bounds__(256), lbStepFp64, LbArgs, lb) { lbStepFp64Impl<false>(k, a); }
+// the same step with a per-node viscosity (non-Newtonian rheology or the
+// Smagorinsky term, LB::collision src/LB.cpp:1322-1325)
+LBDEM_KERNEL(__launch_bounds__(256), lbStepFp64Rheo, LbArgs, lb) { lbStepFp64Impl<true>(k, a); }
 
 // Start of the LB step: the per-step reductions are cleared (particle
 // sums, the float sums of the mixed form, impactor and wall hydrodynamic
@@ -398,8 +404,14 @@ __device__ __noinline__ void fsPostCollision(const Consts& k, const FsArgs& a, l
 #pragma unroll
     for (int q = 0; q < Q; ++q) fsl[q] = ((const double*)a.fold)[(long long)q * k.NP + x];
     NodeState s;
-    collideNode(k, fsl, pf, pf ? a.solid[x] : 0u, a.pkd, a.pkd + 3 * k.nPart, a.pw1, k.nPart,
-                a.massNew[x], ix, iy, iz, s);
+    // with a per-node viscosity, the one the lattice step's collision used
+    // (and stored) is used again
+    if (k.visc)
+      collideNode<true>(k, fsl, pf, pf ? a.solid[x] : 0u, a.pkd, a.pkd + 3 * k.nPart, a.pw1,
+                        k.nPart, a.massNew[x], ix, iy, iz, s, k.visc + x, false);
+    else
+      collideNode(k, fsl, pf, pf ? a.solid[x] : 0u, a.pkd, a.pkd + 3 * k.nPart, a.pw1, k.nPart,
+                  a.massNew[x], ix, iy, iz, s);
   }
 }
 
@@ -507,6 +519,7 @@ LBDEM_KERNEL(, fsSmoothen, FsArgs, fs) {
         a.fsflag[x] |= FS_NEW;
         a.rhoS[x] = rho0;
         a.mass[x] = 0.01 * rho0;
+        if (k.visc) k.visc[x] = k.visc[win];  // the filler's viscosity (src/LB.cpp:1719)
         surplus -= 0.01 * rho0;
       }
     } else if (t == 0) {
@@ -825,6 +838,7 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
     for (int j = 0; j < Q; ++j) fset(k, f, j, x, feqj(j, rho0, ux, uy, uz, usq));
     mass[x] = st == 0 ? rho0 : 0.5 * rho0;
     if (k.mixed && st == 0) nF[x] = (float)rho0;
+    if (k.visc) k.visc[x] = k.initVisc;
   }
 }
 
@@ -1189,6 +1203,13 @@ __global__ void initFields(Consts k, uint8_t* mask, void* f, double* mass, float
     }
     mass[x] = ms;
   }
+}
+
+// every element of v[0 .. n) set to value (the initial per-node viscosity)
+__global__ void fillDouble(double* v, long long n, double value) {
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < n;
+       x += (long long)gridDim.x * blockDim.x)
+    v[x] = value;
 }
 
 // ---- diagnostics --------------------------------------------------------------

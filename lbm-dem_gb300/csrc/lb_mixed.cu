@@ -167,13 +167,15 @@ LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
   __shared__ uint8_t sAct[MIXED_MAX_MINE];       // warp activity bits of this block's chunks
   __shared__ uint16_t sList[MIXED_MAX_MINE];     // which of them to process
   __shared__ unsigned sCount;
+  __shared__ unsigned sConsumed;  // iterations every consumer warp finished
   const int tid = threadIdx.x;
   if (tid == 0) {
     for (int st = 0; st < MIXED_STAGES; ++st) {
       mbarInit(&fullBar[st], 1);                  // thread 0's expect_tx
-      mbarInit(&emptyBar[st], MIXED_THREADS / 32);  // one arrival per warp
+      mbarInit(&emptyBar[st], MIXED_CONSUMERS / 32);  // one arrival per consumer warp
     }
     abortFlag = 0;
+    sConsumed = ~0u;
     fenceBarrierInit();
   }
   for (int i = tid; i < 6 * MAX_OBJ; i += blockDim.x) accO[i] = 0.0f;
@@ -229,11 +231,13 @@ LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
   const unsigned nIter = useList ? sCount : nMine;
   double extra = 0.0;
   unsigned nact = 0, nif = 0;
-  // Thread 0 keeps the stage ring filled: bulk copies of the 19 population
-  // planes, solid indices, densities and mask bytes of a chunk, completing
-  // on the stage's full barrier. Iterations 0 .. MIXED_STAGES-1 are issued up front; iteration
-  // i + MIXED_STAGES - 1 is issued at iteration i once every warp has
-  // released iteration i - 1.
+  // The stage ring: bulk copies of the 19 population planes, solid indices,
+  // densities and mask bytes of a chunk, completing on the stage's full
+  // barrier. The producer warp issues iteration q once every consumer warp
+  // has released iteration q - MIXED_STAGES (empty barrier); without it,
+  // thread 0 issues iterations 0 .. MIXED_STAGES-1 up front and iteration
+  // i + MIXED_STAGES - 1 at its iteration i once every warp has released
+  // iteration i - 1.
   auto issue = [&](unsigned q) {
     const int st = (int)(q % MIXED_STAGES);
     unsigned char* sb = stageMem + st * MIXED_STAGE_BYTES;
@@ -246,18 +250,42 @@ LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
 #pragma unroll 1
     for (int j = 0; j < Q; ++j)
       bulkLoad(sb + j * MIXED_CHUNK * 4, gin + j * NP + off, MIXED_CHUNK * 4, &fullBar[st]);
-    bulkLoad(sb + MIXED_STAGE_SOLID, a.solid + off, MIXED_CHUNK * 4, &fullBar[st]);
-    bulkLoad(sb + MIXED_STAGE_NF, a.nF + off, MIXED_CHUNK * 4, &fullBar[st]);
+    if (LBDEM_MIXED_STAGE_SIDE) {
+      bulkLoad(sb + MIXED_STAGE_SOLID, a.solid + off, MIXED_CHUNK * 4, &fullBar[st]);
+      bulkLoad(sb + MIXED_STAGE_NF, a.nF + off, MIXED_CHUNK * 4, &fullBar[st]);
+    }
     bulkLoad(sb + MIXED_STAGE_MASK, mk + off, MIXED_CHUNK, &fullBar[st]);
   };
   unsigned issued = 0;  // meaningful in thread 0
   // test of the timeout path: no copy is issued, every wait runs out
   const bool noCopies = (k.debugFlags & LBDEM_DEBUG_NO_LATTICE_COPIES) != 0;
   const int waitLimit = noCopies ? WAIT_LIMIT_NO_COPIES : WAIT_LIMIT;
-  if (tid == 0 && !noCopies)
-    for (; issued < nIter && issued < (unsigned)MIXED_STAGES; ++issued) issue(issued);
   const int X = k.X, Y = k.Y, sy = (int)k.sy, sz = (int)k.sz;
   unsigned i = 0;
+#if LBDEM_MIXED_PRODUCER
+  // the producer warp keeps the ring full: iteration q is issued once every
+  // consumer warp has released iteration q - MIXED_STAGES of the same stage
+  if (warp == MIXED_CONSUMERS / 32) {
+    if (lane == 0 && !noCopies) {
+      for (; issued < nIter; ++issued) {
+        if (*(volatile int*)&abortFlag) break;
+        if (issued >= (unsigned)MIXED_STAGES) {
+          const unsigned pq = issued - (unsigned)MIXED_STAGES;
+          if (!mbarWait(&emptyBar[pq % MIXED_STAGES], (pq / MIXED_STAGES) & 1u)) {
+            atomicOr(a.iscal + IS_ERROR, ERR_PIPELINE);
+            abortFlag = 1;
+            break;
+          }
+        }
+        issue(issued);
+      }
+    }
+    i = nIter;  // the producer consumes nothing
+  }
+#else
+  if (tid == 0 && !noCopies)
+    for (; issued < nIter && issued < (unsigned)MIXED_STAGES; ++issued) issue(issued);
+#endif
   for (; i < nIter; ++i) {
     const int st = (int)(i % MIXED_STAGES);
     const unsigned ph = (i / MIXED_STAGES) & 1u;
@@ -286,7 +314,8 @@ LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
 #pragma unroll
     for (int j = 0; j < Q; ++j) g[j] = ((const float*)sb)[j * MIXED_CHUNK + tid];
     const uint8_t m = valid ? sb[MIXED_STAGE_MASK + tid] : (uint8_t)2;
-    const uint32_t sol = ((const uint32_t*)(sb + MIXED_STAGE_SOLID))[tid];
+    const uint32_t sol = LBDEM_MIXED_STAGE_SIDE ? ((const uint32_t*)(sb + MIXED_STAGE_SOLID))[tid]
+                         : ((valid && (m & PFLAG)) ? __ldg(a.solid + x) : 0u);
     const int t = m & TYPE_MASK;
     const bool act = valid && isActiveT(t);
     // particle nodes: their particle's kinematics and old mass, loaded first
@@ -295,11 +324,12 @@ LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
     float massOld = 0.0f;
     if (coupled) {
       kin = loadKinF(a.pkf, sol);
-      massOld = t == 3 ? (float)a.mass[x] : ((const float*)(sb + MIXED_STAGE_NF))[tid];
+      massOld = t == 3 ? (float)a.mass[x]
+                : LBDEM_MIXED_STAGE_SIDE ? ((const float*)(sb + MIXED_STAGE_NF))[tid] : a.nF[x];
     }
     __syncwarp();
     if (lane == 0) mbarArrive(&emptyBar[st]);  // this warp is done with the stage
-    if (tid == 0 && i >= 1 && issued < nIter && !noCopies) {
+    if (!LBDEM_MIXED_PRODUCER && tid == 0 && i >= 1 && issued < nIter && !noCopies) {
       // refill the stage of iteration i - 1 with iteration i - 1 + MIXED_STAGES
       const unsigned pi = i - 1u;
       if (mbarWait(&emptyBar[pi % MIXED_STAGES], (pi / MIXED_STAGES) & 1u)) {
@@ -465,10 +495,19 @@ LBDEM_KERNEL(MIXED_BOUNDS, lbStepMixed, LbArgs, lb) {
   }
   // no bulk copy may still be in flight when the block exits: on an early
   // exit, wait (bounded) for the copies issued beyond the last iteration used
+#if LBDEM_MIXED_PRODUCER
+  if (warp < MIXED_CONSUMERS / 32 && lane == 0) atomicMin(&sConsumed, i);
+  __syncthreads();
+  if (warp == MIXED_CONSUMERS / 32 && lane == 0)
+    for (unsigned q = sConsumed; q < issued; ++q)
+      if (!mbarWait(&fullBar[q % MIXED_STAGES], (q / MIXED_STAGES) & 1u))
+        atomicOr(a.iscal + IS_ERROR, ERR_PIPELINE);
+#else
   if (tid == 0)
     for (unsigned q = i; q < issued; ++q)
       if (!mbarWait(&fullBar[q % MIXED_STAGES], (q / MIXED_STAGES) & 1u))
         atomicOr(a.iscal + IS_ERROR, ERR_PIPELINE);
+#endif
   // block totals
   nact = __reduce_add_sync(FULL, nact);
   nif = __reduce_add_sync(FULL, nif);

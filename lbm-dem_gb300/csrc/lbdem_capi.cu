@@ -260,9 +260,14 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   if (precision != LBDEM_PLAIN_FP64 && precision != LBDEM_MIXED)
     return setErr(ctx, LBDEM_ERR_INVALID, "unknown precision form");
   // ---- validation (the supported subset of the reference's inputs) ----
-  if (!cfg->rheologyNewtonian || cfg->turbulenceSolve || cfg->lbTopography)
+  if (cfg->lbTopography) return setErr(ctx, LBDEM_ERR_INVALID, "topography is not supported");
+  const bool rheology = cfg->rheologyModel != LBDEM_NEWTONIAN || cfg->turbulenceSolve != 0;
+  if (cfg->rheologyModel < LBDEM_NEWTONIAN || cfg->rheologyModel > LBDEM_VOELLMY)
+    return setErr(ctx, LBDEM_ERR_INVALID, "unknown rheology model");
+  if (rheology && precision == LBDEM_MIXED)
     return setErr(ctx, LBDEM_ERR_INVALID,
-                  "only NEWTONIAN rheology without turbulence or topography");
+                  "the mixed form runs NEWTONIAN rheology without turbulence; runs with a "
+                  "per-node viscosity use the plain FP64 form");
   if (cfg->n_bodies != 0) return setErr(ctx, LBDEM_ERR_INVALID, "bodies are not supported");
   for (int i = 0; i < 6; ++i)
     if (cfg->boundary[i] != 7 && cfg->boundary[i] != 8)
@@ -297,7 +302,8 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
                             UNCOVER_SMEM));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, lbStepMixed, MIXED_THREADS,
                                                      MIXED_SMEM));
-    ctx->lbMixedBlocks = std::max(1, perSm) * std::max(1, ctx->smCount);
+    ctx->lbMixedBlocks = std::max(1, std::min(perSm, LBDEM_MIXED_MAX_PER_SM)) *
+                         std::max(1, ctx->smCount);
   }
 
   Consts& k = ctx->k;
@@ -340,6 +346,15 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   k.initVisc = cfg->initVisc / uDynVisc;
   k.omega = 1.0 / (0.5 + 3.0 * k.initVisc);
   k.omegaf = 1.0 - 1.0 / (1.0 + 6.0 * k.initVisc);
+  // rheology parameters in lattice units (src/LB.cpp:320-324; turbConst is
+  // not scaled; unit.Stress = Density Length^2 / Time^2, src/node.cpp:522)
+  k.rheo = cfg->rheologyModel;
+  k.turbulence = cfg->turbulenceSolve != 0 ? 1 : 0;
+  k.plasticVisc = cfg->plasticVisc / uDynVisc;
+  k.yieldStress = cfg->yieldStress / (D * L * L / T / T);
+  k.frictionCoef = cfg->frictionCoefFluid;
+  k.voellmyCoef = cfg->voellmyConstant / k.uAccel;
+  k.turbConst = cfg->turbConst;
   k.mixed = precision == LBDEM_MIXED ? 1 : 0;
   if (k.mixed && k.NP >= (1LL << 31))
     return setErr(ctx, LBDEM_ERR_INVALID, "mixed form: lattice larger than 2^31 nodes");
@@ -499,6 +514,10 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   }
   AL(d.mass, N);
   AL(d.massNew, N);
+  if (rheology) {
+    AL(d.visc, N);
+    k.visc = d.visc;
+  }
   AL(d.rhoS, N);
   AL(d.uS, 3 * N);
   AL(d.hS, 3 * N);
@@ -595,6 +614,8 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   CK(cudaMemcpyAsync(d.uscal + US_FIRSTFLAG, &none, sizeof(none), cudaMemcpyHostToDevice, st));
   // ---- LB::latticeBolzmannInit on the device ----
   const int lg = latticeGrid(ctx);
+  // every node starts with initVisc (node::initialize)
+  if (d.visc) fillDouble<<<lg, 256, 0, st>>>(d.visc, (long long)N, k.initVisc);
   if (ctx->lbSolve) {
     // under lbRestart, LB::initializeTypes without the free-surface
     // interface, then the recycle file (src/LB.cpp:353-367)
@@ -744,6 +765,7 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   if (k.mixed)
     lbStepMixed<<<ctx->gridLattice,
                   MIXED_THREADS, MIXED_SMEM, s>>>(k, a);
+  else if (k.visc) lbStepFp64Rheo<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
   else lbStepFp64<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
   if (ev) cudaEventRecord(ev->second, s);
   if (k.mixed && k.nWall > 0) {
@@ -958,7 +980,8 @@ void lbdemJobArgs(lbdem_ctx* c, int cur, JobArgs* j) {
 // conditions) with the DEM, lattice and coupling steps all on; two such runs
 // share a batch when their switches match (batchKey).
 bool lbdemBatchable(const lbdem_ctx* c) {
-  return c->demSolve && c->lbSolve && pairReplayable(c);
+  // runs with a per-node viscosity keep their own launches
+  return c->demSolve && c->lbSolve && pairReplayable(c) && !c->k.visc;
 }
 int lbdemBatchKey(const lbdem_ctx* c) {
   return c->precision | (c->freeSurface ? 2 : 0) | (c->nObj > 0 ? 4 : 0) | (c->nWall > 0 ? 8 : 0);
@@ -1142,7 +1165,9 @@ extern "C" int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t prec
   add((long long)Q * NP, mixed ? 4 : 8);
   add((long long)Q * NP, mixed ? 4 : 8);
   if (mixed) add(NP, 4);            // nF
-  for (int i = 0; i < 3; ++i) add(N, 8);  // mass, massNew, rhoS
+  for (int i = 0; i < 2; ++i) add(N, 8);  // mass, massNew
+  if (cfg->rheologyModel != LBDEM_NEWTONIAN || cfg->turbulenceSolve) add(N, 8);  // visc
+  add(N, 8);                        // rhoS
   add(3 * N, 8);                    // uS
   add(3 * N, 8);                    // hS
   add(SC_COUNT, 8);
@@ -1326,6 +1351,22 @@ extern "C" int lbdem_download_objects(lbdem_ctx* ctx, const lbdem_object_view* v
     if (e.dst)
       for (int o = 0; o < O; ++o)
         for (int c = 0; c < 3; ++c) e.dst[3 * o + c] = h[(size_t)o * OB_STRIDE + e.off + c];
+  return LBDEM_OK;
+}
+
+extern "C" int lbdem_download_viscosity(lbdem_ctx* ctx, double* visc) {
+  if (!ctx || !visc) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
+  int rc = lbdem_sync(ctx);
+  if (rc) return rc;
+  const size_t N = (size_t)ctx->k.N;
+  std::vector<uint8_t> m(N);
+  CK(cudaMemcpy(m.data(), ctx->d.mask, N, cudaMemcpyDeviceToHost));
+  if (ctx->d.visc) CK(cudaMemcpy(visc, ctx->d.visc, N * sizeof(double), cudaMemcpyDeviceToHost));
+  for (size_t i = 0; i < N; ++i) {
+    if (!isActiveT(m[i] & TYPE_MASK)) visc[i] = 0.0;
+    else if (!ctx->d.visc) visc[i] = ctx->k.initVisc;
+  }
   return LBDEM_OK;
 }
 

@@ -81,6 +81,12 @@ struct Consts {
   int nbOff[Q];
   unsigned pushOff[Q];
   int debugFlags;  // lbdem_options::debug_flags (failure-path tests only)
+  // rheology (plain form): model, parameters in lattice units, and the
+  // per-node viscosity (null for a Newtonian run without turbulence, whose
+  // every node has initVisc)
+  int rheo, turbulence;
+  double plasticVisc, yieldStress, frictionCoef, voellmyCoef, turbConst;
+  double* visc;
 };
 
 struct DeviceWall {
@@ -99,6 +105,7 @@ struct Device {
   double* mass = nullptr;
   float* nF = nullptr;         // fluid-node density, mixed form only
   double* massNew = nullptr;
+  double* visc = nullptr;      // per-node viscosity (rheology runs only)
   double* rhoS = nullptr;      // density of interface nodes
   double* uS = nullptr;        // shifted velocity of interface nodes [3][N]
   double* hS = nullptr;        // hydrodynamic force of interface nodes [3][N]

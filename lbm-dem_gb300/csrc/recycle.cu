@@ -21,9 +21,10 @@
 // the geometry leaves fluid takes the file's type (walls, impactors keep
 // theirs); then, for every node active under those types, in index order,
 // the next record gives its populations and its mass (node::restart,
-// src/node.cpp:38-50). n, u and visc of the record are not used: the
-// lattice step recomputes n and u from the populations before any use, and
-// the viscosity is the configuration's (Newtonian only).
+// src/node.cpp:38-50). n and u of the record are not used: the lattice step
+// recomputes them from the populations before any use. Its viscosity is
+// the node's in a run with a per-node viscosity (non-Newtonian rheology or
+// turbulence); a Newtonian run has one viscosity, the configuration's.
 #include <cuda_runtime.h>
 
 #include <cerrno>
@@ -115,6 +116,8 @@ int lbdemRestartFluid(lbdem_ctx* ctx, const char* path) {
   // LB::restartVariables, then the active-list bit of the first cleanLists
   const double rho0 = k.initDensity;
   std::vector<double> mass(N, 0.0);
+  std::vector<double> visc;
+  if (d.visc) visc.assign(N, k.initVisc);
   std::vector<double> f64;
   std::vector<float> f32, nF;
   if (k.mixed) {
@@ -132,6 +135,7 @@ int lbdemRestartFluid(lbdem_ctx* ctx, const char* path) {
         return fail(ctx, LBDEM_ERR_IO, "restart file: fewer node records than active nodes");
     const double m = rec[4] + rho0;
     mass[x] = m;
+    if (d.visc) visc[x] = rec[5];
     for (int j = 0; j < Q; ++j) {
       if (k.mixed) f32[(size_t)j * NP + x] = (float)(rec[6 + j] - WJ(j));
       else f64[(size_t)j * NP + x] = rec[6 + j];
@@ -142,6 +146,8 @@ int lbdemRestartFluid(lbdem_ctx* ctx, const char* path) {
   e = cudaMemcpyAsync(d.mask, mask.data(), N, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(d.mass, mass.data(), N * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && d.visc)
+    e = cudaMemcpyAsync(d.visc, visc.data(), N * sizeof(double), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     if (k.mixed) {
       e = cudaMemcpyAsync(d.f[0], f32.data(), f32.size() * sizeof(float),
@@ -171,6 +177,11 @@ extern "C" int lbdem_export_recycle_fluid(lbdem_ctx* ctx, const char* path) {
   int rc = lbdem_download_lattice(ctx, type.data(), nullptr, nullptr, n.data(), u.data(),
                                   mass.data(), f.data());
   if (rc) return rc;
+  std::vector<double> viscN;
+  if (ctx->d.visc) {
+    viscN.resize(N);
+    if ((rc = lbdem_download_viscosity(ctx, viscN.data()))) return rc;
+  }
   std::FILE* out = std::fopen(path, "w");
   if (!out) return fail(ctx, LBDEM_ERR_IO, std::string("cannot write ") + path);
   const double rho0 = k.initDensity, visc = k.initVisc;
@@ -180,7 +191,7 @@ extern "C" int lbdem_export_recycle_fluid(lbdem_ctx* ctx, const char* path) {
   for (size_t x = 0; x < N; ++x) {
     if (type[x] != 0 && type[x] != 3) continue;
     std::fprintf(out, "%g %g %g %g %g %g ", n[x] - rho0, u[x], u[N + x], u[2 * N + x],
-                 mass[x] - rho0, visc);
+                 mass[x] - rho0, viscN.empty() ? visc : viscN[x]);
     for (int j = 0; j < Q; ++j) std::fprintf(out, "%g ", f[(size_t)j * N + x]);
     std::fputs("\n", out);
   }

@@ -65,6 +65,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "lbdem_download_lattice": ([c_ctx, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
         "lbdem_download_particles": ([c_ctx, C.POINTER(ParticleView)], C.c_int),
+        "lbdem_download_viscosity": ([c_ctx, C.c_void_p], C.c_int),
         "lbdem_download_objects": ([c_ctx, C.POINTER(ObjectView)], C.c_int),
         "lbdem_download_walls": ([c_ctx, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
                                  C.c_int),
@@ -218,6 +219,12 @@ class Solver:
         out["f"] = out["f"].reshape(19, N)
         return out
 
+    def viscosity(self) -> np.ndarray:
+        """Per-node viscosity (lattice units), 0 at non-active nodes."""
+        v = np.zeros(int(self.info.nodes))
+        self._check(self.lib.lbdem_download_viscosity(self.ctx, _ptr(v)), "download_viscosity")
+        return v
+
     def particles(self) -> dict:
         P = int(self.info.n_particles)
         names3 = ["x0", "x1", "w1", "FHydro", "MHydro", "FContact", "MContact", "FLub",
@@ -258,6 +265,7 @@ class Solver:
         """Everything, keyed like the oracle's state dumps."""
         d = {}
         d.update(self.lattice())
+        d["visc"] = self.viscosity()
         d.update(self.particles())
         d.update(self.objects())
         d.update(self.walls())

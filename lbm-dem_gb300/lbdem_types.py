@@ -53,6 +53,9 @@ class Config(C.Structure):
         ("n_particles", C.c_int32), ("particles", C.POINTER(ParticleIn)),
         ("n_objects", C.c_int32), ("objects", C.POINTER(ObjectIn)),
         ("n_bodies", C.c_int32), ("lbRestartFile", C.c_char_p),
+        ("rheologyModel", C.c_int32), ("plasticVisc", C.c_double),
+        ("yieldStress", C.c_double), ("frictionCoefFluid", C.c_double),
+        ("voellmyConstant", C.c_double),
     ]
 
 

@@ -144,6 +144,11 @@ struct oracle_ctx {
   int boundary[6] = {1, 1, 1, 1, 1, 1};
   double slipCoefficient = 0.0, fluidHeight = 0.0;
   double initDensity = 1.0, initDynVisc = 0.0;
+  // FluidMaterial's rheology (src/node.h:19-50), in lattice units
+  int rheology = LBDEM_NEWTONIAN;
+  double plasticVisc = 0.0, yieldStress = 0.0, frictionCoefFluid = 0.0, voellmyCoefficient = 0.0;
+  bool turbulenceOn = false;
+  double turbConst = 0.0;
   Vec initVelocity, lbF;
   unsigned lbTime = 0;
   std::vector<uint8_t> t, p, hasnode;
@@ -243,6 +248,51 @@ struct oracle_ctx {
       feq[j] = COEFF[j] * n[i] * (1.0 + 3.0 * vu + 4.5 * vu * vu - 1.5 * usq);
     }
   }
+  // node::computeApparentViscosity, src/node.cpp:113-168: the shear-rate
+  // tensor from the non-equilibrium populations, with the node's viscosity
+  // of the last step in tau; the model's apparent viscosity (plus the
+  // Smagorinsky term) clamped to the viscosities of tau 0.500001 and 1.8
+  // (src/lattice.h:26-27). Terms with c_a c_b = 0 add nothing (and leave
+  // every sum's bits as they are), c_a c_b = +-1 adds or subtracts.
+  void computeApparentViscosity(size_t i, const double* feq) {
+    const double minVisc = (0.500001 - 0.5) / 3.0;
+    const double maxVisc = (1.8 - 0.5) / 3.0;
+    const double tau = 0.5 + 3.0 * visc[i];
+    double g[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int j = 0; j < 19; ++j) {
+      const double d = F(j, i) - feq[j];
+      const int c[3] = {(int)V[j][0], (int)V[j][1], (int)V[j][2]};
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+          const int cc = c[a] * c[b];
+          if (cc > 0) g[3 * a + b] += d;
+          else if (cc < 0) g[3 * a + b] += -d;
+        }
+    }
+    const double sc = 1.5 / (tau * n[i]);
+    for (double& v : g) v *= sc;
+    const double mag = std::sqrt(0.5 * (g[0] * g[0] + g[4] * g[4] + g[8] * g[8] +
+                                        2.0 * (g[1] * g[3] + g[6] * g[2] + g[5] * g[7])));
+    const double shearRate = 2.0 * mag;
+    double nuApp = 0.0;
+    const Vec u = U(i);
+    if (rheology == LBDEM_BINGHAM) {
+      nuApp = plasticVisc + yieldStress / shearRate;
+    } else if (rheology == LBDEM_FRICTIONAL) {
+      const double pressure = std::max(0.0, 0.33333333 * (n[i] - 1.0));
+      nuApp = initDynVisc + frictionCoefFluid * pressure / shearRate;
+    } else if (rheology == LBDEM_VOELLMY) {
+      const double pressure = std::max(0.0, 0.33333333 * (n[i] - 1.0));
+      nuApp = (frictionCoefFluid * pressure + norm2(u) / voellmyCoefficient) / shearRate;
+    } else {
+      nuApp = initDynVisc;
+    }
+    if (turbulenceOn) {
+      const double nuTurb = turbConst * shearRate;
+      nuApp += nuTurb;
+    }
+    visc[i] = std::max(minVisc, std::min(maxVisc, nuApp));
+  }
   // node::bounceBackForce, src/node.cpp:306-314
   Vec bounceBackForce(size_t i, int j, const double* sp, double BBi) {
     return (2.0 * (FS(j, i) - sp[j]) - BBi) * vdir(j);
@@ -286,8 +336,8 @@ struct oracle_ctx {
 // ==== initialisation =======================================================
 
 int oracle_ctx::init(const lbdem_config* c) {
-  if (!c->rheologyNewtonian || c->turbulenceSolve || c->lbRestart || c->lbTopography) {
-    err = "only NEWTONIAN rheology without turbulence, restart or topography is supported";
+  if (c->lbRestart || c->lbTopography) {
+    err = "restart and topography are not supported";
     return LBDEM_ERR_INVALID;
   }
   if (c->n_bodies != 0) {
@@ -337,6 +387,15 @@ int oracle_ctx::init(const lbdem_config* c) {
   boundaryLoc[4] = Vec(0.0, 0.0, 0.5 * uLength);
   boundaryLoc[5] = Vec(0.0, 0.0, double(s[2] - 1.5) * uLength);
   initDynVisc = c->initVisc / uDynVisc;
+  // src/LB.cpp:240-326: rheology parameters in lattice units (turbConst is
+  // not scaled); unit.Stress = Density * Length^2 / Time^2 (src/node.cpp:522)
+  rheology = c->rheologyModel;
+  plasticVisc = c->plasticVisc / uDynVisc;
+  yieldStress = c->yieldStress / (uDensity * uLength * uLength / uTime / uTime);
+  frictionCoefFluid = c->frictionCoefFluid;
+  voellmyCoefficient = c->voellmyConstant / uAccel;
+  turbulenceOn = c->turbulenceSolve != 0;
+  turbConst = c->turbConst;
   initVelocity = Vec(c->initVelocity[0], c->initVelocity[1], c->initVelocity[2]) / uSpeed;
   lbF = Vec(c->lbF[0], c->lbF[1], c->lbF[2]) / uAccel;
   for (int k = 0; k < 6; ++k) boundary[k] = c->boundary[k];
@@ -781,6 +840,7 @@ void oracle_ctx::collision() {
     const Vec total = lbF + H(index);
     setU(index, U(index) + 0.5 * total / n[index]);
     computeEquilibrium(index, feq);
+    if (rheology != LBDEM_NEWTONIAN || turbulenceOn) computeApparentViscosity(index, feq);
     const double omega = 1.0 / (0.5 + 3.0 * visc[index]);
     for (int j = 0; j < 19; ++j) F(j, index) += omega * (feq[j] - F(j, index));
     const double omegaf = 1.0 - 1.0 / (1.0 + 6.0 * visc[index]);
@@ -1847,7 +1907,7 @@ void oracle_ctx::dump(const char* path) {
     std::vector<uint8_t> pf(p);
     std::vector<int32_t> sol(N);
     std::vector<double> nn(N, 0.0), vx(N, 0.0), vy(N, 0.0), vz(N, 0.0), mm(N, 0.0),
-        ff(19 * N, 0.0);
+        vs(N, 0.0), ff(19 * N, 0.0);
     for (size_t it = 0; it < N; ++it) {
       sol[it] = (int32_t)solid[it];
       if (hasnode[it] && isActive(it)) {
@@ -1856,6 +1916,7 @@ void oracle_ctx::dump(const char* path) {
         vy[it] = uy[it];
         vz[it] = uz[it];
         mm[it] = mass[it];
+        vs[it] = visc[it];
         for (int j = 0; j < 19; ++j) ff[(size_t)j * N + it] = f[(size_t)j * N + it];
       }
     }
@@ -1868,6 +1929,7 @@ void oracle_ctx::dump(const char* path) {
     w.d("uy", vy);
     w.d("uz", vz);
     w.d("mass", mm);
+    w.d("visc", vs);
     w.d("f", ff, {19, N});
   }
   const size_t P = particles.size();

@@ -63,7 +63,7 @@ void dumpState(const std::string& path, int step, LB& lb, DEM& dem) {
     std::vector<uint8_t> type(N), pflag(N), hasnode(N);
     std::vector<int32_t> solid(N);
     std::vector<double> n(N, 0.0), ux(N, 0.0), uy(N, 0.0), uz(N, 0.0),
-        mass(N, 0.0), f(19 * N, 0.0);
+        mass(N, 0.0), visc(N, 0.0), f(19 * N, 0.0);
     for (size_t it = 0; it < N; ++it) {
       type[it] = (uint8_t)lb.types[it].getType();
       pflag[it] = lb.types[it].isInsideParticle() ? 1 : 0;
@@ -76,6 +76,7 @@ void dumpState(const std::string& path, int step, LB& lb, DEM& dem) {
         uy[it] = nd->u.y;
         uz[it] = nd->u.z;
         mass[it] = nd->mass;
+        visc[it] = nd->visc;
         for (int j = 0; j < 19; ++j) f[(size_t)j * N + it] = nd->f[j];
       }
     }
@@ -88,6 +89,7 @@ void dumpState(const std::string& path, int step, LB& lb, DEM& dem) {
     w.d("uy", uy);
     w.d("uz", uz);
     w.d("mass", mass);
+    w.d("visc", visc);
     w.d("f", f, {19, N});
   }
   const size_t P = dem.particles.size();

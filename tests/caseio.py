@@ -163,8 +163,17 @@ class CaseConfig:
         c.lbSizeY = ks.d("lbSizeY", 0.0)
         c.lbSizeZ = ks.d("lbSizeZ", 0.0)
         rheo = ks.s("rheologyModel", "none")
-        c.rheologyNewtonian = 1 if rheo in ("NEWTONIAN", "none") else 0
-        c.initVisc = ks.d("initVisc", 1.0)
+        model = {"BINGHAM": 1, "FRICTIONAL": 2, "VOELLMY": 3}.get(rheo, 0)
+        c.rheologyModel = model
+        c.rheologyNewtonian = 1 if model == 0 else 0
+        c.initVisc = (1.0 - 0.5) / 3.0 if model == 1 else ks.d("initVisc", 1.0)
+        if model == 1:
+            c.plasticVisc = ks.d("plasticVisc", 0.0)
+            c.yieldStress = ks.d("yieldStress", 0.0)
+        if model in (2, 3):
+            c.frictionCoefFluid = ks.d("frictionCoefFluid", 0.0)
+        if model == 3:
+            c.voellmyConstant = ks.d("voellmyConstant", 1.0)
         c.turbulenceSolve = ks.i("turbulenceSolve", 0)
         c.turbConst = ks.d("turbConst", 0.0)
         for a, ax in enumerate("XYZ"):

@@ -43,6 +43,10 @@ CASES = {
     "c1": (100, 10, 1),
     "units_dyn": (60, 1, 1),
     "example": (20, 1, 10),
+    "rheo_bingham": (40, 1, 1),
+    "rheo_frictional": (40, 1, 1),
+    "rheo_voellmy": (40, 1, 1),
+    "rheo_turbulent": (40, 1, 1),
 }
 
 # The reference's own example input (example/input: unitLength 0.2,

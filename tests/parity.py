@@ -19,7 +19,7 @@ from __future__ import annotations
 
 import numpy as np
 
-LATTICE_FLOAT = ("f", "mass")
+LATTICE_FLOAT = ("f", "mass", "visc")
 PARTICLE_FLOAT = ("p_x0", "p_x1", "p_w1", "p_FHydro", "p_MHydro", "p_FContact", "p_MContact",
                   "p_FLub", "p_MLub", "p_FRep", "p_FTotal", "p_MTotal", "p_xiw", "p_xio",
                   "p_fluidVolume", "p_SHydro")
@@ -68,6 +68,8 @@ def compare(gpu: dict, orc: dict, rtol: float = 1e-10, lattice: bool = True,
             bad.append(f"solid: {int(np.sum(gpu['solid'] != orc['solid']))} nodes differ")
         act = (orc["type"] == 0) | (orc["type"] == 3)
         for k in LATTICE_FLOAT:
+            if k not in gpu or k not in orc:
+                continue
             sel = act if (fluid_mass or k != "mass") else (orc["type"] == 3)
             g = gpu[k][..., sel]
             o = orc[k][..., sel]

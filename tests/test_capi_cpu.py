@@ -69,6 +69,17 @@ def test_create_without_gpu_fails_loudly(lib):
     cfg.close()
 
 
+def test_mixed_form_refuses_a_per_node_viscosity(lib):
+    """Non-Newtonian rheology and the Smagorinsky term run in the plain FP64
+    form; the mixed form refuses them before any device use."""
+    import lbdem
+    for name in ("rheo_bingham", "rheo_turbulent"):
+        cfg = lbdem.LoadedConfig(os.path.join(GOLDEN, name, "parameters.cfg"))
+        with pytest.raises(RuntimeError, match="mixed form runs NEWTONIAN"):
+            lbdem.Solver(cfg, precision=lbdem.MIXED)
+        cfg.close()
+
+
 def test_unsupported_inputs_are_rejected_before_device_use(lib):
     import lbdem
     cfg = lbdem.LoadedConfig(os.path.join(GOLDEN, "tiny_direct", "parameters.cfg"),

@@ -29,7 +29,9 @@ def _pair(name):
     return cfg, lbdem.Solver(cfg, precision=lbdem.PLAIN_FP64), oracle_ffi.Oracle(cfg)
 
 
-@pytest.mark.parametrize("name", ["tiny_direct", "small_cells", "small_dup", "units_dyn"])
+@pytest.mark.parametrize("name", ["tiny_direct", "small_cells", "small_dup", "units_dyn",
+                                  "rheo_bingham", "rheo_frictional", "rheo_voellmy",
+                                  "rheo_turbulent"])
 def test_fp64_matches_oracle_every_step(name, lib, oracle_lib):
     cfg, gpu, orc = _pair(name)
     with tempfile.TemporaryDirectory() as tmp:

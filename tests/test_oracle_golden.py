@@ -58,6 +58,14 @@ def test_oracle_bitwise_equal_to_reference_config1(lib, oracle_lib, tmp_path):
     _run("c1", lib, oracle_lib, tmp_path)
 
 
+@pytest.mark.parametrize("name", ["rheo_bingham", "rheo_frictional", "rheo_voellmy",
+                                  "rheo_turbulent"])
+def test_oracle_bitwise_equal_to_reference_rheology(name, lib, oracle_lib, tmp_path):
+    """Bingham, frictional and Voellmy apparent viscosity and the Smagorinsky
+    term (node::computeApparentViscosity), per-node viscosity included."""
+    _run(name, lib, oracle_lib, tmp_path)
+
+
 def test_oracle_bitwise_equal_to_reference_example(lib, oracle_lib, tmp_path):
     """The reference's own example input in physical units (unitLength 0.2,
     unitTime 1e-3, 123x200x123 lattice, 962 spheres), 20 steps."""
