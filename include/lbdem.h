@@ -90,6 +90,17 @@ typedef struct lbdem_object_in {
   double v[3];
 } lbdem_object_in;
 
+/* One body as read from body.dat (src/DEM.cpp:168-196): a sphere joined to
+ * every impactor by a spring of stiffness k and rest length L0 along y
+ * (DEM::bodyObjectInteraction, src/DEM.cpp:798-869). */
+typedef struct lbdem_body_in {
+  int32_t index;
+  double r;
+  double x[3]; /* position, times scale */
+  double v[3];
+  double k, L0;
+} lbdem_body_in;
+
 /* Every configuration key of parameters.cfg the step depends on, with the
  * reference's names (src/main.cpp:128-185, src/LB.cpp:128-338,
  * src/DEM.cpp:17-78). Unsupported keys (topography, rotation,
@@ -145,6 +156,8 @@ typedef struct lbdem_config {
    * node::computeApparentViscosity (src/node.cpp:113-168). */
   int32_t rheologyModel;
   double plasticVisc, yieldStress, frictionCoefFluid, voellmyConstant;
+  /* body.dat records (n_bodies of them) */
+  const lbdem_body_in* bodies;
 } lbdem_config;
 
 /* Run options that are not part of the reference's configuration. */
@@ -238,6 +251,12 @@ int lbdem_get_info(lbdem_ctx* ctx, lbdem_info* info);
 int lbdem_download_lattice(lbdem_ctx* ctx, uint8_t* type, uint8_t* pflag,
                            int32_t* solid, double* n, double* u, double* mass,
                            double* f);
+
+/* Body state [B][3] (physical units): position, velocity, spring force
+ * and total force of the last DEM step, and the spring length L of
+ * DEM::bodyObjectInteraction [B]. Any pointer may be NULL. */
+int lbdem_download_bodies(lbdem_ctx* ctx, double* x0, double* x1, double* FSpring,
+                          double* FTotal, double* L);
 
 /* Viscosity of every node in lattice units, visc[N]: node::visc
  * (src/node.h:54-114), which LB::collision updates per node for

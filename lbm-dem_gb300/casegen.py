@@ -98,12 +98,15 @@ class Case:
     ``particles`` rows: r, x, y, z, vx, vy, vz, wx, wy, wz (physical units,
     positions as they should be *after* the reader's -0.05 shift).
     ``objects`` rows: r, x, y, z, vx, vy, vz.
+    ``bodies`` rows: r, x, y, z, vx, vy, vz, k, L0 (body.dat,
+    src/DEM.cpp:168-196).
     """
 
     params: dict[str, str] = field(default_factory=lambda: dict(DEFAULT_PARAMS))
     particles: np.ndarray = field(default_factory=lambda: np.zeros((0, 10)))
     objects: np.ndarray = field(default_factory=lambda: np.zeros((0, 7)))
     name: str = "case"
+    bodies: np.ndarray = field(default_factory=lambda: np.zeros((0, 9)))
 
     @property
     def lattice(self) -> tuple[int, int, int]:
@@ -131,7 +134,9 @@ class Case:
             for i, row in enumerate(self.objects):
                 fh.write(f"{i} " + " ".join(f"{float(a):.17g}" for a in row) + "\n")
         with open(os.path.join(directory, "input", "body.dat"), "w") as fh:
-            fh.write("0\n")
+            fh.write(f"{len(self.bodies)}\n")
+            for i, row in enumerate(self.bodies):
+                fh.write(f"{i} " + " ".join(f"{float(a):.17g}" for a in row) + "\n")
         return cfg
 
 
@@ -504,6 +509,20 @@ def named_case(name: str, seed: int = 1) -> Case:
         ov.update(rheo[name])
         return impact_case((28, 40, 28), 27.0, 16, (3.0, 3.4), 5.0, 32.0,
                            -0.08, 5.0, 0.8, 1.0e-4, seed, overrides=ov, name=name)
+    if name in ("bodies", "bodies_lj"):
+        # two bodies above the impactor, each joined to it by a spring along y
+        # (DEM::bodyObjectInteraction): spring-dashpot-cubic (nonLinType 2)
+        # or spring-dashpot with the repulsive Lennard-Jones term (nonLinType 3)
+        lj = name == "bodies_lj"
+        ov = {"objWaitTime": "3", "bodyDensity": "5.0", "springDamp": "0.1",
+              "nonLinType": "3" if lj else "2", "k13": "0.5", "epsilon": "1.0e-3"}
+        c = impact_case((28, 40, 28), 27.0, 16, (3.0, 3.4), 5.0, 32.0,
+                        -0.08, 5.0, 0.8, 1.0e-4, seed, overrides=ov, name=name)
+        ox, oy, oz = c.objects[0, 1:4]
+        L0 = 4.0 if lj else 9.0
+        c.bodies = np.array([[2.0, ox, oy + 10.0, oz, 0.0, 0.0, 0.0, 2.0e-3, L0],
+                             [1.5, ox + 1.0, oy + 12.0, oz, 0.0, 0.01, 0.0, 1.0e-3, L0 + 3.0]])
+        return c
     if name == "units_dyn":
         # a cell-list case in physical units (unitLength 0.5, unitTime 0.02,
         # unitDensity 1000), with boundary0 = 8: every wall is a moving

@@ -323,7 +323,25 @@ extern "C" int lbdem_config_load(const char* cfg_path, const char* input_dir,
     }
     unsigned tot = 0;
     in >> tot;
+    auto* bs = new lbdem_body_in[tot ? tot : 1]();
+    for (unsigned n = 0; n < tot; ++n) {
+      lbdem_body_in& b = bs[n];
+      unsigned idx = 0;
+      double x0, y0, z0;
+      in >> idx >> b.r >> x0 >> y0 >> z0 >> b.v[0] >> b.v[1] >> b.v[2] >> b.k >> b.L0;
+      b.index = (int32_t)idx;
+      b.x[0] = x0 * scale;
+      b.x[1] = y0 * scale;
+      b.x[2] = z0 * scale;
+      if (!in) {
+        delete[] bs;
+        lbdem_config_release(c);
+        setErr(err, err_len, "malformed body.dat");
+        return LBDEM_ERR_IO;
+      }
+    }
     c->n_bodies = (int32_t)tot;
+    c->bodies = bs;
   }
   return LBDEM_OK;
 }
@@ -333,6 +351,9 @@ extern "C" void lbdem_config_release(lbdem_config* c) {
   delete[] c->particles;
   delete[] c->objects;
   delete[] c->lbRestartFile;
+  delete[] c->bodies;
+  c->bodies = nullptr;
+  c->n_bodies = 0;
   c->particles = nullptr;
   c->objects = nullptr;
   c->lbRestartFile = nullptr;

@@ -455,18 +455,94 @@ enum { GA_OBJ = 0, GA_WALL = GA_OBJ + 12 * MAX_OBJ, GA_N = GA_WALL + 6 * MAX_WAL
 // and wall sums are in. The record is read with ld.global.cg (past L1, so
 // no line this block cached earlier in the kernel can be stale) in one batch
 // of independent loads, then written back.
+// The bodies' part of a DEM step, by one thread in the reference's loop
+// order: the resets of evaluateForces (src/DEM.cpp:688-713), from objWaitTime
+// on the springs of DEM::bodyObjectInteraction (:798-869, into the objects'
+// FSpring, before their totals), the bodies' totals (:792-794) and from
+// objWaitTime on their integration (:2730-2739).
+static __device__ __noinline__ void demBodies(const Consts& k, const DemArgs& a, int stepNo) {
+  for (int o = 0; o < k.nObj; ++o)
+    for (int c = 0; c < 3; ++c) a.obj[o * OB_STRIDE + OB_FSPRING + c] = 0.0;
+  for (int b = 0; b < k.nBody; ++b)
+    for (int c = 0; c < 3; ++c) a.body[b * BD_STRIDE + BD_FSPRING + c] = 0.0;
+  if (stepNo >= k.objWaitTime)
+    for (int b = 0; b < k.nBody; ++b) {
+      double* bd = a.body + b * BD_STRIDE;
+      for (int o = 0; o < k.nObj; ++o) {
+        double* ob = a.obj + o * OB_STRIDE;
+        double fs = 0.0, fdo = 0.0, fdb = 0.0;
+        bd[BD_L] = bd[BD_X0 + 1] - ob[OB_X0 + 1];
+        const double rx = bd[BD_X0] - ob[OB_X0], ry = bd[BD_X0 + 1] - ob[OB_X0 + 1],
+                     rz = bd[BD_X0 + 2] - ob[OB_X0 + 2];
+        const double rn = sqrt(rx * rx + ry * ry + rz * rz);
+        const double ny = ry / rn;
+        const double del = bd[BD_L0] - bd[BD_L];
+        const double kb = bd[BD_K];
+        const double bodyDamp = 2.0 * sqrt(bd[BD_M] * kb) * k.springDamp;
+        const double objDamp = 2.0 * sqrt(ob[OB_MASS] * kb) * k.springDamp;
+        const double sigma = bd[BD_R];
+        if (k.nonLinType == 0) {  // spring
+          fs = kb * del * ny;
+        } else if (k.nonLinType >= 1 && k.nonLinType <= 4) {
+          if (k.nonLinType == 1) {  // spring-dashpot
+            fs = (kb * del) * ny;
+          } else if (k.nonLinType == 2) {  // spring-dashpot-cubic
+            fs = (kb * del + k.k13 * kb * (del * del * del)) * ny;
+          } else if (k.nonLinType == 3) {  // spring-dashpot-repLJ
+            fs = (kb * del + (24.0 * k.epsilon / rn) * 2.0 * pow(sigma / rn, 12.0)) * ny;
+          } else {  // spring-dashpot-WCA
+            const double wcacut = pow(2.0, 1.0 / 6.0) * sigma;
+            if (rn <= wcacut)
+              fs = (kb * del + (24.0 * k.epsilon / rn) *
+                                   (2.0 * pow(sigma / rn, 12.0) - pow(sigma / rn, 6.0))) *
+                   ny;
+            else
+              fs = (kb * del) * ny;
+          }
+          fdo = -ob[OB_X1 + 1] * objDamp;
+          fdb = -bd[BD_X1 + 1] * bodyDamp;
+        }
+        ob[OB_FSPRING + 1] -= fs;
+        bd[BD_FSPRING + 1] += fs;
+        ob[OB_FSPRING + 1] += fdo;
+        bd[BD_FSPRING + 1] += fdb;
+      }
+    }
+  const double dtt = k.dt;
+  for (int b = 0; b < k.nBody; ++b) {
+    double* bd = a.body + b * BD_STRIDE;
+    double FT[3];
+    for (int c = 0; c < 3; ++c) {
+      FT[c] = 0.0 + (bd[BD_FGRAV + c] + bd[BD_FSPRING + c]);
+      bd[BD_FTOTAL + c] = FT[c];
+    }
+    if (stepNo >= k.objWaitTime) {
+      const double invm = bd[BD_INVM];
+      for (int c = 0; c < 3; ++c) {
+        bd[BD_X0 + c] = bd[BD_X0 + c] + (dtt * bd[BD_X1 + c] + dtt * dtt * FT[c] * invm);
+        bd[BD_X1 + c] = bd[BD_X1 + c] + dtt * FT[c] * invm;
+      }
+    }
+  }
+}
+
 __device__ __forceinline__ void demObjectsTail(const Consts& k, const DemArgs& a) {
   const int stepNo = a.iscal[IS_DEMSTEP];
+  if (k.nBody > 0) {  // uniform over the block
+    if (threadIdx.x == 0) demBodies(k, a, stepNo);
+    __syncthreads();
+  }
   const int o = threadIdx.x;
   if (o < k.nObj) {
     double* ob = a.obj + o * OB_STRIDE;
-    double FH[3], FC[3], FL[3], FG[3], MH[3], MC[3], ML[3], X0[3], X1[3], W1[3];
+    double FH[3], FC[3], FL[3], FG[3], FS[3], MH[3], MC[3], ML[3], X0[3], X1[3], W1[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       FH[c] = __ldcg(ob + OB_FHYDRO + c);
       FC[c] = __ldcg(ob + OB_FCONTACT + c);
       FL[c] = __ldcg(ob + OB_FLUB + c);
       FG[c] = __ldcg(ob + OB_FGRAV + c);
+      FS[c] = k.nBody > 0 ? __ldcg(ob + OB_FSPRING + c) : 0.0;
       MH[c] = __ldcg(ob + OB_MHYDRO + c);
       MC[c] = __ldcg(ob + OB_MCONTACT + c);
       ML[c] = __ldcg(ob + OB_MLUB + c);
@@ -479,7 +555,7 @@ __device__ __forceinline__ void demObjectsTail(const Consts& k, const DemArgs& a
     double FT[3], MT[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      FT[c] = 0.0 + ((((FH[c] + FC[c]) + FL[c]) + FG[c]) + 0.0);
+      FT[c] = 0.0 + ((((FH[c] + FC[c]) + FL[c]) + FG[c]) + FS[c]);
       MT[c] = 0.0 + ((MH[c] + MC[c]) + ML[c]);
       ob[OB_FTOTAL + c] = FT[c];
       ob[OB_MTOTAL + c] = MT[c];

@@ -85,6 +85,7 @@ struct DemArgs {
   double* scal;
   int* iscal;
   unsigned long long* uscal;
+  double* body;
 };
 
 // Pointers of one run's coupling kernels (impactor uncover and voxelisation,

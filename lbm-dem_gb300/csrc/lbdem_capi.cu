@@ -212,6 +212,7 @@ DemArgs demArgs(lbdem_ctx* c) {
   a.scal = d.scal;
   a.iscal = d.iscal;
   a.uscal = d.uscal;
+  a.body = d.body;
   return a;
 }
 
@@ -268,7 +269,8 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
     return setErr(ctx, LBDEM_ERR_INVALID,
                   "the mixed form runs NEWTONIAN rheology without turbulence; runs with a "
                   "per-node viscosity use the plain FP64 form");
-  if (cfg->n_bodies != 0) return setErr(ctx, LBDEM_ERR_INVALID, "bodies are not supported");
+  if (cfg->n_bodies < 0 || cfg->n_bodies > MAX_BODY || (cfg->n_bodies > 0 && !cfg->bodies))
+    return setErr(ctx, LBDEM_ERR_INVALID, "at most 8 bodies, with their body.dat records");
   for (int i = 0; i < 6; ++i)
     if (cfg->boundary[i] != 7 && cfg->boundary[i] != 8)
       return setErr(ctx, LBDEM_ERR_INVALID, "only no-slip walls (boundary types 7/8)");
@@ -431,10 +433,37 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
       ob[OB_FGRAV + a] = demF[a] * m;
     }
     ob[OB_R] = r;
+    ob[OB_MASS] = m;
     ob[OB_INVM] = 1.0 / m;
     ob[OB_INVI] = 1.0 / I;
     ob[OB_INDEX] = (double)in.index;
     ctx->objIndexField[o] = in.index;
+  }
+  // bodies, src/DEM.cpp:257-266
+  const int B = cfg->n_bodies;
+  ctx->nBody = B;
+  k.nBody = B;
+  k.nonLinType = cfg->nonLinType;
+  k.springDamp = cfg->springDamp;
+  k.k13 = cfg->k13;
+  k.epsilon = cfg->epsilon;
+  std::vector<double> hbody((size_t)std::max(B, 1) * BD_STRIDE, 0.0);
+  for (int b = 0; b < B; ++b) {
+    const lbdem_body_in& in = cfg->bodies[b];
+    double* bd = &hbody[(size_t)b * BD_STRIDE];
+    const double r = in.r;
+    const double m = cfg->bodyDensity * (4.0 / 3.0) * PI_D * (r * r * r);
+    for (int a = 0; a < 3; ++a) {
+      bd[BD_X0 + a] = in.x[a];
+      bd[BD_X1 + a] = in.v[a];
+      bd[BD_FGRAV + a] = demF[a] * m;
+    }
+    bd[BD_R] = r;
+    bd[BD_M] = m;
+    bd[BD_INVM] = 1.0 / m;
+    bd[BD_K] = in.k;
+    bd[BD_L0] = in.L0;
+    bd[BD_L] = in.L0;
   }
   // walls (DEM::initializeWalls: slip/moving flags of boundary[0] for all)
   std::vector<DeviceWall> hw;
@@ -576,6 +605,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   AL(d.cellFill, (size_t)MAX_L);
   AL(d.cellParts, P1);
   AL(d.obj, (size_t)std::max(O, 1) * OB_STRIDE);
+  AL(d.body, (size_t)std::max(B, 1) * BD_STRIDE);
   AL(d.wallF, (size_t)MAX_WALL * 12);
   AL(d.walls, (size_t)MAX_WALL);
   AL(d.uncover, (size_t)UNCOVER_CAP);
@@ -599,6 +629,8 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   CK(cudaMemcpyAsync(d.pinvI, hinvI.data(), P * sizeof(double), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d.pFGrav, hFG.data(), 3 * P * sizeof(double), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d.obj, hobj.data(), hobj.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.body, hbody.data(), hbody.size() * sizeof(double), cudaMemcpyHostToDevice,
+                     st));
   if (!hw.empty()) {
     CK(cudaMemcpyAsync(d.walls, hw.data(), hw.size() * sizeof(DeviceWall), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dWallType, hwt.data(), hwt.size() * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -980,8 +1012,8 @@ void lbdemJobArgs(lbdem_ctx* c, int cur, JobArgs* j) {
 // conditions) with the DEM, lattice and coupling steps all on; two such runs
 // share a batch when their switches match (batchKey).
 bool lbdemBatchable(const lbdem_ctx* c) {
-  // runs with a per-node viscosity keep their own launches
-  return c->demSolve && c->lbSolve && pairReplayable(c) && !c->k.visc;
+  // runs with a per-node viscosity or bodies keep their own launches
+  return c->demSolve && c->lbSolve && pairReplayable(c) && !c->k.visc && c->nBody == 0;
 }
 int lbdemBatchKey(const lbdem_ctx* c) {
   return c->precision | (c->freeSurface ? 2 : 0) | (c->nObj > 0 ? 4 : 0) | (c->nWall > 0 ? 8 : 0);
@@ -1199,6 +1231,7 @@ extern "C" int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t prec
   for (int i = 0; i < 3; ++i) add(MAX_L, 4);   // cell arrays
   add(P1, 4);                                  // cellParts
   add(O1 * OB_STRIDE, 8);
+  add((long long)std::max(cfg->n_bodies, 1) * BD_STRIDE, 8);
   add(MAX_WALL * 12, 8);
   add(MAX_WALL, (long long)sizeof(DeviceWall));
   add(UNCOVER_CAP, 4);
@@ -1351,6 +1384,27 @@ extern "C" int lbdem_download_objects(lbdem_ctx* ctx, const lbdem_object_view* v
     if (e.dst)
       for (int o = 0; o < O; ++o)
         for (int c = 0; c < 3; ++c) e.dst[3 * o + c] = h[(size_t)o * OB_STRIDE + e.off + c];
+  return LBDEM_OK;
+}
+
+extern "C" int lbdem_download_bodies(lbdem_ctx* ctx, double* x0, double* x1, double* FSpring,
+                                     double* FTotal, double* L) {
+  if (!ctx) return LBDEM_ERR_INVALID;
+  DeviceScope devScope(ctx->device);
+  int rc = lbdem_sync(ctx);
+  if (rc) return rc;
+  const int B = ctx->nBody;
+  if (B == 0) return LBDEM_OK;
+  std::vector<double> h((size_t)B * BD_STRIDE);
+  CK(cudaMemcpy(h.data(), ctx->d.body, h.size() * 8, cudaMemcpyDeviceToHost));
+  const struct { double* dst; int off; } m[] = {
+      {x0, BD_X0}, {x1, BD_X1}, {FSpring, BD_FSPRING}, {FTotal, BD_FTOTAL}};
+  for (const auto& e : m)
+    if (e.dst)
+      for (int b = 0; b < B; ++b)
+        for (int q = 0; q < 3; ++q) e.dst[3 * b + q] = h[(size_t)b * BD_STRIDE + e.off + q];
+  if (L)
+    for (int b = 0; b < B; ++b) L[b] = h[(size_t)b * BD_STRIDE + BD_L];
   return LBDEM_OK;
 }
 

@@ -17,6 +17,7 @@ constexpr int MAX_N = 50;        // neighbour-list slots, src/DEM.cpp:476
 constexpr int MAX_L = 100000;    // cell-list cells,     src/DEM.cpp:479
 constexpr int MAX_OBJ = 8;       // impactors handled on the device
 constexpr int MAX_WALL = 6;
+constexpr int MAX_BODY = 8;      // bodies (body.dat) handled on the device
 constexpr int PAIR_VALS = 18;    // per neighbour slot: contact(6) lub(9) rep(3)
 constexpr int UNCOVER_CAP = 8192;// uncovered object nodes resolved per step
 constexpr int ACCF_N = 13;       // mixed-form particle sums: d(3), r (x) d (9), mass(1)
@@ -87,6 +88,9 @@ struct Consts {
   int rheo, turbulence;
   double plasticVisc, yieldStress, frictionCoef, voellmyCoef, turbConst;
   double* visc;
+  // bodies and their springs to the impactors (DEM::bodyObjectInteraction)
+  int nBody, nonLinType;
+  double springDamp, k13, epsilon;
 };
 
 struct DeviceWall {
@@ -140,6 +144,7 @@ struct Device {
   int* cellParts = nullptr;              // [P]
   // objects / walls (small)
   double* obj = nullptr;                 // see OB_* layout, [nObj][OB_STRIDE]
+  double* body = nullptr;                // see BD_* layout, [nBody][BD_STRIDE]
   double* wallF = nullptr;               // [W][12]: FHydro FContact FLub FTotal
   DeviceWall* walls = nullptr;
   uint32_t* uncover = nullptr;           // [UNCOVER_CAP] candidate list
@@ -195,7 +200,16 @@ enum {
   OB_X0 = 0, OB_X1 = 3, OB_W1 = 6, OB_R = 9, OB_INVM = 10, OB_INVI = 11,
   OB_FHYDRO = 12, OB_MHYDRO = 15, OB_FCONTACT = 18, OB_MCONTACT = 21,
   OB_FLUB = 24, OB_MLUB = 27, OB_FGRAV = 30, OB_FTOTAL = 33, OB_MTOTAL = 36,
-  OB_X0PREV = 39, OB_INDEX = 42, OB_STRIDE = 44
+  OB_X0PREV = 39, OB_INDEX = 42,
+  OB_MASS = 44,     // object::m (the body springs' damping)
+  OB_FSPRING = 45,  // object::FSpring, set by the body springs
+  OB_STRIDE = 48
+};
+
+// body record layout (doubles), src/elmt.h:231-258
+enum {
+  BD_X0 = 0, BD_X1 = 3, BD_R = 6, BD_M = 7, BD_INVM = 8, BD_K = 9, BD_L0 = 10, BD_L = 11,
+  BD_FGRAV = 12, BD_FSPRING = 15, BD_FTOTAL = 18, BD_STRIDE = 24
 };
 
 }  // namespace lbdem
@@ -272,7 +286,7 @@ struct lbdem_ctx {
   long long demTimeStep = 0, lbTime = 0;
   bool lbFReset = false;  // lbF reset by the first collision when !forceField
   double lbFConfig[3] = {0, 0, 0};
-  int nPart = 0, nObj = 0, nWall = 0;
+  int nPart = 0, nObj = 0, nWall = 0, nBody = 0;
   double fluidHeight = 0.0;     // physical, as the configuration gives it
   lbdem_output* out = nullptr;  // open screen-phase output files, if any
   bool stressNext = false;      // the next DEM step forms the stress sums

@@ -37,8 +37,9 @@
 // the DEM volume: the total as xx yy zz and the mean off-diagonal pairs
 // (tinyMatrix::print, src/myvector.cpp:382-392), the hydrodynamic,
 // lubrication, contact and electrostatic parts as their normal and shear
-// triples. bodyPosition.dat has only its header, as in the reference for a
-// run without bodies.
+// triples. bodyPosition.dat gets one line per body (IO::exportBodyPosition,
+// src/IO.cpp:1340-1352: position, tab, velocity, tab, spring length L) after
+// the impactor lines of a run with bodies, and only its header otherwise.
 #include <cuda_runtime.h>
 #include <sys/stat.h>
 
@@ -64,6 +65,8 @@ struct lbdem_output {
   bool dem = false;
   std::FILE* fExport = nullptr;
   std::FILE* fPos = nullptr;
+  std::FILE* fBody = nullptr;  // bodyPosition.dat, open while the run has bodies
+  int nBody = 0;
   std::FILE* fForce = nullptr;
   std::FILE* fWall = nullptr;
   std::FILE* fStress = nullptr;
@@ -184,6 +187,16 @@ void writeSlot(lbdem_output* o, const lbdem_output::Slot& s, const double* rec) 
       }
     }
   }
+  if (o->dem && o->nBody > 0) {
+    const double* bd0 = rec + (size_t)o->nObj * OB_STRIDE + (size_t)o->nWall * 12 + STRESS_N;
+    for (int b = 0; b < o->nBody; ++b) {
+      const double* bd = bd0 + (size_t)b * BD_STRIDE;
+      vec(o->fBody, bd + BD_X0);
+      std::fputs("\t", o->fBody);
+      vec(o->fBody, bd + BD_X1);
+      std::fprintf(o->fBody, "\t%g\n", bd[BD_L]);
+    }
+  }
   if (o->dem && o->nWall > 0) {
     const double* wf = rec + (size_t)o->nObj * OB_STRIDE;
     for (int w = 0; w < o->nWall; ++w) {
@@ -255,6 +268,10 @@ int capture(lbdem_ctx* ctx) {
     e = cudaMemcpyAsync(dst + (size_t)o->nObj * OB_STRIDE + (size_t)o->nWall * 12,
                         ctx->d.stress, STRESS_N * sizeof(double), cudaMemcpyDeviceToHost,
                         ctx->stream);
+  if (e == cudaSuccess && o->dem && o->nBody > 0)
+    e = cudaMemcpyAsync(dst + (size_t)o->nObj * OB_STRIDE + (size_t)o->nWall * 12 + STRESS_N,
+                        ctx->d.body, (size_t)o->nBody * BD_STRIDE * sizeof(double),
+                        cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaEventRecord(o->slots[k].ev, ctx->stream);
   if (e != cudaSuccess)
     return fail(ctx, LBDEM_ERR_CUDA, std::string("output copy: ") + cudaGetErrorString(e));
@@ -348,8 +365,8 @@ void lbdemOutputFree(lbdem_ctx* ctx) {
   for (auto& s : o->slots)
     if (s.ev) cudaEventDestroy(s.ev);
   if (o->pinned) cudaFreeHost(o->pinned);
-  for (std::FILE* f : {o->fExport, o->fPos, o->fForce, o->fWall, o->fStress, o->fNormal,
-                       o->fShear})
+  for (std::FILE* f : {o->fExport, o->fPos, o->fBody, o->fForce, o->fWall, o->fStress,
+                       o->fNormal, o->fShear})
     if (f) std::fclose(f);
   delete o;
   ctx->out = nullptr;
@@ -370,7 +387,9 @@ extern "C" int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_
   o->dem = ctx->demSolve;
   o->nObj = ctx->nObj;
   o->nWall = ctx->nWall;
-  o->slotDoubles = (size_t)o->nObj * OB_STRIDE + (size_t)o->nWall * 12 + STRESS_N;
+  o->nBody = ctx->demSolve ? ctx->nBody : 0;
+  o->slotDoubles = (size_t)o->nObj * OB_STRIDE + (size_t)o->nWall * 12 + STRESS_N +
+                   (size_t)o->nBody * BD_STRIDE;
   o->vol = ctx->k.demSize[0] * ctx->k.demSize[1] * ctx->k.demSize[2];
   // realTime of the cycles already run, summed as goCycle sums it
   for (long long i = 0; i < ctx->lbTime; ++i) o->realTime += o->unitTime;
@@ -407,7 +426,8 @@ extern "C" int lbdem_output_open(lbdem_ctx* ctx, const char* dir, double screen_
                                "hydro-xy hydro-yz hydro-zx lub-xy lub-yz lub-zx contact-xy "
                                "contact-yz contact-zx rep-xy rep-yz rep-zx \n");
     ok = ok && o->fPos && body && o->fForce && o->fWall && o->fStress && o->fNormal && o->fShear;
-    if (body) std::fclose(body);
+    if (body && o->nBody > 0) o->fBody = body;
+    else if (body) std::fclose(body);
   }
   if (!ok) {
     lbdemOutputFree(ctx);

@@ -66,6 +66,8 @@ def load_library(path: str | None = None) -> C.CDLL:
                                     C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
         "lbdem_download_particles": ([c_ctx, C.POINTER(ParticleView)], C.c_int),
         "lbdem_download_viscosity": ([c_ctx, C.c_void_p], C.c_int),
+        "lbdem_download_bodies": ([c_ctx, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p], C.c_int),
         "lbdem_download_objects": ([c_ctx, C.POINTER(ObjectView)], C.c_int),
         "lbdem_download_walls": ([c_ctx, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
                                  C.c_int),
@@ -158,6 +160,7 @@ class Solver:
                 self.ctx = None
             raise RuntimeError(f"lbdem_create: {ERRORS.get(rc, rc)}: {msg}")
         self.info = self.get_info()
+        self.n_bodies = int(config.cfg.n_bodies)
 
     def _check(self, rc: int, what: str):
         if rc != 0:
@@ -219,6 +222,16 @@ class Solver:
         out["f"] = out["f"].reshape(19, N)
         return out
 
+    def bodies(self) -> dict:
+        """Body state: b_x0, b_x1, b_FSpring, b_FTotal [B][3], b_L [B]."""
+        B = self.n_bodies
+        out = {k: np.zeros((B, 3)) for k in ("b_x0", "b_x1", "b_FSpring", "b_FTotal")}
+        out["b_L"] = np.zeros(B)
+        self._check(self.lib.lbdem_download_bodies(
+            self.ctx, _ptr(out["b_x0"]), _ptr(out["b_x1"]), _ptr(out["b_FSpring"]),
+            _ptr(out["b_FTotal"]), _ptr(out["b_L"])), "download_bodies")
+        return out
+
     def viscosity(self) -> np.ndarray:
         """Per-node viscosity (lattice units), 0 at non-active nodes."""
         v = np.zeros(int(self.info.nodes))
@@ -269,6 +282,8 @@ class Solver:
         d.update(self.particles())
         d.update(self.objects())
         d.update(self.walls())
+        if self.n_bodies:
+            d.update(self.bodies())
         info = self.get_info()
         d["step"] = np.array([info.time_step])
         d["demTime"] = np.array([info.dem_time])

@@ -22,6 +22,11 @@ class ObjectIn(C.Structure):
                 ("v", C.c_double * 3)]
 
 
+class BodyIn(C.Structure):
+    _fields_ = [("index", C.c_int32), ("r", C.c_double), ("x", C.c_double * 3),
+                ("v", C.c_double * 3), ("k", C.c_double), ("L0", C.c_double)]
+
+
 class Config(C.Structure):
     _fields_ = [
         ("demSolve", C.c_int32), ("lbSolve", C.c_int32),
@@ -55,7 +60,7 @@ class Config(C.Structure):
         ("n_bodies", C.c_int32), ("lbRestartFile", C.c_char_p),
         ("rheologyModel", C.c_int32), ("plasticVisc", C.c_double),
         ("yieldStress", C.c_double), ("frictionCoefFluid", C.c_double),
-        ("voellmyConstant", C.c_double),
+        ("voellmyConstant", C.c_double), ("bodies", C.POINTER(BodyIn)),
     ]
 
 

@@ -119,6 +119,13 @@ struct Object {
   Vec FContact, FHydro, FLub, FGrav, FSpring, FTotal;
   Vec MContact, MHydro, MTotal, MLub;
 };
+// body, src/elmt.h:231-258
+struct Body {
+  unsigned index = 0;
+  double r = 1.0, m = 1.0, _m = 1.0, L0 = 1.0, L = 1.0, k = 1.0;
+  Vec x0, x1;
+  Vec FGrav, FSpring, FTotal;
+};
 struct Wall {
   unsigned index = 0;
   Vec n{1, 0, 0}, p;
@@ -164,6 +171,9 @@ struct oracle_ctx {
          frictionCoefPart = 0, lubNormal = 0, lubTangential = 0, lubRotation = 0,
          lubCutoff = 0, kinVisc = 0, electroForce = 0, debyeLength = 0;
   Vec demF;
+  std::vector<Body> bodies;
+  double bodyDensity = 0.0, springDamp = 0.0, k13 = 0.0, epsilon = 0.0;
+  int nonLinType = 0;
   double maxDisp = 0.0, minPartRadius = 0, maxPartRadius = 0, meanPartRadius = 0;
   bool newNeighborList = false;
   std::vector<Particle> particles;
@@ -322,6 +332,7 @@ struct oracle_ctx {
   void neighborList();
   void evaluateForces();
   void integration();
+  void bodyObjectInteraction();
   void particleContact();
   void particleLubrication();
   void particleElectro();
@@ -340,10 +351,22 @@ int oracle_ctx::init(const lbdem_config* c) {
     err = "restart and topography are not supported";
     return LBDEM_ERR_INVALID;
   }
-  if (c->n_bodies != 0) {
-    err = "bodies are not supported";
-    return LBDEM_ERR_INVALID;
+  bodies.resize(c->n_bodies);
+  for (int b = 0; b < c->n_bodies; ++b) {  // DEM::discreteElementGet, src/DEM.cpp:168-196
+    const lbdem_body_in& in = c->bodies[b];
+    Body& d = bodies[b];
+    d.index = (unsigned)in.index;
+    d.r = in.r;
+    d.x0 = Vec(in.x[0], in.x[1], in.x[2]);
+    d.x1 = Vec(in.v[0], in.v[1], in.v[2]);
+    d.k = in.k;
+    d.L0 = in.L0;
   }
+  bodyDensity = c->bodyDensity;
+  springDamp = c->springDamp;
+  nonLinType = c->nonLinType;
+  k13 = c->k13;
+  epsilon = c->epsilon;
   for (int k = 0; k < 6; ++k)
     if (c->boundary[k] == 4 || c->boundary[k] == 9 || c->boundary[k] == 1) {
       err = "periodic/cylinder boundaries are not supported";
@@ -480,6 +503,12 @@ void oracle_ctx::demInit() {
     o.I = 2.0 / 5.0 * o.m * o.r * o.r;
     o._m = 1.0 / o.m;
     o._I = 1.0 / o.I;
+  }
+  for (Body& b : bodies) {  // src/DEM.cpp:257-266
+    b.m = bodyDensity * (4.0 / 3.0) * PI * (b.r * b.r * b.r);
+    b._m = 1.0 / b.m;
+    b.FGrav = demF * b.m;
+    b.L = b.L0;
   }
   // DEM::initializeWalls, src/DEM.cpp:405-458
   const Vec dirs[6] = {Vec(1, 0, 0), Vec(-1, 0, 0), Vec(0, 1, 0),
@@ -1247,7 +1276,9 @@ void oracle_ctx::evaluateForces() {
     o.MTotal = o.MContact = o.MLub = Vec();
   }
   for (Wall& w : walls) w.FTotal = w.FContact = w.FLub = w.FRep = Vec();
+  for (Body& b : bodies) b.FTotal = b.FSpring = Vec();
   if ((int)demTimeStep >= objWaitTime) {
+    if (!bodies.empty()) bodyObjectInteraction();
     particleLubrication();
     wallLubrication();
     objectContact();
@@ -1269,6 +1300,53 @@ void oracle_ctx::evaluateForces() {
     o.FTotal += o.FHydro + o.FContact + o.FLub + o.FGrav + o.FSpring;
     o.MTotal += o.MHydro + o.MContact + o.MLub;
   }
+  for (Body& b : bodies) b.FTotal += b.FGrav + b.FSpring;
+}
+
+// DEM::bodyObjectInteraction, src/DEM.cpp:798-869: a spring along y between
+// every body and every impactor (nonLinType 0-4)
+void oracle_ctx::bodyObjectInteraction() {
+  for (Body& bd : bodies)
+    for (Object& ob : objects) {
+      double fs = 0.0, fdo = 0.0, fdb = 0.0;
+      bd.L = bd.x0.y - ob.x0.y;
+      const Vec r = bd.x0 - ob.x0;
+      const double rn = std::sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
+      const double ny = r.y / rn;
+      const double del = bd.L0 - bd.L;
+      const double bodyDamp = 2.0 * std::sqrt(bd.m * bd.k) * springDamp;
+      const double objDamp = 2.0 * std::sqrt(ob.m * bd.k) * springDamp;
+      const double sigma = bd.r;
+      if (nonLinType == 0) {
+        fs = bd.k * del * ny;
+      } else if (nonLinType == 1) {
+        fs = (bd.k * del) * ny;
+        fdo = -ob.x1.y * objDamp;
+        fdb = -bd.x1.y * bodyDamp;
+      } else if (nonLinType == 2) {
+        fs = (bd.k * del + k13 * bd.k * (del * del * del)) * ny;
+        fdo = -ob.x1.y * objDamp;
+        fdb = -bd.x1.y * bodyDamp;
+      } else if (nonLinType == 3) {
+        fs = (bd.k * del + (24.0 * epsilon / rn) * 2.0 * std::pow(sigma / rn, 12.0)) * ny;
+        fdo = -ob.x1.y * objDamp;
+        fdb = -bd.x1.y * bodyDamp;
+      } else if (nonLinType == 4) {
+        const double wcacut = std::pow(2.0, 1.0 / 6.0) * sigma;
+        if (rn <= wcacut)
+          fs = (bd.k * del + (24.0 * epsilon / rn) *
+                                 (2.0 * std::pow(sigma / rn, 12.0) - std::pow(sigma / rn, 6.0))) *
+               ny;
+        else
+          fs = (bd.k * del) * ny;
+        fdo = -ob.x1.y * objDamp;
+        fdb = -bd.x1.y * bodyDamp;
+      }
+      ob.FSpring.y -= fs;
+      bd.FSpring.y += fs;
+      ob.FSpring.y += fdo;
+      bd.FSpring.y += fdb;
+    }
 }
 
 // DEM::calculateParticleContactForces, src/DEM.cpp:1487-1791
@@ -1871,6 +1949,15 @@ void oracle_ctx::integration() {
     q.w1.z += dt * q.MTotal.z * q._I;
   }
   if ((int)demTimeStep >= objWaitTime)
+    for (Body& b : bodies) {
+      b.x0.x += dt * b.x1.x + dt * dt * b.FTotal.x * b._m;
+      b.x0.y += dt * b.x1.y + dt * dt * b.FTotal.y * b._m;
+      b.x0.z += dt * b.x1.z + dt * dt * b.FTotal.z * b._m;
+      b.x1.x += dt * b.FTotal.x * b._m;
+      b.x1.y += dt * b.FTotal.y * b._m;
+      b.x1.z += dt * b.FTotal.z * b._m;
+    }
+  if ((int)demTimeStep >= objWaitTime)
     for (Object& o : objects) {
       o.x0.x += dt * o.x1.x + dt * dt * o.FTotal.x * o._m;
       o.x0.y += dt * o.x1.y + dt * dt * o.FTotal.y * o._m;
@@ -2013,6 +2100,25 @@ void oracle_ctx::dump(const char* path) {
   wvec("w_FContact", &Wall::FContact);
   wvec("w_FLub", &Wall::FLub);
   wvec("w_FTotal", &Wall::FTotal);
+  const size_t B = bodies.size();
+  if (B) {
+    std::vector<double> bv(3 * B), bl(B);
+    auto bvec = [&](const char* name, Vec Body::*m) {
+      for (size_t i = 0; i < B; ++i) {
+        const Vec v = bodies[i].*m;
+        bv[3 * i] = v.x;
+        bv[3 * i + 1] = v.y;
+        bv[3 * i + 2] = v.z;
+      }
+      w.d(name, bv, {B, 3});
+    };
+    bvec("b_x0", &Body::x0);
+    bvec("b_x1", &Body::x1);
+    bvec("b_FSpring", &Body::FSpring);
+    bvec("b_FTotal", &Body::FTotal);
+    for (size_t i = 0; i < B; ++i) bl[i] = bodies[i].L;
+    w.d("b_L", bl);
+  }
 }
 
 // ==== C API =================================================================

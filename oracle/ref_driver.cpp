@@ -178,6 +178,25 @@ void dumpState(const std::string& path, int step, LB& lb, DEM& dem) {
   wvec("w_FContact", [](const wall& x) { return x.FContact; });
   wvec("w_FLub", [](const wall& x) { return x.FLub; });
   wvec("w_FTotal", [](const wall& x) { return x.FTotal; });
+  const size_t B = dem.bodies.size();
+  if (B) {
+    std::vector<double> bv(B * 3), bl(B);
+    auto bvec = [&](const char* name, auto get) {
+      for (size_t b = 0; b < B; ++b) {
+        const tVect v = get(dem.bodies[b]);
+        bv[3 * b] = v.x;
+        bv[3 * b + 1] = v.y;
+        bv[3 * b + 2] = v.z;
+      }
+      w.d(name, bv, {B, 3});
+    };
+    bvec("b_x0", [](const body& b) { return b.x0; });
+    bvec("b_x1", [](const body& b) { return b.x1; });
+    bvec("b_FSpring", [](const body& b) { return b.FSpring; });
+    bvec("b_FTotal", [](const body& b) { return b.FTotal; });
+    for (size_t b = 0; b < B; ++b) bl[b] = dem.bodies[b].L;
+    w.d("b_L", bl);
+  }
   w.close();
 }
 

@@ -15,7 +15,8 @@ It reads what the reference reads:
   over the file (src/macros.h:14-19);
 - particles.dat (src/DEM.cpp:80-134: radius and position times ``scale``,
   positions less 0.05), objects.dat (src/DEM.cpp:137-166), body.dat
-  (src/DEM.cpp:168-196, its count only).
+  (src/DEM.cpp:168-196: index, radius, position times ``scale``, velocity,
+  spring stiffness and rest length).
 
 Value conversion follows GetPot's stream rules: an integer key takes the
 leading integer of its token, a real key the leading number, a failed
@@ -32,7 +33,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(os.path.dirname(HERE), "lbm-dem_gb300"))
 
-from lbdem_types import Config, ObjectIn, ParticleIn  # noqa: E402
+from lbdem_types import BodyIn, Config, ObjectIn, ParticleIn  # noqa: E402
 
 _INT = re.compile(r"\s*([+-]?\d+)")
 _REAL = re.compile(r"\s*([+-]?(?:\d+\.?\d*|\.\d+)(?:[eE][+-]?\d+)?|[+-]?(?:inf|nan))",
@@ -234,7 +235,26 @@ class CaseConfig:
                 o.x[a] = float(row[2 + a]) * scale
                 o.v[a] = float(row[5 + a])
         with open(os.path.join(d, "body.dat")) as fh:
-            c.n_bodies = int(fh.read().split()[0])
+            tok = fh.read().split()
+        bt = int(tok[0])
+        bodies = (BodyIn * max(bt, 1))()
+        pos = 1
+        for n in range(bt):
+            row = tok[pos:pos + 10]
+            if len(row) < 10:
+                raise ValueError("malformed body.dat")
+            pos += 10
+            b = bodies[n]
+            b.index = int(row[0])
+            b.r = float(row[1])
+            for a in range(3):
+                b.x[a] = float(row[2 + a]) * scale
+                b.v[a] = float(row[5 + a])
+            b.k = float(row[8])
+            b.L0 = float(row[9])
+        self._bodies = bodies
+        c.n_bodies = bt
+        c.bodies = C.cast(bodies, C.POINTER(BodyIn))
         self._parts, self._objs = parts, objs
         c.n_particles = tot
         c.particles = C.cast(parts, C.POINTER(ParticleIn))

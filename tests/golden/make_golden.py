@@ -47,6 +47,8 @@ CASES = {
     "rheo_frictional": (40, 1, 1),
     "rheo_voellmy": (40, 1, 1),
     "rheo_turbulent": (40, 1, 1),
+    "bodies": (40, 1, 1),
+    "bodies_lj": (40, 1, 1),
 }
 
 # The reference's own example input (example/input: unitLength 0.2,
@@ -76,7 +78,7 @@ def write_example(cdir: str) -> None:
     for f in ("particles.dat", "objects.dat", "body.dat"):
         shutil.copyfile(os.path.join(ex, f), os.path.join(cdir, "input", f))
 
-SMALL_KEYS = ("p_", "o_", "w_", "step", "demTime", "demTimeStep")
+SMALL_KEYS = ("p_", "o_", "w_", "b_", "step", "demTime", "demTimeStep")
 
 
 def array_hash(a: np.ndarray) -> str:

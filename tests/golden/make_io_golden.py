@@ -31,6 +31,7 @@ CASES = {
     "tiny_direct": (12, 3.5, 5.0),
     "small_cells": (24, 5.5, 10.0),
     "c1": (30, 7.5, 14.0),
+    "bodies": (24, 5.5, 10.0),
 }
 FILES = ("export.dat", "objPosition.dat", "objForce.dat", "wallForce.dat", "bodyPosition.dat",
          "stressTensor.dat", "normalStressCont.dat", "shearStressCont.dat")

@@ -24,7 +24,7 @@ PARTICLE_FLOAT = ("p_x0", "p_x1", "p_w1", "p_FHydro", "p_MHydro", "p_FContact", 
                   "p_FLub", "p_MLub", "p_FRep", "p_FTotal", "p_MTotal", "p_xiw", "p_xio",
                   "p_fluidVolume", "p_SHydro")
 OBJECT_FLOAT = ("o_x0", "o_x1", "o_w1", "o_FHydro", "o_MHydro", "o_FContact", "o_FLub",
-                "o_FTotal")
+                "o_FTotal", "b_x0", "b_x1", "b_FSpring", "b_FTotal", "b_L")
 TORQUE_FORCE = {"o_MHydro": "o_FHydro", "o_w1": "o_x1", "p_MHydro": "p_FHydro",
                 "p_MContact": "p_FContact", "p_MLub": "p_FLub", "p_MTotal": "p_FTotal",
                 "p_w1": "p_x1"}

@@ -19,9 +19,10 @@ def _same(a, b):
     diffs = []
     for name, ctype in lbdem_types.Config._fields_:
         va, vb = getattr(a, name), getattr(b, name)
-        if name in ("particles", "objects"):
-            n = a.n_particles if name == "particles" else a.n_objects
-            rt = lbdem_types.ParticleIn if name == "particles" else lbdem_types.ObjectIn
+        if name in ("particles", "objects", "bodies"):
+            n = {"particles": a.n_particles, "objects": a.n_objects, "bodies": a.n_bodies}[name]
+            rt = {"particles": lbdem_types.ParticleIn, "objects": lbdem_types.ObjectIn,
+                  "bodies": lbdem_types.BodyIn}[name]
             sz = C.sizeof(rt) * n
             if n and C.string_at(va, sz) != C.string_at(vb, sz):
                 diffs.append(name)

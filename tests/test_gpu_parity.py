@@ -31,7 +31,7 @@ def _pair(name):
 
 @pytest.mark.parametrize("name", ["tiny_direct", "small_cells", "small_dup", "units_dyn",
                                   "rheo_bingham", "rheo_frictional", "rheo_voellmy",
-                                  "rheo_turbulent"])
+                                  "rheo_turbulent", "bodies", "bodies_lj"])
 def test_fp64_matches_oracle_every_step(name, lib, oracle_lib):
     cfg, gpu, orc = _pair(name)
     with tempfile.TemporaryDirectory() as tmp:

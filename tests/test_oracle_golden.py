@@ -66,6 +66,13 @@ def test_oracle_bitwise_equal_to_reference_rheology(name, lib, oracle_lib, tmp_p
     _run(name, lib, oracle_lib, tmp_path)
 
 
+@pytest.mark.parametrize("name", ["bodies", "bodies_lj"])
+def test_oracle_bitwise_equal_to_reference_bodies(name, lib, oracle_lib, tmp_path):
+    """Bodies joined to the impactor by springs (DEM::bodyObjectInteraction):
+    spring-dashpot-cubic and Lennard-Jones repulsion, body state included."""
+    _run(name, lib, oracle_lib, tmp_path)
+
+
 def test_oracle_bitwise_equal_to_reference_example(lib, oracle_lib, tmp_path):
     """The reference's own example input in physical units (unitLength 0.2,
     unitTime 1e-3, 123x200x123 lattice, 962 spheres), 20 steps."""

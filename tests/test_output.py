@@ -99,7 +99,7 @@ def test_golden_files_follow_the_reference_schedule():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["tiny_direct", "small_cells", "c1"])
+@pytest.mark.parametrize("name", ["tiny_direct", "small_cells", "c1", "bodies"])
 def test_driver_writes_the_reference_files(name, lib, tmp_path):
     c = _cases()[name]
     d = tmp_path / name
