@@ -509,6 +509,14 @@ def named_case(name: str, seed: int = 1) -> Case:
         ov.update(rheo[name])
         return impact_case((28, 40, 28), 27.0, 16, (3.0, 3.4), 5.0, 32.0,
                            -0.08, 5.0, 0.8, 1.0e-4, seed, overrides=ov, name=name)
+    if name in ("slip_stat", "slip_dyn"):
+        # slip walls (boundary0 5: static, 6: moving; DEM::initializeWalls
+        # gives every wall the slip and moving flags of boundary0) with slip
+        # coefficient 0.4, on the small_cells geometry
+        ov = {"objWaitTime": "3", "boundary0": "5" if name == "slip_stat" else "6",
+              "slipCoefficient": "0.4"}
+        return impact_case((28, 40, 28), 27.0, 16, (3.0, 3.4), 5.0, 32.0,
+                           -0.08, 5.0, 0.8, 1.0e-4, seed, overrides=ov, name=name)
     if name in ("bodies", "bodies_lj"):
         # two bodies above the impactor, each joined to it by a spring along y
         # (DEM::bodyObjectInteraction): spring-dashpot-cubic (nonLinType 2)

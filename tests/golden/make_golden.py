@@ -49,6 +49,8 @@ CASES = {
     "rheo_turbulent": (40, 1, 1),
     "bodies": (40, 1, 1),
     "bodies_lj": (40, 1, 1),
+    "slip_stat": (40, 1, 1),
+    "slip_dyn": (40, 1, 1),
 }
 
 # The reference's own example input (example/input: unitLength 0.2,

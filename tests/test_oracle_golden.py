@@ -66,7 +66,7 @@ def test_oracle_bitwise_equal_to_reference_rheology(name, lib, oracle_lib, tmp_p
     _run(name, lib, oracle_lib, tmp_path)
 
 
-@pytest.mark.parametrize("name", ["bodies", "bodies_lj"])
+@pytest.mark.parametrize("name", ["bodies", "bodies_lj", "slip_stat", "slip_dyn"])
 def test_oracle_bitwise_equal_to_reference_bodies(name, lib, oracle_lib, tmp_path):
     """Bodies joined to the impactor by springs (DEM::bodyObjectInteraction):
     spring-dashpot-cubic and Lennard-Jones repulsion, body state included."""
