@@ -251,6 +251,8 @@ __global__ void initTypes(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* obj
                           const int* boundary, const DeviceWall* walls, const int* wallType,
                           const double* obj, double fluidHeightLattice, int freeSurface);
 __global__ void fillDouble(double* v, long long n, double value);
+__global__ void slipStash(Consts k, const uint8_t* mask, void* f);
+__global__ void slipApply(Consts k, const uint8_t* mask, void* f);
 __global__ void initFields(Consts k, uint8_t* mask, void* f, double* mass, float* nF,
                            double fluidHeightLattice, int freeSurface);
 // mass of the active nodes (outside particles unless withParticles), counts

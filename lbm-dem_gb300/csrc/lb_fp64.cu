@@ -114,8 +114,8 @@ __device__ __forceinline__ void lbStepFp64Impl(const Consts& k, const LbArgs& a)
       for (int j = 1; j < Q; ++j) {
         const long long lk = x + nbrOffset(k, j);
         const bool wl = (wallN >> j) & 1u;
-        // a cached node's links are active or box walls (type 7 and 8 stream alike)
-        const int tl = bulk ? (wl ? 7 : 0) : (a.mask[lk] & TYPE_MASK);
+        // a cached node's links are active or box walls (all of type k.wallType)
+        const int tl = bulk ? (wl ? k.wallType : 0) : (a.mask[lk] & TYPE_MASK);
         const double fs = f[j];
         const long long dst = (long long)OPPJ(j) * NP + x;
         allAct = allAct && (isActiveT(tl) || wl);
@@ -125,6 +125,11 @@ __device__ __forceinline__ void lbStepFp64Impl(const Consts& k, const LbArgs& a)
           const double vuj = dotc(j, s.ux, s.uy, s.uz);
           fout[dst] = -fs + WJ(j) * k.initDensity * (2.0 + 9.0 * (vuj * vuj) - 3.0 * usq);
         } else if (tl == 11) {
+          fout[dst] = fs;
+        } else if (tl == 5 || tl == 6) {
+          // slip walls: bounce-back without a wall force (the wall velocity
+          // is zero, BBi == 0); the diagonal links' slip rule is applied by
+          // slipStash / slipApply once every node has streamed
           fout[dst] = fs;
         } else if (tl == 7 || tl == 8) {
           // wall velocity is zero: BBi == 0 for dynamic walls as well
@@ -415,6 +420,39 @@ __device__ __noinline__ void fsPostCollision(const Consts& k, const FsArgs& a, l
   }
 }
 
+// slip-wall tables and partner lookup (LB::streaming and LB::updateMass,
+// src/LB.cpp:1454-1523, 1595-1625; src/lattice.h:137-140); see slipPass
+__constant__ unsigned char c_slip1Check[Q] = {0, 0, 0, 0, 0, 0, 0, 1, 2, 3, 4, 3, 4, 5, 6, 1, 2, 6, 5};
+__constant__ unsigned char c_slip1[Q] = {0, 0, 0, 0, 0, 0, 0, 9, 10, 8, 7, 13, 14, 12, 11, 18, 17, 15, 16};
+__constant__ unsigned char c_slip2Check[Q] = {0, 0, 0, 0, 0, 0, 0, 3, 4, 2, 1, 5, 6, 4, 3, 5, 6, 1, 2};
+__constant__ unsigned char c_slip2[Q] = {0, 0, 0, 0, 0, 0, 0, 10, 9, 7, 8, 14, 13, 11, 12, 17, 18, 16, 15};
+
+// the slip partner of link j of x: 1 or 2 when exactly that check node is
+// active, 0 otherwise
+__device__ __forceinline__ int slipPartner(const Consts& k, const uint8_t* mask, long long x,
+                                           int j, long long& c, int& s) {
+  const long long c1 = x + nbrOffset(k, c_slip1Check[j]);
+  const long long c2 = x + nbrOffset(k, c_slip2Check[j]);
+  const bool a1 = isActiveT(mask[c1] & TYPE_MASK), a2 = isActiveT(mask[c2] & TYPE_MASK);
+  if (a1 && !a2) {
+    c = c1;
+    s = c_slip1[j];
+    return 1;
+  }
+  if (!a1 && a2) {
+    c = c2;
+    s = c_slip2[j];
+    return 2;
+  }
+  return 0;
+}
+__device__ __forceinline__ bool slipOneActive(const Consts& k, const uint8_t* mask, long long x,
+                                              int j) {
+  long long c;
+  int s;
+  return slipPartner(k, mask, x, j, c, s) != 0;
+}
+
 // LB::updateMass (interface part). The neighbour types are read first, all
 // links at once; the mass exchange terms are then summed in link order.
 LBDEM_KERNEL(__launch_bounds__(256, 2), fsUpdateMass, FsArgs, fs) {
@@ -435,14 +473,16 @@ LBDEM_KERNEL(__launch_bounds__(256, 2), fsUpdateMass, FsArgs, fs) {
     coords(k, x, ix, iy, iz);
     const double mx = a.mass[x];
     // links to fluid or interface nodes, to interface nodes, to walls/impactors
-    unsigned liq = 0, ifc = 0, wal = 0;
+    unsigned liq = 0, ifc = 0, wal = 0, slp = 0;
 #pragma unroll
     for (int j = 1; j < Q; ++j) {
       const int tl = a.mask[x + nbrOffset(k, j)] & TYPE_MASK;
       liq |= (unsigned)(tl == 3 || tl == 0) << j;
       ifc |= (unsigned)(tl == 3) << j;
       wal |= (unsigned)(tl == 8 || tl == 12 || tl == 9) << j;
+      slp |= (unsigned)(tl == 6) << j;  // moving slip wall (a static one adds no mass)
     }
+    wal |= slp;
     double fsl[Q];
     if (wal) fsPostCollision(k, a, x, m, ix, iy, iz, fsl);
     double delta = 0.0;
@@ -459,7 +499,9 @@ LBDEM_KERNEL(__launch_bounds__(256, 2), fsUpdateMass, FsArgs, fs) {
         const double ms = k.mixed
             ? (double)((const float*)a.fcur)[(long long)OPPJ(j) * k.NP + x] - fsl[j]
             : ((const double*)a.fcur)[(long long)OPPJ(j) * k.NP + x] - fsl[j];
-        term = (1.0 * mx) * ms;
+        double w = 1.0;  // averageMass = w * mass (src/LB.cpp:1581-1625)
+        if (((slp >> j) & 1u) && j > 6 && slipOneActive(k, a.mask, x, j)) w = 1.0 - k.slipS1;
+        term = (w * mx) * ms;
       } else {
         continue;
       }
@@ -1211,6 +1253,51 @@ __global__ void fillDouble(double* v, long long n, double value) {
        x += (long long)gridDim.x * blockDim.x)
     v[x] = value;
 }
+
+// ---- slip walls (LB::streaming, src/LB.cpp:1454-1523) -------------------------
+//
+// For a diagonal link j (j > 6) of an active node x into a slip wall, the
+// reference sets f_opp(x) = S1 fs_s(c) + S2 fs_j(x) when exactly one of the
+// two nodes x + c_slip1Check[j], x + c_slip2Check[j] is active: c is that
+// node and s = slip1[j] or slip2[j] respectively; otherwise (and for j <= 6)
+// plain bounce-back. The lattice step has already bounced every wall link
+// back, so after it fs_j(x) sits in direction opp(j) of x and fs_s(c) in
+// direction opp(s) of c: the link s of c leads into the other check node,
+// which is the inactive one and, for walls on the box faces, a wall node.
+// As c's own value may be corrected in the same pass, slipStash first
+// writes every corrected value into the wall node's slot of direction
+// opp(j) (x + c_j, a slot no step reads), and slipApply then copies it to x.
+template <bool APPLY>
+__device__ __forceinline__ void slipPass(const Consts& k, const uint8_t* mask, void* f) {
+  const long long NP = k.NP;
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < k.N;
+       x += (long long)gridDim.x * blockDim.x) {
+    if (!isActiveT(mask[x] & TYPE_MASK)) continue;
+    int ix, iy, iz;
+    coords(k, x, ix, iy, iz);
+    const unsigned wallN = boxWallLinks(k, ix, iy, iz);
+    if (!(wallN >> 7)) continue;  // no diagonal link into a wall
+    for (int j = 7; j < Q; ++j) {
+      if (!((wallN >> j) & 1u)) continue;
+      long long c;
+      int s;
+      if (!slipPartner(k, mask, x, j, c, s)) continue;
+      const long long own = (long long)OPPJ(j) * NP + x;
+      const long long stash = (long long)OPPJ(j) * NP + x + nbrOffset(k, j);
+      if (k.mixed) {
+        float* g = (float*)f;
+        if (APPLY) g[own] = g[stash];
+        else g[stash] = k.slipS1f * g[(long long)OPPJ(s) * NP + c] + k.slipS2f * g[own];
+      } else {
+        double* g = (double*)f;
+        if (APPLY) g[own] = g[stash];
+        else g[stash] = k.slipS1 * g[(long long)OPPJ(s) * NP + c] + k.slipS2 * g[own];
+      }
+    }
+  }
+}
+__global__ void slipStash(Consts k, const uint8_t* mask, void* f) { slipPass<false>(k, mask, f); }
+__global__ void slipApply(Consts k, const uint8_t* mask, void* f) { slipPass<true>(k, mask, f); }
 
 // ---- diagnostics --------------------------------------------------------------
 

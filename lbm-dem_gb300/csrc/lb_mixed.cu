@@ -40,9 +40,10 @@ __constant__ int c_dir[Q] = {packDir(0),  packDir(1),  packDir(2),  packDir(3), 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr unsigned ALL_LINKS = 0x7FFFEu;  // bits 1..18
 // neighbour types whose link needs no fix-up after the unrolled streaming
-// loop: fluid 0, gas 2, interface 3, walls 7/8, slip wall 11
-constexpr unsigned PLAIN_TYPES = (1u << 0) | (1u << 2) | (1u << 3) | (1u << 7) | (1u << 8) |
-                                 (1u << 11);
+// loop: fluid 0, gas 2, interface 3, slip walls 5/6 (their diagonal links'
+// slip rule follows the step, slipStash / slipApply), walls 7/8, topography 11
+constexpr unsigned PLAIN_TYPES = (1u << 0) | (1u << 2) | (1u << 3) | (1u << 5) | (1u << 6) |
+                                 (1u << 7) | (1u << 8) | (1u << 11);
 
 // ---- asynchronous bulk copies into shared memory (cp.async.bulk) tracked
 // by mbarriers; every wait is bounded ----

@@ -272,8 +272,10 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   if (cfg->n_bodies < 0 || cfg->n_bodies > MAX_BODY || (cfg->n_bodies > 0 && !cfg->bodies))
     return setErr(ctx, LBDEM_ERR_INVALID, "at most 8 bodies, with their body.dat records");
   for (int i = 0; i < 6; ++i)
-    if (cfg->boundary[i] != 7 && cfg->boundary[i] != 8)
-      return setErr(ctx, LBDEM_ERR_INVALID, "only no-slip walls (boundary types 7/8)");
+    if (cfg->boundary[i] < 5 || cfg->boundary[i] > 8)
+      return setErr(ctx, LBDEM_ERR_INVALID, "only walls on every face (boundary types 5-8)");
+  if (cfg->slipCoefficient < 0.0 || cfg->slipCoefficient > 1.0)
+    return setErr(ctx, LBDEM_ERR_INVALID, "slipCoefficient outside [0, 1]");
   if (cfg->unitTime <= 0.0 || cfg->unitLength <= 0.0)
     return setErr(ctx, LBDEM_ERR_INVALID, "unitLength and unitTime must be positive");
   if (cfg->n_objects > MAX_OBJ) return setErr(ctx, LBDEM_ERR_INVALID, "too many objects");
@@ -482,6 +484,12 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
     }
   ctx->nWall = (int)hw.size();
   k.nWall = ctx->nWall;
+  // every wall takes boundary0's slip and moving flags (src/DEM.cpp:430-447)
+  k.wallType = hwt.empty() ? 7 : hwt[0];
+  k.slipS1 = cfg->slipCoefficient;
+  k.slipS2 = 1.0 - cfg->slipCoefficient;
+  k.slipS1f = (float)k.slipS1;
+  k.slipS2f = (float)k.slipS2;
   // neighbour-list geometry (fixed: radii and the DEM box do not change)
   const double cut = 2.0 * rmax + 2.0;
   const int nl[3] = {(int)(k.demSize[0] / cut), (int)(k.demSize[1] / cut),
@@ -800,9 +808,15 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   else if (k.visc) lbStepFp64Rheo<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
   else lbStepFp64<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
   if (ev) cudaEventRecord(ev->second, s);
-  if (k.mixed && k.nWall > 0) {
+  if (k.mixed && k.nWall > 0 && k.wallType >= 7) {
     lbWallForceMixed<<<dim3(ctx->gridShell, 6), 256, 0, s>>>(k, a);
     ctx->launches += 1;
+  }
+  if (k.wallType == 5 || k.wallType == 6) {
+    // slip walls: the diagonal links' slip rule, after every node has streamed
+    slipStash<<<latticeGrid(ctx), 256, 0, s>>>(k, d.mask, a.fout);
+    slipApply<<<latticeGrid(ctx), 256, 0, s>>>(k, d.mask, a.fout);
+    ctx->launches += 2;
   }
   ctx->cur = 1 - ctx->cur;
   // unit conversions, then the extra-mass redistribution (free surface)
@@ -1013,7 +1027,8 @@ void lbdemJobArgs(lbdem_ctx* c, int cur, JobArgs* j) {
 // share a batch when their switches match (batchKey).
 bool lbdemBatchable(const lbdem_ctx* c) {
   // runs with a per-node viscosity or bodies keep their own launches
-  return c->demSolve && c->lbSolve && pairReplayable(c) && !c->k.visc && c->nBody == 0;
+  return c->demSolve && c->lbSolve && pairReplayable(c) && !c->k.visc && c->nBody == 0 &&
+         c->k.wallType >= 7;
 }
 int lbdemBatchKey(const lbdem_ctx* c) {
   return c->precision | (c->freeSurface ? 2 : 0) | (c->nObj > 0 ? 4 : 0) | (c->nWall > 0 ? 8 : 0);

@@ -91,6 +91,11 @@ struct Consts {
   // bodies and their springs to the impactors (DEM::bodyObjectInteraction)
   int nBody, nonLinType;
   double springDamp, k13, epsilon;
+  // the type of every wall node (5-8) and the slip coefficient S1 = slip,
+  // S2 = 1 - slip of slip walls (LB::streaming, src/LB.cpp:1337-1352)
+  int wallType;
+  double slipS1, slipS2;
+  float slipS1f, slipS2f;
 };
 
 struct DeviceWall {

@@ -30,6 +30,13 @@ TORQUE_FORCE = {"o_MHydro": "o_FHydro", "o_w1": "o_x1", "p_MHydro": "p_FHydro",
                 "p_w1": "p_x1"}
 LEVER = 10.0  # lattice units, of the order of the sphere radii
 ATOL_FRAC = 1e-11  # element-wise absolute floor, as a fraction of the field's scale
+# The per-node viscosity of a non-Newtonian run is a function of the
+# non-equilibrium populations f - feq and of the shear rate in a denominator
+# (node::computeApparentViscosity, src/node.cpp:113-168): the differences of
+# about 1e-16 that reordered reductions leave in the inputs (interface masses,
+# particle velocities) are amplified by |f| / |f - feq|, 1e4 to 1e6. It is
+# therefore held to 1e-8, while the populations it produces stay at rtol.
+FIELD_RTOL = {"visc": 1e-8}
 
 
 def rel_err(a, b, scale=None):
@@ -73,11 +80,12 @@ def compare(gpu: dict, orc: dict, rtol: float = 1e-10, lattice: bool = True,
             sel = act if (fluid_mass or k != "mass") else (orc["type"] == 3)
             g = gpu[k][..., sel]
             o = orc[k][..., sel]
+            rk = max(rtol, FIELD_RTOL.get(k, 0.0))
             e = rel_err(g, o)
-            if not e <= rtol:
+            if not e <= rk:
                 bad.append(f"{k}: rel err {e:.3e}")
             if elem:
-                q = elem_err(g, o, rtol, max(float(np.max(np.abs(o))) if o.size else 0.0, 1e-300))
+                q = elem_err(g, o, rk, max(float(np.max(np.abs(o))) if o.size else 0.0, 1e-300))
                 if not q <= 1.0:
                     bad.append(f"{k}: element-wise error {q:.3e} of tolerance")
     for k in PARTICLE_FLOAT + OBJECT_FLOAT:

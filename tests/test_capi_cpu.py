@@ -84,6 +84,6 @@ def test_unsupported_inputs_are_rejected_before_device_use(lib):
     import lbdem
     cfg = lbdem.LoadedConfig(os.path.join(GOLDEN, "tiny_direct", "parameters.cfg"),
                              overrides={"boundary0": 4, "boundary1": 4})
-    with pytest.raises(RuntimeError, match="no-slip walls"):
+    with pytest.raises(RuntimeError, match="only walls on every face"):
         lbdem.Solver(cfg)
     cfg.close()

@@ -31,7 +31,8 @@ def _pair(name):
 
 @pytest.mark.parametrize("name", ["tiny_direct", "small_cells", "small_dup", "units_dyn",
                                   "rheo_bingham", "rheo_frictional", "rheo_voellmy",
-                                  "rheo_turbulent", "bodies", "bodies_lj"])
+                                  "rheo_turbulent", "bodies", "bodies_lj", "slip_stat",
+                                  "slip_dyn"])
 def test_fp64_matches_oracle_every_step(name, lib, oracle_lib):
     cfg, gpu, orc = _pair(name)
     with tempfile.TemporaryDirectory() as tmp:

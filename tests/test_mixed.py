@@ -43,7 +43,8 @@ def _run(name, steps, every):
 
 
 @pytest.mark.parametrize("name,steps,every", [("small_cells", 60, 5), ("c1", 100, 10),
-                                              ("units_dyn", 60, 5), ("example", 20, 5)])
+                                              ("units_dyn", 60, 5), ("example", 20, 5),
+                                              ("slip_dyn", 40, 5), ("bodies", 40, 5)])
 def test_mixed_impactor_trajectory_within_1e3(name, steps, every, lib, oracle_lib):
     y0, tm, to, mm, mo = _run(name, steps, every)
     disp_o = to[:, 1] - y0
