@@ -508,6 +508,12 @@ int lbdem_server_tune(lbdem_server_options* opt, const lbdem_config* const* cfgs
 int lbdem_download_nodes_noalloc(lbdem_ctx* ctx, int64_t first, int64_t count,
                                  double* f, double* mass);
 
+/* Number of device allocations (cudaMalloc, cudaMallocAsync) this library
+ * has made in the process so far, over all contexts and servers. A
+ * diagnostic: a caller checks with it that a stretch of calls allocated
+ * nothing on the device. */
+int64_t lbdem_device_allocations(void);
+
 #ifdef __cplusplus
 }
 #endif

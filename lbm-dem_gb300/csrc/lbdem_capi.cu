@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -46,6 +47,7 @@ int setErr(lbdem_ctx* c, int code, const std::string& msg) {
 template <class T>
 int dalloc(lbdem_ctx* ctx, T** p, size_t count) {
   const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  lbdemNoteDeviceAllocation();
   cudaError_t e = cudaMallocAsync((void**)p, bytes, ctx->stream);
   if (e != cudaSuccess)
     return setErr(ctx, LBDEM_ERR_OOM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
@@ -1258,6 +1260,14 @@ extern "C" int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t prec
   return LBDEM_OK;
 }
 
+static std::atomic<int64_t> g_deviceAllocations{0};
+
+void lbdemNoteDeviceAllocation() { g_deviceAllocations.fetch_add(1, std::memory_order_relaxed); }
+
+extern "C" int64_t lbdem_device_allocations(void) {
+  return g_deviceAllocations.load(std::memory_order_relaxed);
+}
+
 extern "C" int lbdem_get_info(lbdem_ctx* ctx, lbdem_info* info) {
   if (!ctx || !info) return LBDEM_ERR_INVALID;
   std::memset(info, 0, sizeof(*info));
@@ -1330,6 +1340,7 @@ extern "C" int lbdem_download_lattice(lbdem_ctx* ctx, uint8_t* type, uint8_t* pf
   if ((rc = d2h(ctx, solid, d.solid, N * 4))) return rc;
   if (mass || f) {
     DeviceTemp t;
+    lbdemNoteDeviceAllocation();
     CK(cudaMalloc(&t.p, (size_t)(Q + 1) * N * sizeof(double)));
     double* tmp = t.p;
     exportLattice<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(ctx->k, d.mask, d.f[ctx->cur], d.mass,
@@ -1340,6 +1351,7 @@ extern "C" int lbdem_download_lattice(lbdem_ctx* ctx, uint8_t* type, uint8_t* pf
   }
   if (n || u) {
     DeviceTemp t;
+    lbdemNoteDeviceAllocation();
     CK(cudaMalloc(&t.p, 4 * N * sizeof(double)));
     double* tmp = t.p;
     momentsKernel<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(ctx->k, d.mask,
@@ -1465,6 +1477,7 @@ int massSums(lbdem_ctx* ctx, int withParticles, double* total_mass, int64_t* int
   if (rc) return rc;
   // stream-ordered temporary: no device-wide synchronisation
   double* tmp = nullptr;
+  lbdemNoteDeviceAllocation();
   CK(cudaMallocAsync(&tmp, 3 * sizeof(double), ctx->stream));
   CK(cudaMemsetAsync(tmp, 0, 3 * sizeof(double), ctx->stream));
   massSummaryKernel<<<latticeGrid(ctx), 256, 0, ctx->stream>>>(

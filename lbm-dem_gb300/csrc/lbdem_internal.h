@@ -254,6 +254,10 @@ int lbdemEnqueueBatchCycle(const std::vector<lbdem_ctx*>& runs, const lbdem::Job
                            cudaStream_t s);
 void lbdemAdvanceCounters(lbdem_ctx* c, int cycles);
 
+// Counts one device allocation for lbdem_device_allocations; every
+// cudaMalloc / cudaMallocAsync of the library calls it.
+void lbdemNoteDeviceAllocation();
+
 // Makes a device current for the length of one entry point and puts the
 // calling thread's previous device back on exit, so that contexts on
 // different devices can be driven from one host thread.

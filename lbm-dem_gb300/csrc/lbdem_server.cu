@@ -352,7 +352,8 @@ extern "C" int lbdem_server_create(const lbdem_server_options* opt, lbdem_server
     s->groupRuns = opt->batch_runs;
     const int ng = (opt->max_active + s->groupRuns - 1) / s->groupRuns;
     s->groups.resize(ng);
-    for (auto& g : s->groups)
+    for (auto& g : s->groups) {
+      lbdemNoteDeviceAllocation();
       if (cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking) != cudaSuccess ||
           cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming) != cudaSuccess ||
           cudaMalloc(&g.dJobs, 2 * (size_t)s->groupRuns * sizeof(lbdem::JobArgs)) !=
@@ -360,6 +361,7 @@ extern "C" int lbdem_server_create(const lbdem_server_options* opt, lbdem_server
         lbdem_server_destroy(s);
         return LBDEM_ERR_CUDA;
       }
+    }
   }
   s->budget = opt->device_budget_bytes;
   if (s->budget <= 0) {

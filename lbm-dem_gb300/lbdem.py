@@ -91,6 +91,7 @@ def load_library(path: str | None = None) -> C.CDLL:
                                C.c_int32, C.POINTER(C.c_double)], C.c_int),
         "lbdem_download_nodes_noalloc": ([c_ctx, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p],
                                          C.c_int),
+        "lbdem_device_allocations": ([], C.c_int64),
         "lbdem_checkpoint": ([c_ctx, C.c_char_p], C.c_int),
         "lbdem_export_recycle_fluid": ([c_ctx, C.c_char_p], C.c_int),
         "lbdem_output_open": ([c_ctx, C.c_char_p, C.c_double], C.c_int),
@@ -346,6 +347,12 @@ class Solver:
             self.ctx, int(first), int(count), f.ctypes.data_as(C.c_void_p),
             mass.ctypes.data_as(C.c_void_p)), "download_nodes_noalloc")
         return f, mass
+
+
+def device_allocations() -> int:
+    """Device allocations the library has made in this process so far
+    (lbdem_device_allocations)."""
+    return int(load_library().lbdem_device_allocations())
 
 
 def estimate_device_bytes(cfg: "LoadedConfig", precision: int = PLAIN_FP64) -> int:

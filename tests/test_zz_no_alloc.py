@@ -48,6 +48,40 @@ def test_noalloc_readback_matches_full_download(precision, lib):
         cfg.close()
 
 
+def test_noalloc_makes_no_device_allocation(lib):
+    """Consecutive calls leave the library's allocation count, the context's
+    device footprint and the device's free memory where they were. The
+    first call (which looks up the staging buffer and may load the module)
+    is made before the counts are taken."""
+    import torch
+
+    import lbdem
+    cfg = lbdem.LoadedConfig(os.path.join(GOLDEN, "small_cells", "parameters.cfg"))
+    s = lbdem.Solver(cfg, precision=lbdem.MIXED)
+    try:
+        N = int(s.info.nodes)
+        big = lbdem.NOALLOC_MAX_NODES
+        s.cycle(2)
+        s.nodes_noalloc(0, 64)
+        torch.cuda.synchronize()
+        allocs = lbdem.device_allocations()
+        footprint = int(s.get_info().device_bytes)
+        free0, _ = torch.cuda.mem_get_info()
+        for i in range(12):
+            first = (i * 7919) % (N - big)
+            s.nodes_noalloc(first, big if i % 2 else 1 + i * 1000)
+        free1, _ = torch.cuda.mem_get_info()
+        assert lbdem.device_allocations() == allocs
+        assert int(s.get_info().device_bytes) == footprint
+        assert free1 == free0
+        # the counter does move for a call that allocates (the full download)
+        s.lattice()
+        assert lbdem.device_allocations() > allocs
+    finally:
+        s.close()
+        cfg.close()
+
+
 def test_noalloc_rejects_oversized_and_outside_ranges(lib):
     import lbdem
     cfg = lbdem.LoadedConfig(os.path.join(GOLDEN, "small_cells", "parameters.cfg"))
