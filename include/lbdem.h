@@ -466,6 +466,8 @@ int lbdem_server_poll(lbdem_server* s, double wait_seconds, lbdem_job_result* ou
                       int32_t max_out, int32_t* n_out);
 int lbdem_server_status(const lbdem_server* s, int32_t* queued, int32_t* running,
                         int32_t* unread, int64_t* device_bytes_in_use);
+/* The server's last error message; with s = NULL, the message of this
+ * thread's last failed lbdem_server_tune (the schedule and the failing run). */
 const char* lbdem_server_last_error(const lbdem_server* s);
 /* Ends the runs still resident (without results) and frees everything. */
 void lbdem_server_destroy(lbdem_server* s);

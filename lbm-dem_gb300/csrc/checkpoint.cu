@@ -221,5 +221,15 @@ extern "C" int lbdem_restore(lbdem_ctx* ctx, const char* path) {
       cudaGraphExecDestroy(g);
       g = nullptr;
     }
+  for (auto& g : ctx->oneGraph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  for (auto& g : ctx->quadGraph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
   return LBDEM_OK;
 }

@@ -28,8 +28,18 @@ __device__ __forceinline__ void load3f(const double* a, int P, int i, float* v) 
   v[2] = (float)a[2 * P + i];
 }
 
+// 1/sqrt(r2) for r2 > 0 in FP64 to about 1e-13 relative: the FP32 estimate
+// refined by one Newton step (y (3 - r2 y^2) / 2), a handful of FP64
+// operations where sqrt and a division take several times as many.
+__device__ __forceinline__ double rsqrtNewton(double r2) {
+  const double y = (double)rsqrtf((float)r2);
+  return y * fma(-0.5 * r2, y * y, 1.5);
+}
+
 // Mixed-form pair geometry from the FP64 separation d = xa - xb and relative
 // velocity u = va - vb; rad is the mean radius (2 rad the contact distance).
+// Near contact the distance and gap are taken in FP64 (the gap is a small
+// difference of large numbers), the unit normal in FP32.
 __device__ __forceinline__ PairGeom<float> pairGeomM(double rad, const double* d,
                                                      const double* u) {
   PairGeom<float> g;
@@ -37,12 +47,15 @@ __device__ __forceinline__ PairGeom<float> pairGeomM(double rad, const double* d
   const float r2 = dx * dx + dy * dy + dz * dz;
   const float lim = (float)((2.0 + NEAR_GAP) * rad);
   if (r2 < lim * lim) {
-    const double r12 = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const double r2d = fma(d[0], d[0], fma(d[1], d[1], d[2] * d[2]));
+    const double y = rsqrtNewton(r2d);
+    const double r12 = r2d * y;
     g.r12 = (float)r12;
     g.gap = (float)(r12 - 2.0 * rad);
-    g.n[0] = (float)(d[0] / r12);
-    g.n[1] = (float)(d[1] / r12);
-    g.n[2] = (float)(d[2] / r12);
+    const float yf = (float)y;
+    g.n[0] = dx * yf;
+    g.n[1] = dy * yf;
+    g.n[2] = dz * yf;
   } else {
     const float r12 = sqrtf(r2);
     g.r12 = r12;
@@ -74,7 +87,8 @@ __device__ __forceinline__ float wallGeomM(const DeviceWall& W, const double* x,
     o[0] = (float)ox;
     o[1] = (float)oy;
     o[2] = (float)oz;
-    return (float)sqrt(ox * ox + oy * oy + oz * oz);
+    const double l2 = fma(ox, ox, fma(oy, oy, oz * oz));
+    return l2 > 0.0 ? (float)(l2 * rsqrtNewton(l2)) : 0.0f;
   }
   return l;
 }
@@ -83,11 +97,6 @@ __device__ __forceinline__ void add3f(float* a, const float* b) {
   a[0] += b[0];
   a[1] += b[1];
   a[2] += b[2];
-}
-__device__ __forceinline__ void sub3f(float* a, const float* b) {
-  a[0] -= b[0];
-  a[1] -= b[1];
-  a[2] -= b[2];
 }
 
 }  // namespace
@@ -139,14 +148,93 @@ LBDEM_KERNEL(, demPairsMixed, DemArgs, dem) {
   }
 }
 
-// Gather, wall and impactor terms and integration, one thread per particle:
-// the plain form's demGather with FP32 force sums.
+// Pair sums of the gather: GATHER_MIXED_LANES lanes of a warp per particle,
+// lane l summing the slots l+1, l+1+LANES, ... of the particle's list (the
+// slot loop is a chain of dependent loads: spreading it over lanes hides
+// their latency); the lanes' sums are combined by a fixed shuffle tree and
+// stored per particle for demGatherMixed. FP32 only.
+LBDEM_KERNEL(__launch_bounds__(GATHER_MIXED_THREADS), demSlotSumsMixed, DemArgs, dem) {
+  const int cur = a.iscal[IS_LISTCUR];
+  const int* L = a.list[cur];
+  const float* pbuf = reinterpret_cast<const float*>(a.pairbuf);
+  const int P = k.nPart;
+  const bool afterWait = a.iscal[IS_DEMSTEP] >= k.objWaitTime;
+  constexpr int LANES = GATHER_MIXED_LANES;
+  const int sub = threadIdx.x % LANES;
+  // warp-uniform loop: each warp takes 32/LANES consecutive particles
+  const int first = blockIdx.x * GATHER_MIXED_PARTS + (threadIdx.x / 32) * (32 / LANES);
+  for (int base = first; base < P; base += gridDim.x * GATHER_MIXED_PARTS) {
+    const int i = base + (threadIdx.x % 32) / LANES;
+    const bool valid = i < P;
+    // pairs: contact, electrostatics and (after the wait) lubrication, from
+    // the slot of the pair's owner (the higher index); the contact torques
+    // are summed unscaled and multiplied by the radius in the gather
+    float S[15];  // FC, MC / radius, FL, ML, FR
+#pragma unroll
+    for (int c = 0; c < 15; ++c) S[c] = 0.0f;
+    if (valid) {
+      const int* li = L + (long long)i * MAX_N;
+      const int* pt = a.partner + (long long)i * MAX_N;
+      const int cnt = li[0];
+#pragma unroll 2
+      for (int s = 1 + sub; s <= cnt; s += LANES) {
+        const int j = li[s];
+        const bool own = j < i;
+        const long long e = own ? (long long)i * MAX_N + s : (long long)j * MAX_N + pt[s];
+        const float* pb = pbuf + e * PAIR_VALS;
+        const float sg = own ? 1.0f : -1.0f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          S[c] = __fmaf_rn(sg, pb[c], S[c]);
+          S[3 + c] += pb[3 + c];
+          S[12 + c] = __fmaf_rn(sg, pb[15 + c], S[12 + c]);
+        }
+        if (afterWait && (a.pairflag[e] & 1)) {
+          const float* ml = pb + (own ? 9 : 12);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            S[6 + c] = __fmaf_rn(sg, pb[6 + c], S[6 + c]);
+            S[9 + c] += ml[c];
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int o = LANES / 2; o > 0; o >>= 1)
+#pragma unroll
+      for (int c = 0; c < 15; ++c) S[c] += __shfl_xor_sync(0xffffffffu, S[c], o);
+    // lane c of the particle's group stores sum c (and c + LANES)
+    if (valid) {
+      float* out = a.slotSum + (size_t)i * SLOT_SUM_STRIDE;
+#pragma unroll
+      for (int c = 0; c < 15; ++c)
+        if (c % LANES == sub) out[c] = S[c];
+    }
+  }
+}
+
+// The warp's sum of v added to *slot (one slot per warp: no atomics, a fixed
+// order). Every lane of the warp calls it.
+__device__ __forceinline__ void warpAccum(float v, float* slot) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) *slot += v;
+}
+
+// Gather, wall and impactor terms and integration, one thread per particle
+// (every lane of a warp in the FP64 integration): the plain form's demGather
+// with FP32 force sums, the pair sums from demSlotSumsMixed. The impactor
+// and wall reactions are summed per warp in FP32 (a shuffle tree per term
+// that any lane of the warp has) and per block in warp order, then added to
+// the FP64 totals once per block: shared FP64 atomics from every particle at
+// a wall serialise on their address.
 LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGatherMixed, DemArgs, dem) {
+  constexpr int NW = GATHER_THREADS / 32;
   const int stepNo = a.iscal[IS_DEMSTEP];
-  __shared__ double acc[GA_N];
+  __shared__ float acc[NW][GA_N];
   __shared__ DeviceWall sW[MAX_WALL];
   __shared__ float sWp[MAX_WALL][3], sWn[MAX_WALL][3];
-  for (int t = threadIdx.x; t < GA_N; t += blockDim.x) acc[t] = 0.0;
+  for (int t = threadIdx.x; t < NW * GA_N; t += blockDim.x) (&acc[0][0])[t] = 0.0f;
   if (threadIdx.x < (unsigned)k.nWall) {
     const DeviceWall W = a.walls[threadIdx.x];
     sW[threadIdx.x] = W;
@@ -160,28 +248,24 @@ LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGatherMixed, DemArgs, dem) {
   // lubrication range, plus a margin far above the FP32 error of the test
   const float wallReach =
       (float)tmax(k.lubCut, tmax(k.lubN, tmax(k.lubT, k.lubR))) + 0.01f;
-  const int cur = a.iscal[IS_LISTCUR];
-  const int* L = a.list[cur];
-  const float* pbuf = reinterpret_cast<const float*>(a.pairbuf);
   const int P = k.nPart;
   const bool afterWait = stepNo >= k.objWaitTime;
+  const unsigned FULLM = 0xffffffffu;
+  float* wacc = acc[threadIdx.x >> 5];
   // particles in the cell list's order (from the last rebuild), so that a
   // warp holds neighbours in space and few of its lanes branch into the wall
   // terms; the particle index order where the direct-sum branch is in use
   const int* order = a.iscal[IS_DIRECT] ? nullptr : a.cellParts;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P; t += gridDim.x * blockDim.x) {
-    const int i = order ? order[t] : t;
-    double xa[3], va[3];
+  // warp-uniform loop (the reaction sums take every lane)
+  for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < P;
+       base += gridDim.x * blockDim.x) {
+    const int t = base + (threadIdx.x & 31);
+    const bool valid = t < P;
+    const int i = valid ? (order ? order[t] : t) : 0;
+    double xa[3], va[3], waD[3];
     load3(a.x0, P, i, xa);
     load3(a.x1, P, i, va);
-    double waD[3];
     load3(a.w1, P, i, waD);
-    const float vaf[3] = {(float)va[0], (float)va[1], (float)va[2]};
-    const float wa[3] = {(float)waD[0], (float)waD[1], (float)waD[2]};
-    const double raD = a.r[i];
-    const float ra = (float)raD;
-    float FC[3] = {0, 0, 0}, MC[3] = {0, 0, 0}, FL[3] = {0, 0, 0}, ML[3] = {0, 0, 0},
-          FR[3] = {0, 0, 0};
     float xiw[3], xio[3];
     load3f(a.xiw, P, i, xiw);
     load3f(a.xio, P, i, xio);
@@ -191,41 +275,19 @@ LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGatherMixed, DemArgs, dem) {
     load3(a.MHydro, P, i, MH);
     load3(a.FGrav, P, i, FG);
     const double im = a.invm[i], iI = a.invI[i];
-    const int* li = L + (long long)i * MAX_N;
-    const int* pt = a.partner + (long long)i * MAX_N;
-    const int cnt = li[0];
-    // pairs: contact, electrostatics and (after the wait) lubrication, from
-    // the slot of the pair's owner (the higher index)
-#pragma unroll 4
-    for (int s = 1; s <= cnt; ++s) {
-      const int j = li[s];
-      const bool own = j < i;
-      const long long e = own ? (long long)i * MAX_N + s : (long long)j * MAX_N + pt[s];
-      const float* pb = pbuf + e * PAIR_VALS;
-      if (own) {
-        add3f(FC, pb);
-        add3f(FR, pb + 15);
-      } else {
-        sub3f(FC, pb);
-        sub3f(FR, pb + 15);
-      }
-      MC[0] += ra * pb[3];
-      MC[1] += ra * pb[4];
-      MC[2] += ra * pb[5];
-      if (afterWait && (a.pairflag[e] & 1)) {
-        if (own) {
-          add3f(FL, pb + 6);
-          add3f(ML, pb + 9);
-        } else {
-          sub3f(FL, pb + 6);
-          add3f(ML, pb + 12);
-        }
-      }
-    }
+    const double raD = a.r[i];
+    const float4* ss = reinterpret_cast<const float4*>(a.slotSum + (size_t)i * SLOT_SUM_STRIDE);
+    const float4 s0 = ss[0], s1 = ss[1], s2 = ss[2], s3 = ss[3];
+    const float vaf[3] = {(float)va[0], (float)va[1], (float)va[2]};
+    const float wa[3] = {(float)waD[0], (float)waD[1], (float)waD[2]};
+    const float ra = (float)raD;
+    float FC[3] = {s0.x, s0.y, s0.z}, MC[3] = {ra * s0.w, ra * s1.x, ra * s1.y},
+          FL[3] = {s1.z, s1.w, s2.x}, ML[3] = {s2.y, s2.z, s2.w},
+          FR[3] = {s3.x, s3.y, s3.z};
     // walls a force can reach (FP32 distance test); the others give no
     // force and reset the wall spring, as the contact law does out of contact
     unsigned nearW = 0;
-    {
+    if (valid) {
       const float xf[3] = {(float)xa[0], (float)xa[1], (float)xa[2]};
       for (int w = 0; w < k.nWall; ++w) {
         float l2 = 0.0f;
@@ -238,50 +300,62 @@ LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGatherMixed, DemArgs, dem) {
         if (l2 < lim * lim) nearW |= 1u << w;
       }
     }
+    const unsigned warpNearW = __reduce_or_sync(FULLM, nearW);
     float df[3], dt[3];
     if (afterWait) {
       for (int w = 0; w < k.nWall; ++w) {
-        if (!((nearW >> w) & 1u)) continue;
-        float o[3];
-        const float l = wallGeomM(sW[w], xa, raD, o);
-        float F[3], Tq[3];
-        if (wallLubOne(k, ra, vaf, wa, o[0], o[1], o[2], l, F, Tq)) {
-          add3f(FL, F);
-          add3f(ML, Tq);
-          for (int c = 0; c < 3; ++c)
-            if (F[c] != 0.0f) atomicAdd(&acc[GA_WALL + 6 * w + 3 + c], -(double)F[c]);
+        if (!((warpNearW >> w) & 1u)) continue;  // uniform
+        float F[3] = {0.0f, 0.0f, 0.0f};
+        if ((nearW >> w) & 1u) {
+          float o[3], Tq[3];
+          const float l = wallGeomM(sW[w], xa, raD, o);
+          if (wallLubOne(k, ra, vaf, wa, o[0], o[1], o[2], l, F, Tq)) {
+            add3f(FL, F);
+            add3f(ML, Tq);
+          } else {
+            F[0] = F[1] = F[2] = 0.0f;
+          }
         }
+        for (int c = 0; c < 3; ++c) warpAccum(-F[c], &wacc[GA_WALL + 6 * w + 3 + c]);
       }
       for (int o = 0; o < k.nObj; ++o) {
         const double* ob = a.obj + o * OB_STRIDE;
         const double ro = ob[OB_R];
-        double d[3], u[3];
-        for (int c = 0; c < 3; ++c) {
-          d[c] = xa[c] - ob[OB_X0 + c];
-          u[c] = va[c] - ob[OB_X1 + c];
-        }
-        const PairGeom<float> g = pairGeomM(0.5 * (raD + ro), d, u);
-        const float wo[3] = {(float)ob[OB_W1], (float)ob[OB_W1 + 1], (float)ob[OB_W1 + 2]};
-        objContactOne(k, ra, (float)ro, g, wa, wo, xio, df, dt);
-        add3f(FC, df);
-        MC[0] += ra * dt[0];
-        MC[1] += ra * dt[1];
-        MC[2] += ra * dt[2];
-        for (int c = 0; c < 3; ++c) {
-          if (df[c] != 0.0f) atomicAdd(&acc[GA_OBJ + 12 * o + c], -(double)df[c]);
-          if (dt[c] != 0.0f) atomicAdd(&acc[GA_OBJ + 12 * o + 3 + c], ro * (double)dt[c]);
-        }
-        float lo[9];
-        if (pairLub(k, ra, (float)ro, g, wa, wo, lo)) {
-          add3f(FL, lo);
-          add3f(ML, lo + 3);
+        float R[12] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        bool any = false;
+        if (valid) {
+          double d[3], u[3];
           for (int c = 0; c < 3; ++c) {
-            if (lo[c] != 0.0f) atomicAdd(&acc[GA_OBJ + 12 * o + 6 + c], -(double)lo[c]);
-            if (lo[6 + c] != 0.0f) atomicAdd(&acc[GA_OBJ + 12 * o + 9 + c], (double)lo[6 + c]);
+            d[c] = xa[c] - ob[OB_X0 + c];
+            u[c] = va[c] - ob[OB_X1 + c];
           }
+          const PairGeom<float> g = pairGeomM(0.5 * (raD + ro), d, u);
+          const float wo[3] = {(float)ob[OB_W1], (float)ob[OB_W1 + 1], (float)ob[OB_W1 + 2]};
+          objContactOne(k, ra, (float)ro, g, wa, wo, xio, df, dt);
+          add3f(FC, df);
+          MC[0] += ra * dt[0];
+          MC[1] += ra * dt[1];
+          MC[2] += ra * dt[2];
+          const float rof = (float)ro;
+          for (int c = 0; c < 3; ++c) {
+            R[c] = -df[c];
+            R[3 + c] = rof * dt[c];
+          }
+          float lo[9];
+          if (pairLub(k, ra, rof, g, wa, wo, lo)) {
+            add3f(FL, lo);
+            add3f(ML, lo + 3);
+            for (int c = 0; c < 3; ++c) {
+              R[6 + c] = -lo[c];
+              R[9 + c] = lo[6 + c];
+            }
+          }
+          for (int c = 0; c < 12; ++c) any |= R[c] != 0.0f;
         }
+        if (__any_sync(FULLM, any))
+          for (int c = 0; c < 12; ++c) warpAccum(R[c], &wacc[GA_OBJ + 12 * o + c]);
       }
-    } else {
+    } else if (valid) {
       float nst[3] = {0.0f, 0.0f, 0.0f};
       const double ylid = xa[1] - (k.demSize[1] - 0.3);
       wallContactOne(k, ra, vaf, wa, xiw, 0.0f, (float)ylid, 0.0f, (float)fabs(ylid), nst, df,
@@ -297,19 +371,25 @@ LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGatherMixed, DemArgs, dem) {
       for (int w = 0; w < k.nWall; ++w) {
         if (!((nearW >> w) & 1u)) {
           xiw[0] = xiw[1] = xiw[2] = 0.0f;
-          continue;
         }
-        float o[3];
-        const float l = wallGeomM(sW[w], xa, raD, o);
-        wallContactOne(k, ra, vaf, wa, xiw, o[0], o[1], o[2], l, nst, df, dt);
-        add3f(FC, df);
-        MC[0] += ra * dt[0];
-        MC[1] += ra * dt[1];
-        MC[2] += ra * dt[2];
-        for (int c = 0; c < 3; ++c)
-          if (df[c] != 0.0f) atomicAdd(&acc[GA_WALL + 6 * w + c], -(double)df[c]);
+        if (!((warpNearW >> w) & 1u)) continue;  // uniform
+        float F[3] = {0.0f, 0.0f, 0.0f};
+        if ((nearW >> w) & 1u) {
+          float o[3];
+          const float l = wallGeomM(sW[w], xa, raD, o);
+          wallContactOne(k, ra, vaf, wa, xiw, o[0], o[1], o[2], l, nst, df, dt);
+          add3f(FC, df);
+          MC[0] += ra * dt[0];
+          MC[1] += ra * dt[1];
+          MC[2] += ra * dt[2];
+          F[0] = df[0];
+          F[1] = df[1];
+          F[2] = df[2];
+        }
+        for (int c = 0; c < 3; ++c) warpAccum(-F[c], &wacc[GA_WALL + 6 * w + c]);
       }
     }
+    if (!valid) continue;
     // totals and integration in FP64
     const double dtt = k.dt;
     for (int c = 0; c < 3; ++c) {
@@ -337,8 +417,11 @@ LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGatherMixed, DemArgs, dem) {
   }
   __syncthreads();
   for (int t = threadIdx.x; t < GA_N; t += blockDim.x) {
-    const double v = acc[t];
-    if (v == 0.0) continue;
+    float vf = 0.0f;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) vf += acc[w][t];
+    if (vf == 0.0f) continue;
+    const double v = (double)vf;
     if (t < GA_WALL) {
       const int o = t / 12, c = t % 12;
       const int off = c < 3 ? OB_FCONTACT + c : c < 6 ? OB_MCONTACT + c - 3

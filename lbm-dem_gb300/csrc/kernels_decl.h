@@ -70,6 +70,7 @@ struct DemArgs {
   int* pairList;
   double* pairbuf;
   uint8_t* pairflag;
+  float* slotSum;  // [P][SLOT_SUM_STRIDE] mixed form: demSlotSumsMixed -> demGatherMixed
   int* pcell;
   float4* posf;  // [P] FP32 position and radius, written by nbrCellAssign
   // particle::x_i.y (position at the start, again after the objWaitTime
@@ -268,6 +269,16 @@ __global__ void exportLattice(Consts k, const uint8_t* mask, const void* f, cons
 // threads per block of the gather pass (one thread per particle): small
 // blocks spread a few thousand particles over every SM
 constexpr int GATHER_THREADS = 64;
+// mixed-form pair sums (demSlotSumsMixed): GATHER_MIXED_LANES lanes per
+// particle split its neighbour slots (the slot loop is a chain of dependent
+// loads), so a block of GATHER_MIXED_THREADS holds GATHER_MIXED_PARTS
+// particles
+#ifndef LBDEM_GATHER_LANES
+#define LBDEM_GATHER_LANES 8
+#endif
+constexpr int GATHER_MIXED_LANES = LBDEM_GATHER_LANES;
+constexpr int GATHER_MIXED_THREADS = 128;
+constexpr int GATHER_MIXED_PARTS = GATHER_MIXED_THREADS / GATHER_MIXED_LANES;
 // DEM stress sums: contact, lubrication, electrostatic, hydrodynamic (3x3 each)
 constexpr int STRESS_N = 36;
 __global__ void demStress(Consts k, DemArgs a, const double* SHydro, double* out,
@@ -301,6 +312,8 @@ __global__ void demGatherBatch(const JobArgs* jobs);
 // dem_mixed.cu: the force passes of the mixed form (FP32 force laws)
 __global__ void demPairsMixed(Consts k, DemArgs a);
 __global__ void demPairsMixedBatch(const JobArgs* jobs);
+__global__ void demSlotSumsMixed(Consts k, DemArgs a);
+__global__ void demSlotSumsMixedBatch(const JobArgs* jobs);
 __global__ void demGatherMixed(Consts k, DemArgs a);
 __global__ void demGatherMixedBatch(const JobArgs* jobs);
 

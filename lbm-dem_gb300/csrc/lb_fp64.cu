@@ -249,15 +249,20 @@ __device__ __forceinline__ void lbPrepareBody(const Consts& k, double* pAcc, lon
   if (pAccF)
     for (long long i = i0; i < pAccFLen; i += stride) pAccF[i] = 0.0f;
   const int P = k.nPart;
-  for (long long i = i0; i < 3LL * P; i += stride) {
-    const double xl = px0[i] / k.uLength, vl = px1[i] / k.uSpeed;
-    pkd[i] = xl;
-    pkd[3 * P + i] = vl;
-    if (pkf) {  // [P] x (x0/L, x1/S, w1/W) as three float4 (4th lane 0)
+  if (pkf) {
+    // mixed form: [P] x (x0/L, x1/S, w1/W) as three float4 (4th lane 0), by
+    // FP32 products with the reciprocal units (an FP64 division per value
+    // costs more than the rest of the kernel); the FP64 copy is not used
+    for (long long i = i0; i < 3LL * P; i += stride) {
       const long long p = i % P, c = i / P;
-      pkf[12 * p + c] = (float)xl;
-      pkf[12 * p + 4 + c] = (float)vl;
-      pkf[12 * p + 8 + c] = (float)(pw1[i] / k.uAngVel);
+      pkf[12 * p + c] = (float)px0[i] * k.invLengthF;
+      pkf[12 * p + 4 + c] = (float)px1[i] * k.invSpeedF;
+      pkf[12 * p + 8 + c] = (float)pw1[i] * k.invAngVelF;
+    }
+  } else {
+    for (long long i = i0; i < 3LL * P; i += stride) {
+      pkd[i] = px0[i] / k.uLength;
+      pkd[3 * P + i] = px1[i] / k.uSpeed;
     }
   }
   if (i0 < k.nObj) {
@@ -290,15 +295,47 @@ __device__ __forceinline__ bool fsRegion(const Consts& k, const int* iscal, int&
   return true;
 }
 
+// Walk of a box of rx x ry nodes per layer by a grid-stride loop: the
+// box coordinates of linear index i are carried from one iteration to the
+// next by the stride's own decomposition (no division per node).
+struct BoxWalk {
+  unsigned bx, by, bz, sx, sy, sz;
+  __device__ __forceinline__ BoxWalk(unsigned i, unsigned stride, unsigned rx, unsigned ry) {
+    bx = i % rx;
+    by = (i / rx) % ry;
+    bz = i / (rx * ry);
+    sx = stride % rx;
+    sy = (stride / rx) % ry;
+    sz = stride / (rx * ry);
+  }
+  __device__ __forceinline__ void next(unsigned rx, unsigned ry) {
+    bx += sx;
+    by += sy;
+    bz += sz;
+    if (bx >= rx) {
+      bx -= rx;
+      ++by;
+    }
+    if (by >= ry) {
+      by -= ry;
+      ++bz;
+    }
+  }
+};
+
+// Grid-stride loop over the region's nodes (ix, iy, iz, x); boxes lie in
+// the lattice, so their volumes fit 32 bits as node indices do.
 #define FS_LOOP(k, a, ...)                                                               \
   int _x0, _y0, _z0, _rx, _ry, _rz;                                                      \
   if (fsRegion(k, a.iscal, _x0, _y0, _z0, _rx, _ry, _rz)) {                              \
-    const long long _vol = (long long)_rx * _ry * _rz;                                   \
-    for (long long _i = blockIdx.x * (long long)blockDim.x + threadIdx.x; _i < _vol;     \
-         _i += (long long)gridDim.x * blockDim.x) {                                      \
-      const int ix = _x0 + (int)(_i % _rx);                                              \
-      const int iy = _y0 + (int)((_i / _rx) % _ry);                                      \
-      const int iz = _z0 + (int)(_i / ((long long)_rx * _ry));                           \
+    const unsigned _vol = (unsigned)_rx * (unsigned)_ry * (unsigned)_rz;                 \
+    const unsigned _stride = gridDim.x * blockDim.x;                                     \
+    unsigned _i = blockIdx.x * blockDim.x + threadIdx.x;                                 \
+    BoxWalk _w(_i, _stride, (unsigned)_rx, (unsigned)_ry);                               \
+    for (; _i < _vol; _i += _stride, _w.next((unsigned)_rx, (unsigned)_ry)) {            \
+      const int ix = _x0 + (int)_w.bx;                                                   \
+      const int iy = _y0 + (int)_w.by;                                                   \
+      const int iz = _z0 + (int)_w.bz;                                                   \
       const long long x = ix + iy * k.sy + iz * k.sz;                                    \
       __VA_ARGS__                                                                        \
     }                                                                                    \
@@ -316,16 +353,20 @@ __device__ __forceinline__ void lbFinalizeBody(const Consts& k, double* pF, doub
     if (pAccF) {
       // mixed form: float sums [P][ACCF_STRIDE] of d (3), R_ab = sum r_a d_b
       // (9) and massOld (1); torque = antisymmetric part of R, stresslet = R
-      // in physical units (src/LB.cpp:1941-1958)
-      const float* acc = pAccF + (size_t)i * ACCF_STRIDE;
-      double R[9];
-      for (int c = 0; c < 9; ++c) R[c] = (double)acc[3 + c];
-      for (int c = 0; c < 3; ++c) pF[c * P + i] = (double)acc[c];
-      pM[i] = R[5] - R[7];
-      pM[P + i] = R[6] - R[2];
-      pM[2 * P + i] = R[1] - R[3];
-      for (int c = 0; c < 9; ++c) pS[c * P + i] = R[c] * k.uLength * k.uForce;
-      pV[i] = (double)acc[12];
+      // in physical units (src/LB.cpp:1941-1958). The unit products are
+      // taken in FP32, the precision of the sums, and stored as FP64.
+      const float4* a4 = reinterpret_cast<const float4*>(pAccF + (size_t)i * ACCF_STRIDE);
+      const float4 q0 = a4[0], q1 = a4[1], q2 = a4[2], q3 = a4[3];
+      const float R[9] = {q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+      pF[i] = (double)(q0.x * k.uForceF);
+      pF[P + i] = (double)(q0.y * k.uForceF);
+      pF[2 * P + i] = (double)(q0.z * k.uForceF);
+      pM[i] = (double)((R[5] - R[7]) * k.uTorqueF);
+      pM[P + i] = (double)((R[6] - R[2]) * k.uTorqueF);
+      pM[2 * P + i] = (double)((R[1] - R[3]) * k.uTorqueF);
+      for (int c = 0; c < 9; ++c) pS[c * P + i] = (double)(R[c] * k.sLF);
+      pV[i] = (double)(q3.x * k.uVolumeF);
+      continue;
     }
     for (int c = 0; c < 3; ++c) {
       pF[c * P + i] *= k.uForce;
@@ -345,10 +386,14 @@ __device__ __forceinline__ void lbFinalizeBody(const Consts& k, double* pF, doub
         (scal[SC_EXTRA_MASS] + scal[SC_EXTRA_MASS_LO]) / (double)(unsigned)iscal[IS_NIF];
   }
   if (redistribute) {
-    // LB::redistributeMass(extraMass) over the interface nodes; every thread
-    // forms the same quotient block 0 stores above
-    const double addMass =
-        (scal[SC_EXTRA_MASS] + scal[SC_EXTRA_MASS_LO]) / (double)(unsigned)iscal[IS_NIF];
+    // LB::redistributeMass(extraMass) over the interface nodes; every block
+    // forms the same quotient block 0 stores above (once per block: an FP64
+    // division in every thread costs more than the rest of the kernel)
+    __shared__ double sAddMass;
+    if (threadIdx.x == 0)
+      sAddMass = (scal[SC_EXTRA_MASS] + scal[SC_EXTRA_MASS_LO]) / (double)(unsigned)iscal[IS_NIF];
+    __syncthreads();
+    const double addMass = sAddMass;
     const int nl = fa.iscal[IS_IFLIST];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nl; i += gridDim.x * blockDim.x) {
       const uint32_t x = fa.ifList[i];
@@ -366,7 +411,12 @@ enum : uint8_t { FS_FILLED = 1, FS_EMPTIED = 2, FS_NEW = 4 };
 
 // Region = interface bounding box of the LB step grown by one node.
 // dst += the block's sum of v; with lo, compensated (atomicAddComp)
-__device__ __forceinline__ void blockAddDouble(double v, double* dst, double* lo = nullptr) {
+// with any = whether this thread added anything to v; a block where no
+// thread did adds nothing and skips the FP64 reduction (same result: the
+// sum of zeros is not added either)
+__device__ __forceinline__ void blockAddDouble(double v, bool any, double* dst,
+                                               double* lo = nullptr) {
+  if (!__syncthreads_or(any)) return;
   __shared__ double red[32];
   const unsigned FULL = 0xffffffffu;
 #pragma unroll
@@ -483,6 +533,26 @@ LBDEM_KERNEL(__launch_bounds__(256, 2), fsUpdateMass, FsArgs, fs) {
       slp |= (unsigned)(tl == 6) << j;  // moving slip wall (a static one adds no mass)
     }
     wal |= slp;
+    if (k.mixed && !wal) {
+      // mixed form, no wall or impactor link: the exchange terms from the
+      // FP32 deviations in FP32 (f_opp(x) - f_j(x + c_j) = g_opp - g_j, the
+      // weights cancel), summed in link order, added to the FP64 mass once.
+      // Each term is the exact negative of the neighbour's term for the same
+      // link, as in FP64; only the per-node sum rounds in FP32.
+      const float* F = (const float*)a.fcur;
+      const size_t NP = (size_t)k.NP;
+      const float mxf = (float)mx;
+      float dl = 0.0f;
+#pragma unroll
+      for (int j = 1; j < Q; ++j) {
+        if (!((liq >> j) & 1u)) continue;
+        const long long lk = x + nbrOffset(k, j);
+        const float ms = F[OPPJ(j) * NP + x] - F[j * NP + lk];
+        dl += ((ifc >> j) & 1u) ? (0.5f * ((float)a.mass[lk] + mxf)) * ms : ms;
+      }
+      a.massNew[x] = mx + (double)dl;
+      continue;
+    }
     double fsl[Q];
     if (wal) fsPostCollision(k, a, x, m, ix, iy, iz, fsl);
     double delta = 0.0;
@@ -536,6 +606,7 @@ LBDEM_KERNEL(, fsMutants, FsArgs, fs) {
 // nodes become interface nodes holding 99% of their density.
 LBDEM_KERNEL(, fsSmoothen, FsArgs, fs) {
   double surplus = 0.0;
+  bool touched = false;
   FS_LOOP(k, a, {
     const uint8_t m = a.mask[x];
     const int t = m & TYPE_MASK;
@@ -563,6 +634,7 @@ LBDEM_KERNEL(, fsSmoothen, FsArgs, fs) {
         a.mass[x] = 0.01 * rho0;
         if (k.visc) k.visc[x] = k.visc[win];  // the filler's viscosity (src/LB.cpp:1719)
         surplus -= 0.01 * rho0;
+        touched = true;
       }
     } else if (t == 0) {
       bool hit = false;
@@ -580,23 +652,27 @@ LBDEM_KERNEL(, fsSmoothen, FsArgs, fs) {
         a.rhoS[x] = n;
         a.mass[x] = 0.99 * n;
         surplus += 0.01 * n;
+        touched = true;
       }
     }
   })
-  blockAddDouble(surplus, a.scal + SC_SURPLUS, a.scal + SC_SURPLUS_LO);
+  blockAddDouble(surplus, touched, a.scal + SC_SURPLUS, a.scal + SC_SURPLUS_LO);
 }
 
 // updateMutants + removeIsolated, first pass (src/LB.cpp:1751-1817).
 LBDEM_KERNEL(, fsMutantsAndFill, FsArgs, fs) {
   double surplus = 0.0;
+  bool touched = false;
   FS_LOOP(k, a, {
     const uint8_t fl = a.fsflag[x];
     const uint8_t m = a.mask[x];
     if ((fl & FS_EMPTIED) && !(fl & FS_NEW)) {
       surplus += a.mass[x];
       a.mass[x] = 0.0;
+      touched = true;
     } else if ((fl & FS_FILLED) && !(fl & FS_NEW)) {
       surplus += a.mass[x] - a.rhoS[x];
+      touched = true;
       a.mass[x] = a.rhoS[x];
       if (k.mixed) a.nF[x] = (float)a.rhoS[x];
     } else if ((m & TYPE_MASK) == 3) {
@@ -609,18 +685,20 @@ LBDEM_KERNEL(, fsMutantsAndFill, FsArgs, fs) {
         }
       if (!gasNb) {
         surplus += a.mass[x] - a.rhoS[x];
+        touched = true;
         a.mass[x] = a.rhoS[x];
         if (k.mixed) a.nF[x] = (float)a.rhoS[x];
         a.mask[x] = (uint8_t)((m & ~TYPE_MASK) | 0);
       }
     }
   })
-  blockAddDouble(surplus, a.scal + SC_SURPLUS, a.scal + SC_SURPLUS_LO);
+  blockAddDouble(surplus, touched, a.scal + SC_SURPLUS, a.scal + SC_SURPLUS_LO);
 }
 
 // removeIsolated, second pass (src/LB.cpp:1819-1841), and the interface count.
 LBDEM_KERNEL(, fsEmptyIsolated, FsArgs, fs) {
   double surplus = 0.0;
+  bool touched = false;
   int cnt = 0;
   FS_LOOP(k, a, {
     const uint8_t m = a.mask[x];
@@ -634,13 +712,14 @@ LBDEM_KERNEL(, fsEmptyIsolated, FsArgs, fs) {
       }
     if (!fluidNb) {
       surplus += a.mass[x];
+      touched = true;
       a.mass[x] = 0.0;
       a.mask[x] = (uint8_t)((m & ~TYPE_MASK) | 2);
     } else {
       ++cnt;
     }
   })
-  blockAddDouble(surplus, a.scal + SC_SURPLUS, a.scal + SC_SURPLUS_LO);
+  blockAddDouble(surplus, touched, a.scal + SC_SURPLUS, a.scal + SC_SURPLUS_LO);
   if (cnt) atomicAdd(a.iscal + IS_NIF2, cnt);
 }
 
@@ -650,20 +729,26 @@ LBDEM_KERNEL(, fsEmptyIsolated, FsArgs, fs) {
 // -> gas) lie in the box grown by 1, so their neighbours lie in the box
 // grown by 2. Every thread writes only its own node's mask byte.
 LBDEM_KERNEL(, fsRedistribute, FsArgs, fs) {
-  const double addMass =
-      (a.scal[SC_SURPLUS] + a.scal[SC_SURPLUS_LO]) / (double)(unsigned)a.iscal[IS_NIF2];
+  // the quotient once per block (an FP64 division in every thread costs
+  // more than the rest of the kernel)
+  __shared__ double sAddMass;
+  if (threadIdx.x == 0)
+    sAddMass = (a.scal[SC_SURPLUS] + a.scal[SC_SURPLUS_LO]) / (double)(unsigned)a.iscal[IS_NIF2];
+  __syncthreads();
+  const double addMass = sAddMass;
   int x1, y1, z1, rx1, ry1, rz1;
   if (!fsRegion(k, a.iscal, x1, y1, z1, rx1, ry1, rz1)) return;
   const int x0 = max(a.iscal[IS_BBOX + 0] - 2, 0), y0 = max(a.iscal[IS_BBOX + 1] - 2, 0),
             z0 = max(a.iscal[IS_BBOX + 2] - 2, 0);
-  const long long rx = min(a.iscal[IS_BBOX + 3] + 2, k.X - 1) - x0 + 1,
-                  ry = min(a.iscal[IS_BBOX + 4] + 2, k.Y - 1) - y0 + 1,
-                  rz = min(a.iscal[IS_BBOX + 5] + 2, k.Z - 1) - z0 + 1;
-  const long long vol = rx * ry * rz;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int ix = x0 + (int)(i % rx), iy = y0 + (int)((i / rx) % ry),
-              iz = z0 + (int)(i / (rx * ry));
+  const unsigned rx = min(a.iscal[IS_BBOX + 3] + 2, k.X - 1) - x0 + 1,
+                 ry = min(a.iscal[IS_BBOX + 4] + 2, k.Y - 1) - y0 + 1,
+                 rz = min(a.iscal[IS_BBOX + 5] + 2, k.Z - 1) - z0 + 1;
+  const unsigned vol = rx * ry * rz;
+  const unsigned stride = gridDim.x * blockDim.x;
+  unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  BoxWalk bw(i, stride, rx, ry);
+  for (; i < vol; i += stride, bw.next(rx, ry)) {
+    const int ix = x0 + (int)bw.bx, iy = y0 + (int)bw.by, iz = z0 + (int)bw.bz;
     const long long x = ix + iy * k.sy + iz * k.sz;
     const uint8_t m = a.mask[x];
     uint8_t nm = (uint8_t)(m & ~BULK);
@@ -695,6 +780,7 @@ __device__ __forceinline__ void sphereBox(const Consts& k, double cx, double cy,
 struct SphereL {
   double c[3], r;
   int lo[3], hi[3];
+  SphereBoxTest t;  // the FP32 test relative to lo, FP64 near the surface
 };
 // threads 0 .. nObj-1 fill s[] from the records' position at offset xoff
 // (OB_X0 or OB_X0PREV); the caller synchronises the block afterwards
@@ -706,6 +792,7 @@ __device__ __forceinline__ void loadSpheres(const Consts& k, const double* obj, 
     for (int a = 0; a < 3; ++a) s[o].c[a] = ob[xoff + a] / k.uLength;
     s[o].r = ob[OB_R] / k.uLength;
     sphereBox(k, s[o].c[0], s[o].c[1], s[o].c[2], s[o].r, s[o].lo, s[o].hi);
+    s[o].t = sphereBoxTest(s[o].c[0], s[o].c[1], s[o].c[2], s[o].r, s[o].lo);
   }
 }
 
@@ -721,29 +808,44 @@ __device__ __forceinline__ void uncoverCollectBody(const Consts& k, const uint8_
   loadSpheres(k, obj, OB_X0, cur);
   loadSpheres(k, obj, OB_X0PREV, prev);
   __syncthreads();
-  const double c0x = cur[0].c[0], c0y = cur[0].c[1], c0z = cur[0].c[2], r0 = cur[0].r;
   for (int o = 0; o < k.nObj; ++o) {
     const int* lo = prev[o].lo;
     const int* hi = prev[o].hi;
-    const long long nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
-    const long long vol = nx * ny * nz;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol;
-         i += (long long)gridDim.x * blockDim.x) {
-      const int ix = lo[0] + (int)(i % nx), iy = lo[1] + (int)((i / nx) % ny),
-                iz = lo[2] + (int)(i / (nx * ny));
+    if (hi[0] < lo[0] || hi[1] < lo[1] || hi[2] < lo[2]) continue;
+    // a box within the lattice: its volume fits 32 bits, as node indices do
+    const unsigned nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+    const unsigned vol = nx * ny * nz;
+    const unsigned stride = gridDim.x * blockDim.x;
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    BoxWalk bw(i, stride, nx, ny);
+    for (; i < vol; i += stride, bw.next(nx, ny)) {
+      const int ix = lo[0] + (int)bw.bx, iy = lo[1] + (int)bw.by, iz = lo[2] + (int)bw.bz;
       const long long x = ix + iy * k.sy + iz * k.sz;
       if ((mask[x] & TYPE_MASK) != 12) continue;
       // member of objectNodes: inside its own object's previous sphere
-      if (solid[x] != (uint32_t)o ||
-          !insideSphereFast((double)ix, (double)iy, (double)iz, prev[o].c[0], prev[o].c[1],
-                            prev[o].c[2], prev[o].r))
-        continue;
-      if (insideSphereFast((double)ix, (double)iy, (double)iz, c0x, c0y, c0z, r0)) continue;
+      if (solid[x] != (uint32_t)o || !insideBox(prev[o].t, ix, iy, iz)) continue;
+      if (insideBox(cur[0].t, ix, iy, iz)) continue;
       const int slot = atomicAdd(iscal + IS_NUNCOVER, 1);
       if (slot < UNCOVER_CAP) list[slot] = (uint32_t)x;
       else atomicOr(iscal + IS_ERROR, ERR_UNCOVER_CAP);
     }
   }
+}
+
+// Named barrier 1 over the first nthreads threads of the block (a multiple
+// of 32), and the same barrier returning whether v was non-zero in any of them.
+__device__ __forceinline__ void teamSync(int nthreads) {
+  asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+}
+__device__ __forceinline__ int teamOr(int nthreads, int v) {
+  int r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.s32 p, %1, 0;\n"
+      " bar.red.or.pred q, 1, %2, p;\n selp.s32 %0, 1, 0, q;\n}"
+      : "=r"(r)
+      : "r"(v), "r"(nthreads)
+      : "memory");
+  return r;
 }
 
 // findNewActiveObject, step 2 (one CTA): resolve the uncovered nodes in the
@@ -764,14 +866,19 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
   __syncthreads();
   if (threadIdx.x == 0) iscal[IS_NUNCOVER] = 0;
   if (n == 0) return;
+  // the team: one thread per candidate (whole warps, at most the block); the
+  // others leave, and the team synchronises on named barrier 1, so that a
+  // handful of candidates costs a handful of warps' barriers, not 32
+  const int T = min((int)blockDim.x, (n + 31) & ~31);
+  if ((int)threadIdx.x >= T) return;
   int p2 = 1;
   while (p2 < n) p2 <<= 1;
-  for (int i = threadIdx.x; i < p2; i += blockDim.x) s_idx[i] = i < n ? list[i] : 0xffffffffu;
-  __syncthreads();
+  for (int i = threadIdx.x; i < p2; i += T) s_idx[i] = i < n ? list[i] : 0xffffffffu;
+  teamSync(T);
   // bitonic sort ascending
   for (int size = 2; size <= p2; size <<= 1)
     for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      for (int i = threadIdx.x; i < p2; i += blockDim.x) {
+      for (int i = threadIdx.x; i < p2; i += T) {
         const int j = i ^ stride;
         if (j > i) {
           const bool up = (i & size) == 0;
@@ -782,7 +889,7 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
           }
         }
       }
-      __syncthreads();
+      teamSync(T);
     }
   // the same node can appear once per object box: drop duplicates
   __shared__ int s_n;
@@ -793,7 +900,7 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
         if (i == 0 || s_idx[i] != s_idx[i - 1]) s_idx[w++] = s_idx[i];
       s_n = w;
     }
-    __syncthreads();
+    teamSync(T);
     n = s_n;
   }
   auto find = [&](uint32_t lk) -> int {  // binary search among the candidates
@@ -814,7 +921,7 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
   // - a lower-index candidate is recorded in s_back;
   // - a higher-index candidate reads as an impactor node and gives nothing.
   // s_st bits 0-3 hold the candidate's state, 12 while unresolved.
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int i = threadIdx.x; i < n; i += T) {
     const uint32_t x = s_idx[i];
     int ix, iy, iz;
     coords(k, (long long)x, ix, iy, iz);
@@ -835,11 +942,11 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
     for (int b = nb; b < 9; ++b) s_back[9 * i + b] = -1;
     s_st[i] = (uint8_t)(12 | fix);
   }
-  __syncthreads();
+  teamSync(T);
   for (int iter = 0; iter <= n; ++iter) {
     int changed = 0;
     uint8_t nst[UNCOVER_CAP / 1024];
-    for (int i = threadIdx.x, q = 0; i < n; i += blockDim.x, ++q) {
+    for (int i = threadIdx.x, q = 0; i < n; i += T, ++q) {
       const uint8_t me = s_st[i];
       bool fluidNb = (me & 0x10) != 0, gasNb = (me & 0x20) != 0;
 #pragma unroll
@@ -852,16 +959,16 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
       }
       nst[q] = (uint8_t)((me & 0x30) | (!fluidNb ? 2 : gasNb ? 3 : 0));
     }
-    __syncthreads();
-    for (int i = threadIdx.x, q = 0; i < n; i += blockDim.x, ++q)
+    teamSync(T);
+    for (int i = threadIdx.x, q = 0; i < n; i += T, ++q)
       if (s_st[i] != nst[q]) {
         s_st[i] = nst[q];
         changed = 1;
       }
-    if (!__syncthreads_or(changed)) break;
+    if (!teamOr(T, changed)) break;
   }
   const double rho0 = k.initDensity;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int i = threadIdx.x; i < n; i += T) {
     const long long x = s_idx[i];
     const int st = s_st[i] & 0x0F;
     const uint8_t m = mask[x];
@@ -898,18 +1005,20 @@ __device__ __forceinline__ void voxelizeObjectsBody(const Consts& k, uint8_t* ma
       hi[a] = max(hi[a], sph[o].hi[a]);
     }
   if (hi[0] < 0) return;
-  const long long nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
-  const long long vol = nx * ny * nz;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int ix = lo[0] + (int)(i % nx), iy = lo[1] + (int)((i / nx) % ny),
-              iz = lo[2] + (int)(i / (nx * ny));
+  // a box within the lattice: its volume fits 32 bits, as node indices do
+  // (an empty box visits nothing)
+  const bool boxOk = hi[0] >= lo[0] && hi[1] >= lo[1] && hi[2] >= lo[2];
+  const unsigned nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+  const unsigned vol = boxOk ? nx * ny * nz : 0u;
+  const unsigned stride = gridDim.x * blockDim.x;
+  unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  BoxWalk bw(i, stride, nx, ny);
+  for (; i < vol; i += stride, bw.next(nx, ny)) {
+    const int ix = lo[0] + (int)bw.bx, iy = lo[1] + (int)bw.by, iz = lo[2] + (int)bw.bz;
     const long long x = ix + iy * k.sy + iz * k.sz;
     int last = -1;
     for (int o = 0; o < k.nObj; ++o)
-      if (insideSphereFast((double)ix, (double)iy, (double)iz, sph[o].c[0], sph[o].c[1],
-                       sph[o].c[2], sph[o].r))
-        last = o;
+      if (insideBox(sph[o].t, ix, iy, iz)) last = o;
     // the box reaches one node past the sphere, so it holds every neighbour
     // of a node turned into an impactor node: drop their neighbour cache
     const uint8_t m0 = mask[x];
@@ -1029,9 +1138,20 @@ __device__ __forceinline__ void findNewActiveBody(const Consts& k, uint8_t* mask
         } else {
           int ix, iy, iz;
           coords(k, x, ix, iy, iz);
-          inside = insideSphere((double)ix, (double)iy, (double)iz, px0[pid] / k.uLength,
-                                px0[P + pid] / k.uLength, px0[2 * P + pid] / k.uLength,
-                                pr[pid] / k.uLength);
+          // FP32 test with the centre and radius from FP32 products; within
+          // a band around the surface that covers its error, the FP64 test
+          // with the reference's quotients decides (the same answer)
+          const float cx = (float)px0[pid] * k.invLengthF, cy = (float)px0[P + pid] * k.invLengthF,
+                      cz = (float)px0[2 * P + pid] * k.invLengthF, rf = (float)pr[pid] * k.invLengthF;
+          const float dx = (float)ix - cx, dy = (float)iy - cy, dz = (float)iz - cz;
+          const float d2 = dx * dx + dy * dy + dz * dz, r2 = rf * rf;
+          const float band = 8.0f * (rf + 1.0f) * k.posErrF + 1e-5f * r2 + 1e-5f;
+          if (d2 < r2 - band) inside = true;
+          else if (d2 > r2 + band) inside = false;
+          else
+            inside = insideSphere((double)ix, (double)iy, (double)iz, px0[pid] / k.uLength,
+                                  px0[P + pid] / k.uLength, px0[2 * P + pid] / k.uLength,
+                                  pr[pid] / k.uLength);
         }
         if (inside) atomicMin(&s_min, (unsigned long long)x);
       }
@@ -1316,7 +1436,7 @@ __global__ void massSummaryKernel(Consts k, const uint8_t* mask, const double* m
       if (withParticles || !(m & PFLAG)) s += (k.mixed && t == 0) ? (double)nF[x] : mass[x];
     }
   }
-  blockAddDouble(s, out);
+  blockAddDouble(s, true, out);
   for (int o = 16; o > 0; o >>= 1) {
     ni += __shfl_xor_sync(0xffffffffu, ni, o);
     na += __shfl_xor_sync(0xffffffffu, na, o);

@@ -201,6 +201,7 @@ DemArgs demArgs(lbdem_ctx* c) {
   a.pairList = d.pairList;
   a.pairbuf = d.pairbuf;
   a.pairflag = d.pairflag;
+  a.slotSum = d.slotSum;
   a.pcell = d.pcell;
   a.posf = d.posf;
   a.ppos = d.ppos;
@@ -294,6 +295,9 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   DeviceScope devScope(ctx->device);
   CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
   ctx->stream = ctx->own_stream;
+  CK(cudaStreamCreateWithFlags(&ctx->fsStream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&ctx->fsFork, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&ctx->fsDone, cudaEventDisableTiming));
   CK(cudaDeviceGetAttribute(&ctx->smCount, cudaDevAttrMultiProcessorCount, ctx->device));
   {
     int perSm = 0;
@@ -367,6 +371,15 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   k.omegaF = (float)k.omega;
   k.omegafF = (float)k.omegaf;
   k.sLF = (float)(k.uLength * k.uForce);
+  k.uForceF = (float)k.uForce;
+  k.uTorqueF = (float)k.uTorque;
+  k.uVolumeF = (float)k.uVolume;
+  k.invLengthF = (float)(1.0 / k.uLength);
+  k.invSpeedF = (float)(1.0 / k.uSpeed);
+  k.invAngVelF = (float)(1.0 / k.uAngVel);
+  // three roundings of 2^-24 relative each on a coordinate below the
+  // largest lattice side (a margin of 2 on top)
+  k.posErrF = (float)(2.0 * 3.0 * 0x1p-24 * (double)std::max(k.X, std::max(k.Y, k.Z)) + 1e-6);
   for (int a = 0; a < 3; ++a) {
     k.lbF[a] = cfg->lbF[a] / k.uAccel;
     ctx->lbFConfig[a] = k.lbF[a];
@@ -607,6 +620,9 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   // per slot PAIR_VALS doubles (plain form) or floats (mixed form)
   AL(d.pairbuf, P1 * MAX_N * (k.mixed ? PAIR_VALS / 2 : PAIR_VALS));
   AL(d.pairflag, P1 * MAX_N);
+  if (k.mixed) {
+    AL(d.slotSum, P1 * SLOT_SUM_STRIDE);
+  }
   AL(d.pcell, P1);
   AL(d.posf, P1);
   AL(d.ppos, P1);
@@ -693,6 +709,10 @@ extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (auto& g : ctx->pairGraph)
     if (g) cudaGraphExecDestroy(g);
+  for (auto& g : ctx->oneGraph)
+    if (g) cudaGraphExecDestroy(g);
+  for (auto& g : ctx->quadGraph)
+    if (g) cudaGraphExecDestroy(g);
   for (auto& e : ctx->lbEvents) {
     cudaEventDestroy(e.first);
     cudaEventDestroy(e.second);
@@ -706,6 +726,12 @@ extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
     cudaStreamSynchronize(ctx->own_stream);
     cudaStreamDestroy(ctx->own_stream);
   }
+  if (ctx->fsStream) {
+    cudaStreamSynchronize(ctx->fsStream);
+    cudaStreamDestroy(ctx->fsStream);
+  }
+  if (ctx->fsFork) cudaEventDestroy(ctx->fsFork);
+  if (ctx->fsDone) cudaEventDestroy(ctx->fsDone);
   delete ctx;
 }
 
@@ -753,13 +779,14 @@ extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
   if (k.mixed) {
     demPairsMixed<<<pairGrid, 128, 0, s>>>(k, a);
     if ((rc = enqueueStress(ctx, a))) return rc;
+    demSlotSumsMixed<<<partGrid(ctx, GATHER_MIXED_PARTS), GATHER_MIXED_THREADS, 0, s>>>(k, a);
     demGatherMixed<<<partGrid(ctx, GATHER_THREADS), GATHER_THREADS, 0, s>>>(k, a);
   } else {
     demPairs<<<pairGrid, 128, 0, s>>>(k, a);
     if ((rc = enqueueStress(ctx, a))) return rc;
     demGather<<<partGrid(ctx, GATHER_THREADS), GATHER_THREADS, 0, s>>>(k, a);
   }
-  ctx->launches += 1 + 9 + 2;
+  ctx->launches += 1 + 9 + (k.mixed ? 3 : 2);
   return launchErr(ctx, "dem step");
 }
 
@@ -903,7 +930,22 @@ cudaEvent_t* nextPhaseEvents(lbdem_ctx* c) {
   return c->phaseEvents[c->phaseEventsUsed++].data();
 }
 
-int cycleOnce(lbdem_ctx* ctx) {
+// The next cycle's coupling step (and whatever follows the DEM step) waits
+// for a forked free-surface step.
+int joinFreeSurface(lbdem_ctx* ctx) {
+  if (!ctx->fsPending) return LBDEM_OK;
+  ctx->fsPending = false;
+  CK(cudaStreamWaitEvent(ctx->stream, ctx->fsDone, 0));
+  return LBDEM_OK;
+}
+
+// One goCycle. With forkFs (mixed form, inside a capture of several cycles)
+// the free-surface step goes to fsStream after the lattice step and the
+// next cycle's DEM step runs beside it: that DEM step reads the particle
+// state and the hydrodynamic sums of the lattice step, and the free-surface
+// step of the mixed form reads only the lattice and the kinematics snapshot
+// taken at the start of the lattice step.
+int cycleOnce(lbdem_ctx* ctx, bool forkFs = false) {
   {
     ++ctx->lbTime;
     int rc = LBDEM_OK;
@@ -914,13 +956,26 @@ int cycleOnce(lbdem_ctx* ctx) {
     };
     mark(0);
     if (ctx->demSolve && (rc = lbdem_dem_step(ctx))) return rc;
+    if ((rc = joinFreeSurface(ctx))) return rc;
     mark(1);
     if (ctx->lbSolve && ctx->demTime >= ctx->demInitialRepeat) {
       if (ctx->demSolve && (rc = lbdem_coupling_step(ctx))) return rc;
       mark(2);
       if ((rc = lbdem_lb_step(ctx))) return rc;
       mark(3);
-      if (ctx->freeSurface && (rc = lbdem_free_surface_step(ctx))) return rc;
+      if (ctx->freeSurface && forkFs && ctx->k.mixed) {
+        CK(cudaEventRecord(ctx->fsFork, ctx->stream));
+        CK(cudaStreamWaitEvent(ctx->fsStream, ctx->fsFork, 0));
+        cudaStream_t main = ctx->stream;
+        ctx->stream = ctx->fsStream;
+        rc = lbdem_free_surface_step(ctx);
+        ctx->stream = main;
+        if (rc) return rc;
+        CK(cudaEventRecord(ctx->fsDone, ctx->fsStream));
+        ctx->fsPending = true;
+      } else if (ctx->freeSurface && (rc = lbdem_free_surface_step(ctx))) {
+        return rc;
+      }
       mark(4);
     } else if (ctx->lbSolve && ctx->demTime <= ctx->demInitialRepeat) {
       if (ctx->demSolve && (rc = lbdem_coupling_step(ctx))) return rc;
@@ -950,12 +1005,18 @@ bool pairReplayable(const lbdem_ctx* ctx) {
   return true;
 }
 
-int capturePair(lbdem_ctx* ctx, int parity) {
+// Captures `cycles` (1 or 2) consecutive cycles into *exec and launches it
+// once: the capture advanced the host counters, the first replay is the
+// cycles themselves.
+int captureCycles(lbdem_ctx* ctx, int cycles, cudaGraphExec_t* exec, long long* kernels) {
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   const long long before = ctx->launches;
-  int rc = cycleOnce(ctx);
-  if (rc == LBDEM_OK) rc = cycleOnce(ctx);
+  int rc = LBDEM_OK;
+  for (int c = 0; c < cycles && rc == LBDEM_OK; ++c) rc = cycleOnce(ctx, c + 1 < cycles);
+  // the capture ends on the context's stream with every fork joined
+  const int rj = joinFreeSurface(ctx);
+  if (rc == LBDEM_OK) rc = rj;
   const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
   if (rc) {
     if (g) cudaGraphDestroy(g);
@@ -963,15 +1024,18 @@ int capturePair(lbdem_ctx* ctx, int parity) {
   }
   if (e != cudaSuccess) return setErr(ctx, LBDEM_ERR_CUDA, std::string("graph capture: ") +
                                                                cudaGetErrorString(e));
-  const cudaError_t ei = cudaGraphInstantiate(&ctx->pairGraph[parity], g, 0);
+  const cudaError_t ei = cudaGraphInstantiate(exec, g, 0);
   cudaGraphDestroy(g);
   if (ei != cudaSuccess)
     return setErr(ctx, LBDEM_ERR_CUDA, std::string("graph instantiate: ") +
                                            cudaGetErrorString(ei));
-  ctx->pairKernels = ctx->launches - before;
-  // the capture advanced the host counters; the first replay is the pair itself
-  CK(cudaGraphLaunch(ctx->pairGraph[parity], ctx->stream));
+  *kernels = ctx->launches - before;
+  CK(cudaGraphLaunch(*exec, ctx->stream));
   return LBDEM_OK;
+}
+
+int capturePair(lbdem_ctx* ctx, int parity) {
+  return captureCycles(ctx, 2, &ctx->pairGraph[parity], &ctx->pairKernels);
 }
 
 }  // namespace
@@ -1071,7 +1135,9 @@ int lbdemEnqueueBatchCycle(const std::vector<lbdem_ctx*>& runs, const JobArgs* j
   });
   const int gathG = gmax([](lbdem_ctx* c) { return partGrid(c, GATHER_THREADS); });
   if (mixed) {
+    const int sumG = gmax([](lbdem_ctx* c) { return partGrid(c, GATHER_MIXED_PARTS); });
     demPairsMixedBatch<<<G(pairG), 128, 0, s>>>(jobs);
+    demSlotSumsMixedBatch<<<G(sumG), GATHER_MIXED_THREADS, 0, s>>>(jobs);
     demGatherMixedBatch<<<G(gathG), GATHER_THREADS, 0, s>>>(jobs);
   } else {
     demPairsBatch<<<G(pairG), 128, 0, s>>>(jobs);
@@ -1143,6 +1209,28 @@ extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
   int32_t i = 0;
   while (i < n) {
     int rc = LBDEM_OK;
+    // with no output open, four steady cycles are replayed from one graph
+    // (in the mixed form three of their free-surface steps overlap the next
+    // cycle's DEM step)
+    if (n - i >= 4 && !ctx->out && pairReplayable(ctx)) {
+      const int parity = ctx->cur;
+      if (!ctx->quadGraph[parity]) {
+        if ((rc = captureCycles(ctx, 4, &ctx->quadGraph[parity], &ctx->quadKernels))) return rc;
+      } else {
+        CK(cudaGraphLaunch(ctx->quadGraph[parity], ctx->stream));
+        // host counters as four cycles advance them (cur flips four times)
+        for (int c = 0; c < 4; ++c) {
+          ++ctx->lbTime;
+          if (ctx->demSolve) {
+            ++ctx->demTimeStep;
+            ctx->demTime += ctx->k.dt;
+          }
+        }
+        ctx->launches += ctx->quadKernels;
+      }
+      i += 4;
+      continue;
+    }
     // a pair replays two cycles; an output line due after the first of them
     // needs that cycle on its own
     if (n - i >= 2 && pairReplayable(ctx) && !lbdemOutputBlocksPair(ctx)) {
@@ -1168,7 +1256,32 @@ extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
     }
     ctx->stressNext = lbdemOutputStressNext(ctx);
     ctx->pStressNext = lbdemOutputParticleStressNext(ctx);
-    rc = cycleOnce(ctx);
+    if (!ctx->stressNext && !ctx->pStressNext && pairReplayable(ctx)) {
+      // a single steady cycle: replayed from its own graph (one per starting
+      // buffer), as pairs are
+      const int parity = ctx->cur;
+      if (!ctx->oneGraph[parity]) {
+        rc = captureCycles(ctx, 1, &ctx->oneGraph[parity], &ctx->oneKernels);
+      } else {
+        const cudaError_t e = cudaGraphLaunch(ctx->oneGraph[parity], ctx->stream);
+        if (e != cudaSuccess)
+          rc = setErr(ctx, LBDEM_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+        // the host counters as cycleOnce advances them (the lattice step,
+        // which swaps the buffers, runs once the DEM time reaches
+        // demInitialRepeat)
+        const double demTimeAfter = ctx->demTime + (ctx->demSolve ? ctx->k.dt : 0.0);
+        const bool lbRuns = ctx->lbSolve && demTimeAfter >= ctx->demInitialRepeat;
+        ++ctx->lbTime;
+        if (ctx->demSolve) {
+          ++ctx->demTimeStep;
+          ctx->demTime += ctx->k.dt;
+        }
+        if (lbRuns) ctx->cur = 1 - ctx->cur;
+        ctx->launches += ctx->oneKernels;
+      }
+    } else {
+      rc = cycleOnce(ctx);
+    }
     ctx->stressNext = ctx->pStressNext = false;
     if (rc) return rc;
     if ((rc = lbdemOutputAfterCycle(ctx))) return rc;
@@ -1242,6 +1355,7 @@ extern "C" int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t prec
   add(P1 * (MAX_N / 2), 4);                    // pairList
   add(P1 * MAX_N * (mixed ? PAIR_VALS / 2 : PAIR_VALS), 8);  // pairbuf
   add(P1 * MAX_N, 1);                          // pairflag
+  if (mixed) add(P1 * SLOT_SUM_STRIDE, 4);     // slotSum
   add(P1, 4);
   add(P1, 4);                                  // pcell, ppos
   add(P1, 16);                                 // posf

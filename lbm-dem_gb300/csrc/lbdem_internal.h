@@ -19,6 +19,9 @@ constexpr int MAX_OBJ = 8;       // impactors handled on the device
 constexpr int MAX_WALL = 6;
 constexpr int MAX_BODY = 8;      // bodies (body.dat) handled on the device
 constexpr int PAIR_VALS = 18;    // per neighbour slot: contact(6) lub(9) rep(3)
+// per particle, mixed form: the 15 pair sums of the gather (FC, MC / radius,
+// FL, ML, FR), padded to a 64-byte line
+constexpr int SLOT_SUM_STRIDE = 16;
 constexpr int UNCOVER_CAP = 8192;// uncovered object nodes resolved per step
 constexpr int ACCF_N = 13;       // mixed-form particle sums: d(3), r (x) d (9), mass(1)
 constexpr int ACCF_STRIDE = 16;  // floats per particle: its sums share one 64-byte line
@@ -64,6 +67,11 @@ struct Consts {
   int mixed;             // FP32 deviation storage / FP32 collision form
   float omegaF, omegafF, lbFf[3];
   float sLF;             // unit.Length * unit.Force, stresslet scale (mixed form)
+  float uForceF, uTorqueF, uVolumeF;  // the units in FP32 (mixed form)
+  float invLengthF, invSpeedF, invAngVelF;  // their reciprocals (mixed form)
+  // bound on |fl32(x0 / L) - x0 / L| in lattice units for positions in the
+  // lattice, when formed as float(x0) * invLengthF
+  float posErrF;
   double lbF[3];        // after the forceField reset rule of LB::collision
   double initVel[3];
   int nObj, nWall, nPart;
@@ -140,6 +148,7 @@ struct Device {
   int* pairList = nullptr;               // [25 P] owner slots i*50+s with list[i][s] < i
   double* pairbuf = nullptr;             // [P][50][PAIR_VALS]
   uint8_t* pairflag = nullptr;           // [P][50] bit0 = lubrication valid
+  float* slotSum = nullptr;              // [P][SLOT_SUM_STRIDE] mixed form
   int* pcell = nullptr;                  // [P] cell of particle
   float4* posf = nullptr;                // [P] FP32 position and radius (list rebuilds)
   int* ppos = nullptr;                   // [P] position in its cell (1-based)
@@ -284,6 +293,11 @@ struct lbdem_ctx {
   lbdem::Device d;
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
+  // mixed form, captured cycles: the free-surface step of a cycle runs on
+  // fsStream beside the next cycle's DEM step (fsFork / fsDone order it)
+  cudaStream_t fsStream = nullptr;
+  cudaEvent_t fsFork = nullptr, fsDone = nullptr;
+  bool fsPending = false;  // a forked free-surface step not yet joined
   int device = 0;
   int precision = LBDEM_PLAIN_FP64;
   int check_every = 0;
@@ -325,5 +339,9 @@ struct lbdem_ctx {
   long long launches = 0;
   // two goCycles as one CUDA graph, per starting lattice buffer
   cudaGraphExec_t pairGraph[2] = {nullptr, nullptr};
+  cudaGraphExec_t oneGraph[2] = {nullptr, nullptr};  // single cycles, per start buffer
+  cudaGraphExec_t quadGraph[2] = {nullptr, nullptr};  // four cycles (no output open)
+  long long quadKernels = 0;
+  long long oneKernels = 0;
   long long pairKernels = 0;
 };

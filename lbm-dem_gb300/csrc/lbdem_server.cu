@@ -16,7 +16,8 @@
 // different groups overlap on the device (a group's latency-bound phases,
 // such as the DEM gather, leave room for another group's lattice step). A
 // run is taken into or out of a group only while neither it nor the group
-// has work in flight, so no cross-stream ordering is needed. Runs outside
+// has work in flight (a new run's initialisation counts as its first work in
+// flight), so no cross-stream ordering is needed. Runs outside
 // the groups (their first cycles, an odd last cycle) advance on their own
 // streams.
 #include <cuda_runtime.h>
@@ -82,6 +83,9 @@ struct lbdem_server {
 
 namespace {
 
+// the message of the last failed lbdem_server_tune of this thread
+thread_local std::string t_tuneErr;
+
 int serverErr(lbdem_server* s, int code, const std::string& msg) {
   s->err = msg;
   return code;
@@ -94,8 +98,17 @@ void releaseJob(lbdem_server* s, Job* j) {
   delete j;
 }
 
-// End a job: its state after the last slice (or the failing status).
-void finishJob(lbdem_server* s, Job* j, int status) {
+// End a job: its state after the last slice (or the failing status, whose
+// description becomes the server's last error).
+void finishJob(lbdem_server* s, Job* j, int status, const char* where = nullptr) {
+  if (status != LBDEM_OK) {
+    std::string m = "job " + std::to_string(j->id) + " failed";
+    if (where) m += std::string(" in ") + where;
+    if (j->ctx && !j->ctx->err.empty()) m += ": " + j->ctx->err;
+    const cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess) m += std::string(" (CUDA: ") + cudaGetErrorString(e) + ")";
+    s->err = m;
+  }
   lbdem_job_result r;
   std::memset(&r, 0, sizeof r);
   r.job_id = j->id;
@@ -129,6 +142,8 @@ void finishJob(lbdem_server* s, Job* j, int status) {
       r.active_node_updates = p.active_node_updates;
     }
     r.status = rc;
+    if (rc != LBDEM_OK)
+      s->err = "job " + std::to_string(j->id) + " failed at its end: " + j->ctx->err;
   }
   r.end_time = s->now();
   s->finished.push_back(r);
@@ -161,10 +176,16 @@ void admit(lbdem_server* s) {
     if (rc == LBDEM_OK && cudaEventCreateWithFlags(&j->sliceDone, cudaEventDisableTiming) !=
                               cudaSuccess)
       rc = LBDEM_ERR_CUDA;
+    // the run's initialisation is work in flight on its own stream: until it
+    // completes the run neither joins a group (whose launches run on the
+    // group's stream, unordered with the run's own) nor gets a slice
+    if (rc == LBDEM_OK && cudaEventRecord(j->sliceDone, j->ctx->stream) != cudaSuccess)
+      rc = LBDEM_ERR_CUDA;
     if (rc != LBDEM_OK) {
-      finishJob(s, j, rc);
+      finishJob(s, j, rc, "its initialisation");
       continue;
     }
+    j->inFlight = true;
     s->used += j->bytes;
     j->counted = true;
     s->active.push_back(j);
@@ -207,14 +228,14 @@ int buildGroupGraph(lbdem_server* s, lbdem_server::Group& g) {
   return LBDEM_OK;
 }
 
-void dropJob(lbdem_server* s, Job* j, int status) {
+void dropJob(lbdem_server* s, Job* j, int status, const char* where = nullptr) {
   j->batched = false;
   for (size_t q = 0; q < s->active.size(); ++q)
     if (s->active[q] == j) {
       s->active.erase(s->active.begin() + q);
       break;
     }
-  finishJob(s, j, status);
+  finishJob(s, j, status, where);
 }
 
 // A group's turn: when its last slice is done, members that cannot take two
@@ -227,7 +248,9 @@ bool progressGroup(lbdem_server* s, lbdem_server::Group& g) {
     if (e == cudaErrorNotReady) return false;
     g.inFlight = false;
     if (e != cudaSuccess) {
-      for (Job* j : g.members) dropJob(s, j, LBDEM_ERR_CUDA);
+      const std::string where = "a shared-launch group of " + std::to_string(g.members.size()) +
+                                " runs (" + cudaGetErrorString(e) + ")";
+      for (Job* j : g.members) dropJob(s, j, LBDEM_ERR_CUDA, where.c_str());
       g.members.clear();
       return true;
     }
@@ -305,7 +328,13 @@ bool progress(lbdem_server* s) {
       changed = true;
       if (e != cudaSuccess) {
         s->active.erase(s->active.begin() + q);
-        finishJob(s, j, LBDEM_ERR_CUDA);
+        const std::string where = std::string("its own slice (") + cudaGetErrorString(e) + ")";
+        finishJob(s, j, LBDEM_ERR_CUDA, where.c_str());
+        continue;
+      }
+      // now idle: a run that fits a group waits for the group's next turn
+      if (!s->groups.empty() && j->cycles - j->done >= 2 && lbdemBatchable(j->ctx)) {
+        ++q;
         continue;
       }
     }
@@ -321,7 +350,7 @@ bool progress(lbdem_server* s) {
       rc = LBDEM_ERR_CUDA;
     if (rc != LBDEM_OK) {
       s->active.erase(s->active.begin() + q);
-      finishJob(s, j, rc);
+      finishJob(s, j, rc, "enqueueing its slice");
       changed = true;
       continue;
     }
@@ -437,7 +466,7 @@ extern "C" int lbdem_server_status(const lbdem_server* s, int32_t* queued, int32
 }
 
 extern "C" const char* lbdem_server_last_error(const lbdem_server* s) {
-  return s ? s->err.c_str() : "null server";
+  return s ? s->err.c_str() : t_tuneErr.c_str();
 }
 
 extern "C" void lbdem_server_destroy(lbdem_server* s) {
@@ -458,6 +487,7 @@ extern "C" void lbdem_server_destroy(lbdem_server* s) {
 extern "C" int lbdem_server_tune(lbdem_server_options* opt, const lbdem_config* const* cfgs,
                                  int32_t n, int32_t cycles, double* best_seconds) {
   if (!opt || !cfgs || n < 1 || cycles < 1) return LBDEM_ERR_INVALID;
+  t_tuneErr.clear();
   const int32_t batchC[] = {0, 2, 4, 8};
   const int32_t chunkC[] = {8, 32};
   double best = -1.0;
@@ -484,6 +514,9 @@ extern "C" int lbdem_server_tune(lbdem_server_options* opt, const lbdem_config* 
         done += got;
       }
       const double t = std::chrono::duration<double>(Clock::now() - t0).count();
+      if (rc != LBDEM_OK)
+        t_tuneErr = "schedule batch_runs " + std::to_string(b) + ", chunks_per_block " +
+                    std::to_string(c) + ": " + s->err;
       lbdem_server_destroy(s);
       if (rc != LBDEM_OK) return rc;
       if (best < 0.0 || t < best) {

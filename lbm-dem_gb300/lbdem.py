@@ -443,7 +443,8 @@ def tune_server(cfgs, cycles=40, precision=MIXED, device=0, max_active=0, slice_
     t = C.c_double()
     rc = lib.lbdem_server_tune(C.byref(o), arr, len(cfgs), int(cycles), C.byref(t))
     if rc:
-        raise RuntimeError(f"lbdem_server_tune: {ERRORS.get(rc, rc)}")
+        raise RuntimeError(f"lbdem_server_tune: {ERRORS.get(rc, rc)}: "
+                           f"{lib.lbdem_server_last_error(None).decode()}")
     return o.batch_runs, o.chunks_per_block, t.value
 
     def __del__(self):
