@@ -22,7 +22,10 @@ constexpr int PAIR_VALS = 18;    // per neighbour slot: contact(6) lub(9) rep(3)
 // per particle, mixed form: the 15 pair sums of the gather (FC, MC / radius,
 // FL, ML, FR), padded to a 64-byte line
 constexpr int SLOT_SUM_STRIDE = 16;
-constexpr int UNCOVER_CAP = 8192;// uncovered object nodes resolved per step
+#ifndef LBDEM_UNCOVER_CAP
+#define LBDEM_UNCOVER_CAP 8192
+#endif
+constexpr int UNCOVER_CAP = LBDEM_UNCOVER_CAP;  // uncovered object nodes resolved per step
 constexpr int ACCF_N = 13;       // mixed-form particle sums: d(3), r (x) d (9), mass(1)
 constexpr int ACCF_STRIDE = 16;  // floats per particle: its sums share one 64-byte line
 
