@@ -390,19 +390,23 @@ LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGatherMixed, DemArgs, dem) {
       }
     }
     if (!valid) continue;
-    // totals and integration in FP64
+    // totals in FP32 (the precision of the force sums), integration in FP64:
+    // v' = v + dt F/m, x' = x + dt v + dt^2 F/m = x + dt v', w' = w + dt M/I
     const double dtt = k.dt;
+    const double dtm = dtt * im, dtI = dtt * iI;
     for (int c = 0; c < 3; ++c) {
-      const double FT = FH[c] + (double)FC[c] + (double)FL[c] + FG[c] + (double)FR[c];
-      const double MT = MH[c] + (double)MC[c] + (double)ML[c];
-      const double xn = xa[c] + (dtt * va[c] + dtt * dtt * FT * im);
+      const float FTf = (float)FH[c] + FC[c] + FL[c] + (float)FG[c] + FR[c];
+      const float MTf = (float)MH[c] + MC[c] + ML[c];
+      const double FT = (double)FTf, MT = (double)MTf;
+      const double vn = fma(dtm, FT, va[c]);
+      const double xn = fma(dtt, vn, xa[c]);
       a.x0[c * P + i] = xn;
       if (c == 1) {  // particle::disp.y and x_i.y (src/DEM.cpp:2705, 2721-2724)
         a.dispY[i] = a.xinitY[i] - xn;
         if (stepNo == k.objWaitTime) a.xinitY[i] = xn;
       }
-      a.x1[c * P + i] = va[c] + dtt * FT * im;
-      a.w1[c * P + i] = waD[c] + dtt * MT * iI;
+      a.x1[c * P + i] = vn;
+      a.w1[c * P + i] = fma(dtI, MT, waD[c]);
       a.FContact[c * P + i] = FC[c];
       a.MContact[c * P + i] = MC[c];
       a.FLub[c * P + i] = FL[c];

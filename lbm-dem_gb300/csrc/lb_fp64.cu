@@ -375,8 +375,10 @@ __device__ __forceinline__ void lbFinalizeBody(const Consts& k, double* pF, doub
     pV[i] *= k.uVolume;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    for (int w = 0; w < k.nWall; ++w)
-      for (int c = 0; c < 3; ++c) wallF[w * 12 + c] *= k.uForce;
+    // (the mixed form's wall-force sweep adds its sums in physical units)
+    if (!k.mixed)
+      for (int w = 0; w < k.nWall; ++w)
+        for (int c = 0; c < 3; ++c) wallF[w * 12 + c] *= k.uForce;
     for (int o = 0; o < k.nObj; ++o)
       for (int c = 0; c < 3; ++c) {
         obj[o * OB_STRIDE + OB_FHYDRO + c] *= k.uForce;
@@ -866,11 +868,13 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
   __syncthreads();
   if (threadIdx.x == 0) iscal[IS_NUNCOVER] = 0;
   if (n == 0) return;
-  // the team: one thread per candidate (whole warps, at most the block); the
-  // others leave, and the team synchronises on named barrier 1, so that a
-  // handful of candidates costs a handful of warps' barriers, not 32
+  // the team: one thread per candidate (whole warps, at most the block)
+  // resolves the types, synchronising on named barrier 1, so that a handful
+  // of candidates costs a handful of warps' barriers, not 32; the other
+  // threads wait at the block barrier before the initialisation
   const int T = min((int)blockDim.x, (n + 31) & ~31);
-  if ((int)threadIdx.x >= T) return;
+  __shared__ int s_n;
+  if ((int)threadIdx.x < T) {
   int p2 = 1;
   while (p2 < n) p2 <<= 1;
   for (int i = threadIdx.x; i < p2; i += T) s_idx[i] = i < n ? list[i] : 0xffffffffu;
@@ -892,7 +896,6 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
       teamSync(T);
     }
   // the same node can appear once per object box: drop duplicates
-  __shared__ int s_n;
   if (k.nObj > 1) {
     if (threadIdx.x == 0) {
       int w = 0;
@@ -967,27 +970,37 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
       }
     if (!teamOr(T, changed)) break;
   }
+  if (threadIdx.x == 0) s_n = n;
+  }  // the team
+  // the new nodes' initialisation by the whole block, one (node, direction)
+  // per thread: the equilibria are FP64, and a thread per node would form
+  // nineteen of them one after the other
+  __syncthreads();
+  n = s_n;
   const double rho0 = k.initDensity;
-  for (int i = threadIdx.x; i < n; i += T) {
+  for (int q = threadIdx.x; q < n * Q; q += blockDim.x) {
+    const int i = q / Q, j = q - i * Q;
     const long long x = s_idx[i];
     const int st = s_st[i] & 0x0F;
-    const uint8_t m = mask[x];
-    mask[x] = (uint8_t)((m & ~TYPE_MASK) | st);
-    if (st != 2) markActive(k, x);
-    if (st == 2) {
-      mass[x] = 0.0;
-      continue;
+    if (j == 0) {
+      const uint8_t m = mask[x];
+      mask[x] = (uint8_t)((m & ~TYPE_MASK) | st);
+      if (st != 2) markActive(k, x);
+      if (st == 2) mass[x] = 0.0;
     }
+    if (st == 2) continue;
     // node::initialize(initDensity, initVelocity or 0, mass, visc, lbF)
     const double vx = st == 0 ? k.initVel[0] : 0.0, vy = st == 0 ? k.initVel[1] : 0.0,
                  vz = st == 0 ? k.initVel[2] : 0.0;
     const double ux = k.lbF[0] / 2.0 / rho0 + vx, uy = k.lbF[1] / 2.0 / rho0 + vy,
                  uz = k.lbF[2] / 2.0 / rho0 + vz;
     const double usq = ux * ux + uy * uy + uz * uz;
-    for (int j = 0; j < Q; ++j) fset(k, f, j, x, feqj(j, rho0, ux, uy, uz, usq));
-    mass[x] = st == 0 ? rho0 : 0.5 * rho0;
-    if (k.mixed && st == 0) nF[x] = (float)rho0;
-    if (k.visc) k.visc[x] = k.initVisc;
+    fset(k, f, j, x, feqj(j, rho0, ux, uy, uz, usq));
+    if (j == 0) {
+      mass[x] = st == 0 ? rho0 : 0.5 * rho0;
+      if (k.mixed && st == 0) nF[x] = (float)rho0;
+      if (k.visc) k.visc[x] = k.initVisc;
+    }
   }
 }
 

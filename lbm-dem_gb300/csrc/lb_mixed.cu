@@ -618,7 +618,7 @@ LBDEM_KERNEL(, lbWallForceMixed, LbArgs, lb) {
   }
   __syncthreads();
   for (int i = threadIdx.x; i < 3 * MAX_WALL; i += blockDim.x)
-    if (accW[i] != 0.0f) atomicAdd(a.wallF + (i / 3) * 12 + (i % 3), (double)accW[i]);
+    if (accW[i] != 0.0f) atomicAdd(a.wallF + (i / 3) * 12 + (i % 3), (double)accW[i] * k.uForce);
 }
 
 }  // namespace lbdem

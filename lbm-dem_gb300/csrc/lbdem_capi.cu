@@ -298,6 +298,9 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   CK(cudaStreamCreateWithFlags(&ctx->fsStream, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&ctx->fsFork, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&ctx->fsDone, cudaEventDisableTiming));
+  CK(cudaStreamCreateWithFlags(&ctx->sideStream, cudaStreamNonBlocking));
+  for (cudaEvent_t* e : {&ctx->prepFork, &ctx->prepDone, &ctx->wallFork, &ctx->wallDone})
+    CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   CK(cudaDeviceGetAttribute(&ctx->smCount, cudaDevAttrMultiProcessorCount, ctx->device));
   {
     int perSm = 0;
@@ -732,6 +735,12 @@ extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
   }
   if (ctx->fsFork) cudaEventDestroy(ctx->fsFork);
   if (ctx->fsDone) cudaEventDestroy(ctx->fsDone);
+  if (ctx->sideStream) {
+    cudaStreamSynchronize(ctx->sideStream);
+    cudaStreamDestroy(ctx->sideStream);
+  }
+  for (cudaEvent_t e : {ctx->prepFork, ctx->prepDone, ctx->wallFork, ctx->wallDone})
+    if (e) cudaEventDestroy(e);
   delete ctx;
 }
 
@@ -780,6 +789,10 @@ extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
     demPairsMixed<<<pairGrid, 128, 0, s>>>(k, a);
     if ((rc = enqueueStress(ctx, a))) return rc;
     demSlotSumsMixed<<<partGrid(ctx, GATHER_MIXED_PARTS), GATHER_MIXED_THREADS, 0, s>>>(k, a);
+    if (ctx->wallPendingMain) {  // the gather's last block reads the wall sums
+      CK(cudaStreamWaitEvent(s, ctx->wallDone, 0));
+      ctx->wallPendingMain = false;
+    }
     demGatherMixed<<<partGrid(ctx, GATHER_THREADS), GATHER_THREADS, 0, s>>>(k, a);
   } else {
     demPairs<<<pairGrid, 128, 0, s>>>(k, a);
@@ -791,6 +804,16 @@ extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
 }
 
 // LB::latticeBoltzmannCouplingStep
+// Start of the lattice step: per-step resets and the kinematics snapshot
+// (lbPrepare) on stream st.
+static void enqueuePrepare(lbdem_ctx* ctx, cudaStream_t st) {
+  Device& d = ctx->d;
+  const int P1 = std::max(ctx->nPart, 1);
+  lbPrepare<<<std::max(1, std::min(16 * P1 / 256 + 1, 1024)), 256, 0, st>>>(
+      ctx->k, d.pFHydro, 16LL * P1, d.pAccF, (long long)ACCF_STRIDE * P1, d.obj, d.wallF, d.scal,
+      d.iscal, d.px0, d.px1, d.pw1, d.pkd, d.pkf);
+}
+
 extern "C" int lbdem_coupling_step(lbdem_ctx* ctx) {
   if (!ctx) return LBDEM_ERR_INVALID;
   DeviceScope devScope(ctx->device);
@@ -798,6 +821,15 @@ extern "C" int lbdem_coupling_step(lbdem_ctx* ctx) {
   Device& d = ctx->d;
   cudaStream_t s = ctx->stream;
   const int lg = latticeGrid(ctx);
+  if (ctx->overlap && k.mixed && ctx->lbSolve && ctx->demTime >= ctx->demInitialRepeat) {
+    // the lattice step's preparation (accumulator resets, kinematics
+    // snapshot) touches nothing the coupling kernels read or write
+    CK(cudaEventRecord(ctx->prepFork, s));
+    CK(cudaStreamWaitEvent(ctx->sideStream, ctx->prepFork, 0));
+    enqueuePrepare(ctx, ctx->sideStream);
+    CK(cudaEventRecord(ctx->prepDone, ctx->sideStream));
+    ctx->prepPending = true;
+  }
   if (ctx->nObj > 0) {
     uncoverCollect<<<ctx->gridObj, 256, 0, s>>>(k, d.mask, d.solid, d.obj, d.uncover, d.iscal);
     uncoverResolve<<<1, 1024, UNCOVER_SMEM, s>>>(k, d.mask, d.f[ctx->cur], d.mass, d.nF, d.uncover,
@@ -824,10 +856,12 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   const Consts& k = ctx->k;
   Device& d = ctx->d;
   cudaStream_t s = ctx->stream;
-  const int P1 = std::max(ctx->nPart, 1);
-  lbPrepare<<<std::max(1, std::min(16 * P1 / 256 + 1, 1024)), 256, 0, s>>>(
-      k, d.pFHydro, 16LL * P1, d.pAccF, (long long)ACCF_STRIDE * P1, d.obj, d.wallF, d.scal, d.iscal,
-      d.px0, d.px1, d.pw1, d.pkd, d.pkf);
+  if (ctx->prepPending) {
+    CK(cudaStreamWaitEvent(s, ctx->prepDone, 0));
+    ctx->prepPending = false;
+  } else {
+    enqueuePrepare(ctx, s);
+  }
   LbArgs a = lbArgs(ctx);
   auto* ev = nextLbEvents(ctx);
   if (ev) cudaEventRecord(ev->first, s);
@@ -838,7 +872,15 @@ extern "C" int lbdem_lb_step(lbdem_ctx* ctx) {
   else lbStepFp64<<<ctx->smCount * 4, 256, 0, s>>>(k, a);
   if (ev) cudaEventRecord(ev->second, s);
   if (k.mixed && k.nWall > 0 && k.wallType >= 7) {
-    lbWallForceMixed<<<dim3(ctx->gridShell, 6), 256, 0, s>>>(k, a);
+    if (ctx->overlap) {
+      CK(cudaEventRecord(ctx->wallFork, s));
+      CK(cudaStreamWaitEvent(ctx->sideStream, ctx->wallFork, 0));
+      lbWallForceMixed<<<dim3(ctx->gridShell, 6), 256, 0, ctx->sideStream>>>(k, a);
+      CK(cudaEventRecord(ctx->wallDone, ctx->sideStream));
+      ctx->wallPendingFs = ctx->wallPendingMain = true;
+    } else {
+      lbWallForceMixed<<<dim3(ctx->gridShell, 6), 256, 0, s>>>(k, a);
+    }
     ctx->launches += 1;
   }
   if (k.wallType == 5 || k.wallType == 6) {
@@ -866,6 +908,10 @@ extern "C" int lbdem_free_surface_step(lbdem_ctx* ctx) {
   const int g = ctx->gridFs;
   FsArgs a = fsArgs(ctx);
   fsUpdateMass<<<g, 256, 0, s>>>(k, a);
+  if (ctx->wallPendingFs) {  // the wall sweep reads node types that fsMutants changes
+    CK(cudaStreamWaitEvent(s, ctx->wallDone, 0));
+    ctx->wallPendingFs = false;
+  }
   fsMutants<<<g, 256, 0, s>>>(k, a);
   fsSmoothen<<<g, 256, 0, s>>>(k, a);
   fsMutantsAndFill<<<g, 256, 0, s>>>(k, a);
@@ -1013,10 +1059,18 @@ int captureCycles(lbdem_ctx* ctx, int cycles, cudaGraphExec_t* exec, long long* 
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   const long long before = ctx->launches;
   int rc = LBDEM_OK;
+  ctx->overlap = ctx->k.mixed != 0;
   for (int c = 0; c < cycles && rc == LBDEM_OK; ++c) rc = cycleOnce(ctx, c + 1 < cycles);
+  ctx->overlap = false;
   // the capture ends on the context's stream with every fork joined
   const int rj = joinFreeSurface(ctx);
   if (rc == LBDEM_OK) rc = rj;
+  if (ctx->wallPendingMain || ctx->wallPendingFs || ctx->prepPending) {
+    const cudaEvent_t e = ctx->prepPending ? ctx->prepDone : ctx->wallDone;
+    const cudaError_t ew = cudaStreamWaitEvent(ctx->stream, e, 0);
+    if (rc == LBDEM_OK && ew != cudaSuccess) rc = setErr(ctx, LBDEM_ERR_CUDA, "graph capture join");
+    ctx->wallPendingMain = ctx->wallPendingFs = ctx->prepPending = false;
+  }
   const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
   if (rc) {
     if (g) cudaGraphDestroy(g);

@@ -301,6 +301,14 @@ struct lbdem_ctx {
   cudaStream_t fsStream = nullptr;
   cudaEvent_t fsFork = nullptr, fsDone = nullptr;
   bool fsPending = false;  // a forked free-surface step not yet joined
+  // mixed form, captured cycles: lbPrepare runs on sideStream beside the
+  // coupling step, and the wall-force sweep beside the finalisation and the
+  // interface mass update (joined before the interface types change) and
+  // the next DEM step (joined before the gather, which reads the wall sums)
+  bool overlap = false;
+  cudaStream_t sideStream = nullptr;
+  cudaEvent_t prepFork = nullptr, prepDone = nullptr, wallFork = nullptr, wallDone = nullptr;
+  bool prepPending = false, wallPendingFs = false, wallPendingMain = false;
   int device = 0;
   int precision = LBDEM_PLAIN_FP64;
   int check_every = 0;
