@@ -62,6 +62,11 @@ __device__ __forceinline__ void demBeginBody(const Consts& k, const DemArgs& a, 
     const double vx = a.x1[i], vy = a.x1[P + i], vz = a.x1[2 * P + i];
     const double n2 = vx * vx + vy * vy + vz * vz;
     if (n2 > m) m = n2;
+    if (a.kinf) {  // mixed form: this step's FP32 kinematics for the pair pass
+      a.kinf[2 * i] = make_float4((float)vx, (float)vy, (float)vz, (float)a.r[i]);
+      a.kinf[2 * i + 1] =
+          make_float4((float)a.w1[i], (float)a.w1[P + i], (float)a.w1[2 * P + i], 0.0f);
+    }
   }
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;

@@ -71,6 +71,41 @@ __device__ __forceinline__ PairGeom<float> pairGeomM(double rad, const double* d
   return g;
 }
 
+// The same for a particle pair from the FP64 separation d and the FP32
+// relative velocity u and radii; near contact the mean radius is taken from
+// the FP64 radii of particles i and j.
+__device__ __forceinline__ PairGeom<float> pairGeomMf(const DemArgs& a, int i, int j, float ra,
+                                                      float rb, const double* d, const float* u) {
+  PairGeom<float> g;
+  const float dx = (float)d[0], dy = (float)d[1], dz = (float)d[2];
+  const float r2 = dx * dx + dy * dy + dz * dz;
+  const float lim = (float)(2.0 + NEAR_GAP) * (0.5f * (ra + rb));
+  if (r2 < lim * lim) {
+    const double rad = 0.5 * (a.r[i] + a.r[j]);
+    const double r2d = fma(d[0], d[0], fma(d[1], d[1], d[2] * d[2]));
+    const double y = rsqrtNewton(r2d);
+    const double r12 = r2d * y;
+    g.r12 = (float)r12;
+    g.gap = (float)(r12 - 2.0 * rad);
+    const float yf = (float)y;
+    g.n[0] = dx * yf;
+    g.n[1] = dy * yf;
+    g.n[2] = dz * yf;
+  } else {
+    const float r12 = sqrtf(r2);
+    g.r12 = r12;
+    g.gap = r12 - (ra + rb);
+    const float inv = 1.0f / r12;
+    g.n[0] = dx * inv;
+    g.n[1] = dy * inv;
+    g.n[2] = dz * inv;
+  }
+  g.u[0] = u[0];
+  g.u[1] = u[1];
+  g.u[2] = u[2];
+  return g;
+}
+
 // Offset of particle x from wall W along its normal, and its length: the
 // differences from the wall point in FP64, the rest in FP32 except within
 // NEAR_GAP radii of contact, where the offset is taken in FP64.
@@ -115,17 +150,17 @@ LBDEM_KERNEL(, demPairsMixed, DemArgs, dem) {
     const int idx = a.pairList[e];
     const int i = idx / MAX_N, s = idx % MAX_N;
     const int j = L[idx];
-    double d[3], u[3];
-    for (int c = 0; c < 3; ++c) {
-      d[c] = a.x0[c * P + i] - a.x0[c * P + j];
-      u[c] = a.x1[c * P + i] - a.x1[c * P + j];
-    }
-    float wa[3], wb[3];
-    load3f(a.w1, P, i, wa);
-    load3f(a.w1, P, j, wb);
-    const double raD = a.r[i], rbD = a.r[j];
-    const float ra = (float)raD, rb = (float)rbD;
-    const PairGeom<float> g = pairGeomM(0.5 * (raD + rbD), d, u);
+    // separation in FP64 (near contact the gap is a small difference of
+    // large numbers); velocities, angular velocities and radii from this
+    // step's FP32 copies
+    double d[3];
+    for (int c = 0; c < 3; ++c) d[c] = a.x0[c * P + i] - a.x0[c * P + j];
+    const float4 va4 = a.kinf[2 * i], vb4 = a.kinf[2 * j];
+    const float4 wa4 = a.kinf[2 * i + 1], wb4 = a.kinf[2 * j + 1];
+    const float wa[3] = {wa4.x, wa4.y, wa4.z}, wb[3] = {wb4.x, wb4.y, wb4.z};
+    const float ra = va4.w, rb = vb4.w;
+    const float uf[3] = {va4.x - vb4.x, va4.y - vb4.y, va4.z - vb4.z};
+    const PairGeom<float> g = pairGeomMf(a, i, j, ra, rb, d, uf);
     float out[PAIR_VALS];
     uint8_t flag = 0;
     if (lubOn && pairLub(k, ra, rb, g, wa, wb, out + 6)) flag |= 1;

@@ -73,6 +73,7 @@ struct DemArgs {
   float* slotSum;  // [P][SLOT_SUM_STRIDE] mixed form: demSlotSumsMixed -> demGatherMixed
   int* pcell;
   float4* posf;  // [P] FP32 position and radius, written by nbrCellAssign
+  float4* kinf;  // [P][2] mixed form: (v, r) and (w, 0) in FP32, written by demBegin
   // particle::x_i.y (position at the start, again after the objWaitTime
   // step) and disp.y = x_i.y - x0.y after each integration (src/DEM.cpp:288,
   // 2705, 2721-2724); read only by the particle recycle file
@@ -137,13 +138,18 @@ __device__ __forceinline__ void stageRecord(T& dst, const T& src) {
   for (int i = threadIdx.x; i < (int)(sizeof(T) / 8); i += blockDim.x) d[i] = s[i];
 }
 
+// Parameters of the single-run entry points: grid constants, so that
+// passing them on by reference (to functions that are not inlined) reads
+// the parameter space instead of copying the records to local memory.
+#define LBDEM_KPARAMS(ARGT) const __grid_constant__ Consts k, const __grid_constant__ ARGT a
+
 // A kernel taking (Consts, ARGT) in two entry points: NAME for one run
 // (arguments by value) and NAME##Batch for many runs at once, which stages
 // run blockIdx.z's record in shared memory. Both run NAME##Body, which
 // follows the macro as the function body.
 #define LBDEM_KERNEL(BOUNDS, NAME, ARGT, FIELD)                                  \
   __device__ __forceinline__ void NAME##Body(const Consts& k, const ARGT& a);   \
-  __global__ void BOUNDS NAME(Consts k, ARGT a) { NAME##Body(k, a); }           \
+  __global__ void BOUNDS NAME(LBDEM_KPARAMS(ARGT)) { NAME##Body(k, a); }       \
   __global__ void BOUNDS NAME##Batch(const JobArgs* jobs) {                     \
     __shared__ __align__(16) Consts sk;                                          \
     __shared__ __align__(16) ARGT sa;                                            \
@@ -204,13 +210,13 @@ constexpr int MIXED_SMEM = MIXED_STAGES * MIXED_STAGE_BYTES;
 constexpr int MIXED_MAX_MINE = 2048;
 
 // lb_fp64.cu / lb_mixed.cu
-__global__ void lbStepFp64(Consts k, LbArgs a);
+__global__ void lbStepFp64(LBDEM_KPARAMS(LbArgs));
 __global__ void lbStepFp64Batch(const JobArgs* jobs);
-__global__ void lbStepFp64Rheo(Consts k, LbArgs a);
+__global__ void lbStepFp64Rheo(LBDEM_KPARAMS(LbArgs));
 __global__ void lbStepFp64RheoBatch(const JobArgs* jobs);
-__global__ void lbStepMixed(Consts k, LbArgs a);
+__global__ void lbStepMixed(LBDEM_KPARAMS(LbArgs));
 __global__ void lbStepMixedBatch(const JobArgs* jobs);
-__global__ void lbWallForceMixed(Consts k, LbArgs a);
+__global__ void lbWallForceMixed(LBDEM_KPARAMS(LbArgs));
 __global__ void lbWallForceMixedBatch(const JobArgs* jobs);
 __global__ void lbPrepare(Consts k, double* pAcc, long long pAccLen, float* pAccF,
                           long long pAccFLen, double* obj, double* wallF, double* scal,
@@ -219,17 +225,17 @@ __global__ void lbPrepare(Consts k, double* pAcc, long long pAccLen, float* pAcc
 __global__ void lbFinalizeKernel(Consts k, double* pF, double* pM, double* pV, double* obj,
                                  double* wallF, double* scal, const int* iscal,
                                  const float* pAccF, double* pS, FsArgs fa, int redistribute);
-__global__ void fsUpdateMass(Consts k, FsArgs a);
+__global__ void fsUpdateMass(LBDEM_KPARAMS(FsArgs));
 __global__ void fsUpdateMassBatch(const JobArgs* jobs);
-__global__ void fsMutants(Consts k, FsArgs a);
+__global__ void fsMutants(LBDEM_KPARAMS(FsArgs));
 __global__ void fsMutantsBatch(const JobArgs* jobs);
-__global__ void fsSmoothen(Consts k, FsArgs a);
+__global__ void fsSmoothen(LBDEM_KPARAMS(FsArgs));
 __global__ void fsSmoothenBatch(const JobArgs* jobs);
-__global__ void fsMutantsAndFill(Consts k, FsArgs a);
+__global__ void fsMutantsAndFill(LBDEM_KPARAMS(FsArgs));
 __global__ void fsMutantsAndFillBatch(const JobArgs* jobs);
-__global__ void fsEmptyIsolated(Consts k, FsArgs a);
+__global__ void fsEmptyIsolated(LBDEM_KPARAMS(FsArgs));
 __global__ void fsEmptyIsolatedBatch(const JobArgs* jobs);
-__global__ void fsRedistribute(Consts k, FsArgs a);
+__global__ void fsRedistribute(LBDEM_KPARAMS(FsArgs));
 __global__ void fsRedistributeBatch(const JobArgs* jobs);
 __global__ void uncoverCollect(Consts k, const uint8_t* mask, const uint32_t* solid,
                                const double* obj,
@@ -237,6 +243,8 @@ __global__ void uncoverCollect(Consts k, const uint8_t* mask, const uint32_t* so
 // dynamic shared memory of uncoverResolve: candidates, their lower-index
 // candidate neighbours and states
 constexpr int UNCOVER_SMEM = UNCOVER_CAP * (4 + 9 * 2 + 1);
+// uncovered nodes up to this many are resolved by one thread in order
+constexpr int UNCOVER_SERIAL = 256;
 __global__ void uncoverResolve(Consts k, uint8_t* mask, void* f, double* mass, float* nF,
                                uint32_t* list, int* iscal);
 __global__ void voxelizeObjects(Consts k, uint8_t* mask, uint32_t* solid, uint8_t* objIdx,
@@ -286,35 +294,35 @@ __global__ void demStress(Consts k, DemArgs a, const double* SHydro, double* out
 
 // dem_fp64.cu
 __global__ void demBegin(Consts k, DemArgs a, int forceRebuild);
-__global__ void nbrCellAssign(Consts k, DemArgs a);
+__global__ void nbrCellAssign(LBDEM_KPARAMS(DemArgs));
 __global__ void nbrCellAssignBatch(const JobArgs* jobs);
-__global__ void nbrCellScan(Consts k, DemArgs a);
+__global__ void nbrCellScan(LBDEM_KPARAMS(DemArgs));
 __global__ void nbrCellScanBatch(const JobArgs* jobs);
-__global__ void nbrCellScatter(Consts k, DemArgs a);
+__global__ void nbrCellScatter(LBDEM_KPARAMS(DemArgs));
 __global__ void nbrCellScatterBatch(const JobArgs* jobs);
-__global__ void nbrCellSort(Consts k, DemArgs a);
+__global__ void nbrCellSort(LBDEM_KPARAMS(DemArgs));
 __global__ void nbrCellSortBatch(const JobArgs* jobs);
-__global__ void nbrBuildCells(Consts k, DemArgs a);
+__global__ void nbrBuildCells(LBDEM_KPARAMS(DemArgs));
 __global__ void nbrBuildCellsBatch(const JobArgs* jobs);
-__global__ void nbrBuildDirect(Consts k, DemArgs a);
+__global__ void nbrBuildDirect(LBDEM_KPARAMS(DemArgs));
 __global__ void nbrBuildDirectBatch(const JobArgs* jobs);
-__global__ void nbrDirectHistory(Consts k, DemArgs a);
+__global__ void nbrDirectHistory(LBDEM_KPARAMS(DemArgs));
 __global__ void nbrDirectHistoryBatch(const JobArgs* jobs);
-__global__ void nbrPartners(Consts k, DemArgs a);
+__global__ void nbrPartners(LBDEM_KPARAMS(DemArgs));
 __global__ void nbrPartnersBatch(const JobArgs* jobs);
-__global__ void nbrPairList(Consts k, DemArgs a);
+__global__ void nbrPairList(LBDEM_KPARAMS(DemArgs));
 __global__ void nbrPairListBatch(const JobArgs* jobs);
 // the DEM step number comes from iscal[IS_DEMSTEP] (advanced by demBegin)
-__global__ void demPairs(Consts k, DemArgs a);
+__global__ void demPairs(LBDEM_KPARAMS(DemArgs));
 __global__ void demPairsBatch(const JobArgs* jobs);
-__global__ void demGather(Consts k, DemArgs a);
+__global__ void demGather(LBDEM_KPARAMS(DemArgs));
 __global__ void demGatherBatch(const JobArgs* jobs);
 // dem_mixed.cu: the force passes of the mixed form (FP32 force laws)
-__global__ void demPairsMixed(Consts k, DemArgs a);
+__global__ void demPairsMixed(LBDEM_KPARAMS(DemArgs));
 __global__ void demPairsMixedBatch(const JobArgs* jobs);
-__global__ void demSlotSumsMixed(Consts k, DemArgs a);
+__global__ void demSlotSumsMixed(LBDEM_KPARAMS(DemArgs));
 __global__ void demSlotSumsMixedBatch(const JobArgs* jobs);
-__global__ void demGatherMixed(Consts k, DemArgs a);
+__global__ void demGatherMixed(LBDEM_KPARAMS(DemArgs));
 __global__ void demGatherMixedBatch(const JobArgs* jobs);
 
 // many-run entry points of the kernels with their own parameter lists

@@ -505,6 +505,41 @@ __device__ __forceinline__ bool slipOneActive(const Consts& k, const uint8_t* ma
   return slipPartner(k, mask, x, j, c, s) != 0;
 }
 
+// The exchange sum of one interface node in FP64 (the plain form, and the
+// mixed form's nodes with a wall or impactor link), in link order. Kept out
+// of line so that the mixed form's FP32 path keeps few registers.
+__device__ __noinline__ double fsMassDeltaFp64(const Consts& k, const FsArgs& a, long long x,
+                                               uint8_t m, int ix, int iy, int iz, double mx,
+                                               unsigned liq, unsigned ifc, unsigned wal,
+                                               unsigned slp) {
+  double fsl[Q];
+  if (wal) fsPostCollision(k, a, x, m, ix, iy, iz, fsl);
+  double delta = 0.0;
+  bool first = true;
+#pragma unroll
+  for (int j = 1; j < Q; ++j) {
+    double term;
+    if ((liq >> j) & 1u) {
+      const long long lk = x + nbrOffset(k, j);
+      const double ms = fdiff(k, a.fcur, OPPJ(j), x, j, lk);
+      term = ((ifc >> j) & 1u) ? 0.5 * (a.mass[lk] + mx) * ms : 1.0 * ms;
+    } else if ((wal >> j) & 1u) {
+      // f_opp(x) after streaming minus the population x sent into the wall
+      const double ms = k.mixed
+          ? (double)((const float*)a.fcur)[(long long)OPPJ(j) * k.NP + x] - fsl[j]
+          : ((const double*)a.fcur)[(long long)OPPJ(j) * k.NP + x] - fsl[j];
+      double w = 1.0;  // averageMass = w * mass (src/LB.cpp:1581-1625)
+      if (((slp >> j) & 1u) && j > 6 && slipOneActive(k, a.mask, x, j)) w = 1.0 - k.slipS1;
+      term = (w * mx) * ms;
+    } else {
+      continue;
+    }
+    delta = first ? term : delta + term;
+    first = false;
+  }
+  return delta;
+}
+
 // LB::updateMass (interface part). The neighbour types are read first, all
 // links at once; the mass exchange terms are then summed in link order.
 LBDEM_KERNEL(__launch_bounds__(256, 2), fsUpdateMass, FsArgs, fs) {
@@ -555,32 +590,7 @@ LBDEM_KERNEL(__launch_bounds__(256, 2), fsUpdateMass, FsArgs, fs) {
       a.massNew[x] = mx + (double)dl;
       continue;
     }
-    double fsl[Q];
-    if (wal) fsPostCollision(k, a, x, m, ix, iy, iz, fsl);
-    double delta = 0.0;
-    bool first = true;
-#pragma unroll
-    for (int j = 1; j < Q; ++j) {
-      double term;
-      if ((liq >> j) & 1u) {
-        const long long lk = x + nbrOffset(k, j);
-        const double ms = fdiff(k, a.fcur, OPPJ(j), x, j, lk);
-        term = ((ifc >> j) & 1u) ? 0.5 * (a.mass[lk] + mx) * ms : 1.0 * ms;
-      } else if ((wal >> j) & 1u) {
-        // f_opp(x) after streaming minus the population x sent into the wall
-        const double ms = k.mixed
-            ? (double)((const float*)a.fcur)[(long long)OPPJ(j) * k.NP + x] - fsl[j]
-            : ((const double*)a.fcur)[(long long)OPPJ(j) * k.NP + x] - fsl[j];
-        double w = 1.0;  // averageMass = w * mass (src/LB.cpp:1581-1625)
-        if (((slp >> j) & 1u) && j > 6 && slipOneActive(k, a.mask, x, j)) w = 1.0 - k.slipS1;
-        term = (w * mx) * ms;
-      } else {
-        continue;
-      }
-      delta = first ? term : delta + term;
-      first = false;
-    }
-    a.massNew[x] = mx + delta;
+    a.massNew[x] = mx + fsMassDeltaFp64(k, a, x, m, ix, iy, iz, mx, liq, ifc, wal, slp);
   }
 }
 
@@ -835,19 +845,92 @@ __device__ __forceinline__ void uncoverCollectBody(const Consts& k, const uint8_
 }
 
 // Named barrier 1 over the first nthreads threads of the block (a multiple
-// of 32), and the same barrier returning whether v was non-zero in any of them.
+// of 32), and the same barrier returning whether v was non-zero in any of
+// them (the non-aligned forms: a warp may arrive with its lanes diverged).
 __device__ __forceinline__ void teamSync(int nthreads) {
-  asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+  asm volatile("barrier.sync 1, %0;" ::"r"(nthreads) : "memory");
 }
 __device__ __forceinline__ int teamOr(int nthreads, int v) {
   int r;
   asm volatile(
       "{\n .reg .pred p, q;\n setp.ne.s32 p, %1, 0;\n"
-      " bar.red.or.pred q, 1, %2, p;\n selp.s32 %0, 1, 0, q;\n}"
+      " barrier.red.or.pred q, 1, %2, p;\n selp.s32 %0, 1, 0, q;\n}"
       : "=r"(r)
       : "r"(v), "r"(nthreads)
       : "memory");
   return r;
+}
+
+// uncoverResolve for n <= 32 candidates of one impactor, by one warp:
+// lane l holds candidate l (after a shuffle bitonic sort, ascending node
+// index). Each lane records which lower lanes are its neighbours (a bit
+// mask) and the fixed types of its other neighbours; the fixed-point
+// iteration then takes two ballots per round. Results go to s_idx / s_st
+// (bits 0-3 the new type) for the block's initialisation.
+__device__ __forceinline__ void uncoverResolveWarp(const Consts& k, const uint8_t* mask,
+                                                const uint32_t* list, int n, uint32_t* s_idx,
+                                                uint8_t* s_st, int* s_n) {
+  const unsigned FULLM = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  uint32_t x = lane < n ? list[lane] : 0xffffffffu;
+#pragma unroll
+  for (int size = 2; size <= 32; size <<= 1)
+#pragma unroll
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      const uint32_t other = __shfl_xor_sync(FULLM, x, stride);
+      const bool up = (lane & size) == 0, low = (lane & stride) == 0;
+      x = (low == up) ? min(x, other) : max(x, other);
+    }
+  const bool valid = lane < n;
+  int ix = 0, iy = 0, iz = 0;
+  if (valid) coords(k, (long long)x, ix, iy, iz);
+  uint32_t lk[Q];
+  unsigned inb = 0;  // links within the lattice
+#pragma unroll
+  for (int j = 1; j < Q; ++j) {
+    const int tx = ix + CX(j), ty = iy + CY(j), tz = iz + CZ(j);
+    const bool in = valid && tx >= 0 && tx < k.X && ty >= 0 && ty < k.Y && tz >= 0 && tz < k.Z;
+    inb |= (unsigned)in << j;
+    lk[j] = in ? x + (uint32_t)nbrOffset(k, j) : 0xffffffffu;
+  }
+  // which links end on a candidate; lower candidates as a lane mask
+  unsigned candLinks = 0, back = 0;
+  for (int b = 0; b < n; ++b) {
+    const uint32_t xb = __shfl_sync(FULLM, x, b);
+#pragma unroll
+    for (int j = 1; j < Q; ++j)
+      if (lk[j] == xb) {
+        candLinks |= 1u << j;
+        if (b < lane) back |= 1u << b;
+      }
+  }
+  // the other neighbours' types (a higher candidate reads as an impactor node)
+  bool fixFluid = false, fixGas = false;
+  uint8_t tls[Q];
+#pragma unroll
+  for (int j = 1; j < Q; ++j)
+    tls[j] = ((inb & ~candLinks) >> j) & 1u ? (uint8_t)(mask[lk[j]] & TYPE_MASK) : (uint8_t)0xFF;
+#pragma unroll
+  for (int j = 1; j < Q; ++j) {
+    fixFluid |= tls[j] == 0;
+    fixGas |= tls[j] == 2;
+  }
+  uint8_t st = 12;  // unresolved: neither fluid nor gas to its neighbours
+  for (int it = 0; it <= n; ++it) {
+    const unsigned fluidL = __ballot_sync(FULLM, valid && st == 0);
+    const unsigned gasL = __ballot_sync(FULLM, valid && st == 2);
+    const bool fluidNb = fixFluid || (back & fluidL) != 0;
+    const bool gasNb = fixGas || (back & gasL) != 0;
+    const uint8_t nst = !fluidNb ? 2 : gasNb ? 3 : 0;
+    const bool changed = valid && nst != st;
+    if (valid) st = nst;
+    if (!__any_sync(FULLM, changed)) break;
+  }
+  if (valid) {
+    s_idx[lane] = x;
+    s_st[lane] = st;
+  }
+  if (lane == 0) *s_n = n;
 }
 
 // findNewActiveObject, step 2 (one CTA): resolve the uncovered nodes in the
@@ -874,7 +957,11 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
   // threads wait at the block barrier before the initialisation
   const int T = min((int)blockDim.x, (n + 31) & ~31);
   __shared__ int s_n;
-  if ((int)threadIdx.x < T) {
+  if (n <= 32 && k.nObj == 1) {
+    // up to 32 candidates of one impactor: warp 0 alone, one candidate per
+    // lane, in registers (no duplicates: one object box)
+    if (threadIdx.x < 32) uncoverResolveWarp(k, mask, list, n, s_idx, s_st, &s_n);
+  } else if ((int)threadIdx.x < T) {
   int p2 = 1;
   while (p2 < n) p2 <<= 1;
   for (int i = threadIdx.x; i < p2; i += T) s_idx[i] = i < n ? list[i] : 0xffffffffu;
@@ -928,15 +1015,23 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
     const uint32_t x = s_idx[i];
     int ix, iy, iz;
     coords(k, (long long)x, ix, iy, iz);
-    uint8_t fix = 0;
-    int nb = 0;
+    // the neighbours' types, all loads issued before any is used
+    uint8_t tls[Q];
+#pragma unroll
     for (int j = 1; j < Q; ++j) {
       const int tx = ix + CX(j), ty = iy + CY(j), tz = iz + CZ(j);
-      if (tx < 0 || tx >= k.X || ty < 0 || ty >= k.Y || tz < 0 || tz >= k.Z) continue;
+      const bool in = tx >= 0 && tx < k.X && ty >= 0 && ty < k.Y && tz >= 0 && tz < k.Z;
+      tls[j] = in ? (uint8_t)(mask[x + (uint32_t)nbrOffset(k, j)] & TYPE_MASK) : (uint8_t)0xFF;
+    }
+    uint8_t fix = 0;
+    int nb = 0;
+#pragma unroll
+    for (int j = 1; j < Q; ++j) {
+      if (tls[j] == 0xFF) continue;
       const uint32_t lk = x + (uint32_t)nbrOffset(k, j);
       const int mid = find(lk);
       if (mid < 0) {
-        const int tl = mask[lk] & TYPE_MASK;
+        const int tl = tls[j];
         fix |= (uint8_t)((tl == 0 ? 0x10 : 0) | (tl == 2 ? 0x20 : 0));
       } else if (mid < i && nb < 9) {
         s_back[9 * i + nb++] = (int16_t)mid;
@@ -946,38 +1041,72 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
     s_st[i] = (uint8_t)(12 | fix);
   }
   teamSync(T);
-  for (int iter = 0; iter <= n; ++iter) {
-    int changed = 0;
-    uint8_t nst[UNCOVER_CAP / 1024];
-    for (int i = threadIdx.x, q = 0; i < n; i += T, ++q) {
-      const uint8_t me = s_st[i];
-      bool fluidNb = (me & 0x10) != 0, gasNb = (me & 0x20) != 0;
+  // the new state of candidate i from the states of its lower-index
+  // candidate neighbours and its fixed neighbour bits
+  auto resolve = [&](int i) -> uint8_t {
+    const uint8_t me = s_st[i];
+    bool fluidNb = (me & 0x10) != 0, gasNb = (me & 0x20) != 0;
 #pragma unroll
-      for (int b = 0; b < 9; ++b) {
-        const int m = s_back[9 * i + b];
-        if (m < 0) break;
-        const int tl = s_st[m] & 0x0F;
-        fluidNb |= tl == 0;
-        gasNb |= tl == 2;
-      }
-      nst[q] = (uint8_t)((me & 0x30) | (!fluidNb ? 2 : gasNb ? 3 : 0));
+    for (int b = 0; b < 9; ++b) {
+      const int m = s_back[9 * i + b];
+      if (m < 0) break;
+      const int tl = s_st[m] & 0x0F;
+      fluidNb |= tl == 0;
+      gasNb |= tl == 2;
     }
-    teamSync(T);
-    for (int i = threadIdx.x, q = 0; i < n; i += T, ++q)
-      if (s_st[i] != nst[q]) {
-        s_st[i] = nst[q];
-        changed = 1;
+    return (uint8_t)((me & 0x30) | (!fluidNb ? 2 : gasNb ? 3 : 0));
+  };
+  if (n <= UNCOVER_SERIAL) {
+    // few candidates: one thread in ascending order, the reference's own
+    // serial order (each sees the lower-index ones already resolved)
+    if (threadIdx.x == 0)
+      for (int i = 0; i < n; ++i) s_st[i] = resolve(i);
+  } else {
+    // many: fixed-point iteration, every candidate at once; the lower-index
+    // dependencies form chains, so it settles within n + 1 rounds
+    for (int iter = 0; iter <= n; ++iter) {
+      int changed = 0;
+      uint8_t nst[UNCOVER_CAP / 1024];
+#pragma unroll
+      for (int q = 0; q < UNCOVER_CAP / 1024; ++q) {
+        const int i = threadIdx.x + q * T;
+        if (i < n) nst[q] = resolve(i);
       }
-    if (!teamOr(T, changed)) break;
+      teamSync(T);
+#pragma unroll
+      for (int q = 0; q < UNCOVER_CAP / 1024; ++q) {
+        const int i = threadIdx.x + q * T;
+        if (i < n && s_st[i] != nst[q]) {
+          s_st[i] = nst[q];
+          changed = 1;
+        }
+      }
+      if (!teamOr(T, changed)) break;
+    }
   }
+  teamSync(T);
   if (threadIdx.x == 0) s_n = n;
   }  // the team
   // the new nodes' initialisation by the whole block, one (node, direction)
   // per thread: the equilibria are FP64, and a thread per node would form
   // nineteen of them one after the other
+  // node::initialize(initDensity, initVelocity or 0, mass, visc, lbF): the
+  // equilibria depend only on the direction and on whether the node becomes
+  // fluid (initial velocity) or interface (none), so the 2 x 19 values are
+  // formed once
+  __shared__ double s_feq[2][Q];
+  const double rho0 = k.initDensity;
+  if (threadIdx.x < 2 * Q) {
+    const int c = threadIdx.x / Q, j = threadIdx.x - c * Q;
+    const double vx = c == 0 ? k.initVel[0] : 0.0, vy = c == 0 ? k.initVel[1] : 0.0,
+                 vz = c == 0 ? k.initVel[2] : 0.0;
+    const double ux = k.lbF[0] / 2.0 / rho0 + vx, uy = k.lbF[1] / 2.0 / rho0 + vy,
+                 uz = k.lbF[2] / 2.0 / rho0 + vz;
+    const double usq = ux * ux + uy * uy + uz * uz;
+    s_feq[c][j] = feqj(j, rho0, ux, uy, uz, usq);
+  }
   __syncthreads();
   n = s_n;
-  const double rho0 = k.initDensity;
   for (int q = threadIdx.x; q < n * Q; q += blockDim.x) {
     const int i = q / Q, j = q - i * Q;
     const long long x = s_idx[i];
@@ -989,13 +1118,7 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
       if (st == 2) mass[x] = 0.0;
     }
     if (st == 2) continue;
-    // node::initialize(initDensity, initVelocity or 0, mass, visc, lbF)
-    const double vx = st == 0 ? k.initVel[0] : 0.0, vy = st == 0 ? k.initVel[1] : 0.0,
-                 vz = st == 0 ? k.initVel[2] : 0.0;
-    const double ux = k.lbF[0] / 2.0 / rho0 + vx, uy = k.lbF[1] / 2.0 / rho0 + vy,
-                 uz = k.lbF[2] / 2.0 / rho0 + vz;
-    const double usq = ux * ux + uy * uy + uz * uz;
-    fset(k, f, j, x, feqj(j, rho0, ux, uy, uz, usq));
+    fset(k, f, j, x, s_feq[st == 0 ? 0 : 1][j]);
     if (j == 0) {
       mass[x] = st == 0 ? rho0 : 0.5 * rho0;
       if (k.mixed && st == 0) nF[x] = (float)rho0;

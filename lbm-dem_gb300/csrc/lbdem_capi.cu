@@ -202,6 +202,7 @@ DemArgs demArgs(lbdem_ctx* c) {
   a.pairbuf = d.pairbuf;
   a.pairflag = d.pairflag;
   a.slotSum = d.slotSum;
+  a.kinf = d.kinf;
   a.pcell = d.pcell;
   a.posf = d.posf;
   a.ppos = d.ppos;
@@ -234,13 +235,18 @@ int enqueueNeighbourList(lbdem_ctx* ctx) {
   DemArgs a = demArgs(ctx);
   cudaStream_t s = ctx->stream;
   const int pg = partGrid(ctx, 128);
-  nbrCellAssign<<<pg, 128, 0, s>>>(k, a);
-  nbrCellScan<<<1, 1024, 0, s>>>(k, a);
-  nbrCellScatter<<<pg, 128, 0, s>>>(k, a);
-  nbrCellSort<<<ctx->gridCells, 128, 0, s>>>(k, a);
-  nbrBuildCells<<<nbrCellsGrid(ctx), 128, 0, s>>>(k, a);
-  nbrBuildDirect<<<pg, 128, 0, s>>>(k, a);
-  nbrDirectHistory<<<pg, 128, 0, s>>>(k, a);
+  // only the branch the run uses (fixed at creation; each kernel also checks
+  // the device flags and returns unless the list is rebuilt in this step)
+  if (!ctx->directList) {
+    nbrCellAssign<<<pg, 128, 0, s>>>(k, a);
+    nbrCellScan<<<1, 1024, 0, s>>>(k, a);
+    nbrCellScatter<<<pg, 128, 0, s>>>(k, a);
+    nbrCellSort<<<ctx->gridCells, 128, 0, s>>>(k, a);
+    nbrBuildCells<<<nbrCellsGrid(ctx), 128, 0, s>>>(k, a);
+  } else {
+    nbrBuildDirect<<<pg, 128, 0, s>>>(k, a);
+    nbrDirectHistory<<<pg, 128, 0, s>>>(k, a);
+  }
   nbrPartners<<<nbrCellsGrid(ctx), 128, 0, s>>>(k, a);  // a warp per particle
   nbrPairList<<<std::max(1, std::min(ctx->nPart * MAX_N / 256 + 1, ctx->smCount * 8)), 256, 0,
                 s>>>(k, a);
@@ -513,6 +519,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   const int nl[3] = {(int)(k.demSize[0] / cut), (int)(k.demSize[1] / cut),
                      (int)(k.demSize[2] / cut)};
   const int direct = std::min(nl[0], nl[1]) < 3 ? 1 : 0;
+  ctx->directList = direct != 0;
   if (!direct && (long long)nl[0] * nl[1] * nl[2] > MAX_L)
     return setErr(ctx, LBDEM_ERR_OVERFLOW, "more than 100000 neighbour cells");
   {
@@ -625,6 +632,7 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   AL(d.pairflag, P1 * MAX_N);
   if (k.mixed) {
     AL(d.slotSum, P1 * SLOT_SUM_STRIDE);
+    AL(d.kinf, 2 * P1);
   }
   AL(d.pcell, P1);
   AL(d.posf, P1);
@@ -799,7 +807,7 @@ extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
     if ((rc = enqueueStress(ctx, a))) return rc;
     demGather<<<partGrid(ctx, GATHER_THREADS), GATHER_THREADS, 0, s>>>(k, a);
   }
-  ctx->launches += 1 + 9 + (k.mixed ? 3 : 2);
+  ctx->launches += 1 + (ctx->directList ? 4 : 7) + (k.mixed ? 3 : 2);
   return launchErr(ctx, "dem step");
 }
 
@@ -1410,6 +1418,7 @@ extern "C" int lbdem_estimate_device_bytes(const lbdem_config* cfg, int32_t prec
   add(P1 * MAX_N * (mixed ? PAIR_VALS / 2 : PAIR_VALS), 8);  // pairbuf
   add(P1 * MAX_N, 1);                          // pairflag
   if (mixed) add(P1 * SLOT_SUM_STRIDE, 4);     // slotSum
+  if (mixed) add(2 * P1, 16);                  // kinf
   add(P1, 4);
   add(P1, 4);                                  // pcell, ppos
   add(P1, 16);                                 // posf

@@ -154,6 +154,7 @@ struct Device {
   float* slotSum = nullptr;              // [P][SLOT_SUM_STRIDE] mixed form
   int* pcell = nullptr;                  // [P] cell of particle
   float4* posf = nullptr;                // [P] FP32 position and radius (list rebuilds)
+  float4* kinf = nullptr;                // [P][2] mixed form: (v, r), (w, 0) in FP32
   int* ppos = nullptr;                   // [P] position in its cell (1-based)
   int* cellCount = nullptr;              // [MAX_L]
   int* cellStart = nullptr;              // [MAX_L]
@@ -301,6 +302,7 @@ struct lbdem_ctx {
   cudaStream_t fsStream = nullptr;
   cudaEvent_t fsFork = nullptr, fsDone = nullptr;
   bool fsPending = false;  // a forked free-surface step not yet joined
+  bool directList = false;  // DEM neighbour list by direct sums (fixed at creation)
   // mixed form, captured cycles: lbPrepare runs on sideStream beside the
   // coupling step, and the wall-force sweep beside the finalisation and the
   // interface mass update (joined before the interface types change) and
