@@ -266,27 +266,38 @@ __device__ __forceinline__ void warpAccum(float v, float* slot) {
 LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGatherMixed, DemArgs, dem) {
   constexpr int NW = GATHER_THREADS / 32;
   const int stepNo = a.iscal[IS_DEMSTEP];
+  // Each warp keeps its own reaction sums and its own copy of the wall and
+  // impactor data in shared memory, so no block barrier stands between the
+  // start of the kernel and the particle loads.
   __shared__ float acc[NW][GA_N];
-  __shared__ DeviceWall sW[MAX_WALL];
-  __shared__ float sWp[MAX_WALL][3], sWn[MAX_WALL][3];
-  for (int t = threadIdx.x; t < NW * GA_N; t += blockDim.x) (&acc[0][0])[t] = 0.0f;
-  if (threadIdx.x < (unsigned)k.nWall) {
-    const DeviceWall W = a.walls[threadIdx.x];
-    sW[threadIdx.x] = W;
+  __shared__ DeviceWall sW[NW][MAX_WALL];
+  __shared__ float sWp[NW][MAX_WALL][3], sWn[NW][MAX_WALL][3];
+  __shared__ double sOb[NW][MAX_OBJ][10];  // r, x0, x1, w1
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* wacc = acc[wid];
+  for (int t = lane; t < GA_N; t += 32) wacc[t] = 0.0f;
+  if (lane < k.nWall) {
+    const DeviceWall W = a.walls[lane];
+    sW[wid][lane] = W;
     for (int c = 0; c < 3; ++c) {
-      sWp[threadIdx.x][c] = (float)W.p[c];
-      sWn[threadIdx.x][c] = (float)W.n[c];
+      sWp[wid][lane][c] = (float)W.p[c];
+      sWn[wid][lane][c] = (float)W.n[c];
     }
   }
-  __syncthreads();
-  // reach of the wall forces beyond a particle's radius: the largest
-  // lubrication range, plus a margin far above the FP32 error of the test
+  for (int t = lane; t < 10 * k.nObj; t += 32) {
+    const int o = t / 10, c = t - o * 10;
+    sOb[wid][o][c] = a.obj[o * OB_STRIDE + (c == 0 ? OB_R : c < 4 ? OB_X0 + c - 1
+                                           : c < 7 ? OB_X1 + c - 4 : OB_W1 + c - 7)];
+  }
+  __syncwarp();
+  // reach of the wall and impactor forces beyond the contact distance: the
+  // largest lubrication range, plus a margin far above the FP32 error of the
+  // distance tests
   const float wallReach =
       (float)tmax(k.lubCut, tmax(k.lubN, tmax(k.lubT, k.lubR))) + 0.01f;
   const int P = k.nPart;
   const bool afterWait = stepNo >= k.objWaitTime;
   const unsigned FULLM = 0xffffffffu;
-  float* wacc = acc[threadIdx.x >> 5];
   // particles in the cell list's order (from the last rebuild), so that a
   // warp holds neighbours in space and few of its lanes branch into the wall
   // terms; the particle index order where the direct-sum branch is in use
@@ -322,13 +333,13 @@ LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGatherMixed, DemArgs, dem) {
     // walls a force can reach (FP32 distance test); the others give no
     // force and reset the wall spring, as the contact law does out of contact
     unsigned nearW = 0;
+    const float xf[3] = {(float)xa[0], (float)xa[1], (float)xa[2]};
     if (valid) {
-      const float xf[3] = {(float)xa[0], (float)xa[1], (float)xa[2]};
       for (int w = 0; w < k.nWall; ++w) {
         float l2 = 0.0f;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          const float oc = (xf[c] - sWp[w][c]) * sWn[w][c] * sWn[w][c];
+          const float oc = (xf[c] - sWp[wid][w][c]) * sWn[wid][w][c] * sWn[wid][w][c];
           l2 += oc * oc;
         }
         const float lim = ra + wallReach;
@@ -343,7 +354,7 @@ LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGatherMixed, DemArgs, dem) {
         float F[3] = {0.0f, 0.0f, 0.0f};
         if ((nearW >> w) & 1u) {
           float o[3], Tq[3];
-          const float l = wallGeomM(sW[w], xa, raD, o);
+          const float l = wallGeomM(sW[wid][w], xa, raD, o);
           if (wallLubOne(k, ra, vaf, wa, o[0], o[1], o[2], l, F, Tq)) {
             add3f(FL, F);
             add3f(ML, Tq);
@@ -354,18 +365,30 @@ LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGatherMixed, DemArgs, dem) {
         for (int c = 0; c < 3; ++c) warpAccum(-F[c], &wacc[GA_WALL + 6 * w + 3 + c]);
       }
       for (int o = 0; o < k.nObj; ++o) {
-        const double* ob = a.obj + o * OB_STRIDE;
-        const double ro = ob[OB_R];
+        const double* ob = sOb[wid][o];
+        const double ro = ob[0];
         float R[12] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
         bool any = false;
+        // an impactor beyond the particle's reach gives no force and resets
+        // the particle's impactor spring, as the contact law does out of
+        // contact (FP32 distance test)
+        bool nearO = false;
         if (valid) {
+          const float ex = xf[0] - (float)ob[1], ey = xf[1] - (float)ob[2],
+                      ez = xf[2] - (float)ob[3];
+          const float lim = ra + (float)ro + wallReach;
+          nearO = ex * ex + ey * ey + ez * ez < lim * lim;
+          if (!nearO) xio[0] = xio[1] = xio[2] = 0.0f;
+        }
+        if (!__any_sync(FULLM, nearO)) continue;  // uniform
+        if (nearO) {
           double d[3], u[3];
           for (int c = 0; c < 3; ++c) {
-            d[c] = xa[c] - ob[OB_X0 + c];
-            u[c] = va[c] - ob[OB_X1 + c];
+            d[c] = xa[c] - ob[1 + c];
+            u[c] = va[c] - ob[4 + c];
           }
           const PairGeom<float> g = pairGeomM(0.5 * (raD + ro), d, u);
-          const float wo[3] = {(float)ob[OB_W1], (float)ob[OB_W1 + 1], (float)ob[OB_W1 + 2]};
+          const float wo[3] = {(float)ob[7], (float)ob[8], (float)ob[9]};
           objContactOne(k, ra, (float)ro, g, wa, wo, xio, df, dt);
           add3f(FC, df);
           MC[0] += ra * dt[0];
@@ -411,7 +434,7 @@ LBDEM_KERNEL(__launch_bounds__(GATHER_THREADS), demGatherMixed, DemArgs, dem) {
         float F[3] = {0.0f, 0.0f, 0.0f};
         if ((nearW >> w) & 1u) {
           float o[3];
-          const float l = wallGeomM(sW[w], xa, raD, o);
+          const float l = wallGeomM(sW[wid][w], xa, raD, o);
           wallContactOne(k, ra, vaf, wa, xiw, o[0], o[1], o[2], l, nst, df, dt);
           add3f(FC, df);
           MC[0] += ra * dt[0];

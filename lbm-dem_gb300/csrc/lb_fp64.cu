@@ -957,6 +957,24 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
   // threads wait at the block barrier before the initialisation
   const int T = min((int)blockDim.x, (n + 31) & ~31);
   __shared__ int s_n;
+  // node::initialize(initDensity, initVelocity or 0, mass, visc, lbF): the
+  // equilibria depend only on the direction and on whether the node becomes
+  // fluid (initial velocity) or interface (none), so the 2 x 19 values are
+  // formed once, by the block's last threads while the others resolve
+  __shared__ double s_feq[2][Q];
+  const double rho0 = k.initDensity;
+  {
+    const int q = (int)blockDim.x - 1 - (int)threadIdx.x;
+    if (q < 2 * Q) {
+      const int c = q / Q, j = q - c * Q;
+      const double vx = c == 0 ? k.initVel[0] : 0.0, vy = c == 0 ? k.initVel[1] : 0.0,
+                   vz = c == 0 ? k.initVel[2] : 0.0;
+      const double ux = k.lbF[0] / 2.0 / rho0 + vx, uy = k.lbF[1] / 2.0 / rho0 + vy,
+                   uz = k.lbF[2] / 2.0 / rho0 + vz;
+      const double usq = ux * ux + uy * uy + uz * uz;
+      s_feq[c][j] = feqj(j, rho0, ux, uy, uz, usq);
+    }
+  }
   if (n <= 32 && k.nObj == 1) {
     // up to 32 candidates of one impactor: warp 0 alone, one candidate per
     // lane, in registers (no duplicates: one object box)
@@ -1090,21 +1108,6 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
   // the new nodes' initialisation by the whole block, one (node, direction)
   // per thread: the equilibria are FP64, and a thread per node would form
   // nineteen of them one after the other
-  // node::initialize(initDensity, initVelocity or 0, mass, visc, lbF): the
-  // equilibria depend only on the direction and on whether the node becomes
-  // fluid (initial velocity) or interface (none), so the 2 x 19 values are
-  // formed once
-  __shared__ double s_feq[2][Q];
-  const double rho0 = k.initDensity;
-  if (threadIdx.x < 2 * Q) {
-    const int c = threadIdx.x / Q, j = threadIdx.x - c * Q;
-    const double vx = c == 0 ? k.initVel[0] : 0.0, vy = c == 0 ? k.initVel[1] : 0.0,
-                 vz = c == 0 ? k.initVel[2] : 0.0;
-    const double ux = k.lbF[0] / 2.0 / rho0 + vx, uy = k.lbF[1] / 2.0 / rho0 + vy,
-                 uz = k.lbF[2] / 2.0 / rho0 + vz;
-    const double usq = ux * ux + uy * uy + uz * uz;
-    s_feq[c][j] = feqj(j, rho0, ux, uy, uz, usq);
-  }
   __syncthreads();
   n = s_n;
   for (int q = threadIdx.x; q < n * Q; q += blockDim.x) {
