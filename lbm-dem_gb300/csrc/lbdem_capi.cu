@@ -305,7 +305,9 @@ extern "C" int lbdem_create(const lbdem_config* cfg, const lbdem_options* opt,
   CK(cudaEventCreateWithFlags(&ctx->fsFork, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&ctx->fsDone, cudaEventDisableTiming));
   CK(cudaStreamCreateWithFlags(&ctx->sideStream, cudaStreamNonBlocking));
-  for (cudaEvent_t* e : {&ctx->prepFork, &ctx->prepDone, &ctx->wallFork, &ctx->wallDone})
+  CK(cudaStreamCreateWithFlags(&ctx->demStream, cudaStreamNonBlocking));
+  for (cudaEvent_t* e : {&ctx->prepFork, &ctx->prepDone, &ctx->wallFork, &ctx->wallDone,
+                         &ctx->demFork, &ctx->demDone})
     CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   CK(cudaDeviceGetAttribute(&ctx->smCount, cudaDevAttrMultiProcessorCount, ctx->device));
   {
@@ -743,11 +745,13 @@ extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
   }
   if (ctx->fsFork) cudaEventDestroy(ctx->fsFork);
   if (ctx->fsDone) cudaEventDestroy(ctx->fsDone);
-  if (ctx->sideStream) {
-    cudaStreamSynchronize(ctx->sideStream);
-    cudaStreamDestroy(ctx->sideStream);
-  }
-  for (cudaEvent_t e : {ctx->prepFork, ctx->prepDone, ctx->wallFork, ctx->wallDone})
+  for (cudaStream_t* st : {&ctx->sideStream, &ctx->demStream})
+    if (*st) {
+      cudaStreamSynchronize(*st);
+      cudaStreamDestroy(*st);
+    }
+  for (cudaEvent_t e : {ctx->prepFork, ctx->prepDone, ctx->wallFork, ctx->wallDone, ctx->demFork,
+                        ctx->demDone})
     if (e) cudaEventDestroy(e);
   delete ctx;
 }
@@ -780,6 +784,28 @@ static int enqueueStress(lbdem_ctx* ctx, const DemArgs& a) {
 }
 
 // DEM::discreteElementStep (multiStep = 1)
+// The DEM step up to its gather (DEM::discreteElementStep: the neighbour
+// list check and rebuild, the pair forces, the slot sums) on ctx->stream.
+static int enqueueDemPre(lbdem_ctx* ctx) {
+  const Consts& k = ctx->k;
+  DemArgs a = demArgs(ctx);
+  cudaStream_t s = ctx->stream;
+  demBegin<<<partGrid(ctx, 256), 256, 0, s>>>(k, a, 0);
+  int rc = enqueueNeighbourList(ctx);
+  if (rc) return rc;
+  const int pairGrid = std::max(1, std::min(ctx->nPart * (MAX_N / 2) / 128 + 1, ctx->smCount * 16));
+  if (k.mixed) {
+    demPairsMixed<<<pairGrid, 128, 0, s>>>(k, a);
+    if ((rc = enqueueStress(ctx, a))) return rc;
+    demSlotSumsMixed<<<partGrid(ctx, GATHER_MIXED_PARTS), GATHER_MIXED_THREADS, 0, s>>>(k, a);
+  } else {
+    demPairs<<<pairGrid, 128, 0, s>>>(k, a);
+    if ((rc = enqueueStress(ctx, a))) return rc;
+  }
+  ctx->launches += 1 + (ctx->directList ? 4 : 7) + (k.mixed ? 2 : 1);
+  return LBDEM_OK;
+}
+
 extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
   if (!ctx) return LBDEM_ERR_INVALID;
   DeviceScope devScope(ctx->device);
@@ -788,26 +814,21 @@ extern "C" int lbdem_dem_step(lbdem_ctx* ctx) {
   const Consts& k = ctx->k;
   DemArgs a = demArgs(ctx);
   cudaStream_t s = ctx->stream;
-  demBegin<<<partGrid(ctx, 256), 256, 0, s>>>(k, a, 0);
-  int rc = enqueueNeighbourList(ctx);
-  if (rc) return rc;
-  const int pairGrid = std::max(1, std::min(ctx->nPart * (MAX_N / 2) / 128 + 1, ctx->smCount * 16));
-  // the gathers also update the impactor (last block)
-  if (k.mixed) {
-    demPairsMixed<<<pairGrid, 128, 0, s>>>(k, a);
-    if ((rc = enqueueStress(ctx, a))) return rc;
-    demSlotSumsMixed<<<partGrid(ctx, GATHER_MIXED_PARTS), GATHER_MIXED_THREADS, 0, s>>>(k, a);
-    if (ctx->wallPendingMain) {  // the gather's last block reads the wall sums
-      CK(cudaStreamWaitEvent(s, ctx->wallDone, 0));
-      ctx->wallPendingMain = false;
-    }
-    demGatherMixed<<<partGrid(ctx, GATHER_THREADS), GATHER_THREADS, 0, s>>>(k, a);
-  } else {
-    demPairs<<<pairGrid, 128, 0, s>>>(k, a);
-    if ((rc = enqueueStress(ctx, a))) return rc;
-    demGather<<<partGrid(ctx, GATHER_THREADS), GATHER_THREADS, 0, s>>>(k, a);
+  int rc;
+  if (ctx->demPrePending) {  // enqueued beside the previous cycle's lattice step
+    CK(cudaStreamWaitEvent(s, ctx->demDone, 0));
+    ctx->demPrePending = false;
+  } else if ((rc = enqueueDemPre(ctx))) {
+    return rc;
   }
-  ctx->launches += 1 + (ctx->directList ? 4 : 7) + (k.mixed ? 3 : 2);
+  // the gathers also update the impactor (last block)
+  if (ctx->wallPendingMain) {  // the gather's last block reads the wall sums
+    CK(cudaStreamWaitEvent(s, ctx->wallDone, 0));
+    ctx->wallPendingMain = false;
+  }
+  if (k.mixed) demGatherMixed<<<partGrid(ctx, GATHER_THREADS), GATHER_THREADS, 0, s>>>(k, a);
+  else demGather<<<partGrid(ctx, GATHER_THREADS), GATHER_THREADS, 0, s>>>(k, a);
+  ctx->launches += 1;
   return launchErr(ctx, "dem step");
 }
 
@@ -1014,6 +1035,20 @@ int cycleOnce(lbdem_ctx* ctx, bool forkFs = false) {
     mark(1);
     if (ctx->lbSolve && ctx->demTime >= ctx->demInitialRepeat) {
       if (ctx->demSolve && (rc = lbdem_coupling_step(ctx))) return rc;
+      if (forkFs && ctx->overlap && ctx->demSolve && !ctx->out) {
+        // the next cycle's DEM step up to its gather reads only particle
+        // state, which nothing from here to that gather changes, and writes
+        // only DEM data: it runs beside this cycle's lattice step
+        CK(cudaEventRecord(ctx->demFork, ctx->stream));
+        CK(cudaStreamWaitEvent(ctx->demStream, ctx->demFork, 0));
+        cudaStream_t main = ctx->stream;
+        ctx->stream = ctx->demStream;
+        rc = enqueueDemPre(ctx);
+        ctx->stream = main;
+        if (rc) return rc;
+        CK(cudaEventRecord(ctx->demDone, ctx->demStream));
+        ctx->demPrePending = true;
+      }
       mark(2);
       if ((rc = lbdem_lb_step(ctx))) return rc;
       mark(3);
@@ -1073,6 +1108,11 @@ int captureCycles(lbdem_ctx* ctx, int cycles, cudaGraphExec_t* exec, long long* 
   // the capture ends on the context's stream with every fork joined
   const int rj = joinFreeSurface(ctx);
   if (rc == LBDEM_OK) rc = rj;
+  if (ctx->demPrePending) {  // not expected: the last cycle forks no DEM step
+    const cudaError_t ew = cudaStreamWaitEvent(ctx->stream, ctx->demDone, 0);
+    if (rc == LBDEM_OK && ew != cudaSuccess) rc = setErr(ctx, LBDEM_ERR_CUDA, "graph capture join");
+    ctx->demPrePending = false;
+  }
   if (ctx->wallPendingMain || ctx->wallPendingFs || ctx->prepPending) {
     const cudaEvent_t e = ctx->prepPending ? ctx->prepDone : ctx->wallDone;
     const cudaError_t ew = cudaStreamWaitEvent(ctx->stream, e, 0);

@@ -311,6 +311,11 @@ struct lbdem_ctx {
   cudaStream_t sideStream = nullptr;
   cudaEvent_t prepFork = nullptr, prepDone = nullptr, wallFork = nullptr, wallDone = nullptr;
   bool prepPending = false, wallPendingFs = false, wallPendingMain = false;
+  // the next cycle's DEM step up to its gather, on demStream beside this
+  // cycle's lattice and free-surface steps (joined before that gather)
+  cudaStream_t demStream = nullptr;
+  cudaEvent_t demFork = nullptr, demDone = nullptr;
+  bool demPrePending = false;
   int device = 0;
   int precision = LBDEM_PLAIN_FP64;
   int check_every = 0;
