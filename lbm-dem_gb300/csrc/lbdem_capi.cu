@@ -1311,17 +1311,20 @@ extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
   int32_t i = 0;
   while (i < n) {
     int rc = LBDEM_OK;
-    // with no output open, four steady cycles are replayed from one graph
-    // (in the mixed form three of their free-surface steps overlap the next
-    // cycle's DEM step)
-    if (n - i >= 4 && !ctx->out && pairReplayable(ctx)) {
+    // with no output open, LBDEM_GRAPH_CYCLES steady cycles are replayed
+    // from one graph (in the mixed form each cycle but the last overlaps its
+    // free-surface step and its lattice step with the next cycle's DEM step)
+    if (n - i >= LBDEM_GRAPH_CYCLES && !ctx->out && pairReplayable(ctx)) {
       const int parity = ctx->cur;
       if (!ctx->quadGraph[parity]) {
-        if ((rc = captureCycles(ctx, 4, &ctx->quadGraph[parity], &ctx->quadKernels))) return rc;
+        if ((rc = captureCycles(ctx, LBDEM_GRAPH_CYCLES, &ctx->quadGraph[parity],
+                                &ctx->quadKernels)))
+          return rc;
       } else {
         CK(cudaGraphLaunch(ctx->quadGraph[parity], ctx->stream));
-        // host counters as four cycles advance them (cur flips four times)
-        for (int c = 0; c < 4; ++c) {
+        // host counters as the cycles advance them (an even number of
+        // buffer swaps)
+        for (int c = 0; c < LBDEM_GRAPH_CYCLES; ++c) {
           ++ctx->lbTime;
           if (ctx->demSolve) {
             ++ctx->demTimeStep;
@@ -1330,7 +1333,7 @@ extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
         }
         ctx->launches += ctx->quadKernels;
       }
-      i += 4;
+      i += LBDEM_GRAPH_CYCLES;
       continue;
     }
     // a pair replays two cycles; an output line due after the first of them

@@ -22,6 +22,12 @@ constexpr int PAIR_VALS = 18;    // per neighbour slot: contact(6) lub(9) rep(3)
 // per particle, mixed form: the 15 pair sums of the gather (FC, MC / radius,
 // FL, ML, FR), padded to a 64-byte line
 constexpr int SLOT_SUM_STRIDE = 16;
+// steady cycles per replayed graph when no output file is open (even: the
+// lattice buffers are back where they started)
+#ifndef LBDEM_GRAPH_CYCLES
+#define LBDEM_GRAPH_CYCLES 16
+#endif
+static_assert(LBDEM_GRAPH_CYCLES % 2 == 0, "an even number of cycles per graph");
 #ifndef LBDEM_UNCOVER_CAP
 #define LBDEM_UNCOVER_CAP 8192
 #endif
@@ -358,7 +364,7 @@ struct lbdem_ctx {
   // two goCycles as one CUDA graph, per starting lattice buffer
   cudaGraphExec_t pairGraph[2] = {nullptr, nullptr};
   cudaGraphExec_t oneGraph[2] = {nullptr, nullptr};  // single cycles, per start buffer
-  cudaGraphExec_t quadGraph[2] = {nullptr, nullptr};  // four cycles (no output open)
+  cudaGraphExec_t quadGraph[2] = {nullptr, nullptr};  // LBDEM_GRAPH_CYCLES cycles (no output)
   long long quadKernels = 0;
   long long oneKernels = 0;
   long long pairKernels = 0;
