@@ -226,10 +226,11 @@ extern "C" int lbdem_restore(lbdem_ctx* ctx, const char* path) {
       cudaGraphExecDestroy(g);
       g = nullptr;
     }
-  for (auto& g : ctx->quadGraph)
-    if (g) {
-      cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
+  for (auto& row : ctx->groupGraph)
+    for (auto& g : row)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
   return LBDEM_OK;
 }

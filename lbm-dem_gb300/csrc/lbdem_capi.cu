@@ -724,8 +724,9 @@ extern "C" void lbdem_destroy(lbdem_ctx* ctx) {
     if (g) cudaGraphExecDestroy(g);
   for (auto& g : ctx->oneGraph)
     if (g) cudaGraphExecDestroy(g);
-  for (auto& g : ctx->quadGraph)
-    if (g) cudaGraphExecDestroy(g);
+  for (auto& row : ctx->groupGraph)
+    for (auto& g : row)
+      if (g) cudaGraphExecDestroy(g);
   for (auto& e : ctx->lbEvents) {
     cudaEventDestroy(e.first);
     cudaEventDestroy(e.second);
@@ -1311,29 +1312,33 @@ extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
   int32_t i = 0;
   while (i < n) {
     int rc = LBDEM_OK;
-    // with no output open, LBDEM_GRAPH_CYCLES steady cycles are replayed
-    // from one graph (in the mixed form each cycle but the last overlaps its
-    // free-surface step and its lattice step with the next cycle's DEM step)
-    if (n - i >= LBDEM_GRAPH_CYCLES && !ctx->out && pairReplayable(ctx)) {
+    // with no output open, groups of steady cycles are replayed from one
+    // graph: LBDEM_GRAPH_CYCLES of them for a call of many cycles, 4 for a
+    // short call (a run's first replay of a group captures it: short runs
+    // would pay more for capturing long groups than they save); in the mixed
+    // form each cycle but the last overlaps its lattice and free-surface
+    // steps with the next cycle's DEM step
+    const int big = (n >= 4 * LBDEM_GRAPH_CYCLES) ? 1 : 0;
+    const int G = big ? LBDEM_GRAPH_CYCLES : 4;
+    if (n - i >= G && !ctx->out && pairReplayable(ctx)) {
       const int parity = ctx->cur;
-      if (!ctx->quadGraph[parity]) {
-        if ((rc = captureCycles(ctx, LBDEM_GRAPH_CYCLES, &ctx->quadGraph[parity],
-                                &ctx->quadKernels)))
+      if (!ctx->groupGraph[big][parity]) {
+        if ((rc = captureCycles(ctx, G, &ctx->groupGraph[big][parity], &ctx->groupKernels[big])))
           return rc;
       } else {
-        CK(cudaGraphLaunch(ctx->quadGraph[parity], ctx->stream));
+        CK(cudaGraphLaunch(ctx->groupGraph[big][parity], ctx->stream));
         // host counters as the cycles advance them (an even number of
         // buffer swaps)
-        for (int c = 0; c < LBDEM_GRAPH_CYCLES; ++c) {
+        for (int c = 0; c < G; ++c) {
           ++ctx->lbTime;
           if (ctx->demSolve) {
             ++ctx->demTimeStep;
             ctx->demTime += ctx->k.dt;
           }
         }
-        ctx->launches += ctx->quadKernels;
+        ctx->launches += ctx->groupKernels[big];
       }
-      i += LBDEM_GRAPH_CYCLES;
+      i += G;
       continue;
     }
     // a pair replays two cycles; an output line due after the first of them

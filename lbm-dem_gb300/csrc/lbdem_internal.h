@@ -364,8 +364,10 @@ struct lbdem_ctx {
   // two goCycles as one CUDA graph, per starting lattice buffer
   cudaGraphExec_t pairGraph[2] = {nullptr, nullptr};
   cudaGraphExec_t oneGraph[2] = {nullptr, nullptr};  // single cycles, per start buffer
-  cudaGraphExec_t quadGraph[2] = {nullptr, nullptr};  // LBDEM_GRAPH_CYCLES cycles (no output)
-  long long quadKernels = 0;
+  // groups of steady cycles when no output is open: [0] 4 cycles, [1]
+  // LBDEM_GRAPH_CYCLES cycles (calls of many cycles), per start buffer
+  cudaGraphExec_t groupGraph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  long long groupKernels[2] = {0, 0};
   long long oneKernels = 0;
   long long pairKernels = 0;
 };
