@@ -89,9 +89,10 @@ def test_mixed_lattice_close_to_fp64(lib, oracle_lib):
 
 
 def test_graph_replays_match_single_cycles(lib):
-    """Cycles replayed from the four-cycle graphs (where the free-surface
-    step of a cycle runs beside the next cycle's DEM step) against the same
-    cycles issued one call at a time (single-cycle graphs, no overlap). The
+    """Cycles replayed from the groups of captured cycles (where the next
+    cycle's DEM step runs beside a cycle's lattice and free-surface steps)
+    against the same cycles issued one call at a time (single-cycle graphs,
+    no overlap). The
     mixed form sums particle forces with float atomics in no fixed order, so
     the two runs agree to rounding, not bit for bit: tolerances 1e-5
     absolute on populations, 1e-9 relative on particle positions, node types
@@ -100,9 +101,10 @@ def test_graph_replays_match_single_cycles(lib):
     cfg = lbdem.LoadedConfig(os.path.join(GOLDEN, "small_cells", "parameters.cfg"))
     a = lbdem.Solver(cfg, precision=lbdem.MIXED)
     b = lbdem.Solver(cfg, precision=lbdem.MIXED)
-    for _ in range(40):
+    # 80 cycles in one call: five replays of the sixteen-cycle groups
+    for _ in range(80):
         a.cycle(1)
-    b.cycle(40)
+    b.cycle(80)
     la, lb = a.lattice(), b.lattice()
     pa, pb = a.particles(), b.particles()
     same = np.mean(la["type"] == lb["type"])
@@ -115,7 +117,7 @@ def test_graph_replays_match_single_cycles(lib):
     oa, ob = a.objects()["o_x0"], b.objects()["o_x0"]
     assert np.max(np.abs(oa - ob)) <= 1e-9 * np.max(np.abs(ob))
     ia, ib = a.get_info(), b.get_info()
-    assert ia.time_step == ib.time_step == 40
+    assert ia.time_step == ib.time_step == 80
     a.close()
     b.close()
     cfg.close()
