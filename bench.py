@@ -513,10 +513,11 @@ def serving(args) -> dict:
             srv.submit(c, cycles)
         res = srv.drain()
         wall = time.perf_counter() - t0
+        err = srv.last_error()
         srv.close()
         bad = [r for r in res if r["status"] != 0]
         if bad:
-            raise RuntimeError(f"serving run failed: status {bad[0]['status']}")
+            raise RuntimeError(f"serving run failed: status {bad[0]['status']}: {err}")
         lat = [r["end_time"] - r["submit_time"] for r in res]
         upd = sum(r["active_node_updates"] for r in res)
         starts = [r["start_time"] for r in res]
@@ -537,10 +538,11 @@ def serving(args) -> dict:
             wait = min(0.01, arrivals[k] - now) if k < len(jobs) else 0.05
             res += srv.poll(max(wait, 0.0))
         wall = time.perf_counter() - t0
+        err = srv.last_error()
         srv.close()
         bad = [r for r in res if r["status"] != 0]
         if bad:
-            raise RuntimeError(f"serving run failed: status {bad[0]['status']}")
+            raise RuntimeError(f"serving run failed: status {bad[0]['status']}: {err}")
         lat = [r["end_time"] - r["submit_time"] for r in res]
         span = max(r["end_time"] for r in res) - min(r["submit_time"] for r in res)
         return {"p50_s": round(pct(lat, 50), 3), "p99_s": round(pct(lat, 99), 3),

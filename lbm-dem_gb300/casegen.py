@@ -531,6 +531,15 @@ def named_case(name: str, seed: int = 1) -> Case:
         c.bodies = np.array([[2.0, ox, oy + 10.0, oz, 0.0, 0.0, 0.0, 2.0e-3, L0],
                              [1.5, ox + 1.0, oy + 12.0, oz, 0.0, 0.01, 0.0, 1.0e-3, L0 + 3.0]])
         return c
+    if name in ("uncover_mid", "uncover_wide"):
+        # a large, fast impactor entering the fluid: 36-80 (mid: radius 10 at
+        # 0.2) or 200-350 (wide: radius 16 at 0.4) nodes uncovered behind it
+        # in every step, for the resolution of many uncovered nodes at once
+        # (LB::findNewActiveObject, src/LB.cpp:846)
+        wide = name == "uncover_wide"
+        lat, r, vy = ((44, 60, 44), 16.0, -0.4) if wide else ((40, 52, 40), 10.0, -0.2)
+        return impact_case(lat, 30.0, 12, (3.0, 3.4), r, 30.0 + r + 1.5, vy, 5.0, 0.8,
+                           1.0e-4, seed, overrides={"objWaitTime": "2"}, name=name)
     if name == "units_dyn":
         # a cell-list case in physical units (unitLength 0.5, unitTime 0.02,
         # unitDensity 1000), with boundary0 = 8: every wall is a moving

@@ -348,6 +348,12 @@ __device__ __forceinline__ void lbFinalizeBody(const Consts& k, double* pF, doub
                                                double* scal, const int* iscal,
                                                const float* pAccF, double* pS,
                                                const FsArgs& fa, int redistribute) {
+  // the redistribution amount, once per block (an FP64 division in every
+  // thread costs more than the rest of the kernel), formed first so that its
+  // latency overlaps the particle conversions
+  __shared__ double sAddMass;
+  if (threadIdx.x == 0)
+    sAddMass = (scal[SC_EXTRA_MASS] + scal[SC_EXTRA_MASS_LO]) / (double)(unsigned)iscal[IS_NIF];
   const int P = k.nPart;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
     if (pAccF) {
@@ -384,16 +390,10 @@ __device__ __forceinline__ void lbFinalizeBody(const Consts& k, double* pF, doub
         obj[o * OB_STRIDE + OB_FHYDRO + c] *= k.uForce;
         obj[o * OB_STRIDE + OB_MHYDRO + c] *= k.uTorque;
       }
-    scal[SC_ADD_MASS] =
-        (scal[SC_EXTRA_MASS] + scal[SC_EXTRA_MASS_LO]) / (double)(unsigned)iscal[IS_NIF];
+    scal[SC_ADD_MASS] = sAddMass;
   }
   if (redistribute) {
-    // LB::redistributeMass(extraMass) over the interface nodes; every block
-    // forms the same quotient block 0 stores above (once per block: an FP64
-    // division in every thread costs more than the rest of the kernel)
-    __shared__ double sAddMass;
-    if (threadIdx.x == 0)
-      sAddMass = (scal[SC_EXTRA_MASS] + scal[SC_EXTRA_MASS_LO]) / (double)(unsigned)iscal[IS_NIF];
+    // LB::redistributeMass(extraMass) over the interface nodes
     __syncthreads();
     const double addMass = sAddMass;
     const int nl = fa.iscal[IS_IFLIST];
@@ -861,75 +861,122 @@ __device__ __forceinline__ int teamOr(int nthreads, int v) {
   return r;
 }
 
-// uncoverResolve for n <= 32 candidates of one impactor, by one warp:
-// lane l holds candidate l (after a shuffle bitonic sort, ascending node
-// index). Each lane records which lower lanes are its neighbours (a bit
-// mask) and the fixed types of its other neighbours; the fixed-point
-// iteration then takes two ballots per round. Results go to s_idx / s_st
-// (bits 0-3 the new type) for the block's initialisation.
+// uncoverResolve for n <= 32 H candidates of one impactor, by one warp:
+// lane l holds candidates l and, for H = 2, l + 32 (after a shuffle bitonic
+// sort, ascending node index). Each candidate records which lower-index
+// candidates are its neighbours (a bit mask over the 32 H positions) and the
+// fixed types of its other neighbours; the fixed-point iteration then takes
+// two ballots per half per round. Results go to s_idx / s_st (bits 0-3 the
+// new type) for the block's initialisation.
+template <int H>
 __device__ __forceinline__ void uncoverResolveWarp(const Consts& k, const uint8_t* mask,
-                                                const uint32_t* list, int n, uint32_t* s_idx,
-                                                uint8_t* s_st, int* s_n) {
+                                                   const uint32_t* list, int n, uint32_t* s_idx,
+                                                   uint8_t* s_st, int* s_n) {
   const unsigned FULLM = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  uint32_t x = lane < n ? list[lane] : 0xffffffffu;
+  uint32_t x[H];
 #pragma unroll
-  for (int size = 2; size <= 32; size <<= 1)
+  for (int h = 0; h < H; ++h) x[h] = 32 * h + lane < n ? list[32 * h + lane] : 0xffffffffu;
+  // bitonic sort of the 32 H keys, key e = 32 h + lane ascending
+#pragma unroll
+  for (int size = 2; size <= 32 * H; size <<= 1)
 #pragma unroll
     for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      const uint32_t other = __shfl_xor_sync(FULLM, x, stride);
-      const bool up = (lane & size) == 0, low = (lane & stride) == 0;
-      x = (low == up) ? min(x, other) : max(x, other);
-    }
-  const bool valid = lane < n;
-  int ix = 0, iy = 0, iz = 0;
-  if (valid) coords(k, (long long)x, ix, iy, iz);
-  uint32_t lk[Q];
-  unsigned inb = 0;  // links within the lattice
+      if (stride == 32) {  // (H = 2) the partner is the lane's other key
+        const bool up = (lane & size) == 0;
+        const uint32_t lo = min(x[0], x[H - 1]), hi = max(x[0], x[H - 1]);
+        x[0] = up ? lo : hi;
+        x[H - 1] = up ? hi : lo;
+      } else {
 #pragma unroll
-  for (int j = 1; j < Q; ++j) {
-    const int tx = ix + CX(j), ty = iy + CY(j), tz = iz + CZ(j);
-    const bool in = valid && tx >= 0 && tx < k.X && ty >= 0 && ty < k.Y && tz >= 0 && tz < k.Z;
-    inb |= (unsigned)in << j;
-    lk[j] = in ? x + (uint32_t)nbrOffset(k, j) : 0xffffffffu;
-  }
-  // which links end on a candidate; lower candidates as a lane mask
-  unsigned candLinks = 0, back = 0;
-  for (int b = 0; b < n; ++b) {
-    const uint32_t xb = __shfl_sync(FULLM, x, b);
-#pragma unroll
-    for (int j = 1; j < Q; ++j)
-      if (lk[j] == xb) {
-        candLinks |= 1u << j;
-        if (b < lane) back |= 1u << b;
+        for (int h = 0; h < H; ++h) {
+          const int e = 32 * h + lane;
+          const uint32_t other = __shfl_xor_sync(FULLM, x[h], stride);
+          const bool up = (e & size) == 0, low = (e & stride) == 0;
+          x[h] = (low == up) ? min(x[h], other) : max(x[h], other);
+        }
       }
+    }
+  bool valid[H];
+  uint32_t lk[H][Q];
+  unsigned inb[H];
+#pragma unroll
+  for (int h = 0; h < H; ++h) {
+    valid[h] = 32 * h + lane < n;
+    int ix = 0, iy = 0, iz = 0;
+    if (valid[h]) coords(k, (long long)x[h], ix, iy, iz);
+    inb[h] = 0;
+#pragma unroll
+    for (int j = 1; j < Q; ++j) {
+      const int tx = ix + CX(j), ty = iy + CY(j), tz = iz + CZ(j);
+      const bool in =
+          valid[h] && tx >= 0 && tx < k.X && ty >= 0 && ty < k.Y && tz >= 0 && tz < k.Z;
+      inb[h] |= (unsigned)in << j;
+      lk[h][j] = in ? x[h] + (uint32_t)nbrOffset(k, j) : 0xffffffffu;
+    }
+  }
+  // which links end on a candidate; lower candidates as a position mask
+  unsigned candLinks[H];
+  unsigned long long back[H];
+#pragma unroll
+  for (int h = 0; h < H; ++h) {
+    candLinks[h] = 0;
+    back[h] = 0;
+  }
+  for (int b = 0; b < n; ++b) {
+    const uint32_t xb = __shfl_sync(FULLM, x[H == 2 && b >= 32 ? 1 : 0], b & 31);
+#pragma unroll
+    for (int h = 0; h < H; ++h)
+#pragma unroll
+      for (int j = 1; j < Q; ++j)
+        if (lk[h][j] == xb) {
+          candLinks[h] |= 1u << j;
+          if (b < 32 * h + lane) back[h] |= 1ull << b;
+        }
   }
   // the other neighbours' types (a higher candidate reads as an impactor node)
-  bool fixFluid = false, fixGas = false;
-  uint8_t tls[Q];
+  bool fixFluid[H], fixGas[H];
 #pragma unroll
-  for (int j = 1; j < Q; ++j)
-    tls[j] = ((inb & ~candLinks) >> j) & 1u ? (uint8_t)(mask[lk[j]] & TYPE_MASK) : (uint8_t)0xFF;
+  for (int h = 0; h < H; ++h) {
+    uint8_t tls[Q];
 #pragma unroll
-  for (int j = 1; j < Q; ++j) {
-    fixFluid |= tls[j] == 0;
-    fixGas |= tls[j] == 2;
+    for (int j = 1; j < Q; ++j)
+      tls[j] = ((inb[h] & ~candLinks[h]) >> j) & 1u ? (uint8_t)(mask[lk[h][j]] & TYPE_MASK)
+                                                    : (uint8_t)0xFF;
+    fixFluid[h] = fixGas[h] = false;
+#pragma unroll
+    for (int j = 1; j < Q; ++j) {
+      fixFluid[h] |= tls[j] == 0;
+      fixGas[h] |= tls[j] == 2;
+    }
   }
-  uint8_t st = 12;  // unresolved: neither fluid nor gas to its neighbours
+  uint8_t st[H];  // 12: unresolved, neither fluid nor gas to its neighbours
+#pragma unroll
+  for (int h = 0; h < H; ++h) st[h] = 12;
   for (int it = 0; it <= n; ++it) {
-    const unsigned fluidL = __ballot_sync(FULLM, valid && st == 0);
-    const unsigned gasL = __ballot_sync(FULLM, valid && st == 2);
-    const bool fluidNb = fixFluid || (back & fluidL) != 0;
-    const bool gasNb = fixGas || (back & gasL) != 0;
-    const uint8_t nst = !fluidNb ? 2 : gasNb ? 3 : 0;
-    const bool changed = valid && nst != st;
-    if (valid) st = nst;
+    unsigned long long fluidL = 0, gasL = 0;
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      fluidL |= (unsigned long long)__ballot_sync(FULLM, valid[h] && st[h] == 0) << (32 * h);
+      gasL |= (unsigned long long)__ballot_sync(FULLM, valid[h] && st[h] == 2) << (32 * h);
+    }
+    bool changed = false;
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      const bool fluidNb = fixFluid[h] || (back[h] & fluidL) != 0;
+      const bool gasNb = fixGas[h] || (back[h] & gasL) != 0;
+      const uint8_t nst = !fluidNb ? 2 : gasNb ? 3 : 0;
+      changed |= valid[h] && nst != st[h];
+      if (valid[h]) st[h] = nst;
+    }
     if (!__any_sync(FULLM, changed)) break;
   }
-  if (valid) {
-    s_idx[lane] = x;
-    s_st[lane] = st;
-  }
+#pragma unroll
+  for (int h = 0; h < H; ++h)
+    if (valid[h]) {
+      s_idx[32 * h + lane] = x[h];
+      s_st[32 * h + lane] = st[h];
+    }
   if (lane == 0) *s_n = n;
 }
 
@@ -975,10 +1022,13 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
       s_feq[c][j] = feqj(j, rho0, ux, uy, uz, usq);
     }
   }
-  if (n <= 32 && k.nObj == 1) {
-    // up to 32 candidates of one impactor: warp 0 alone, one candidate per
-    // lane, in registers (no duplicates: one object box)
-    if (threadIdx.x < 32) uncoverResolveWarp(k, mask, list, n, s_idx, s_st, &s_n);
+  if (n <= 64 && k.nObj == 1) {
+    // up to 64 candidates of one impactor: warp 0 alone, one or two
+    // candidates per lane, in registers (no duplicates: one object box)
+    if (threadIdx.x < 32) {
+      if (n <= 32) uncoverResolveWarp<1>(k, mask, list, n, s_idx, s_st, &s_n);
+      else uncoverResolveWarp<2>(k, mask, list, n, s_idx, s_st, &s_n);
+    }
   } else if ((int)threadIdx.x < T) {
   int p2 = 1;
   while (p2 < n) p2 <<= 1;

@@ -427,6 +427,11 @@ class Server:
                 return res
         raise RuntimeError("server drain timed out")
 
+    def last_error(self) -> str:
+        """lbdem_server_last_error: the description of the last failed job or
+        call of this server ("" if none failed)."""
+        return self.lib.lbdem_server_last_error(self.h).decode() if self.h else ""
+
     def close(self):
         if self.h:
             self.lib.lbdem_server_destroy(self.h)

@@ -51,6 +51,8 @@ CASES = {
     "bodies_lj": (40, 1, 1),
     "slip_stat": (40, 1, 1),
     "slip_dyn": (40, 1, 1),
+    "uncover_mid": (40, 1, 1),
+    "uncover_wide": (40, 1, 1),
 }
 
 # The reference's own example input (example/input: unitLength 0.2,

@@ -32,13 +32,14 @@ def _pair(name):
 @pytest.mark.parametrize("name", ["tiny_direct", "small_cells", "small_dup", "units_dyn",
                                   "rheo_bingham", "rheo_frictional", "rheo_voellmy",
                                   "rheo_turbulent", "bodies", "bodies_lj", "slip_stat",
-                                  "slip_dyn"])
+                                  "slip_dyn", "uncover_mid", "uncover_wide"])
 def test_fp64_matches_oracle_every_step(name, lib, oracle_lib):
     cfg, gpu, orc = _pair(name)
+    steps = 40 if name.startswith("uncover") else 60
     with tempfile.TemporaryDirectory() as tmp:
         bad = compare(gpu.state(), orc.state(tmp), RTOL)
         assert not bad, f"{name} after init: {bad}"
-        for s in range(1, 61):
+        for s in range(1, steps + 1):
             gpu.cycle(1)
             orc.cycle(1)
             bad = compare(gpu.state(), orc.state(tmp), RTOL)

@@ -79,6 +79,37 @@ def test_oracle_bitwise_equal_to_reference_example(lib, oracle_lib, tmp_path):
     _run("example", lib, oracle_lib, tmp_path)
 
 
+@pytest.mark.parametrize("name", ["uncover_mid", "uncover_wide"])
+def test_oracle_bitwise_equal_to_reference_uncover(name, lib, oracle_lib, tmp_path):
+    """A large, fast impactor: 36-80 (mid) and 200-350 (wide) nodes uncovered
+    per step, resolved together (LB::findNewActiveObject)."""
+    _run(name, lib, oracle_lib, tmp_path)
+
+
+def test_uncover_cases_reach_many_nodes(lib, oracle_lib, tmp_path):
+    """The uncover cases free more than 32, more than 64 and more than 256
+    nodes in single steps (type 12, an impactor node, becoming another type),
+    the sizes at which the resolution of uncovered nodes changes method."""
+    import lbdem
+    import oracle_ffi
+    per_step = []
+    for name in ("uncover_mid", "uncover_wide"):
+        cfg_path, _ = golden_case(name)
+        cfg = lbdem.LoadedConfig(cfg_path)
+        orc = oracle_ffi.Oracle(cfg)
+        prev = orc.state(str(tmp_path))["type"].copy()
+        for _ in range(40):
+            orc.cycle(1)
+            t = orc.state(str(tmp_path))["type"]
+            per_step.append(int(np.sum((prev == 12) & (t != 12))))
+            prev = t.copy()
+        orc.close()
+        cfg.close()
+    assert any(32 < n <= 64 for n in per_step), per_step
+    assert any(64 < n <= 256 for n in per_step), per_step
+    assert any(n > 256 for n in per_step), per_step
+
+
 def test_golden_cases_exercise_every_branch():
     """The small cases must cover the reference's branches the GPU path
     reimplements: fill/empty conversions, impactor cover/uncover, contacts,
