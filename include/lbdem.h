@@ -432,7 +432,8 @@ typedef struct lbdem_server_options {
 typedef struct lbdem_job_result {
   int64_t job_id;
   int32_t status;         /* LBDEM_OK or the failing call's status         */
-  int32_t cycles;         /* goCycles run                                  */
+  int32_t cycles;         /* goCycles run (for a failed run: up to the end of
+                             the slice whose error bits showed the failure) */
   double submit_time, start_time, end_time; /* s since lbdem_server_create */
   double impactor_x0[3], impactor_x1[3];    /* object 0 at the end         */
   double fluid_mass;      /* as lbdem_mass_summary                         */
@@ -454,7 +455,11 @@ typedef struct lbdem_job_result {
  * rebuilt when the group's runs change, each group on its own stream. Set
  * CUDA_DEVICE_MAX_CONNECTIONS (for example 32) before the first CUDA call
  * when more than 8 streams are to run concurrently. A finished run frees its memory for the
- * next job. The server's calls must come from one host thread. */
+ * next job. Each run's device error bits are read back after every slice: a
+ * run that diverged (LBDEM_ERR_NONFINITE, a sphere out of the domain:
+ * LBDEM_ERR_DEVICE_STATE) or overflowed a list ends at that slice with its
+ * status, and lbdem_server_last_error describes it. The server's calls must
+ * come from one host thread. */
 int lbdem_server_create(const lbdem_server_options* opt, lbdem_server** out);
 /* Queue a run of `cycles` goCycles; the configuration and its tables are
  * copied. A run larger than the whole budget is refused (LBDEM_ERR_OOM). */

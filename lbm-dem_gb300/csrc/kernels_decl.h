@@ -271,6 +271,9 @@ __global__ void massSummaryKernel(Consts k, const uint8_t* mask, const double* m
 __global__ void momentsKernel(Consts k, const uint8_t* mask, const void* f, double* n,
                               double* u);
 __global__ void nonfiniteCheck(Consts k, const uint8_t* mask, const void* f, int* iscal);
+__global__ void motionFiniteCheck(const double* px0, const double* px1, const double* pFH,
+                                  int n3, const double* obj, int nObj, const double* scal,
+                                  int* iscal);
 __global__ void exportLattice(Consts k, const uint8_t* mask, const void* f, const double* mass,
                               const float* nF, double* fOut, double* massOut);
 

@@ -781,9 +781,17 @@ __device__ __forceinline__ void sphereBox(const Consts& k, double cx, double cy,
                                           double r, int* lo, int* hi) {
   const double c[3] = {cx, cy, cz};
   const int lim[3] = {k.X, k.Y, k.Z};
+  // clamped in double before the conversion, so that a sphere of a diverged
+  // run (a coordinate beyond the int range, or NaN) gets an empty box
   for (int a = 0; a < 3; ++a) {
-    lo[a] = max(0, (int)floor(c[a] - r) - 1);
-    hi[a] = min(lim[a] - 1, (int)ceil(c[a] + r) + 1);
+    const double l = floor(c[a] - r) - 1.0, h = ceil(c[a] + r) + 1.0;
+    if (!(l <= h)) {
+      lo[a] = 0;
+      hi[a] = -1;
+      continue;
+    }
+    lo[a] = (int)fmin(fmax(l, 0.0), (double)lim[a]);
+    hi[a] = (int)fmin(fmax(h, -1.0), (double)(lim[a] - 1));
   }
 }
 
@@ -1671,6 +1679,26 @@ __global__ void exportLattice(Consts k, const uint8_t* mask, const void* f, cons
     for (int j = 0; j < Q; ++j) fOut[(long long)j * k.N + x] = act ? fget(k, f, j, x) : 0.0;
     massOut[x] = (k.mixed && t == 0 && k.freeSurface) ? (double)nF[x] : mass[x];
   }
+}
+
+// Particle and impactor positions, velocities and hydrodynamic forces, and
+// the interface mass share of the last step, finite (a few KB per run): the
+// run server's check after each slice. A diverged lattice reaches the
+// spheres' forces and the interface sums within cycles, and diverged
+// contacts the spheres' motion.
+__global__ void motionFiniteCheck(const double* px0, const double* px1, const double* pFH,
+                                  int n3, const double* obj, int nObj, const double* scal,
+                                  int* iscal) {
+  bool bad = false;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x)
+    bad |= !isfinite(px0[i]) || !isfinite(px1[i]) || !isfinite(pFH[i]);
+  if (blockIdx.x == 0 && (int)threadIdx.x < 3 * nObj) {
+    const double* ob = obj + (threadIdx.x / 3) * OB_STRIDE;
+    const int c = threadIdx.x % 3;
+    bad |= !isfinite(ob[OB_X0 + c]) || !isfinite(ob[OB_X1 + c]) || !isfinite(ob[OB_FHYDRO + c]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) bad |= !isfinite(scal[SC_ADD_MASS]);
+  if (bad) atomicOr(iscal + IS_ERROR, ERR_NONFINITE);
 }
 
 __global__ void nonfiniteCheck(Consts k, const uint8_t* mask, const void* f, int* iscal) {

@@ -1199,6 +1199,20 @@ bool lbdemBatchable(const lbdem_ctx* c) {
   return c->demSolve && c->lbSolve && pairReplayable(c) && !c->k.visc && c->nBody == 0 &&
          c->k.wallType >= 7;
 }
+int lbdemEnqueueErrorRead(lbdem_ctx* c, int* dst, cudaStream_t st) {
+  const int n3 = 3 * c->nPart;
+  const int blocks = std::max(1, std::min((n3 + 255) / 256, 64));
+  motionFiniteCheck<<<blocks, 256, 0, st>>>(c->d.px0, c->d.px1, c->d.pFHydro, n3, c->d.obj,
+                                           c->nObj, c->d.scal, c->d.iscal);
+  if (cudaGetLastError() != cudaSuccess) return LBDEM_ERR_CUDA;
+  return cudaMemcpyAsync(dst, c->d.iscal + IS_ERROR, sizeof(int), cudaMemcpyDeviceToHost, st) ==
+                 cudaSuccess
+             ? LBDEM_OK
+             : LBDEM_ERR_CUDA;
+}
+int lbdemErrorStatus(lbdem_ctx* c, int bits, const char* when) {
+  return deviceError(c, bits, when);
+}
 int lbdemBatchKey(const lbdem_ctx* c) {
   return c->precision | (c->freeSurface ? 2 : 0) | (c->nObj > 0 ? 4 : 0) | (c->nWall > 0 ? 8 : 0);
 }

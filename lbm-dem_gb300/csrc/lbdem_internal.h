@@ -272,6 +272,15 @@ int lbdemBatchKey(const lbdem_ctx* c);
 int lbdemEnqueueBatchCycle(const std::vector<lbdem_ctx*>& runs, const lbdem::JobArgs* jobs,
                            cudaStream_t s);
 void lbdemAdvanceCounters(lbdem_ctx* c, int cycles);
+// Enqueues on stream st a check that the run's particle and impactor
+// positions, velocities and hydrodynamic forces and its interface mass share
+// are finite (ERR_NONFINITE otherwise), then a copy
+// of its device error bits into dst (pinned host memory), for a check once
+// st reaches that point.
+int lbdemEnqueueErrorRead(lbdem_ctx* c, int* dst, cudaStream_t st);
+// The status of error bits read that way (LBDEM_OK for 0); sets the run's
+// message.
+int lbdemErrorStatus(lbdem_ctx* c, int bits, const char* when);
 
 // Counts one device allocation for lbdem_device_allocations; every
 // cudaMalloc / cudaMallocAsync of the library calls it.

@@ -20,6 +20,12 @@
 // flight), so no cross-stream ordering is needed. Runs outside
 // the groups (their first cycles, an odd last cycle) advance on their own
 // streams.
+//
+// Every slice (and a run's initialisation) ends with a copy of the run's
+// device error bits into a pinned word; when the slice is seen complete, a
+// set bit (a non-finite value, a sphere driven out of the domain, a list
+// overflow) ends that run there with its status and message, and the others
+// carry on.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -48,6 +54,8 @@ struct Job {
   double submitTime = 0.0, startTime = 0.0;
   lbdem_ctx* ctx = nullptr;
   cudaEvent_t sliceDone = nullptr;
+  int* err = nullptr;  // its device error bits, read back after each slice
+  int errSlot = -1;    // (a slot of the server's pinned error words)
   bool inFlight = false;
   bool counted = false;  // its bytes are part of the server's memory in use
   bool batched = false;  // a member of a batch group
@@ -76,6 +84,10 @@ struct lbdem_server {
   };
   std::vector<Group> groups;
   int groupRuns = 0;
+  // one pinned word per run slot: a run's device error bits, copied after
+  // each of its slices, so that a diverged run ends at that slice
+  int* errPool = nullptr;
+  std::vector<int> errFree;
   double now() const {
     return std::chrono::duration<double>(Clock::now() - origin).count();
   }
@@ -92,6 +104,7 @@ int serverErr(lbdem_server* s, int code, const std::string& msg) {
 }
 
 void releaseJob(lbdem_server* s, Job* j) {
+  if (j->errSlot >= 0) s->errFree.push_back(j->errSlot);
   if (j->sliceDone) cudaEventDestroy(j->sliceDone);
   if (j->ctx) lbdem_destroy(j->ctx);
   if (j->counted) s->used -= j->bytes;
@@ -169,13 +182,20 @@ void admit(lbdem_server* s) {
     o.device = s->opt.device;
     o.chunks_per_block = s->opt.chunks_per_block;
     // the run's initialisation overlaps the other runs' work; its device
-    // errors surface at the run's end
+    // errors are read back behind it and end the run when it completes
     o.async_init = 1;
     j->startTime = s->now();
     int rc = lbdem_create(&j->cfg, &o, &j->ctx);
     if (rc == LBDEM_OK && cudaEventCreateWithFlags(&j->sliceDone, cudaEventDisableTiming) !=
                               cudaSuccess)
       rc = LBDEM_ERR_CUDA;
+    if (rc == LBDEM_OK) {  // a free error word (max_active of them, one per resident run)
+      j->errSlot = s->errFree.back();
+      s->errFree.pop_back();
+      j->err = s->errPool + j->errSlot;
+      *j->err = 0;
+      rc = lbdemEnqueueErrorRead(j->ctx, j->err, j->ctx->stream);
+    }
     // the run's initialisation is work in flight on its own stream: until it
     // completes the run neither joins a group (whose launches run on the
     // group's stream, unordered with the run's own) nor gets a slice
@@ -255,6 +275,19 @@ bool progressGroup(lbdem_server* s, lbdem_server::Group& g) {
       return true;
     }
   }
+  // members whose error bits came back set end at this slice; the group's
+  // graph is then rebuilt without them
+  bool dropped = false;
+  for (size_t q = 0; q < g.members.size();) {
+    Job* j = g.members[q];
+    if (!*j->err) {
+      ++q;
+      continue;
+    }
+    g.members.erase(g.members.begin() + q);
+    dropJob(s, j, lbdemErrorStatus(j->ctx, *j->err, " after a slice"), "a shared-launch slice");
+    dropped = true;
+  }
   auto fits = [&](Job* j, int key) {
     return j->cycles - j->done >= 2 && lbdemBatchable(j->ctx) &&
            lbdemBatchKey(j->ctx) == key;
@@ -273,7 +306,7 @@ bool progressGroup(lbdem_server* s, lbdem_server::Group& g) {
     if (key < 0) key = lbdemBatchKey(j->ctx);
     if (lbdemBatchKey(j->ctx) == key) next.push_back(j);
   }
-  const bool changed = next != g.members;
+  const bool changed = dropped || next != g.members;
   g.members = next;
   for (Job* j : g.members) j->batched = true;
   if (changed && !g.members.empty() && buildGroupGraph(s, g) != LBDEM_OK) {
@@ -290,6 +323,7 @@ bool progressGroup(lbdem_server* s, lbdem_server::Group& g) {
       serverErr(s, LBDEM_ERR_CUDA, "batch graph launch");
       break;
     }
+  for (Job* j : g.members) lbdemEnqueueErrorRead(j->ctx, j->err, g.stream);
   cudaEventRecord(g.done, g.stream);
   for (Job* j : g.members) {
     j->done += slice;
@@ -332,6 +366,11 @@ bool progress(lbdem_server* s) {
         finishJob(s, j, LBDEM_ERR_CUDA, where.c_str());
         continue;
       }
+      if (*j->err) {  // diverged (or overflowed): the run ends at this slice
+        s->active.erase(s->active.begin() + q);
+        finishJob(s, j, lbdemErrorStatus(j->ctx, *j->err, " after a slice"), "a slice");
+        continue;
+      }
       // now idle: a run that fits a group waits for the group's next turn
       if (!s->groups.empty() && j->cycles - j->done >= 2 && lbdemBatchable(j->ctx)) {
         ++q;
@@ -346,6 +385,7 @@ bool progress(lbdem_server* s) {
     }
     const int32_t n = std::min(s->opt.slice_cycles, j->cycles - j->done);
     int rc = lbdem_cycle(j->ctx, n);
+    if (rc == LBDEM_OK) rc = lbdemEnqueueErrorRead(j->ctx, j->err, j->ctx->stream);
     if (rc == LBDEM_OK && cudaEventRecord(j->sliceDone, j->ctx->stream) != cudaSuccess)
       rc = LBDEM_ERR_CUDA;
     if (rc != LBDEM_OK) {
@@ -392,11 +432,18 @@ extern "C" int lbdem_server_create(const lbdem_server_options* opt, lbdem_server
       }
     }
   }
+  if (cudaHostAlloc(&s->errPool, sizeof(int) * (size_t)opt->max_active, cudaHostAllocDefault) !=
+      cudaSuccess) {
+    s->errPool = nullptr;
+    lbdem_server_destroy(s);
+    return LBDEM_ERR_CUDA;
+  }
+  for (int i = opt->max_active - 1; i >= 0; --i) s->errFree.push_back(i);
   s->budget = opt->device_budget_bytes;
   if (s->budget <= 0) {
     size_t freeB = 0, totalB = 0;
     if (cudaMemGetInfo(&freeB, &totalB) != cudaSuccess) {
-      delete s;
+      lbdem_server_destroy(s);
       return LBDEM_ERR_CUDA;
     }
     s->budget = (int64_t)(0.9 * (double)freeB);
@@ -481,6 +528,7 @@ extern "C" void lbdem_server_destroy(lbdem_server* s) {
   }
   for (Job* j : s->active) releaseJob(s, j);
   for (Job* j : s->pending) delete j;
+  if (s->errPool) cudaFreeHost(s->errPool);
   delete s;
 }
 

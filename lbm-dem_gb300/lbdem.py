@@ -26,6 +26,9 @@ MIXED = 1
 NOALLOC_MAX_NODES = 16384  # LBDEM_NOALLOC_MAX_NODES in include/lbdem.h
 DEBUG_NO_LATTICE_COPIES = 1  # LBDEM_DEBUG_NO_LATTICE_COPIES
 
+ERR_NONFINITE = 5      # LBDEM_ERR_NONFINITE
+ERR_OVERFLOW = 6       # LBDEM_ERR_OVERFLOW
+ERR_DEVICE_STATE = 7   # LBDEM_ERR_DEVICE_STATE
 ERRORS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
     4: "input error", 5: "non-finite state", 6: "list overflow",

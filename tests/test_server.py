@@ -132,3 +132,52 @@ def test_tuner_picks_a_candidate_schedule(lib):
     for cf in cfgs:
         cf.close()
     assert b in (0, 2, 4, 8) and c in (8, 32) and t > 0.0
+
+
+def _diverging_case(tmp_path):
+    """A run that diverges within 200 cycles: relaxation time 0.501 and an
+    initial fluid velocity of 0.2 across a 24x32x24 box (the oracle's
+    populations turn non-finite at cycle 156, its spheres leave the domain
+    at cycle 192)."""
+    import casegen
+    import lbdem
+    c = casegen.impact_case((24, 32, 24), 20.0, 6, (3.0, 3.4), 4.0, 26.0, -0.05, 5.0, 0.501,
+                            1.0e-4, 1, overrides={"objWaitTime": "2", "initVelocityX": "0.2"},
+                            name="diverge")
+    return lbdem.LoadedConfig(c.write(str(tmp_path / "diverge")))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("solo", [False, True], ids=["batched", "solo"])
+@pytest.mark.parametrize("prec_name", ["fp64", "mixed"])
+def test_diverged_run_ends_at_its_slice(prec_name, solo, lib, tmp_path):
+    """A run that diverges ends at the slice whose read-back shows it, with a
+    non-finite (or out-of-domain) status and a message; the runs beside it
+    finish with the results they have alone."""
+    import lbdem
+    prec = lbdem.PLAIN_FP64 if prec_name == "fp64" else lbdem.MIXED
+    bad_cfg = _diverging_case(tmp_path)
+    good_cfg = _cfg("small_cells")
+    srv = lbdem.Server(precision=prec, max_active=2, slice_cycles=8,
+                       batch_runs=0 if solo else 2)
+    bad_id = srv.submit(bad_cfg, 400)
+    good_id = srv.submit(good_cfg, CYCLES)
+    res = {r["job_id"]: r for r in srv.drain()}
+    err = srv.last_error()
+    srv.close()
+    bad, good = res[bad_id], res[good_id]
+    assert bad["status"] in (lbdem.ERR_NONFINITE, lbdem.ERR_DEVICE_STATE), bad
+    assert bad["cycles"] < 260, bad["cycles"]
+    assert "after a slice" in err and "failed in a" in err, err
+    if not solo:
+        assert bad["batched_cycles"] > 0
+    assert good["status"] == 0 and good["cycles"] == CYCLES
+    y0, x0, x1 = _solo("small_cells", prec)
+    got0 = np.array(good["impactor_x0"])
+    if prec == lbdem.PLAIN_FP64:
+        np.testing.assert_allclose(got0, x0, rtol=1e-10, atol=0)
+    else:
+        disp, ref = got0 - y0, x0 - y0
+        assert np.max(np.abs(disp - ref)) <= 1e-3 * max(np.max(np.abs(ref)), 1e-12)
+    bad_cfg.close()
+    good_cfg.close()
