@@ -427,7 +427,9 @@ def accuracy(args, cfg) -> dict:
     - the impactor trajectory error (largest difference of the vertical
       displacement, relative to the largest FP64 displacement);
     - the maximum penetration fluidHeight + r - y of each form;
-    - each form's fluid-mass drift over the run.
+    - each form's fluid-mass drift over the run;
+    - the particle position RMS difference at the end, absolute (length
+      units) and relative to the RMS particle displacement of the FP64 form.
     """
     import lbdem
     import numpy as np
@@ -440,6 +442,7 @@ def accuracy(args, cfg) -> dict:
     for p, sv in runs.items():
         traj[p].append(float(sv.objects()["o_x0"][0][1]))
         mass[p].append(sv.mass_total())
+    xinit = runs[lbdem.PLAIN_FP64].particles()["p_x0"]
     done = 0
     while done < S:
         n = min(blk, S - done)
@@ -449,8 +452,13 @@ def accuracy(args, cfg) -> dict:
             traj[p].append(float(sv.objects()["o_x0"][0][1]))
             mass[p].append(sv.mass_total())
         done += n
+    xend = {p: sv.particles()["p_x0"] for p, sv in runs.items()}
     for sv in runs.values():
         sv.close()
+    prms = float(np.sqrt(np.mean(np.sum((xend[lbdem.MIXED] - xend[lbdem.PLAIN_FP64]) ** 2,
+                                        axis=1)))) if len(xinit) else 0.0
+    pdisp = float(np.sqrt(np.mean(np.sum((xend[lbdem.PLAIN_FP64] - xinit) ** 2, axis=1)))) \
+        if len(xinit) else 0.0
     ym, yf = np.array(traj[lbdem.MIXED]), np.array(traj[lbdem.PLAIN_FP64])
     dm, df = ym - ym[0], yf - yf[0]
     pen = {p: float(np.max(fill + r0 - np.array(traj[p]))) for p in runs}
@@ -463,6 +471,9 @@ def accuracy(args, cfg) -> dict:
         "max_penetration_rel_err": abs(pen[lbdem.MIXED] - pen[lbdem.PLAIN_FP64]) /
                                    max(abs(pen[lbdem.PLAIN_FP64]), 1e-300),
         "mass_drift": {"mixed": drift[lbdem.MIXED], "fp64": drift[lbdem.PLAIN_FP64]},
+        "particle_position_rms": prms,
+        "particle_position_rms_rel": prms / max(pdisp, 1e-300),
+        "particle_displacement_rms_fp64": pdisp,
     }
 
 
