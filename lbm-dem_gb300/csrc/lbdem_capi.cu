@@ -1414,6 +1414,43 @@ extern "C" int lbdem_cycle(lbdem_ctx* ctx, int32_t n) {
   return lbdemOutputDrain(ctx, false);
 }
 
+namespace {
+// Pinned host staging for the small record downloads, one block per host
+// thread, taken on first use and kept for the life of the process (a
+// cudaFreeHost could wait for the whole device, which runs sharing the GPU
+// must not do).
+constexpr size_t SMALL_READ_BYTES = 64 * 1024;
+thread_local unsigned char* t_stage = nullptr;
+
+// lbdem_sync followed by a read of `bytes` bytes at device address src into
+// dst, in one host round trip: the error word and the record are copied
+// into pinned staging behind the stream's work, then the stream is waited
+// for once. Larger records take the two-step path.
+int syncAndRead(lbdem_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  if (bytes + 16 > SMALL_READ_BYTES) {
+    if (int rc = lbdem_sync(ctx)) return rc;
+    CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    return LBDEM_OK;
+  }
+  if (!t_stage && cudaHostAlloc((void**)&t_stage, SMALL_READ_BYTES, cudaHostAllocPortable) !=
+                      cudaSuccess) {
+    t_stage = nullptr;
+    if (int rc = lbdem_sync(ctx)) return rc;
+    CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    return LBDEM_OK;
+  }
+  int* err = reinterpret_cast<int*>(t_stage);
+  CK(cudaMemcpyAsync(err, ctx->d.iscal + IS_ERROR, sizeof(int), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(t_stage + 16, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (int rc = lbdemOutputDrain(ctx, true)) return rc;
+  if (int rc = deviceError(ctx, *err, "")) return rc;
+  std::memcpy(dst, t_stage + 16, bytes);
+  return LBDEM_OK;
+}
+}  // namespace
+
 extern "C" int lbdem_sync(lbdem_ctx* ctx) {
   if (!ctx) return LBDEM_ERR_INVALID;
   DeviceScope devScope(ctx->device);
@@ -1636,11 +1673,9 @@ extern "C" int lbdem_download_particles(lbdem_ctx* ctx, const lbdem_particle_vie
 extern "C" int lbdem_download_objects(lbdem_ctx* ctx, const lbdem_object_view* v) {
   if (!ctx || !v) return LBDEM_ERR_INVALID;
   DeviceScope devScope(ctx->device);
-  int rc = lbdem_sync(ctx);
-  if (rc) return rc;
   const int O = ctx->nObj;
   std::vector<double> h((size_t)std::max(O, 1) * OB_STRIDE);
-  CK(cudaMemcpy(h.data(), ctx->d.obj, h.size() * 8, cudaMemcpyDeviceToHost));
+  if (int rc = syncAndRead(ctx, h.data(), ctx->d.obj, h.size() * 8)) return rc;
   const struct { double* dst; int off; } m[] = {
       {v->x0, OB_X0},       {v->x1, OB_X1},       {v->w1, OB_W1},
       {v->FHydro, OB_FHYDRO}, {v->MHydro, OB_MHYDRO}, {v->FContact, OB_FCONTACT},
@@ -1657,12 +1692,10 @@ extern "C" int lbdem_download_bodies(lbdem_ctx* ctx, double* x0, double* x1, dou
                                      double* FTotal, double* L) {
   if (!ctx) return LBDEM_ERR_INVALID;
   DeviceScope devScope(ctx->device);
-  int rc = lbdem_sync(ctx);
-  if (rc) return rc;
   const int B = ctx->nBody;
-  if (B == 0) return LBDEM_OK;
+  if (B == 0) return lbdem_sync(ctx);
   std::vector<double> h((size_t)B * BD_STRIDE);
-  CK(cudaMemcpy(h.data(), ctx->d.body, h.size() * 8, cudaMemcpyDeviceToHost));
+  if (int rc = syncAndRead(ctx, h.data(), ctx->d.body, h.size() * 8)) return rc;
   const struct { double* dst; int off; } m[] = {
       {x0, BD_X0}, {x1, BD_X1}, {FSpring, BD_FSPRING}, {FTotal, BD_FTOTAL}};
   for (const auto& e : m)
