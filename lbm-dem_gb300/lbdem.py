@@ -261,14 +261,21 @@ class Solver:
                     "download_particles")
         return {"p_" + k: a for k, a in arr.items()}
 
+    _OBJECT_FIELDS = ("x0", "x1", "w1", "FHydro", "MHydro", "FContact", "MContact", "FLub",
+                      "MLub", "FTotal")
+
     def objects(self) -> dict:
-        O = int(self.info.n_objects)
-        names = ["x0", "x1", "w1", "FHydro", "MHydro", "FContact", "MContact", "FLub",
-                 "MLub", "FTotal"]
-        arr = {k: np.zeros((O, 3)) for k in names}
-        v = ObjectView(**{k: a.ctypes.data_as(_P) for k, a in arr.items()})
-        self._check(self.lib.lbdem_download_objects(self.ctx, C.byref(v)), "download_objects")
-        return {"o_" + k: a for k, a in arr.items()}
+        """lbdem_download_objects: the impactors' state, fresh arrays of shape
+        (n_objects, 3) per field. The host buffer and its view are made once
+        per solver (the call is cheap enough for a read-back every step)."""
+        if getattr(self, "_obj_view", None) is None:
+            O = int(self.info.n_objects)
+            self._obj_buf = np.zeros((len(self._OBJECT_FIELDS), O, 3))
+            self._obj_view = ObjectView(**{k: self._obj_buf[i].ctypes.data_as(_P)
+                                           for i, k in enumerate(self._OBJECT_FIELDS)})
+        self._check(self.lib.lbdem_download_objects(self.ctx, C.byref(self._obj_view)),
+                    "download_objects")
+        return {"o_" + k: self._obj_buf[i].copy() for i, k in enumerate(self._OBJECT_FIELDS)}
 
     def walls(self) -> dict:
         W = int(self.info.n_walls)
