@@ -25,7 +25,7 @@ import subprocess
 import sys
 import time
 
-# Many runs share the GPU through their own streams; the driver maps streams
+# Many runs share the GPU through their own streams; the CUDA driver maps streams
 # onto this many hardware work queues (default 8), so more than 8 runs would
 # wait on one another's queues. Must be set before the CUDA context exists.
 os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
