@@ -1235,77 +1235,50 @@ __device__ __forceinline__ void voxelizeObjectsBody(const Consts& k, uint8_t* ma
 
 // updateIndices, step 1: every particle claims the nodes of the last active
 // list inside it; the highest particle index wins (src/LB.cpp:695-710).
-// A warp claims for one particle at a time (lanes over the particle's node
-// box). The particles' FP64 setup (lattice-unit centre and radius, node box,
-// FP32 test constants) is formed one particle per lane for the warp's next
-// 32 particles and kept in shared memory: the FP64 divisions once per
-// particle, not once per lane (FP64 issues at a small fraction of the FP32
-// rate on this GPU).
-constexpr int CLAIM_MAX_WARPS = 8;  // blocks of up to 256 threads
 __device__ __forceinline__ void flagClaimBody(const Consts& k, const uint8_t* mask,
                                               uint32_t* claim, const double* px0,
                                               const double* pr, const int* iscal,
                                               unsigned long long* uscal) {
-  __shared__ SphereBoxTest sSt[CLAIM_MAX_WARPS][32];
-  __shared__ int sHi[CLAIM_MAX_WARPS][32][3];
   if (!iscal[IS_NEWNBR]) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) uscal[US_FIRSTFLAG] = ~0ull;
   const int P = k.nPart;
   const int warpsPerBlock = blockDim.x >> 5;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp >= CLAIM_MAX_WARPS) return;
-  // this warp's particles: p0, p0 + S, p0 + 2 S, ...
-  const long long S = (long long)gridDim.x * warpsPerBlock;
-  const long long p0 = (long long)blockIdx.x * warpsPerBlock + warp;
-  for (long long i0 = 0; p0 + i0 * S < P; i0 += 32) {
-    const long long pl = p0 + (i0 + lane) * S;
-    if (pl < P) {
-      const int q = (int)pl;
-      const double cx = px0[q] / k.uLength, cy = px0[P + q] / k.uLength,
-                   cz = px0[2 * P + q] / k.uLength, r = pr[q] / k.uLength;
-      int lo[3], hi[3];
-      sphereBox(k, cx, cy, cz, r, lo, hi);
-      sSt[warp][lane] = sphereBoxTest(cx, cy, cz, r, lo);
-      for (int a = 0; a < 3; ++a) sHi[warp][lane][a] = hi[a];
-    }
-    __syncwarp();
-    for (int t = 0; t < 32; ++t) {
-      const long long pt = p0 + (i0 + t) * S;
-      if (pt >= P) break;  // warp-uniform
-      const SphereBoxTest st = sSt[warp][t];
-      const int* lo = st.lo;
-      const int* hi = sHi[warp][t];
-      const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
-      if (nx <= 0 || ny <= 0 || nz <= 0) continue;
-      const int vol = nx * ny * nz;
-      const uint32_t mark = (uint32_t)pt + 1u;
-      // lane l visits box nodes l, l + 32, ...: its box coordinates advance
-      // by the decomposition of 32 with carries (no division per node), and
-      // nodes clearly outside the sphere are dropped before their mask is read
-      int bx = lane % nx, by = (lane / nx) % ny, bz = lane / (nx * ny);
-      const int sx = 32 % nx, sy = (32 / nx) % ny, sz = 32 / (nx * ny);
-      for (int i = lane; i < vol; i += 32) {
-        const int ix = lo[0] + bx, iy = lo[1] + by, iz = lo[2] + bz;
-        bx += sx;
-        by += sy;
-        bz += sz;
-        if (bx >= nx) {
-          bx -= nx;
-          ++by;
-        }
-        if (by >= ny) {
-          by -= ny;
-          ++bz;
-        }
-        const float dx = (float)(ix - lo[0]) - st.fx, dy = (float)(iy - lo[1]) - st.fy,
-                    dz = (float)(iz - lo[2]) - st.fz;
-        if (dx * dx + dy * dy + dz * dz > st.r2out) continue;
-        const long long x = ix + iy * k.sy + iz * k.sz;
-        if (!(mask[x] & ABIT)) continue;
-        if (insideBox(st, ix, iy, iz)) atomicMax(claim + x, mark);
+  const int lane = threadIdx.x & 31;
+  for (int p = blockIdx.x * warpsPerBlock + (threadIdx.x >> 5); p < P;
+       p += gridDim.x * warpsPerBlock) {
+    const double cx = px0[p] / k.uLength, cy = px0[P + p] / k.uLength,
+                 cz = px0[2 * P + p] / k.uLength, r = pr[p] / k.uLength;
+    int lo[3], hi[3];
+    sphereBox(k, cx, cy, cz, r, lo, hi);
+    const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+    if (nx <= 0 || ny <= 0 || nz <= 0) continue;
+    const int vol = nx * ny * nz;
+    const SphereBoxTest st = sphereBoxTest(cx, cy, cz, r, lo);
+    // lane l visits box nodes l, l + 32, ...: its box coordinates advance by
+    // the decomposition of 32 with carries (no division per node), and nodes
+    // clearly outside the sphere are dropped before their mask is read
+    int bx = lane % nx, by = (lane / nx) % ny, bz = lane / (nx * ny);
+    const int sx = 32 % nx, sy = (32 / nx) % ny, sz = 32 / (nx * ny);
+    for (int i = lane; i < vol; i += 32) {
+      const int ix = lo[0] + bx, iy = lo[1] + by, iz = lo[2] + bz;
+      bx += sx;
+      by += sy;
+      bz += sz;
+      if (bx >= nx) {
+        bx -= nx;
+        ++by;
       }
+      if (by >= ny) {
+        by -= ny;
+        ++bz;
+      }
+      const float dx = (float)(ix - lo[0]) - st.fx, dy = (float)(iy - lo[1]) - st.fy,
+                  dz = (float)(iz - lo[2]) - st.fz;
+      if (dx * dx + dy * dy + dz * dz > st.r2out) continue;
+      const long long x = ix + iy * k.sy + iz * k.sz;
+      if (!(mask[x] & ABIT)) continue;
+      if (insideBox(st, ix, iy, iz)) atomicMax(claim + x, (uint32_t)p + 1u);
     }
-    __syncwarp();  // the next 32 particles' setup overwrites this warp's slots
   }
 }
 
