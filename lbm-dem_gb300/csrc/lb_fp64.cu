@@ -283,6 +283,15 @@ __device__ __forceinline__ void lbPrepareBody(const Consts& k, double* pAcc, lon
   }
 }
 
+// A node of the lattice's outer layer (the box walls). An impactor that
+// reaches the walls turns wall nodes into impactor nodes (as the reference
+// does); once uncovered, such a node becomes gas whatever its neighbours,
+// since an active node there would stream beyond the lattice (the
+// reference's neighbour offsets leave the node array there too).
+__device__ __forceinline__ bool onOuterLayer(const Consts& k, int ix, int iy, int iz) {
+  return ix == 0 || iy == 0 || iz == 0 || ix == k.X - 1 || iy == k.Y - 1 || iz == k.Z - 1;
+}
+
 __device__ __forceinline__ bool fsRegion(const Consts& k, const int* iscal, int& x0, int& y0,
                                          int& z0, int& rx, int& ry, int& rz) {
   if (iscal[IS_BBOX + 3] < 0) return false;
@@ -622,7 +631,9 @@ LBDEM_KERNEL(, fsSmoothen, FsArgs, fs) {
   FS_LOOP(k, a, {
     const uint8_t m = a.mask[x];
     const int t = m & TYPE_MASK;
-    if (t == 2) {
+    // a gas node of the outer layer (an uncovered wall node) stays gas: its
+    // links leave the lattice
+    if (t == 2 && !onOuterLayer(k, ix, iy, iz)) {
       long long win = -1;
 #pragma unroll 1
       for (int j = 1; j < Q; ++j) {
@@ -905,7 +916,7 @@ __device__ __forceinline__ void uncoverResolveWarp(const Consts& k, const uint8_
         }
       }
     }
-  bool valid[H];
+  bool valid[H], edge[H];
   uint32_t lk[H][Q];
   unsigned inb[H];
 #pragma unroll
@@ -913,6 +924,7 @@ __device__ __forceinline__ void uncoverResolveWarp(const Consts& k, const uint8_
     valid[h] = 32 * h + lane < n;
     int ix = 0, iy = 0, iz = 0;
     if (valid[h]) coords(k, (long long)x[h], ix, iy, iz);
+    edge[h] = onOuterLayer(k, ix, iy, iz);
     inb[h] = 0;
 #pragma unroll
     for (int j = 1; j < Q; ++j) {
@@ -973,7 +985,7 @@ __device__ __forceinline__ void uncoverResolveWarp(const Consts& k, const uint8_
     for (int h = 0; h < H; ++h) {
       const bool fluidNb = fixFluid[h] || (back[h] & fluidL) != 0;
       const bool gasNb = fixGas[h] || (back[h] & gasL) != 0;
-      const uint8_t nst = !fluidNb ? 2 : gasNb ? 3 : 0;
+      const uint8_t nst = (!fluidNb || edge[h]) ? 2 : gasNb ? 3 : 0;
       changed |= valid[h] && nst != st[h];
       if (valid[h]) st[h] = nst;
     }
@@ -1114,6 +1126,7 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
       }
     }
     for (int b = nb; b < 9; ++b) s_back[9 * i + b] = -1;
+    if (onOuterLayer(k, ix, iy, iz)) fix |= 0x40;
     s_st[i] = (uint8_t)(12 | fix);
   }
   teamSync(T);
@@ -1130,7 +1143,7 @@ __device__ __forceinline__ void uncoverResolveBody(const Consts& k, uint8_t* mas
       fluidNb |= tl == 0;
       gasNb |= tl == 2;
     }
-    return (uint8_t)((me & 0x30) | (!fluidNb ? 2 : gasNb ? 3 : 0));
+    return (uint8_t)((me & 0x70) | ((!fluidNb || (me & 0x40)) ? 2 : gasNb ? 3 : 0));
   };
   if (n <= UNCOVER_SERIAL) {
     // few candidates: one thread in ascending order, the reference's own
