@@ -216,7 +216,10 @@ int lbdem_set_stream(lbdem_ctx* ctx, void* cuda_stream);
 
 /* DEM::discreteElementStep, src/DEM.cpp:359-401 */
 int lbdem_dem_step(lbdem_ctx* ctx);
-/* LB::latticeBoltzmannCouplingStep, src/LB.cpp:432-467 */
+/* LB::latticeBoltzmannCouplingStep, src/LB.cpp:432-467. One departure: a
+ * wall-layer node that an impactor covered and then uncovered becomes gas
+ * (the reference makes it fluid or interface when it has fluid
+ * neighbours, and then streams it beyond the lattice). */
 int lbdem_coupling_step(lbdem_ctx* ctx);
 /* LB::latticeBolzmannStep, src/LB.cpp:400-418 */
 int lbdem_lb_step(lbdem_ctx* ctx);
